@@ -1,0 +1,327 @@
+#!/usr/bin/env python3
+"""Headline benchmark: closest-hit Mrays/s on the LBVH microbenchmark.
+
+Workload (one GPU): icosphere subdivided 8 times (1,310,720 triangles)
+displaced by 3-octave value noise; 4,194,304 coherent primary rays (one per
+pixel centre of a 2048x2048 pinhole camera) plus 4,194,304 incoherent rays
+(area-weighted surface points, cosine directions). A step is one
+closest-hit traversal of all 8,388,608 rays (runCollisionSystem, through
+wpbr_collide_device on resident buffers). Inputs (268 MB of rays) exceed the
+129 MB L2, so no flush is needed between steps.
+
+Also reported: `e2e` through wpbr_collide with pinned host buffers
+(host->device rays and device->host hits inside the timed region), the GPU
+LBVH build rate, the any-hit rate, the roofline of the traversal kernel and
+the oracle's CPU baseline (the reference's prune-free traversal restated in
+C++, all host threads, bounded sample).
+
+`--impl reference` times that CPU implementation alone (the reference cannot
+be built here: its ECS, math and allocator libraries are not vendored).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+RES = 2048
+LEVEL = 8
+METRIC = "Mrays/s closest-hit"
+WORKLOAD = "LBVH microbench: icosphere L8 (1,310,720 tris, 3-octave noise), 4M coherent + 4M incoherent rays"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.count(",") >= 8]
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows]
+        mx = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_ray():
+    """DRAM bytes per ray of the traversal kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "trace_c1_traffic.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("dram_bytes_per_ray")
+    return None
+
+
+def cpu_trace_rate(desc, rays, seconds, threads=None):
+    """Oracle (the reference's prune-free candidate traversal) on host cores."""
+    import numpy as np
+    from oracle import binding as O
+
+    L = O.lib()
+    if threads:
+        L.orc_set_threads(threads)
+    cores = L.orc_num_threads()
+    o = O.OracleScene(desc)
+    n = rays.shape[0]
+    idx = np.concatenate([np.arange(0, n // 2, 97), np.arange(n // 2, n, 97)])
+    probe = rays[idx[:20000:7]]
+    t = time.perf_counter()
+    o.trace(probe, mode=0)
+    rate = probe.shape[0] / max(time.perf_counter() - t, 1e-6)
+    m = int(min(idx.size, max(2000, rate * seconds)))
+    sel = np.sort(np.random.default_rng(11).choice(idx, m, replace=False))
+    sample = rays[sel]
+    t = time.perf_counter()
+    o.trace(sample, mode=0)
+    dt = time.perf_counter() - t
+    return dict(value=m / dt / 1e6, unit="Mrays/s", cores=cores, kind="port",
+                sample="%d of the 8,388,608 rays (every 97th, half coherent half incoherent), prune-free "
+                       "candidate traversal + min-t reduce as in JobProcessRayCasts/Results, %.1f s" % (m, dt)), o
+
+
+def run_reference(args):
+    import numpy as np
+    import woodenpbrengine_gb300 as W
+
+    g = W.SceneGen(1, 0, (RES, RES), level=LEVEL, rays=True)
+    rays = g.rays()
+    from oracle import binding as O
+
+    o = O.OracleScene(g.desc)
+    cores = O.lib().orc_num_threads()
+    n = rays.shape[0]
+    step_rays = []
+    times = []
+    rng = np.random.default_rng(3)
+    per_step = 4000
+    probe = rays[rng.choice(n, 2000, replace=False)]
+    t = time.perf_counter()
+    o.trace(probe, mode=0)
+    rate = probe.shape[0] / max(time.perf_counter() - t, 1e-6)
+    per_step = int(max(2000, rate * 2.0))
+    for s in range(args.warmup + args.steps):
+        sel = rng.choice(n, per_step, replace=False)
+        t = time.perf_counter()
+        o.trace(rays[sel], mode=0)
+        dt = time.perf_counter() - t
+        if s >= args.warmup:
+            times.append(dt)
+            step_rays.append(per_step)
+    tot = sum(times)
+    v = sum(step_rays) / tot / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_rays_per_step": per_step},
+        "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                         "sample": "%d random rays of the set per step, prune-free candidate traversal" % per_step},
+        "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from __graft_entry__ import build
+
+        build()
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+
+    from __graft_entry__ import build
+
+    build()
+    import woodenpbrengine_gb300 as W
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", rank=rank, world_size=world)
+    stream = torch.cuda.current_stream()
+    g = W.SceneGen(1, 0, (RES, RES), level=LEVEL, rays=True)
+    rays = g.rays()
+    n = rays.shape[0]
+    ctx = W.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload(g.desc)
+
+    # --- LBVH build rate (reported beside the headline) ---
+    for _ in range(2):
+        ctx.build()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    nb = 5
+    for _ in range(nb):
+        ctx.build()
+    torch.cuda.synchronize()
+    build_s = (time.perf_counter() - t) / nb
+    info = ctx.bvh_info()
+
+    # --- headline: closest-hit traversal over resident rays ---
+    d_rays = torch.from_numpy(rays).to("cuda")
+    d_hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        ctx.collide_device(d_rays.data_ptr(), n, d_hits.data_ptr(), W.TRACE_CLOSEST)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.collide_device(d_rays.data_ptr(), n, d_hits.data_ptr(), W.TRACE_CLOSEST)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    ctx.check_device_errors()
+    if dist:
+        t_ = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t_, op=dist.ReduceOp.MAX)
+        ms = float(t_.item())
+        dist.barrier()
+    ms_step = ms / args.steps
+    value = world * n * args.steps / (ms / 1e3) / 1e6
+    hits = d_hits.cpu().numpy()
+    hit_frac = float(np.mean(hits[:, 1].view(np.uint32) != 0xFFFFFFFF))
+
+    # any-hit
+    ea = torch.cuda.Event(enable_timing=True)
+    eb = torch.cuda.Event(enable_timing=True)
+    ctx.collide_device(d_rays.data_ptr(), n, d_hits.data_ptr(), W.TRACE_ANY)
+    ea.record(stream)
+    for _ in range(5):
+        ctx.collide_device(d_rays.data_ptr(), n, d_hits.data_ptr(), W.TRACE_ANY)
+    eb.record(stream)
+    torch.cuda.synchronize()
+    any_rate = n * 5 / (ea.elapsed_time(eb) / 1e3) / 1e6
+
+    # byte model: 48 B/ray + 32 B per box test + 36 B per triangle test
+    sample = rays[::64]
+    _, st = ctx.collide(sample, stats=True)
+    V = float(st[:, 0].mean())
+    P = float(st[:, 1].mean())
+    bytes_per_ray = 48.0 + 32.0 * V + 36.0 * P
+    achieved = bytes_per_ray * n / (ms_step / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    tpr = ncu_traffic_per_ray()
+
+    # --- e2e through the public host-buffer API (pinned) ---
+    h_rays = torch.from_numpy(rays).pin_memory().numpy()
+    h_hits = torch.empty((n, 4), dtype=torch.float32).pin_memory().numpy()
+    import ctypes as C
+
+    lib = W.lib()
+    fp = C.POINTER(C.c_float)
+    rp, hp = h_rays.ctypes.data_as(fp), h_hits.ctypes.data_as(fp)
+    lib.wpbr_collide(ctx.handle, rp, n, hp, 0)
+    e2e_steps = max(3, args.steps // 2)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(e2e_steps):
+        st_ = lib.wpbr_collide(ctx.handle, rp, n, hp, 0)
+        assert st_ == 0
+    e2e_s = (time.perf_counter() - t) / e2e_steps
+    e2e = world * n / e2e_s / 1e6
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu, _ = cpu_trace_rate(g.desc, rays, args.cpu_seconds)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; the reference publishes no dataset)",
+        "config": {"workload": WORKLOAD, "rays_per_step": n, "triangles": info["n_prims"],
+                   "bvh_nodes": info["n_nodes"], "treelets": info["n_treelets"], "bvh_depth": info["max_depth"],
+                   "hit_fraction": hit_frac, "l2": "inputs larger than L2 (268 MB of rays), no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 16 * n},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind,
+                     "traffic": (tpr * n) if tpr else None,
+                     "bytes_model": "48 + 32*V + 36*P per ray, V=%.2f box tests, P=%.2f triangle tests" % (V, P)},
+        "clocks": ck,
+        "build": {"mprims_per_s": info["n_prims"] / build_s / 1e6, "ms": build_s * 1e3},
+        "anyhit_mrays_per_s": any_rate,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

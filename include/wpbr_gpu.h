@@ -1,0 +1,174 @@
+/*
+ * wpbr_gpu.h — C ABI of the GB300 ray-pipeline library (libwpbr_gpu.so).
+ *
+ * Drop-in for WoodenPBREngine's per-sample ray pipeline: the ECS jobs that
+ * MEngine runs through JOB_RUN (WoodenPBREngine/MEngine.cpp:44-50) in the
+ * order of MEngine::buildLBVH (:341-350), runCollisionSystem (:352-361) and
+ * MEngine::render (:380-448). The reference exposes that surface as C++ job
+ * classes over ECS components; this library exposes one context per GPU and
+ * plain pointers and sizes, so any host (C++, Python ctypes, cgo, JNI) can bind
+ * it. Reference interface replaced by each entry point is cited beside it.
+ *
+ * Conventions
+ *  - Every call returns wpbr_status; wpbr_last_error() describes the last
+ *    failure of a context. No exception crosses the ABI.
+ *  - A context is externally synchronised (one host thread at a time). All its
+ *    GPU work is issued on its stream (wpbr_set_stream; default: a stream the
+ *    context creates). Calls taking HOST buffers synchronise before returning;
+ *    calls taking DEVICE buffers (suffix _device) are asynchronous.
+ *  - Rays are 8 floats: origin xyz, unused, direction xyz, tmax (+inf for the
+ *    reference's unbounded rays). Hits are 4 floats: t (+inf on a miss), the
+ *    primitive id's bits (0xFFFFFFFF on a miss), barycentric weights of the
+ *    triangle's second and third vertex (0 for spheres).
+ *  - Primitive ids: spheres first, then triangles (see wpbr_scene.h).
+ *  - No CPU fallback: without a usable CUDA device the calls that need one
+ *    return WPBR_ERR_NO_DEVICE.
+ */
+#ifndef WPBR_GPU_H
+#define WPBR_GPU_H
+
+#include <stdint.h>
+
+#include "wpbr_record.h"
+#include "wpbr_scene.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define WPBR_API __attribute__((visibility("default")))
+#else
+#define WPBR_API
+#endif
+
+typedef enum wpbr_status {
+  WPBR_OK = 0,
+  WPBR_ERR_INVALID_ARG = 1,
+  WPBR_ERR_OOM = 2,
+  WPBR_ERR_CUDA = 3,
+  WPBR_ERR_TRAVERSAL_LIMIT = 4, /* a traversal stack or loop bound was hit */
+  WPBR_ERR_NOT_BUILT = 5,       /* scene / BVH / render setup missing */
+  WPBR_ERR_NO_DEVICE = 6
+} wpbr_status;
+
+typedef struct wpbr_ctx wpbr_ctx;
+
+/* ---- context --------------------------------------------------------- */
+/* Replaces MEngine's singleton ECS (MEngine.h:9-36) for one GPU. */
+WPBR_API wpbr_status wpbr_create(int device, wpbr_ctx** out);
+WPBR_API void wpbr_destroy(wpbr_ctx* ctx);
+WPBR_API const char* wpbr_last_error(const wpbr_ctx* ctx);
+WPBR_API wpbr_status wpbr_set_stream(wpbr_ctx* ctx, void* cuda_stream);
+WPBR_API void* wpbr_get_stream(const wpbr_ctx* ctx);
+/* wpbr_quirk bits (wpbr_scene.h); applies to later builds and renders. */
+WPBR_API wpbr_status wpbr_set_quirks(wpbr_ctx* ctx, uint32_t quirks);
+WPBR_API wpbr_status wpbr_synchronize(wpbr_ctx* ctx);
+/* Device error word (traversal limits etc.) since the last call; cleared. */
+WPBR_API wpbr_status wpbr_check_device_errors(wpbr_ctx* ctx);
+
+/* ---- scene ------------------------------------------------------------- */
+/* MEngine::buildScene (MEngine.cpp:82-339) inputs + preprocess (:374-378):
+ * copies the scene to the device, sets up the camera
+ * (SCameraPerspective::create, CSCameraPerspective.h:17-39) and builds the
+ * environment sampling distribution
+ * (JobLightInfiniteAreaPreprocessSampling, CLightInfiniteArea.cpp:113-139). */
+WPBR_API wpbr_status wpbr_scene_upload(wpbr_ctx* ctx, const wpbr_scene_desc* scene);
+/* camera setup result: raster_camera[16] (row-major), dx[3], dy[3] */
+WPBR_API wpbr_status wpbr_camera_info(wpbr_ctx* ctx, float* raster_camera, float* dx, float* dy);
+/* The same setup without a context or GPU (host arithmetic only). */
+WPBR_API wpbr_status wpbr_camera_setup(const wpbr_camera* camera, float* raster_camera, float* dx, float* dy);
+/* environment distribution (A21): cond_cdf[H*(W+1)], cond_int[H],
+ * marg_cdf[H+1], marg_int[1]; host pointers, any may be NULL */
+WPBR_API wpbr_status wpbr_env_distribution(wpbr_ctx* ctx, float* cond_cdf, float* cond_int, float* marg_cdf,
+                                           float* marg_int);
+
+/* ---- BVH --------------------------------------------------------------- */
+/* MEngine::buildLBVH (MEngine.cpp:341-350): JobUpdateBoundsAndCentroid*,
+ * JobGenerateShapesCentroidBound, JobGenerateShapesMortonCode,
+ * JobSortsShapesByMortonCode, JobEmitLBVH, JobBuildUpperSAH (SLBVH.cpp). */
+WPBR_API wpbr_status wpbr_bvh_build(wpbr_ctx* ctx);
+/* out[4] = n_prims, n_nodes, n_treelets, max_depth */
+WPBR_API wpbr_status wpbr_bvh_info(wpbr_ctx* ctx, uint32_t* out4);
+/* Copies the build products to host arrays (NULL skips): per primitive (input
+ * order) bounds[6], centroids[3], Morton codes; cbounds[6]; the array the tree
+ * is built over (sorted_codes, sorted_prims); treelet starts; the flattened
+ * CSceneTreeLBVH (nodes[3] = offset, n_shapes, axis; node_bounds[6]; shapes). */
+WPBR_API wpbr_status wpbr_bvh_export(wpbr_ctx* ctx, float* prim_bounds, float* centroids, float* cbounds,
+                                     uint32_t* codes, uint32_t* sorted_codes, uint32_t* sorted_prims,
+                                     uint32_t* treelet_start, uint32_t* nodes, float* node_bounds,
+                                     uint32_t* shapes);
+
+/* ---- collision ----------------------------------------------------------- */
+/* runCollisionSystem (MEngine.cpp:352-361): JobProcessRayCasts,
+ * Job{Sphere,Triangle}...InteractionRequests, JobProcessRayCastsResults.
+ * CLOSEST returns the reference's hit (closest non-zero t, first candidate in
+ * near-first order on ties); ANY stops at the first hit (occlusion only). */
+enum wpbr_trace_mode { WPBR_TRACE_CLOSEST = 0, WPBR_TRACE_ANY = 1 };
+WPBR_API wpbr_status wpbr_collide(wpbr_ctx* ctx, const float* rays, uint64_t n, float* hits, uint32_t mode);
+WPBR_API wpbr_status wpbr_collide_device(wpbr_ctx* ctx, const void* d_rays, uint64_t n, void* d_hits,
+                                         uint32_t mode);
+/* Per-ray node visits and primitive tests (u32 pairs), for the byte model. */
+WPBR_API wpbr_status wpbr_collide_stats(wpbr_ctx* ctx, const float* rays, uint64_t n, float* hits,
+                                        uint32_t* stats, uint32_t mode);
+
+/* ---- rendering -------------------------------------------------------------- */
+/* Film + sample streams for spp passes (JobGenerateFilmTiles,
+ * JobCreateCameraSamples, CSFilm.cpp:10-68); clears the film. */
+WPBR_API wpbr_status wpbr_render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t stream);
+/* One sample pass through the fused wavefront kernels (graph-captured):
+ * the per-spp job list of MEngine::render (MEngine.cpp:393-442) plus
+ * JobAccumalateLIFromSamples. */
+WPBR_API wpbr_status wpbr_render_pass(wpbr_ctx* ctx, uint32_t pass);
+/* All spp passes. */
+WPBR_API wpbr_status wpbr_render(wpbr_ctx* ctx);
+/* Film accumulators to host: acc_L[W*H*3], acc_w[W*H] (pre-tonemap). */
+WPBR_API wpbr_status wpbr_film_read(wpbr_ctx* ctx, float* acc_L, float* acc_w);
+/* JobOutputFilmTitles + JobOutputFilm (CSFilm.cpp:129-242): 8-bit RGB. */
+WPBR_API wpbr_status wpbr_film_tonemap(wpbr_ctx* ctx, uint8_t* rgb8);
+
+/* Staged path: the reference's jobs one by one (see wpbr_job_id), each a
+ * separate kernel over per-pixel state buffers. */
+typedef enum wpbr_job_id {
+  WPBR_JOB_CAMERA_RAYS = 0,       /* JobSamplerUpdateCameraSamples + JobCameraPerspGenerateRaysDifferential */
+  WPBR_JOB_COLLIDE_PRIMARY = 1,   /* runCollisionSystem on camera rays (full interactions) */
+  WPBR_JOB_EMITTED_LIGHT = 2,     /* JobScatteringRequestEmittedLight..AccumulateEmittedLight */
+  WPBR_JOB_BSDF_SETUP = 3,        /* JobGenerateBSDFRequests + material jobs + JobBSDFComputeTransform */
+  WPBR_JOB_SAMPLE_LIGHT = 4,      /* JobScatteringSampleLight + SampleLightLI + light sampling jobs */
+  WPBR_JOB_SHADOW_LIGHT = 5,      /* JobScatteringCastShadowRays + runCollisionSystem + ProcessShadowRay */
+  WPBR_JOB_BSDF_COMPUTE = 6,      /* JobBSDF{Conductor,Specular,Dielectric}*Compute */
+  WPBR_JOB_INTEGRATE_LIGHT = 7,   /* JobScatteringIntegrateImportanceLight */
+  WPBR_JOB_SAMPLE_BSDF = 8,       /* JobScatteringSampleBSDF + JobBSDF*Sample */
+  WPBR_JOB_SHADOW_BSDF = 9,       /* ...CastShadowRaysWithInteraction + runCollisionSystem + Process... */
+  WPBR_JOB_LIGHT_COMPUTE = 10,    /* JobSphereLightProcessComputeRequests + JobLightInfiniteAreaLiCompute */
+  WPBR_JOB_INTEGRATE_BSDF = 11,   /* JobScatteringIntegrateImportanceBSDF */
+  WPBR_JOB_FILM_ACCUMULATE = 12,  /* JobAccumalateLIFromSamples */
+  WPBR_JOB_COUNT = 13
+} wpbr_job_id;
+WPBR_API wpbr_status wpbr_job_run(wpbr_ctx* ctx, uint32_t job, uint32_t pass);
+/* Copies the staged path's per-pixel state for the pixel rectangle
+ * [x0,x1)x[y0,y1) into host arrays (NULL fields skipped). */
+WPBR_API wpbr_status wpbr_job_record(wpbr_ctx* ctx, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,
+                                     wpbr_pass_record* rec);
+
+/* ---- synthetic scenes (benchmark and test inputs) -------------------------- */
+typedef struct wpbr_scenegen wpbr_scenegen;
+enum { WPBR_SCENEGEN_RAYS = 1u };
+/* config 0 plain render, 1 LBVH microbench (level = icosphere subdivisions,
+ * 0 -> 8; flag RAYS also builds res_x*res_y coherent + as many incoherent
+ * rays), 2 full frame. Host-only, no GPU needed. */
+WPBR_API wpbr_status wpbr_scenegen_create(uint32_t config, uint32_t seed, uint32_t res_x, uint32_t res_y,
+                                          uint32_t level, uint32_t flags, wpbr_scenegen** out);
+WPBR_API const wpbr_scene_desc* wpbr_scenegen_desc(const wpbr_scenegen* g);
+WPBR_API uint64_t wpbr_scenegen_ray_count(const wpbr_scenegen* g);
+WPBR_API const float* wpbr_scenegen_rays(const wpbr_scenegen* g);
+WPBR_API void wpbr_scenegen_destroy(wpbr_scenegen* g);
+
+/* Library build identification (host-only). */
+WPBR_API const char* wpbr_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WPBR_GPU_H */

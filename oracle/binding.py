@@ -1,0 +1,169 @@
+"""ctypes binding of oracle/_build/liboracle.so — TEST INFRASTRUCTURE ONLY."""
+import ctypes as C
+import os
+
+import numpy as np
+
+from woodenpbrengine_gb300 import _abi as A
+
+from .build import OUT, build_oracle
+
+_FP = C.POINTER(C.c_float)
+_UP = C.POINTER(C.c_uint32)
+_VP = C.c_void_p
+_SIGS = {
+    "orc_scene_create": (_VP, [C.POINTER(A.SceneDesc), C.c_uint32]),
+    "orc_scene_destroy": (None, [_VP]),
+    "orc_num_threads": (C.c_int, []),
+    "orc_set_threads": (None, [C.c_int]),
+    "orc_bvh_sizes": (None, [_VP, _UP]),
+    "orc_bvh_export": (None, [_VP, _FP, _FP, _FP, _UP, _UP, _UP, _UP, _UP, _FP, _UP]),
+    "orc_trace": (None, [_VP, _FP, C.c_uint64, C.c_int, _FP, _UP]),
+    "orc_camera": (None, [_VP, _FP, _FP, _FP]),
+    "orc_env_distribution": (None, [_VP, _FP, _FP, _FP, _FP]),
+    "orc_render_pass": (None, [_VP] + [C.c_uint32] * 8 + [C.POINTER(A.PassRecord)]),
+    "orc_render": (None, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, _FP, _FP]),
+    "orc_fresnel_dielectric": (C.c_float, [C.c_float] * 3),
+    "orc_fresnel_conductor": (C.c_float, [C.c_float] * 4),
+    "orc_tr_d": (C.c_float, [C.c_float] * 5),
+    "orc_power_heuristic": (C.c_float, [C.c_float] * 2),
+    "orc_mitchell": (C.c_float, [C.c_float]),
+    "orc_left_shift3": (C.c_uint32, [C.c_uint32]),
+    "orc_roughness_to_alpha": (C.c_float, [C.c_float]),
+    "orc_sample2d": (None, [C.c_uint32] * 6 + [_FP]),
+    "orc_sample1d": (C.c_float, [C.c_uint32] * 6),
+    "orc_philox": (None, [_UP, _UP, _UP]),
+    "orc_fmath": (None, [C.c_int, _FP, _FP, _FP, C.c_uint64]),
+    "orc_fmath_d": (None, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint64]),
+}
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle() if not os.path.exists(OUT) else OUT
+        L = C.CDLL(path)
+        for k, (r, a) in _SIGS.items():
+            f = getattr(L, k)
+            f.restype = r
+            f.argtypes = a
+        _lib = L
+    return _lib
+
+
+def _fp(a):
+    return a.ctypes.data_as(_FP) if a is not None else None
+
+
+def _up(a):
+    return a.ctypes.data_as(_UP) if a is not None else None
+
+
+class OracleScene:
+    def __init__(self, desc, quirks=0):
+        self._h = lib().orc_scene_create(desc, quirks)
+
+    def close(self):
+        if self._h:
+            lib().orc_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sizes(self):
+        s = np.zeros(4, np.uint32)
+        lib().orc_bvh_sizes(self._h, _up(s))
+        return dict(n_prims=int(s[0]), n_nodes=int(s[1]), n_treelets=int(s[2]), max_depth=int(s[3]))
+
+    def bvh_export(self):
+        z = self.sizes()
+        N, M, T = z["n_prims"], z["n_nodes"], z["n_treelets"]
+        r = dict(prim_bounds=np.zeros(N * 6, np.float32), centroids=np.zeros(N * 3, np.float32),
+                 cbounds=np.zeros(6, np.float32), codes=np.zeros(N, np.uint32), sorted_codes=np.zeros(N, np.uint32),
+                 sorted_prims=np.zeros(N, np.uint32), treelet_start=np.zeros(max(T, 1), np.uint32),
+                 nodes=np.zeros(M * 3, np.uint32), node_bounds=np.zeros(M * 6, np.float32),
+                 shapes=np.zeros(N, np.uint32))
+        lib().orc_bvh_export(self._h, _fp(r["prim_bounds"]), _fp(r["centroids"]), _fp(r["cbounds"]), _up(r["codes"]),
+                             _up(r["sorted_codes"]), _up(r["sorted_prims"]), _up(r["treelet_start"]),
+                             _up(r["nodes"]), _fp(r["node_bounds"]), _up(r["shapes"]))
+        r["treelet_start"] = r["treelet_start"][:T]
+        r.update(z)
+        return r
+
+    def trace(self, rays, mode=1, stats=False):
+        """mode 0 faithful (prune-free candidate list), 1 pruned closest, 2 any-hit."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        hits = np.zeros((n, 4), np.float32)
+        st = np.zeros((n, 2), np.uint32) if stats else None
+        lib().orc_trace(self._h, _fp(rays), n, mode, _fp(hits), _up(st))
+        return (hits, st) if stats else hits
+
+    def camera(self):
+        rc = np.zeros(16, np.float32)
+        dx = np.zeros(3, np.float32)
+        dy = np.zeros(3, np.float32)
+        lib().orc_camera(self._h, _fp(rc), _fp(dx), _fp(dy))
+        return rc.reshape(4, 4), dx, dy
+
+    def env_distribution(self, W, H):
+        cc = np.zeros(H * (W + 1), np.float32)
+        ci = np.zeros(H, np.float32)
+        mc = np.zeros(H + 1, np.float32)
+        mi = np.zeros(1, np.float32)
+        lib().orc_env_distribution(self._h, _fp(cc), _fp(ci), _fp(mc), _fp(mi))
+        return cc, ci, mc, mi
+
+    def render_pass(self, p, spp, seed, stream, rect, fields=None):
+        x0, y0, x1, y1 = rect
+        rec, arrays = A.make_record((x1 - x0) * (y1 - y0), fields)
+        lib().orc_render_pass(self._h, p, spp, seed, stream, x0, y0, x1, y1, C.byref(rec))
+        return arrays
+
+    def render(self, W, H, spp, seed=0, stream=0):
+        L = np.zeros(W * H * 3, np.float32)
+        w = np.zeros(W * H, np.float32)
+        lib().orc_render(self._h, spp, seed, stream, _fp(L), _fp(w))
+        return L.reshape(H, W, 3), w.reshape(H, W)
+
+
+def philox(ctr, key):
+    c = np.asarray(ctr, np.uint32)
+    k = np.asarray(key, np.uint32)
+    o = np.zeros(4, np.uint32)
+    lib().orc_philox(_up(c), _up(k), _up(o))
+    return o
+
+
+FM = dict(sin=0, cos=1, atan2=2, acos=3, exp=4, log=5, tan=6)
+
+
+def fmath(name, x, y=None):
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(y if y is not None else np.zeros_like(x), np.float32)
+    o = np.zeros_like(x)
+    lib().orc_fmath(FM[name], _fp(x), _fp(y), _fp(o), x.size)
+    return o
+
+
+def fmath_d(name, x):
+    x = np.ascontiguousarray(x, np.float64)
+    o = np.zeros_like(x)
+    dp = C.POINTER(C.c_double)
+    lib().orc_fmath_d(0 if name == "sin" else 1, x.ctypes.data_as(dp), o.ctypes.data_as(dp), x.size)
+    return o
+
+
+def sample2d(seed, stream, spp, pixel, p, dim):
+    u = np.zeros(2, np.float32)
+    lib().orc_sample2d(seed, stream, spp, pixel, p, dim, _fp(u))
+    return u
+
+
+def sample1d(seed, stream, spp, pixel, p, dim):
+    return lib().orc_sample1d(seed, stream, spp, pixel, p, dim)

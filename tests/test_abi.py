@@ -1,0 +1,90 @@
+"""The C-ABI library loads without a GPU, exports every entry point declared
+in include/*.h, keeps the documented struct layouts, and its host-only parts
+(scene generator, camera setup) agree with the oracle."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", f)).read()
+            names |= set(re.findall(r"WPBR_API\s+[^;(]*?\b(wpbr_\w+)\s*\(", txt))
+    return names
+
+
+def test_library_exports_every_declared_symbol(W):
+    decl = declared_symbols()
+    assert len(decl) >= 30
+    L = C.CDLL(W.LIB_PATH)
+    missing = [n for n in sorted(decl) if not hasattr(L, n)]
+    assert not missing, missing
+    assert set(W.EXPORTED) <= decl
+    assert W.lib().wpbr_version().decode().startswith("wpbr-gb300")
+
+
+def test_struct_layouts(W):
+    A = W._abi
+    assert C.sizeof(A.Material) == 64
+    assert C.sizeof(A.Sphere) == 144
+    assert C.sizeof(A.Mesh) == 16
+    assert C.sizeof(A.Light) == 20
+    assert C.sizeof(A.PassRecord) == 32 * 8
+
+
+def test_host_entry_points_validate_arguments(W):
+    h = C.c_void_p()
+    assert W.lib().wpbr_scenegen_create(0, 0, 0, 16, 0, 0, C.byref(h)) == W.ERR_INVALID_ARG
+    assert W.lib().wpbr_scenegen_create(9, 0, 16, 16, 0, 0, C.byref(h)) == W.ERR_INVALID_ARG
+    assert W.lib().wpbr_camera_setup(None, None, None, None) == W.ERR_INVALID_ARG
+    assert W.lib().wpbr_create(0, None) == W.ERR_INVALID_ARG
+
+
+def test_no_device_is_reported_not_faked(W):
+    if W.device_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    assert W.lib().wpbr_create(0, C.byref(h)) == W.ERR_NO_DEVICE
+
+
+def test_scenegen_counts_and_determinism(W):
+    g = W.SceneGen(1, 0, (8, 8), level=8)
+    d = g.desc.contents
+    assert d.n_triangles == 1310720 and d.n_vertices == 655362 and d.n_spheres == 0
+    pos = np.ctypeslib.as_array(d.positions, shape=(d.n_vertices * 3,)).copy()
+    g2 = W.SceneGen(1, 0, (8, 8), level=8)
+    d2 = g2.desc.contents
+    assert np.array_equal(pos, np.ctypeslib.as_array(d2.positions, shape=(d2.n_vertices * 3,)))
+    r = np.linalg.norm(pos.reshape(-1, 3), axis=1)
+    assert 0.89 < r.min() and r.max() < 1.11
+    c0 = W.SceneGen(0, 0, (256, 256)).desc.contents
+    assert c0.n_spheres == 65 and c0.n_triangles == 2 and c0.n_lights == 1
+    c2 = W.SceneGen(2, 0, (64, 36), level=4).desc.contents
+    assert c2.n_spheres == 256 and c2.envmap.contents.width == 1024 and c2.envmap.contents.height == 512
+
+
+def test_c1_ray_set(W):
+    g = W.SceneGen(1, 0, (64, 64), level=5, rays=True)
+    rays = g.rays()
+    assert rays.shape == (2 * 64 * 64, 8)
+    d = rays[:, 4:7]
+    assert np.allclose(np.linalg.norm(d, axis=1), 1.0, atol=1e-6)
+    assert np.all(np.isinf(rays[:, 7]))
+
+
+@pytest.mark.parametrize("config,res,level", [(0, (256, 256), 0), (2, (1920, 1080), 4)])
+def test_camera_setup_matches_oracle(W, O, config, res, level):
+    g = W.SceneGen(config, 0, res, level=level)
+    rc, dx, dy = W.camera_setup(g.desc.contents.camera)
+    o = O.OracleScene(g.desc)
+    orc, odx, ody = o.camera()
+    assert np.array_equal(rc.view(np.uint32), orc.view(np.uint32))
+    assert np.array_equal(dx.view(np.uint32), odx.view(np.uint32))
+    assert np.array_equal(dy.view(np.uint32), ody.view(np.uint32))

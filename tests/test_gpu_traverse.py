@@ -1,0 +1,68 @@
+"""GPU collision (wpbr_collide) against the oracle's prune-free reference
+traversal: hit primitive ids and t bit-exact, barycentrics bit-exact."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(hg, ho):
+    pg, po = hg[:, 1].view(np.uint32), ho[:, 1].view(np.uint32)
+    bad = np.nonzero(pg != po)[0]
+    assert bad.size == 0, (bad.size, bad[:8], pg[bad[:8]], po[bad[:8]], hg[bad[:4]], ho[bad[:4]])
+    assert np.array_equal(hg.view(np.uint32), ho.view(np.uint32))
+
+
+@pytest.mark.parametrize("level,res", [(5, (128, 128)), (7, (256, 256))])
+def test_closest_hit_parity_c1(W, O, ctx, level, res):
+    g = W.SceneGen(1, 0, res, level=level, rays=True)
+    ctx.set_quirks(0)
+    ctx.upload(g.desc)
+    ctx.build()
+    rays = g.rays()
+    hg = ctx.collide(rays)
+    ho = O.OracleScene(g.desc).trace(rays, mode=0)
+    _check(hg, ho)
+    assert 0.3 < np.mean(hg[:, 1].view(np.uint32) != 0xFFFFFFFF) < 1.0
+    ha = ctx.collide(rays, mode=W.TRACE_ANY)
+    assert np.array_equal(ha[:, 1].view(np.uint32) == 0xFFFFFFFF, hg[:, 1].view(np.uint32) == 0xFFFFFFFF)
+    ctx.check_device_errors()
+
+
+def test_closest_hit_parity_c1_full_size_sample(W, O, ctx):
+    g = W.SceneGen(1, 0, (2048, 2048), level=8, rays=True)
+    ctx.set_quirks(0)
+    ctx.upload(g.desc)
+    ctx.build()
+    rays = g.rays()
+    assert rays.shape[0] == 8 * 1024 * 1024
+    hg = ctx.collide(rays)
+    idx = np.random.default_rng(5).choice(rays.shape[0], 60000, replace=False)
+    ho = O.OracleScene(g.desc).trace(rays[idx], mode=0)
+    _check(hg[idx], ho)
+    ctx.check_device_errors()
+
+
+def test_degenerate_rays_and_quirk(W, O, ctx):
+    g = W.SceneGen(0, 0, (64, 64))
+    rng = np.random.default_rng(7)
+    n = 20000
+    o = rng.uniform(-15, 15, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d[: n // 4, 1:] = 0.0          # axis-aligned directions (inf reciprocals)
+    d[n // 4: n // 2, 0] = 0.0     # one zero component
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d[n // 2: n // 2 + 100, 1] = -1.0  # straight down onto the ground quad
+    d[n // 2: n // 2 + 100, [0, 2]] = 0.0
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, :3] = o
+    rays[:, 4:7] = d
+    rays[:, 7] = np.inf
+    for q in (0, W.Q_TRI_PERMUTATION_BUG):
+        ctx.set_quirks(q)
+        ctx.upload(g.desc)
+        ctx.build()
+        hg = ctx.collide(rays)
+        ho = O.OracleScene(g.desc, q).trace(rays, mode=0)
+        _check(hg, ho)
+    ctx.set_quirks(0)

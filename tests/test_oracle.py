@@ -1,0 +1,87 @@
+"""The oracle itself: known-answer checks of its restated formulas, internal
+consistency (the pruned traversal equals the reference's prune-free
+candidate list; the flattened tree is well formed) and the committed golden
+fixtures (regression pins; the reference ships none)."""
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_fresnel_known_answers(O):
+    L = O.lib()
+    for et in (1.3, 1.5, 1.7):
+        assert L.orc_fresnel_dielectric(1.0, 1.0, et) == pytest.approx(((et - 1) / (et + 1)) ** 2, rel=1e-6)
+    # exiting with sin(theta_t) >= 1: total internal reflection
+    assert L.orc_fresnel_dielectric(-0.1, 1.0, 1.5) == 1.0
+    for eta, k in ((0.2, 3.0), (1.5, 1.0), (3.0, 0.2)):
+        ref = ((eta - 1) ** 2 + k * k) / ((eta + 1) ** 2 + k * k)
+        assert L.orc_fresnel_conductor(1.0, 1.0, eta, k) == pytest.approx(ref, rel=1e-5)
+
+
+def test_microfacet_and_mis_known_answers(O):
+    L = O.lib()
+    for a in (0.05, 0.25, 0.5):
+        af = float(np.float32(a))
+        # D(n) = 1 / (PI a^2) with PI = 3.14 (pch.h:30), evaluated in double
+        assert L.orc_tr_d(af, af, 0.0, 0.0, 1.0) == np.float32(1.0 / (3.14 * af * af))
+    assert L.orc_power_heuristic(1.0, 1.0) == 0.5
+    assert L.orc_power_heuristic(3.0, 4.0) == pytest.approx(9 / 25, rel=1e-7)
+    B = np.float32(1 / 3)
+    assert L.orc_mitchell(0.0) == pytest.approx((6 - 2 * B) / 6, rel=1e-6)
+    assert abs(L.orc_mitchell(1.0)) < 1e-6  # |2x| = 2: support edge (float rounding of B, C)
+    assert L.orc_left_shift3(1) == 1 and L.orc_left_shift3(2) == 8
+    assert L.orc_left_shift3(1023) == 0x09249249 and L.orc_left_shift3(1024) == 0x09249249
+
+
+def test_pruned_traversal_equals_faithful(W, O):
+    for config, level in ((1, 5), (1, 6)):
+        g = W.SceneGen(config, 0, (128, 128), level=level, rays=True)
+        o = O.OracleScene(g.desc)
+        rays = g.rays()
+        hf = o.trace(rays, mode=0)
+        hp = o.trace(rays, mode=1)
+        assert np.array_equal(hf.view(np.uint32), hp.view(np.uint32))
+        ha = o.trace(rays, mode=2)
+        assert np.array_equal(ha[:, 1].view(np.uint32) == 0xFFFFFFFF, hf[:, 1].view(np.uint32) == 0xFFFFFFFF)
+
+
+def check_tree(e):
+    nodes = e["nodes"].reshape(-1, 3)
+    nb = e["node_bounds"].reshape(-1, 6)
+    N, M = e["n_prims"], e["n_nodes"]
+    covered = np.zeros(N, np.int64)
+    for i in range(M):
+        off, n, axis = nodes[i]
+        if n > 0:
+            covered[off:off + n] += 1
+        else:
+            assert axis < 3 and i + 1 < M and i + 1 < off < M
+            for c in (i + 1, off):
+                assert np.all(nb[c, :3] >= nb[i, :3]) and np.all(nb[c, 3:] <= nb[i, 3:])
+    assert np.all(covered == 1)
+    assert sorted(e["shapes"].tolist()) == list(range(N))
+
+
+@pytest.mark.parametrize("quirks", [0, 16])
+def test_oracle_tree_well_formed(W, O, quirks):
+    g = W.SceneGen(1, 0, (8, 8), level=5)
+    o = O.OracleScene(g.desc, quirks)
+    e = o.bvh_export()
+    check_tree(e)
+    sc = e["sorted_codes"]
+    key = sc if quirks else (sc & 0xFFFFFF)
+    assert np.all(np.diff(key.astype(np.int64)) >= 0)  # sorted by the key the tree uses
+    assert np.array_equal(e["codes"][e["sorted_prims"]], sc)
+
+
+def test_golden_fixtures(W, O):
+    from tests.golden.make_golden import compute
+
+    ref = np.load(os.path.join(GOLDEN, "oracle_golden.npz"))
+    now = compute(W, O)
+    assert set(ref.files) == set(now)
+    for k in ref.files:
+        assert np.array_equal(ref[k].view(np.uint8), np.asarray(now[k]).view(np.uint8)), k

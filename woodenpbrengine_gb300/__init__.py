@@ -1,0 +1,286 @@
+"""GB300 wavefront implementation of WoodenPBREngine's per-sample ray pipeline.
+
+Python binding of the C ABI in include/wpbr_gpu.h (libwpbr_gpu.so, built
+in-tree by woodenpbrengine_gb300.build). The library is the product; this
+module only marshals numpy arrays through ctypes. There is no CPU fallback:
+without the built library the import of `lib()` raises, and without a CUDA
+device the context constructor raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi as A
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libwpbr_gpu.so")
+
+OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TRAVERSAL_LIMIT, ERR_NOT_BUILT, ERR_NO_DEVICE = range(7)
+TRACE_CLOSEST, TRACE_ANY = 0, 1
+Q_TRI_PERMUTATION_BUG, Q_ENV_LI_SAMPLE_FIX, Q_SPHERE_PDF_FIX, Q_ENV_DISTRIB_INDEX_BUG, Q_FULL_MORTON_SORT = (
+    1, 2, 4, 8, 16)
+MAT_CONDUCTOR, MAT_DIELECTRIC, MAT_SPECULAR = 0, 1, 2
+LIGHT_SPHERE, LIGHT_ENV = 0, 1
+
+JOBS = [
+    "CAMERA_RAYS", "COLLIDE_PRIMARY", "EMITTED_LIGHT", "BSDF_SETUP", "SAMPLE_LIGHT", "SHADOW_LIGHT",
+    "BSDF_COMPUTE", "INTEGRATE_LIGHT", "SAMPLE_BSDF", "SHADOW_BSDF", "LIGHT_COMPUTE", "INTEGRATE_BSDF",
+    "FILM_ACCUMULATE",
+]
+JOB = {name: i for i, name in enumerate(JOBS)}
+
+# exported symbols and their ctypes signatures (restype, argtypes)
+_VP = C.c_void_p
+_FP = C.POINTER(C.c_float)
+_UP = C.POINTER(C.c_uint32)
+_SIGS = {
+    "wpbr_version": (C.c_char_p, []),
+    "wpbr_create": (C.c_int, [C.c_int, C.POINTER(_VP)]),
+    "wpbr_destroy": (None, [_VP]),
+    "wpbr_last_error": (C.c_char_p, [_VP]),
+    "wpbr_set_stream": (C.c_int, [_VP, _VP]),
+    "wpbr_get_stream": (_VP, [_VP]),
+    "wpbr_set_quirks": (C.c_int, [_VP, C.c_uint32]),
+    "wpbr_synchronize": (C.c_int, [_VP]),
+    "wpbr_check_device_errors": (C.c_int, [_VP]),
+    "wpbr_scene_upload": (C.c_int, [_VP, C.POINTER(A.SceneDesc)]),
+    "wpbr_camera_info": (C.c_int, [_VP, _FP, _FP, _FP]),
+    "wpbr_env_distribution": (C.c_int, [_VP, _FP, _FP, _FP, _FP]),
+    "wpbr_camera_setup": (C.c_int, [C.POINTER(A.Camera), _FP, _FP, _FP]),
+    "wpbr_bvh_build": (C.c_int, [_VP]),
+    "wpbr_bvh_info": (C.c_int, [_VP, _UP]),
+    "wpbr_bvh_export": (C.c_int, [_VP, _FP, _FP, _FP, _UP, _UP, _UP, _UP, _UP, _FP, _UP]),
+    "wpbr_collide": (C.c_int, [_VP, _FP, C.c_uint64, _FP, C.c_uint32]),
+    "wpbr_collide_device": (C.c_int, [_VP, _VP, C.c_uint64, _VP, C.c_uint32]),
+    "wpbr_collide_stats": (C.c_int, [_VP, _FP, C.c_uint64, _FP, _UP, C.c_uint32]),
+    "wpbr_render_setup": (C.c_int, [_VP, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "wpbr_render_pass": (C.c_int, [_VP, C.c_uint32]),
+    "wpbr_render": (C.c_int, [_VP]),
+    "wpbr_film_read": (C.c_int, [_VP, _FP, _FP]),
+    "wpbr_film_tonemap": (C.c_int, [_VP, C.POINTER(C.c_uint8)]),
+    "wpbr_job_run": (C.c_int, [_VP, C.c_uint32, C.c_uint32]),
+    "wpbr_job_record": (C.c_int, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(A.PassRecord)]),
+    "wpbr_scenegen_create": (C.c_int, [C.c_uint32] * 6 + [C.POINTER(_VP)]),
+    "wpbr_scenegen_desc": (C.POINTER(A.SceneDesc), [_VP]),
+    "wpbr_scenegen_ray_count": (C.c_uint64, [_VP]),
+    "wpbr_scenegen_rays": (_FP, [_VP]),
+    "wpbr_scenegen_destroy": (None, [_VP]),
+}
+EXPORTED = sorted(_SIGS)
+
+_lib = None
+
+
+class WpbrError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("wpbr status %d: %s" % (status, msg))
+        self.status = status
+
+
+def lib():
+    """Load libwpbr_gpu.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libwpbr_gpu.so is not built; run woodenpbrengine_gb300.build.build_library()")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _fp(a):
+    return a.ctypes.data_as(_FP) if a is not None else None
+
+
+def _up(a):
+    return a.ctypes.data_as(_UP) if a is not None else None
+
+
+class SceneGen:
+    """Seeded synthetic scene (host-only; see csrc/scene_gen.cpp)."""
+
+    def __init__(self, config, seed=0, res=(256, 256), level=0, rays=False):
+        self._h = _VP()
+        st = lib().wpbr_scenegen_create(config, seed, res[0], res[1], level, 1 if rays else 0, C.byref(self._h))
+        if st != OK:
+            raise WpbrError(st, "scenegen_create(config=%d)" % config)
+        self.config = config
+
+    @property
+    def desc(self):
+        return lib().wpbr_scenegen_desc(self._h)
+
+    def rays(self):
+        n = lib().wpbr_scenegen_ray_count(self._h)
+        if n == 0:
+            return np.zeros((0, 8), np.float32)
+        p = lib().wpbr_scenegen_rays(self._h)
+        return np.ctypeslib.as_array(p, shape=(n * 8,)).reshape(n, 8).copy()
+
+    def close(self):
+        if self._h:
+            lib().wpbr_scenegen_destroy(self._h)
+            self._h = _VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """One wpbr_ctx (one GPU). Thin, checked wrappers over the C ABI."""
+
+    def __init__(self, device=0):
+        self._h = _VP()
+        st = lib().wpbr_create(device, C.byref(self._h))
+        if st != OK:
+            raise WpbrError(st, "wpbr_create(device=%d) failed" % device)
+
+    def _check(self, st, what):
+        if st != OK:
+            raise WpbrError(st, "%s: %s" % (what, lib().wpbr_last_error(self._h).decode()))
+
+    def close(self):
+        if self._h:
+            lib().wpbr_destroy(self._h)
+            self._h = _VP()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr):
+        self._check(lib().wpbr_set_stream(self._h, stream_ptr), "set_stream")
+
+    def set_quirks(self, q):
+        self._check(lib().wpbr_set_quirks(self._h, q), "set_quirks")
+
+    def synchronize(self):
+        self._check(lib().wpbr_synchronize(self._h), "synchronize")
+
+    def check_device_errors(self):
+        self._check(lib().wpbr_check_device_errors(self._h), "device errors")
+
+    def upload(self, desc):
+        self._check(lib().wpbr_scene_upload(self._h, desc), "scene_upload")
+
+    def camera_info(self):
+        rc = np.zeros(16, np.float32)
+        dx = np.zeros(3, np.float32)
+        dy = np.zeros(3, np.float32)
+        self._check(lib().wpbr_camera_info(self._h, _fp(rc), _fp(dx), _fp(dy)), "camera_info")
+        return rc.reshape(4, 4), dx, dy
+
+    def env_distribution(self, W, H):
+        cc = np.zeros(H * (W + 1), np.float32)
+        ci = np.zeros(H, np.float32)
+        mc = np.zeros(H + 1, np.float32)
+        mi = np.zeros(1, np.float32)
+        self._check(lib().wpbr_env_distribution(self._h, _fp(cc), _fp(ci), _fp(mc), _fp(mi)), "env_distribution")
+        return cc, ci, mc, mi
+
+    def build(self):
+        self._check(lib().wpbr_bvh_build(self._h), "bvh_build")
+
+    def bvh_info(self):
+        out = np.zeros(4, np.uint32)
+        self._check(lib().wpbr_bvh_info(self._h, _up(out)), "bvh_info")
+        return dict(n_prims=int(out[0]), n_nodes=int(out[1]), n_treelets=int(out[2]), max_depth=int(out[3]))
+
+    def bvh_export(self):
+        info = self.bvh_info()
+        N, M, T = info["n_prims"], info["n_nodes"], info["n_treelets"]
+        r = dict(prim_bounds=np.zeros(N * 6, np.float32), centroids=np.zeros(N * 3, np.float32),
+                 cbounds=np.zeros(6, np.float32), codes=np.zeros(N, np.uint32), sorted_codes=np.zeros(N, np.uint32),
+                 sorted_prims=np.zeros(N, np.uint32), treelet_start=np.zeros(max(T, 1), np.uint32),
+                 nodes=np.zeros(M * 3, np.uint32), node_bounds=np.zeros(M * 6, np.float32),
+                 shapes=np.zeros(N, np.uint32))
+        self._check(lib().wpbr_bvh_export(
+            self._h, _fp(r["prim_bounds"]), _fp(r["centroids"]), _fp(r["cbounds"]), _up(r["codes"]),
+            _up(r["sorted_codes"]), _up(r["sorted_prims"]), _up(r["treelet_start"]), _up(r["nodes"]),
+            _fp(r["node_bounds"]), _up(r["shapes"])), "bvh_export")
+        r["treelet_start"] = r["treelet_start"][:T]
+        r.update(info)
+        return r
+
+    def collide(self, rays, mode=TRACE_CLOSEST, stats=False):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        hits = np.zeros((n, 4), np.float32)
+        if stats:
+            st = np.zeros((n, 2), np.uint32)
+            self._check(lib().wpbr_collide_stats(self._h, _fp(rays), n, _fp(hits), _up(st), mode), "collide_stats")
+            return hits, st
+        self._check(lib().wpbr_collide(self._h, _fp(rays), n, _fp(hits), mode), "collide")
+        return hits
+
+    def collide_device(self, d_rays, n, d_hits, mode=TRACE_CLOSEST):
+        self._check(lib().wpbr_collide_device(self._h, d_rays, n, d_hits, mode), "collide_device")
+
+    def render_setup(self, spp, seed=0, stream=0):
+        self._check(lib().wpbr_render_setup(self._h, spp, seed, stream), "render_setup")
+
+    def render_pass(self, p):
+        self._check(lib().wpbr_render_pass(self._h, p), "render_pass")
+
+    def render(self):
+        self._check(lib().wpbr_render(self._h), "render")
+
+    def film(self, W, H):
+        L = np.zeros(W * H * 3, np.float32)
+        w = np.zeros(W * H, np.float32)
+        self._check(lib().wpbr_film_read(self._h, _fp(L), _fp(w)), "film_read")
+        return L.reshape(H, W, 3), w.reshape(H, W)
+
+    def tonemap(self, W, H):
+        out = np.zeros(W * H * 3, np.uint8)
+        self._check(lib().wpbr_film_tonemap(self._h, out.ctypes.data_as(C.POINTER(C.c_uint8))), "tonemap")
+        return out.reshape(H, W, 3)
+
+    def job(self, name, p):
+        self._check(lib().wpbr_job_run(self._h, JOB[name], p), "job " + name)
+
+    def record(self, x0, y0, x1, y1, fields=None):
+        rec, arrays = A.make_record((x1 - x0) * (y1 - y0), fields)
+        self._check(lib().wpbr_job_record(self._h, x0, y0, x1, y1, C.byref(rec)), "job_record")
+        return arrays
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def camera_setup(camera):
+    """A1 on the host: (raster_camera 4x4, dxCamera, dyCamera) for a wpbr_camera."""
+    rc = np.zeros(16, np.float32)
+    dx = np.zeros(3, np.float32)
+    dy = np.zeros(3, np.float32)
+    st = lib().wpbr_camera_setup(C.byref(camera), _fp(rc), _fp(dx), _fp(dy))
+    if st != OK:
+        raise WpbrError(st, "camera_setup")
+    return rc.reshape(4, 4), dx, dy
+
+
+def device_available():
+    """True when a CUDA device answers (no exception when there is none)."""
+    try:
+        c = Context(0)
+    except (WpbrError, ImportError, OSError):
+        return False
+    c.close()
+    return True

@@ -1,0 +1,502 @@
+// context.cu — the C ABI (include/wpbr_gpu.h): context lifetime, scene
+// upload, BVH build/export, collision, rendering entry points.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "camera.cuh"
+#include "common.cuh"
+#include "ctx.hpp"
+#include "wpbr_gpu.h"
+
+namespace wpbr {
+
+wpbr_status set_err(wpbr_ctx* ctx, wpbr_status st, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return st;
+}
+wpbr_status cuda_err(wpbr_ctx* ctx, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  if (e == cudaErrorMemoryAllocation) return set_err(ctx, WPBR_ERR_OOM, m);
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return set_err(ctx, WPBR_ERR_NO_DEVICE, m);
+  return set_err(ctx, WPBR_ERR_CUDA, m);
+}
+
+SceneView scene_view(const wpbr_ctx* ctx) {
+  SceneView S{};
+  S.ns = ctx->ns;
+  S.nt = ctx->nt;
+  S.N = ctx->N;
+  S.sph_o2w = ctx->sph_o2w.p;
+  S.sph_w2o = ctx->sph_w2o.p;
+  S.sph_r = ctx->sph_r.p;
+  S.sph_mat = ctx->sph_mat.p;
+  S.pos = ctx->pos.p;
+  S.idx = ctx->idx.p;
+  S.nrm = ctx->has_nrm ? ctx->nrm.p : nullptr;
+  S.tan = ctx->has_nrm ? ctx->tan.p : nullptr;
+  S.uv = ctx->has_uv ? ctx->uv.p : nullptr;
+  S.tri_mat = ctx->tri_mat.p;
+  S.tri_flags = ctx->tri_flags.p;
+  S.mats = ctx->mats.p;
+  S.lights = ctx->lights.p;
+  S.nlights = (uint32_t)ctx->h_lights.size();
+  S.has_env = ctx->has_env ? 1 : 0;
+  EnvView& e = S.env;
+  e.W = ctx->envW;
+  e.H = ctx->envH;
+  e.rgb = ctx->env_rgb.p;
+  e.cond_func = ctx->cond_func.p;
+  e.cond_cdf = ctx->cond_cdf.p;
+  e.cond_int = ctx->cond_int.p;
+  e.marg_func = ctx->marg_func.p;
+  e.marg_cdf = ctx->marg_cdf.p;
+  e.marg_int = ctx->env_marg_int;
+  e.l2w = ctx->env_l2w;
+  e.w2l = ctx->env_w2l;
+  e.le = ctx->env_le;
+  S.cam = ctx->cam;
+  S.quirks = ctx->quirks;
+  return S;
+}
+
+}  // namespace wpbr
+
+using namespace wpbr;
+
+namespace {
+
+template <typename T>
+cudaError_t upload(DevBuf<T>& d, const T* h, size_t n, cudaStream_t s) {
+  cudaError_t e = d.ensure(n);
+  if (e != cudaSuccess || n == 0) return e;
+  return cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+WPBR_API const char* wpbr_version(void) { return "wpbr-gb300 1.0 (sm_103a)"; }
+
+WPBR_API wpbr_status wpbr_create(int device, wpbr_ctx** out) {
+  if (!out) return WPBR_ERR_INVALID_ARG;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return WPBR_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return WPBR_ERR_INVALID_ARG;
+  wpbr_ctx* ctx = new (std::nothrow) wpbr_ctx();
+  if (!ctx) return WPBR_ERR_OOM;
+  ctx->device = device;
+  e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = ctx->d_err.ensure(1);
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_err.p, 0, 4);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return e == cudaErrorMemoryAllocation ? WPBR_ERR_OOM : WPBR_ERR_CUDA;
+  }
+  ctx->own_stream = true;
+  *out = ctx;
+  return WPBR_OK;
+}
+
+WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->rs.graph) cudaGraphExecDestroy(ctx->rs.graph);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  // DevBuf members free their memory through cudaFree in release(); collect them
+  ctx->d_err.release();
+  ctx->sph_o2w.release(); ctx->sph_w2o.release(); ctx->sph_r.release(); ctx->pos.release();
+  ctx->nrm.release(); ctx->tan.release(); ctx->uv.release(); ctx->sph_mat.release(); ctx->idx.release();
+  ctx->tri_mat.release(); ctx->tri_flags.release(); ctx->mats.release(); ctx->lights.release();
+  ctx->env_rgb.release(); ctx->cond_func.release(); ctx->cond_cdf.release(); ctx->cond_int.release();
+  ctx->marg_func.release(); ctx->marg_cdf.release(); ctx->marg_int.release(); ctx->env_lum.release();
+  BvhState& B = ctx->bvh;
+  B.pb_lo.release(); B.pb_hi.release(); B.centroid.release(); B.codes.release(); B.cb_enc.release();
+  B.k0.release(); B.k1.release(); B.v0.release(); B.v1.release(); B.hist.release(); B.scan_tmp.release();
+  B.flags.release(); B.tid.release(); B.tstart.release(); B.tsize.release(); B.troot.release();
+  B.rng_lo.release(); B.rng_hi.release(); B.child0.release(); B.child1.release(); B.parent.release();
+  B.visits.release(); B.size.release(); B.nb_lo.release(); B.nb_hi.release();
+  B.cur.release(); B.nxt.release(); B.pos_seg.release(); B.bucket.release(); B.fl.release(); B.tr.release();
+  B.fscan.release(); B.tscan.release(); B.posF.release(); B.posT.release();
+  B.seg_a.release(); B.seg_b.release(); B.seg_start.release(); B.seg_end.release(); B.seg_node.release();
+  B.seg_k.release(); B.seg_mid.release(); B.seg_dim.release(); B.seg_benc.release(); B.seg_cenc.release();
+  B.seg_bucket_cnt.release(); B.seg_bucket_enc.release(); B.small_start.release(); B.small_end.release();
+  B.small_node.release(); B.counters.release(); B.sah_axis.release(); B.lin_node.release();
+  B.lin_bounds.release(); B.is_int.release(); B.int_index.release(); B.depth_max.release();
+  B.nodes2.release(); B.prims.release();
+  RenderState& R = ctx->rs;
+  R.acc.release(); R.hit_prim.release(); R.shadow_rays.release(); R.shadow_hit.release(); R.pstate.release();
+  R.Lbuf.release(); R.pfilm.release(); R.pass_dev.release();
+  ctx->io_rays.release(); ctx->io_hits.release(); ctx->io_stats.release();
+  for (auto& f : R.f) f.release();
+  for (auto& u : R.u) u.release();
+  delete ctx;
+}
+
+WPBR_API const char* wpbr_last_error(const wpbr_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+WPBR_API wpbr_status wpbr_set_stream(wpbr_ctx* ctx, void* stream) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  if (ctx->own_stream && ctx->stream) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+  }
+  ctx->stream = (cudaStream_t)stream;
+  ctx->own_stream = false;
+  if (ctx->rs.graph) {
+    cudaGraphExecDestroy(ctx->rs.graph);
+    ctx->rs.graph = nullptr;
+  }
+  ctx->rs.graph_ok = false;
+  return WPBR_OK;
+}
+
+WPBR_API void* wpbr_get_stream(const wpbr_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+WPBR_API wpbr_status wpbr_set_quirks(wpbr_ctx* ctx, uint32_t quirks) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  if (quirks & ~0x1Fu) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_quirks: unknown bits");
+  uint32_t changed = ctx->quirks ^ quirks;
+  ctx->quirks = quirks;
+  // the sort order changes the tree; the index bug changes the env distribution
+  if (changed & WPBR_Q_FULL_MORTON_SORT) ctx->bvh.built = false;
+  if ((changed & WPBR_Q_ENV_DISTRIB_INDEX_BUG) && ctx->has_scene && ctx->has_env) {
+    wpbr_status s = env_preprocess(ctx);
+    if (s != WPBR_OK) return s;
+  }
+  ctx->rs.graph_ok = false;
+  if (ctx->rs.graph) {
+    cudaGraphExecDestroy(ctx->rs.graph);
+    ctx->rs.graph = nullptr;
+  }
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_synchronize(wpbr_ctx* ctx) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "synchronize");
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_check_device_errors(wpbr_ctx* ctx) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  uint32_t v = 0;
+  WPBR_CUDA(cudaMemcpyAsync(&v, ctx->d_err.p, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  WPBR_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (v) {
+    WPBR_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, 4, ctx->stream));
+    WPBR_CUDA(cudaStreamSynchronize(ctx->stream));
+    char buf[96];
+    snprintf(buf, sizeof(buf), "device error word 0x%x (1 stack overflow, 2 loop limit, 4 build)", v);
+    return set_err(ctx, WPBR_ERR_TRAVERSAL_LIMIT, buf);
+  }
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_scene_upload(wpbr_ctx* ctx, const wpbr_scene_desc* d) {
+  if (!ctx || !d) return WPBR_ERR_INVALID_ARG;
+  // validation (the reference asserts or crashes on these)
+  if (d->n_triangles && (!d->indices || !d->positions))
+    return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: triangles without indices/positions");
+  if (d->n_spheres && !d->spheres) return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: spheres pointer is null");
+  for (uint64_t i = 0; i < 3ull * d->n_triangles; ++i)
+    if (d->indices[i] >= d->n_vertices) return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: vertex index out of range");
+  for (uint32_t i = 0; i < d->n_spheres; ++i)
+    if (d->spheres[i].material >= d->n_materials || !(d->spheres[i].radius > 0.0f))
+      return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: sphere material or radius invalid");
+  std::vector<uint32_t> tmat(d->n_triangles, 0xFFFFFFFFu), tfl(d->n_triangles, 0);
+  for (uint32_t m = 0; m < d->n_meshes; ++m) {
+    const wpbr_mesh& ms = d->meshes[m];
+    if ((uint64_t)ms.tri_begin + ms.tri_count > d->n_triangles || ms.material >= d->n_materials)
+      return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: mesh range or material invalid");
+    uint32_t fl = ms.flags;
+    if (!d->normals || !d->tangents) fl &= ~(uint32_t)WPBR_MESH_NORMALS_TANGENTS;
+    if (!d->uvs) fl &= ~(uint32_t)WPBR_MESH_UVS;
+    for (uint32_t t = ms.tri_begin; t < ms.tri_begin + ms.tri_count; ++t) {
+      tmat[t] = ms.material;
+      tfl[t] = fl;
+    }
+  }
+  for (uint32_t t = 0; t < d->n_triangles; ++t)
+    if (tmat[t] == 0xFFFFFFFFu) return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: triangle not covered by a mesh");
+  int n_env = 0;
+  for (uint32_t i = 0; i < d->n_lights; ++i) {
+    if (d->lights[i].type == WPBR_LIGHT_SPHERE && d->lights[i].sphere_index >= d->n_spheres)
+      return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: sphere light index out of range");
+    if (d->lights[i].type == WPBR_LIGHT_ENV) ++n_env;
+    if (d->lights[i].type > WPBR_LIGHT_ENV) return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: unknown light type");
+  }
+  if (n_env > 0 && !d->envmap) return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: env light without envmap");
+  if (d->envmap && (d->envmap->width < 2 || d->envmap->height < 2 || !d->envmap->rgb))
+    return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: envmap must be at least 2x2");
+  if (d->camera.res_x == 0 || d->camera.res_y == 0)
+    return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: camera resolution is zero");
+  if (d->n_spheres + (uint64_t)d->n_triangles >= (1ull << 29))
+    return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: more than 2^29 primitives");
+
+  cudaStream_t st = ctx->stream;
+  ctx->has_scene = false;
+  ctx->bvh.built = false;
+  ctx->rs.ready = false;
+  ctx->ns = d->n_spheres;
+  ctx->nt = d->n_triangles;
+  ctx->nv = d->n_vertices;
+  ctx->N = ctx->ns + ctx->nt;
+  std::vector<Xf> o2w(ctx->ns), w2o(ctx->ns);
+  std::vector<float> rad(ctx->ns);
+  std::vector<uint32_t> smat(ctx->ns);
+  for (uint32_t i = 0; i < ctx->ns; ++i) {
+    o2w[i] = xf_from(d->spheres[i].object_to_world);
+    w2o[i] = xf_from(d->spheres[i].world_to_object);
+    rad[i] = d->spheres[i].radius;
+    smat[i] = d->spheres[i].material;
+  }
+  WPBR_CUDA(upload(ctx->sph_o2w, o2w.data(), ctx->ns, st));
+  WPBR_CUDA(upload(ctx->sph_w2o, w2o.data(), ctx->ns, st));
+  WPBR_CUDA(upload(ctx->sph_r, rad.data(), ctx->ns, st));
+  WPBR_CUDA(upload(ctx->sph_mat, smat.data(), ctx->ns, st));
+  WPBR_CUDA(upload(ctx->pos, d->positions, 3ull * ctx->nv, st));
+  ctx->has_nrm = d->normals && d->tangents;
+  ctx->has_uv = d->uvs != nullptr;
+  if (ctx->has_nrm) {
+    WPBR_CUDA(upload(ctx->nrm, d->normals, 3ull * ctx->nv, st));
+    WPBR_CUDA(upload(ctx->tan, d->tangents, 3ull * ctx->nv, st));
+  }
+  if (ctx->has_uv) WPBR_CUDA(upload(ctx->uv, d->uvs, 2ull * ctx->nv, st));
+  WPBR_CUDA(upload(ctx->idx, d->indices, 3ull * ctx->nt, st));
+  WPBR_CUDA(upload(ctx->tri_mat, tmat.data(), ctx->nt, st));
+  WPBR_CUDA(upload(ctx->tri_flags, tfl.data(), ctx->nt, st));
+  WPBR_CUDA(upload(ctx->mats, d->materials, d->n_materials, st));
+  ctx->nmat = d->n_materials;
+  ctx->h_lights.assign(d->lights, d->lights + d->n_lights);
+  WPBR_CUDA(upload(ctx->lights, d->lights, d->n_lights, st));
+  ctx->has_env = d->envmap != nullptr;
+  if (ctx->has_env) {
+    const wpbr_envmap& e = *d->envmap;
+    ctx->envW = (int)e.width;
+    ctx->envH = (int)e.height;
+    size_t n = (size_t)e.width * e.height;
+    std::vector<float4> rgb(n);
+    for (size_t i = 0; i < n; ++i) rgb[i] = make_float4(e.rgb[3 * i], e.rgb[3 * i + 1], e.rgb[3 * i + 2], 0.0f);
+    WPBR_CUDA(upload(ctx->env_rgb, rgb.data(), n, st));
+    WPBR_CUDA(ctx->cond_func.ensure(n));
+    WPBR_CUDA(ctx->cond_cdf.ensure((size_t)e.height * (e.width + 1)));
+    WPBR_CUDA(ctx->cond_int.ensure(e.height));
+    WPBR_CUDA(ctx->marg_func.ensure(e.height));
+    WPBR_CUDA(ctx->marg_cdf.ensure(e.height + 1));
+    WPBR_CUDA(ctx->marg_int.ensure(1));
+    ctx->env_l2w = xf_from(e.light_to_world);
+    ctx->env_w2l = xf_from(e.world_to_light);
+    ctx->env_le = RGB3{1.0f, 1.0f, 1.0f};
+    for (uint32_t i = 0; i < d->n_lights; ++i)
+      if (d->lights[i].type == WPBR_LIGHT_ENV) ctx->env_le = RGB3{d->lights[i].Le[0], d->lights[i].Le[1], d->lights[i].Le[2]};
+  }
+  ctx->cam = camera_setup(d->camera);
+  WPBR_CUDA(cudaStreamSynchronize(st));
+  ctx->has_scene = true;
+  wpbr_status s = env_preprocess(ctx);
+  if (s != WPBR_OK) return s;
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_camera_info(wpbr_ctx* ctx, float* raster_camera, float* dx, float* dy) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  if (!ctx->has_scene) return set_err(ctx, WPBR_ERR_NOT_BUILT, "camera_info: no scene");
+  if (raster_camera)
+    for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < 4; ++j) raster_camera[4 * i + j] = ctx->cam.raster_camera.m[i][j];
+  if (dx) { dx[0] = ctx->cam.dx.x; dx[1] = ctx->cam.dx.y; dx[2] = ctx->cam.dx.z; }
+  if (dy) { dy[0] = ctx->cam.dy.x; dy[1] = ctx->cam.dy.y; dy[2] = ctx->cam.dy.z; }
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_camera_setup(const wpbr_camera* camera, float* raster_camera, float* dx, float* dy) {
+  if (!camera || !raster_camera || !dx || !dy) return WPBR_ERR_INVALID_ARG;
+  CameraParams c = camera_setup(*camera);
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) raster_camera[4 * i + j] = c.raster_camera.m[i][j];
+  dx[0] = c.dx.x; dx[1] = c.dx.y; dx[2] = c.dx.z;
+  dy[0] = c.dy.x; dy[1] = c.dy.y; dy[2] = c.dy.z;
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_env_distribution(wpbr_ctx* ctx, float* cond_cdf, float* cond_int, float* marg_cdf,
+                                           float* marg_int) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  if (!ctx->has_env) return set_err(ctx, WPBR_ERR_NOT_BUILT, "env_distribution: no environment light");
+  cudaStream_t st = ctx->stream;
+  size_t W = ctx->envW, H = ctx->envH;
+  if (cond_cdf) WPBR_CUDA(cudaMemcpyAsync(cond_cdf, ctx->cond_cdf.p, sizeof(float) * H * (W + 1), cudaMemcpyDeviceToHost, st));
+  if (cond_int) WPBR_CUDA(cudaMemcpyAsync(cond_int, ctx->cond_int.p, sizeof(float) * H, cudaMemcpyDeviceToHost, st));
+  if (marg_cdf) WPBR_CUDA(cudaMemcpyAsync(marg_cdf, ctx->marg_cdf.p, sizeof(float) * (H + 1), cudaMemcpyDeviceToHost, st));
+  if (marg_int) WPBR_CUDA(cudaMemcpyAsync(marg_int, ctx->marg_int.p, sizeof(float), cudaMemcpyDeviceToHost, st));
+  WPBR_CUDA(cudaStreamSynchronize(st));
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_bvh_build(wpbr_ctx* ctx) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  return bvh_build(ctx);
+}
+
+WPBR_API wpbr_status wpbr_bvh_info(wpbr_ctx* ctx, uint32_t* out4) {
+  if (!ctx || !out4) return WPBR_ERR_INVALID_ARG;
+  if (!ctx->bvh.built) return set_err(ctx, WPBR_ERR_NOT_BUILT, "bvh_info: BVH not built");
+  out4[0] = ctx->bvh.N;
+  out4[1] = ctx->bvh.M;
+  out4[2] = ctx->bvh.T;
+  out4[3] = ctx->bvh.max_depth;
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_bvh_export(wpbr_ctx* ctx, float* prim_bounds, float* centroids, float* cbounds,
+                                     uint32_t* codes, uint32_t* sorted_codes, uint32_t* sorted_prims,
+                                     uint32_t* treelet_start, uint32_t* nodes, float* node_bounds, uint32_t* shapes) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  BvhState& B = ctx->bvh;
+  if (!B.built) return set_err(ctx, WPBR_ERR_NOT_BUILT, "bvh_export: BVH not built");
+  cudaStream_t st = ctx->stream;
+  size_t N = B.N;
+  if (N == 0) return WPBR_OK;
+  std::vector<float4> lo, hi, ce;
+  if (prim_bounds) {
+    lo.resize(N);
+    hi.resize(N);
+    WPBR_CUDA(cudaMemcpyAsync(lo.data(), B.pb_lo.p, 16 * N, cudaMemcpyDeviceToHost, st));
+    WPBR_CUDA(cudaMemcpyAsync(hi.data(), B.pb_hi.p, 16 * N, cudaMemcpyDeviceToHost, st));
+  }
+  if (centroids) {
+    ce.resize(N);
+    WPBR_CUDA(cudaMemcpyAsync(ce.data(), B.centroid.p, 16 * N, cudaMemcpyDeviceToHost, st));
+  }
+  uint32_t cb[6];
+  if (cbounds) WPBR_CUDA(cudaMemcpyAsync(cb, B.cb_enc.p, 24, cudaMemcpyDeviceToHost, st));
+  if (codes) WPBR_CUDA(cudaMemcpyAsync(codes, B.codes.p, 4 * N, cudaMemcpyDeviceToHost, st));
+  if (sorted_codes) WPBR_CUDA(cudaMemcpyAsync(sorted_codes, B.skey, 4 * N, cudaMemcpyDeviceToHost, st));
+  if (sorted_prims) WPBR_CUDA(cudaMemcpyAsync(sorted_prims, B.sprim, 4 * N, cudaMemcpyDeviceToHost, st));
+  if (shapes) WPBR_CUDA(cudaMemcpyAsync(shapes, B.sprim, 4 * N, cudaMemcpyDeviceToHost, st));
+  if (treelet_start) WPBR_CUDA(cudaMemcpyAsync(treelet_start, B.tstart.p, 4 * (size_t)B.T, cudaMemcpyDeviceToHost, st));
+  if (nodes) WPBR_CUDA(cudaMemcpyAsync(nodes, B.lin_node.p, 12 * (size_t)B.M, cudaMemcpyDeviceToHost, st));
+  if (node_bounds) WPBR_CUDA(cudaMemcpyAsync(node_bounds, B.lin_bounds.p, 24 * (size_t)B.M, cudaMemcpyDeviceToHost, st));
+  WPBR_CUDA(cudaStreamSynchronize(st));
+  for (size_t i = 0; prim_bounds && i < N; ++i) {
+    float v[6] = {lo[i].x, lo[i].y, lo[i].z, hi[i].x, hi[i].y, hi[i].z};
+    memcpy(prim_bounds + 6 * i, v, sizeof(v));
+  }
+  for (size_t i = 0; centroids && i < N; ++i) {
+    centroids[3 * i] = ce[i].x;
+    centroids[3 * i + 1] = ce[i].y;
+    centroids[3 * i + 2] = ce[i].z;
+  }
+  if (cbounds)
+    for (int k = 0; k < 6; ++k) {
+      uint32_t u = cb[k];
+      uint32_t bits = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+      memcpy(&cbounds[k], &bits, 4);
+    }
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_collide_device(wpbr_ctx* ctx, const void* d_rays, uint64_t n, void* d_hits, uint32_t mode) {
+  if (!ctx || (n && (!d_rays || !d_hits)) || mode > WPBR_TRACE_ANY) return WPBR_ERR_INVALID_ARG;
+  return trace_rays(ctx, (const float4*)d_rays, n, (float4*)d_hits, mode, nullptr);
+}
+
+static wpbr_status collide_host(wpbr_ctx* ctx, const float* rays, uint64_t n, float* hits, uint32_t* stats,
+                                uint32_t mode) {
+  if (!ctx || (n && (!rays || !hits)) || mode > WPBR_TRACE_ANY) return WPBR_ERR_INVALID_ARG;
+  if (n == 0) return WPBR_OK;
+  // grow-only staging buffers owned by the context (no allocation per call)
+  cudaStream_t st = ctx->stream;
+  WPBR_CUDA(ctx->io_rays.ensure(2 * n));
+  WPBR_CUDA(ctx->io_hits.ensure(n));
+  if (stats) WPBR_CUDA(ctx->io_stats.ensure(2 * n));
+  WPBR_CUDA(cudaMemcpyAsync(ctx->io_rays.p, rays, 32 * n, cudaMemcpyHostToDevice, st));
+  wpbr_status s = trace_rays(ctx, ctx->io_rays.p, n, ctx->io_hits.p, mode, stats ? ctx->io_stats.p : nullptr);
+  if (s != WPBR_OK) return s;
+  WPBR_CUDA(cudaMemcpyAsync(hits, ctx->io_hits.p, 16 * n, cudaMemcpyDeviceToHost, st));
+  if (stats) WPBR_CUDA(cudaMemcpyAsync(stats, ctx->io_stats.p, 8 * n, cudaMemcpyDeviceToHost, st));
+  WPBR_CUDA(cudaStreamSynchronize(st));
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_collide(wpbr_ctx* ctx, const float* rays, uint64_t n, float* hits, uint32_t mode) {
+  return collide_host(ctx, rays, n, hits, nullptr, mode);
+}
+
+WPBR_API wpbr_status wpbr_collide_stats(wpbr_ctx* ctx, const float* rays, uint64_t n, float* hits, uint32_t* stats,
+                                        uint32_t mode) {
+  if (!stats) return WPBR_ERR_INVALID_ARG;
+  return collide_host(ctx, rays, n, hits, stats, mode);
+}
+
+WPBR_API wpbr_status wpbr_render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t stream) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  return render_setup(ctx, spp, seed, stream);
+}
+
+WPBR_API wpbr_status wpbr_render_pass(wpbr_ctx* ctx, uint32_t pass) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  return render_pass_fused(ctx, pass);
+}
+
+WPBR_API wpbr_status wpbr_render(wpbr_ctx* ctx) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  if (!ctx->rs.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render: render_setup not called");
+  for (uint32_t p = 0; p < ctx->rs.spp; ++p) {
+    wpbr_status s = render_pass_fused(ctx, p);
+    if (s != WPBR_OK) return s;
+  }
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_film_read(wpbr_ctx* ctx, float* acc_L, float* acc_w) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  RenderState& R = ctx->rs;
+  if (!R.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "film_read: render_setup not called");
+  size_t n = (size_t)R.W * R.H;
+  std::vector<float> a(n * 4);
+  WPBR_CUDA(cudaMemcpyAsync(a.data(), R.acc.p, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost, ctx->stream));
+  WPBR_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (size_t i = 0; i < n; ++i) {
+    if (acc_L) {
+      acc_L[3 * i] = a[4 * i];
+      acc_L[3 * i + 1] = a[4 * i + 1];
+      acc_L[3 * i + 2] = a[4 * i + 2];
+    }
+    if (acc_w) acc_w[i] = a[4 * i + 3];
+  }
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_film_tonemap(wpbr_ctx* ctx, uint8_t* rgb8) {
+  if (!ctx || !rgb8) return WPBR_ERR_INVALID_ARG;
+  return film_tonemap(ctx, rgb8);
+}
+
+WPBR_API wpbr_status wpbr_job_run(wpbr_ctx* ctx, uint32_t job, uint32_t pass) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  return job_run(ctx, job, pass);
+}
+
+WPBR_API wpbr_status wpbr_job_record(wpbr_ctx* ctx, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,
+                                     wpbr_pass_record* rec) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  return job_record(ctx, x0, y0, x1, y1, rec);
+}
+
+}  // extern "C"

@@ -1,0 +1,146 @@
+// ctx.hpp — the per-GPU context behind the C ABI (wpbr_ctx) and its device
+// buffers. Host code only.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "camera.cuh"
+#include "views.cuh"
+#include "wpbr_gpu.h"
+
+namespace wpbr {
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t ensure(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    size_t bytes = (count ? count : 1) * sizeof(T);
+    cudaError_t e = cudaMalloc((void**)&p, bytes);
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+// Build products and scratch of the LBVH build (bvh_build.cu).
+struct BvhState {
+  bool built = false;
+  uint32_t N = 0, T = 0, M = 0, n_int = 0, max_depth = 0;
+  // per primitive (input order)
+  DevBuf<float4> pb_lo, pb_hi, centroid;
+  DevBuf<uint32_t> codes;
+  DevBuf<uint32_t> cb_enc;  // 6 encoded centroid-bound words
+  // sort
+  DevBuf<uint32_t> k0, k1, v0, v1, hist, scan_tmp;
+  uint32_t* skey = nullptr;   // sorted codes (points into k0/k1)
+  uint32_t* sprim = nullptr;  // sorted primitive ids
+  // treelets / Karras
+  DevBuf<uint32_t> flags, tid, tstart, tsize, troot;
+  DevBuf<uint32_t> rng_lo, rng_hi, child0, child1;  // unified-id arrays
+  DevBuf<uint32_t> parent, visits, size;            // size 2N+T
+  DevBuf<float4> nb_lo, nb_hi;                      // node bounds, unified ids
+  // SAH
+  DevBuf<uint32_t> cur, nxt, pos_seg, bucket, fl, tr, fscan, tscan, posF, posT;
+  DevBuf<uint32_t> seg_a, seg_b, seg_start, seg_end, seg_node, seg_k, seg_mid, seg_dim;
+  DevBuf<uint32_t> seg_benc, seg_cenc, seg_bucket_cnt, seg_bucket_enc;
+  DevBuf<uint32_t> small_start, small_end, small_node, counters;
+  DevBuf<uint32_t> sah_axis;
+  // flattened tree (CSceneTreeLBVH) + traversal layout
+  DevBuf<uint32_t> lin_node;  // M*3: offset, n_shapes, axis
+  DevBuf<float> lin_bounds;   // M*6
+  DevBuf<uint32_t> is_int, int_index, depth_max;
+  DevBuf<Node2> nodes2;
+  DevBuf<float4> prims;
+  BvhView view{};
+};
+
+struct RenderState {
+  bool ready = false;
+  uint32_t spp = 0, seed = 0, stream = 0;
+  uint32_t W = 0, H = 0;
+  DevBuf<float> acc;  // W*H*4 (L rgb, weight)
+  // fused-path per-pixel state
+  DevBuf<uint32_t> hit_prim;
+  DevBuf<float4> shadow_rays;   // 2 rays (2 float4 each) per pixel
+  DevBuf<uint32_t> shadow_hit;  // 2 per pixel
+  DevBuf<float4> pstate;        // compact shading state, kStateF4 per pixel
+  DevBuf<float4> Lbuf;          // per pixel L (xyz) + pFilm packed in w? separate:
+  DevBuf<float2> pfilm;
+  // staged-path (job-by-job) state: one slot per wpbr_pass_record field
+  DevBuf<float> f[32];
+  DevBuf<uint32_t> u[8];
+  bool graph_ok = false;
+  cudaGraphExec_t graph = nullptr;
+  uint32_t graph_pass = 0xFFFFFFFFu;
+  DevBuf<uint32_t> pass_dev;  // pass index read by the captured kernels
+};
+
+}  // namespace wpbr
+
+struct wpbr_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  uint32_t quirks = 0;
+  wpbr::DevBuf<uint32_t> d_err;
+  // scene
+  bool has_scene = false;
+  uint32_t ns = 0, nt = 0, nv = 0, N = 0;
+  wpbr::DevBuf<wpbr::Xf> sph_o2w, sph_w2o;
+  wpbr::DevBuf<float> sph_r, pos, nrm, tan, uv;
+  wpbr::DevBuf<uint32_t> sph_mat, idx, tri_mat, tri_flags;
+  bool has_nrm = false, has_uv = false;
+  wpbr::DevBuf<wpbr_material> mats;
+  uint32_t nmat = 0;
+  wpbr::DevBuf<wpbr_light> lights;
+  std::vector<wpbr_light> h_lights;
+  bool has_env = false;
+  int envW = 0, envH = 0;
+  wpbr::DevBuf<float4> env_rgb;
+  wpbr::DevBuf<float> cond_func, cond_cdf, cond_int, marg_func, marg_cdf, marg_int, env_lum;
+  wpbr::Xf env_l2w, env_w2l;
+  wpbr::RGB3 env_le{1, 1, 1};
+  float env_marg_int = 0.0f;
+  wpbr::CameraParams cam{};
+  wpbr::BvhState bvh;
+  wpbr::RenderState rs;
+  // staging for the host-buffer collide entry points
+  wpbr::DevBuf<float4> io_rays, io_hits;
+  wpbr::DevBuf<uint32_t> io_stats;
+};
+
+namespace wpbr {
+wpbr_status set_err(wpbr_ctx* ctx, wpbr_status st, const std::string& msg);
+wpbr_status cuda_err(wpbr_ctx* ctx, cudaError_t e, const char* what);
+SceneView scene_view(const wpbr_ctx* ctx);
+wpbr_status bvh_build(wpbr_ctx* ctx);
+wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* d_hits, uint32_t mode,
+                       uint32_t* d_stats);
+wpbr_status env_preprocess(wpbr_ctx* ctx);
+wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t stream);
+wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass);
+wpbr_status job_run(wpbr_ctx* ctx, uint32_t job, uint32_t pass);
+wpbr_status job_record(wpbr_ctx* ctx, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1, wpbr_pass_record* rec);
+wpbr_status film_tonemap(wpbr_ctx* ctx, uint8_t* out);
+// scan helper (exclusive, in place allowed): out[i] = sum in[0..i); returns total in *total_dev (device, may be null)
+cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, DevBuf<uint32_t>& tmp, cudaStream_t s);
+}  // namespace wpbr
+
+#define WPBR_CUDA(call)                                          \
+  do {                                                           \
+    cudaError_t e_ = (call);                                     \
+    if (e_ != cudaSuccess) return wpbr::cuda_err(ctx, e_, #call); \
+  } while (0)

@@ -1,0 +1,769 @@
+// render.cu — the per-sample job list of MEngine::render
+// (WoodenPBREngine/MEngine.cpp:380-448) as wavefront kernels.
+//
+// Two forms share the same device functions:
+//  * the staged path (wpbr_job_run): one kernel per reference job group over
+//    per-pixel state buffers, each recordable for stage-by-stage parity;
+//  * the fused path (wpbr_render_pass): camera+primary traversal, shading +
+//    sample generation (spawn), one traversal launch for both shadow rays,
+//    MIS finish, film gather — five kernels per sample pass, captured once as
+//    a CUDA graph that reads the pass index from device memory.
+#include <cstring>
+
+#include "common.cuh"
+#include "ctx.hpp"
+#include "shade.cuh"
+#include "traverse.cuh"
+#include "wpbr_sampling.h"
+
+namespace wpbr {
+
+namespace {
+
+constexpr int kTB = 128;
+
+// Staged-path field slots (float and uint buffers in RenderState).
+enum FF {
+  F_PFILM, F_RAY_O, F_RAY_D, F_RAY_DX, F_RAY_DY, F_HIT_T, F_SI_P, F_SI_N, F_SI_WO, F_SI_SN, F_SI_SDPDU, F_SI_DPDU,
+  F_SI_DPDV, F_SI_DNDU, F_SI_DNDV, F_FRAME, F_LE, F_L_WI, F_L_LI, F_L_PDF, F_L_F, F_L_FPDF, F_B_WI, F_B_F, F_B_PDF,
+  F_B_LI, F_B_LPDF, F_L, F_COUNT
+};
+constexpr int kFW_h[F_COUNT] = {2, 3, 3, 3, 3, 1, 3, 3, 3, 3, 3, 3, 3, 3, 3, 9, 3, 3, 3, 1, 3, 1, 3, 3, 1, 3, 1, 3};
+__constant__ int kFW_d[F_COUNT] = {2, 3, 3, 3, 3, 1, 3, 3, 3, 3, 3, 3, 3, 3, 3, 9, 3, 3, 3, 1, 3, 1, 3, 3, 1, 3, 1, 3};
+#ifdef __CUDA_ARCH__
+#define kFW kFW_d
+#else
+#define kFW kFW_h
+#endif
+enum UF { U_HIT_PRIM, U_LIGHT_IDX, U_L_FLAGS, U_B_FLAGS, U_LOK, U_COUNT };
+
+struct Staged {
+  float* f[F_COUNT];
+  uint32_t* u[U_COUNT];
+};
+
+struct PassCtx {
+  SceneView S;
+  BvhView Bv;
+  wpbr_rng::Stream rs;
+  uint32_t W, H;
+  uint32_t* err;
+};
+
+__device__ __forceinline__ V3 ld3(const float* f, uint32_t i) { return V3{f[3 * i], f[3 * i + 1], f[3 * i + 2]}; }
+__device__ __forceinline__ void st3(float* f, uint32_t i, V3 v) {
+  f[3 * i] = v.x;
+  f[3 * i + 1] = v.y;
+  f[3 * i + 2] = v.z;
+}
+__device__ __forceinline__ RGB3 ldc(const float* f, uint32_t i) { return RGB3{f[3 * i], f[3 * i + 1], f[3 * i + 2]}; }
+__device__ __forceinline__ void stc(float* f, uint32_t i, RGB3 c) {
+  f[3 * i] = c.r;
+  f[3 * i + 1] = c.g;
+  f[3 * i + 2] = c.b;
+}
+
+__device__ __forceinline__ uint32_t prim_material(const SceneView& S, uint32_t prim) {
+  return prim < S.ns ? S.sph_mat[prim] : S.tri_mat[prim - S.ns];
+}
+
+// Full interaction for the winning primitive: re-runs its intersection test
+// (identical bits) and builds the surface interaction.
+__device__ SurfInt make_si(const SceneView& S, uint32_t prim, V3 o, V3 d) {
+  if (prim < S.ns) {
+    V3 rlo, rld, ph;
+    sphere_intersect(S.sph_w2o[prim], S.sph_r[prim], o, d, &rlo, &rld, &ph);
+    return sphere_si(S.sph_o2w[prim], S.sph_w2o[prim], S.sph_r[prim], rld, ph);
+  }
+  uint32_t t = prim - S.ns;
+  const uint32_t* ix = S.idx + 3 * (size_t)t;
+  TriData td;
+  uint32_t fl = S.tri_flags[t];
+  td.has_ns = (fl & WPBR_MESH_NORMALS_TANGENTS) != 0;
+  td.has_uv = (fl & WPBR_MESH_UVS) != 0;
+  for (int k = 0; k < 3; ++k) {
+    uint32_t v = ix[k];
+    td.p[k] = V3{S.pos[3 * v], S.pos[3 * v + 1], S.pos[3 * v + 2]};
+    td.n[k] = td.has_ns ? V3{S.nrm[3 * v], S.nrm[3 * v + 1], S.nrm[3 * v + 2]} : V3{0, 0, 0};
+    td.s[k] = td.has_ns ? V3{S.tan[3 * v], S.tan[3 * v + 1], S.tan[3 * v + 2]} : V3{0, 0, 0};
+    td.uv[k] = td.has_uv ? V2{S.uv[2 * v], S.uv[2 * v + 1]} : V2{0, 0};
+  }
+  float b0, b1, b2;
+  tri_intersect(td.p[0], td.p[1], td.p[2], o, d, S.quirks, &b0, &b1, &b2);
+  return triangle_si(td, d, b0, b1, b2);
+}
+
+__device__ __forceinline__ void pixel_xy(uint32_t pix, uint32_t W, uint32_t* x, uint32_t* y) {
+  *x = pix % W;
+  *y = pix / W;
+}
+
+// JobSamplerUpdateCameraSamples (CSSampler.cpp:7-23): pFilm = pixel + u2
+__device__ __forceinline__ void camera_sample(const PassCtx& P, uint32_t pix, uint32_t pass, float* fx, float* fy) {
+  uint32_t x, y;
+  pixel_xy(pix, P.W, &x, &y);
+  float u0, u1;
+  wpbr_rng::sample2d(P.rs, pix, pass, wpbr_rng::DIM_CAMERA, &u0, &u1);
+  *fx = (float)x + u0;
+  *fy = (float)y + u1;
+}
+
+// JobScatteringSampleLight (SScattering.cpp:82-88), index clamped
+__device__ __forceinline__ uint32_t pick_light(const PassCtx& P, uint32_t pix, uint32_t pass) {
+  uint32_t nl = P.S.nlights;
+  float ul = wpbr_rng::sample1d(P.rs, pix, pass, wpbr_rng::DIM_LIGHT_PICK);
+  float fl = (ul + 0.5f) * (float)(nl - 1);
+  uint32_t li = (uint32_t)fl;
+  return li > nl - 1 ? nl - 1 : li;
+}
+
+struct LightSample {
+  V3 wi;
+  RGB3 li;
+  float pdf;
+  bool ok;
+};
+__device__ LightSample sample_light(const PassCtx& P, const wpbr_light& lt, V3 p, uint32_t pix, uint32_t pass) {
+  float u0, u1;
+  wpbr_rng::sample2d(P.rs, pix, pass, wpbr_rng::DIM_LIGHT, &u0, &u1);
+  LightSample s;
+  s.wi = V3{0, 0, 0};
+  s.li = rgb1(0.0f);
+  s.pdf = 0.0f;
+  s.ok = true;
+  if (lt.type == WPBR_LIGHT_SPHERE) {
+    sphere_light_sample(P.S.sph_o2w[lt.sphere_index], P.S.sph_r[lt.sphere_index], p, u0, u1, &s.wi, &s.pdf);
+    s.li = RGB3{lt.Le[0], lt.Le[1], lt.Le[2]};
+  } else {
+    env_li_sample(P.S.env, P.S.quirks, u0, u1, &s.wi, &s.li, &s.pdf, &s.ok);
+  }
+  return s;
+}
+
+__device__ void light_compute(const PassCtx& P, const wpbr_light& lt, V3 p, V3 wi, RGB3* li, float* pdf) {
+  if (lt.type == WPBR_LIGHT_SPHERE) {
+    *pdf = sphere_light_pdf(P.S.sph_o2w[lt.sphere_index], P.S.sph_r[lt.sphere_index], p, P.S.quirks);
+    *li = RGB3{lt.Le[0], lt.Le[1], lt.Le[2]};
+  } else {
+    env_li_compute(P.S.env, wi, li, pdf);
+  }
+}
+
+__device__ __forceinline__ uint32_t light_prim(const wpbr_light& lt) {
+  return lt.type == WPBR_LIGHT_SPHERE ? lt.sphere_index : 0xFFFFFFFEu;
+}
+
+__device__ __forceinline__ uint32_t trace_closest(const PassCtx& P, V3 o, V3 d) {
+  HitRec h = P.Bv.max_depth < 60 ? trace_ray<false, 64>(P.S, P.Bv, o, d, inf_(), nullptr, nullptr, P.err)
+                                 : trace_ray<false, 256>(P.S, P.Bv, o, d, inf_(), nullptr, nullptr, P.err);
+  return h.prim;
+}
+
+// ============================== staged jobs =================================
+#define kNaN __int_as_float(0x7fc00000)
+
+__global__ void kj_camera(PassCtx P, uint32_t pass, Staged G) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H) return;
+  for (int f = 0; f < F_COUNT; ++f)
+    for (int c = 0; c < kFW[f]; ++c) G.f[f][(size_t)pix * kFW[f] + c] = kNaN;
+  for (int u = 0; u < U_COUNT; ++u) G.u[u][pix] = 0xFFFFFFFFu;
+  float fx, fy;
+  camera_sample(P, pix, pass, &fx, &fy);
+  RayD r = camera_ray(P.S.cam, fx, fy);
+  G.f[F_PFILM][2 * pix] = fx;
+  G.f[F_PFILM][2 * pix + 1] = fy;
+  st3(G.f[F_RAY_O], pix, r.o);
+  st3(G.f[F_RAY_D], pix, r.d);
+  st3(G.f[F_RAY_DX], pix, r.dxd);
+  st3(G.f[F_RAY_DY], pix, r.dyd);
+  stc(G.f[F_L], pix, rgb1(0.0f));
+}
+
+__global__ void kj_collide(PassCtx P, Staged G) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H) return;
+  V3 o = ld3(G.f[F_RAY_O], pix), d = ld3(G.f[F_RAY_D], pix);
+  HitRec h = P.Bv.max_depth < 60 ? trace_ray<false, 64>(P.S, P.Bv, o, d, inf_(), nullptr, nullptr, P.err)
+                                 : trace_ray<false, 256>(P.S, P.Bv, o, d, inf_(), nullptr, nullptr, P.err);
+  G.u[U_HIT_PRIM][pix] = h.prim;
+  G.f[F_HIT_T][pix] = h.t;
+  if (h.prim == kNoHit) return;
+  SurfInt s = make_si(P.S, h.prim, o, d);
+  st3(G.f[F_SI_P], pix, s.p);
+  st3(G.f[F_SI_N], pix, s.n);
+  st3(G.f[F_SI_WO], pix, s.wo);
+  st3(G.f[F_SI_SN], pix, s.sn);
+  st3(G.f[F_SI_SDPDU], pix, s.sdpdu);
+  st3(G.f[F_SI_DPDU], pix, s.dpdu);
+  st3(G.f[F_SI_DPDV], pix, s.dpdv);
+  st3(G.f[F_SI_DNDU], pix, s.dndu);
+  st3(G.f[F_SI_DNDV], pix, s.dndv);
+}
+
+__global__ void kj_emitted(PassCtx P, Staged G) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H) return;
+  if (G.u[U_HIT_PRIM][pix] != kNoHit || !P.S.has_env) return;
+  RGB3 le = env_le(P.S.env, ld3(G.f[F_RAY_D], pix));
+  stc(G.f[F_LE], pix, le);
+  stc(G.f[F_L], pix, radd(ldc(G.f[F_L], pix), le));
+}
+
+__device__ __forceinline__ Frame load_frame(const float* f, uint32_t pix) {
+  const float* q = f + 9 * (size_t)pix;
+  return Frame{V3{q[0], q[1], q[2]}, V3{q[3], q[4], q[5]}, V3{q[6], q[7], q[8]}};
+}
+
+__global__ void kj_bsdf_setup(PassCtx P, Staged G) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H || G.u[U_HIT_PRIM][pix] == kNoHit) return;
+  SurfInt s;
+  s.sdpdu = ld3(G.f[F_SI_SDPDU], pix);
+  s.sn = ld3(G.f[F_SI_SN], pix);
+  Frame fr = bsdf_frame(s);
+  float* q = G.f[F_FRAME] + 9 * (size_t)pix;
+  q[0] = fr.ss.x; q[1] = fr.ss.y; q[2] = fr.ss.z;
+  q[3] = fr.ts.x; q[4] = fr.ts.y; q[5] = fr.ts.z;
+  q[6] = fr.ns.x; q[7] = fr.ns.y; q[8] = fr.ns.z;
+}
+
+__global__ void kj_sample_light(PassCtx P, uint32_t pass, Staged G) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H || G.u[U_HIT_PRIM][pix] == kNoHit || P.S.nlights == 0) return;
+  uint32_t li = pick_light(P, pix, pass);
+  G.u[U_LIGHT_IDX][pix] = li;
+  LightSample ls = sample_light(P, P.S.lights[li], ld3(G.f[F_SI_P], pix), pix, pass);
+  st3(G.f[F_L_WI], pix, ls.wi);
+  stc(G.f[F_L_LI], pix, ls.li);
+  G.f[F_L_PDF][pix] = ls.pdf;
+  G.u[U_LOK][pix] = ls.ok ? 1u : 0u;
+  G.u[U_L_FLAGS][pix] = 0u;
+}
+
+__global__ void kj_shadow_light(PassCtx P, Staged G) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H || G.u[U_HIT_PRIM][pix] == kNoHit || P.S.nlights == 0) return;
+  if (!G.u[U_LOK][pix] || rblack(ldc(G.f[F_L_LI], pix))) return;
+  V3 wi = ld3(G.f[F_L_WI], pix);
+  V3 o = add(ld3(G.f[F_SI_P], pix), mul(wi, (float)0.1));
+  uint32_t hp = trace_closest(P, o, wi);
+  uint32_t lp = light_prim(P.S.lights[G.u[U_LIGHT_IDX][pix]]);
+  G.u[U_L_FLAGS][pix] = 1u | ((hp == kNoHit || hp == lp) ? 2u : 0u);
+}
+
+__global__ void kj_bsdf_compute(PassCtx P, Staged G) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H || G.u[U_HIT_PRIM][pix] == kNoHit || P.S.nlights == 0) return;
+  if (!(G.u[U_L_FLAGS][pix] & 2u)) return;
+  Frame fr = load_frame(G.f[F_FRAME], pix);
+  const wpbr_material& m = P.S.mats[prim_material(P.S, G.u[U_HIT_PRIM][pix])];
+  float pdf;
+  RGB3 f = bsdf_eval(m, to_local(fr, ld3(G.f[F_SI_WO], pix)), to_local(fr, ld3(G.f[F_L_WI], pix)), &pdf);
+  stc(G.f[F_L_F], pix, f);
+  G.f[F_L_FPDF][pix] = pdf;
+}
+
+__global__ void kj_integrate_light(PassCtx P, Staged G) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H || G.u[U_HIT_PRIM][pix] == kNoHit || P.S.nlights == 0) return;
+  if (!(G.u[U_L_FLAGS][pix] & 2u)) return;
+  float bpdf = G.f[F_L_FPDF][pix];
+  if (bpdf == 0.0f) return;
+  float lpdf = G.f[F_L_PDF][pix];
+  float w = power_heuristic(lpdf, bpdf);
+  RGB3 c = rmuls(rmul(ldc(G.f[F_L_LI], pix), ldc(G.f[F_L_F], pix)), w / lpdf);
+  stc(G.f[F_L], pix, radd(ldc(G.f[F_L], pix), c));
+}
+
+__global__ void kj_sample_bsdf(PassCtx P, uint32_t pass, Staged G) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H || G.u[U_HIT_PRIM][pix] == kNoHit || P.S.nlights == 0) return;
+  Frame fr = load_frame(G.f[F_FRAME], pix);
+  const wpbr_material& m = P.S.mats[prim_material(P.S, G.u[U_HIT_PRIM][pix])];
+  float u0, u1;
+  wpbr_rng::sample2d(P.rs, pix, pass, wpbr_rng::DIM_BSDF, &u0, &u1);
+  V3 wi_l;
+  float pdf;
+  bool valid;
+  RGB3 f = bsdf_sample(m, to_local(fr, ld3(G.f[F_SI_WO], pix)), u0, u1, &wi_l, &pdf, &valid);
+  st3(G.f[F_B_WI], pix, to_world(fr, wi_l));
+  stc(G.f[F_B_F], pix, f);
+  G.f[F_B_PDF][pix] = pdf;
+  G.u[U_B_FLAGS][pix] = valid ? 1u : 0u;
+}
+
+__global__ void kj_shadow_bsdf(PassCtx P, Staged G) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H || G.u[U_HIT_PRIM][pix] == kNoHit || P.S.nlights == 0) return;
+  uint32_t fl = G.u[U_B_FLAGS][pix];
+  if (!(fl & 1u)) return;
+  V3 wi = ld3(G.f[F_B_WI], pix);
+  V3 o = add(ld3(G.f[F_SI_P], pix), mul(wi, (float)0.01));
+  uint32_t hp = trace_closest(P, o, wi);
+  uint32_t lp = light_prim(P.S.lights[G.u[U_LIGHT_IDX][pix]]);
+  G.u[U_B_FLAGS][pix] = fl | 2u | ((hp == kNoHit || hp == lp) ? 4u : 0u);
+}
+
+__global__ void kj_light_compute(PassCtx P, Staged G) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H || G.u[U_HIT_PRIM][pix] == kNoHit || P.S.nlights == 0) return;
+  if (!(G.u[U_B_FLAGS][pix] & 4u)) return;
+  RGB3 li;
+  float pdf;
+  light_compute(P, P.S.lights[G.u[U_LIGHT_IDX][pix]], ld3(G.f[F_SI_P], pix), ld3(G.f[F_B_WI], pix), &li, &pdf);
+  stc(G.f[F_B_LI], pix, li);
+  G.f[F_B_LPDF][pix] = pdf;
+}
+
+__global__ void kj_integrate_bsdf(PassCtx P, Staged G) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H || G.u[U_HIT_PRIM][pix] == kNoHit || P.S.nlights == 0) return;
+  if (!(G.u[U_B_FLAGS][pix] & 4u)) return;
+  RGB3 li = ldc(G.f[F_B_LI], pix);
+  if (rblack(li)) return;
+  float bpdf = G.f[F_B_PDF][pix];
+  float w = (bpdf == 1.0f) ? 1.0f : power_heuristic(bpdf, G.f[F_B_LPDF][pix]);
+  RGB3 c = rmuls(rmul(li, ldc(G.f[F_B_F], pix)), w / bpdf);
+  stc(G.f[F_L], pix, radd(ldc(G.f[F_L], pix), c));
+}
+
+// JobAccumalateLIFromSamples (CSFilm.cpp:70-122) as a gather: each pixel
+// sums, in the reference's row-major sample order, the Mitchell-weighted
+// samples of its 32x32 tile whose splat footprint covers it.
+__device__ void film_gather(uint32_t W, uint32_t H, uint32_t x, uint32_t y, const float2* pf, const float4* Lb,
+                            float4* acc) {
+  uint32_t tx0 = (x / 32) * 32, ty0 = (y / 32) * 32;
+  uint32_t tx1 = min(tx0 + 31, W - 1), ty1 = min(ty0 + 31, H - 1);
+  float4 a = acc[(size_t)y * W + x];
+  RGB3 L{a.x, a.y, a.z};
+  float ws = a.w;
+  int sy0 = max((int)ty0, (int)y - 2), sy1 = min((int)ty1, (int)y + 2);
+  int sx0 = max((int)tx0, (int)x - 2), sx1 = min((int)tx1, (int)x + 2);
+  for (int sy = sy0; sy <= sy1; ++sy)
+    for (int sx = sx0; sx <= sx1; ++sx) {
+      size_t sp = (size_t)sy * W + sx;
+      float2 f = pf[sp];
+      float dx0 = f.x - 0.5f, dy0 = f.y - 0.5f;
+      int pminx = (int)ceilf(dx0 - 2.0f), pmaxx = (int)floorf(dx0 + 2.0f);
+      int pminy = (int)ceilf(dy0 - 2.0f), pmaxy = (int)floorf(dy0 + 2.0f);
+      pminx = max(pminx, (int)tx0);
+      pminy = max(pminy, (int)ty0);
+      pmaxx = min(pmaxx, (int)tx1);
+      pmaxy = min(pmaxy, (int)ty1);
+      if ((int)x < pminx || (int)x > pmaxx || (int)y < pminy || (int)y > pmaxy) continue;
+      float w = mitchell1(((float)x - f.x) / 2.0f) * mitchell1(((float)y - f.y) / 2.0f);
+      float4 s = Lb[sp];
+      RGB3 c{s.x, s.y, s.z};
+      if (!rblack(c)) L = radd(L, rmuls(c, w));
+      ws = ws + w;
+    }
+  acc[(size_t)y * W + x] = make_float4(L.r, L.g, L.b, ws);
+}
+
+__global__ void kj_film_pack(PassCtx P, Staged G, float2* pf, float4* Lb) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H) return;
+  pf[pix] = make_float2(G.f[F_PFILM][2 * pix], G.f[F_PFILM][2 * pix + 1]);
+  RGB3 L = ldc(G.f[F_L], pix);
+  Lb[pix] = make_float4(L.r, L.g, L.b, 0.0f);
+}
+
+__global__ void k_film(uint32_t W, uint32_t H, const float2* pf, const float4* Lb, float4* acc) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= W * H) return;
+  film_gather(W, H, pix % W, pix / W, pf, Lb, acc);
+}
+
+// ============================== fused pass ==================================
+// Compact per-pixel state written by k_spawn and read by k_finish.
+constexpr int kStateF4 = 6;
+enum : uint32_t { SF_VALID = 1u, SF_TRACE_L = 2u, SF_TRACE_B = 4u, SF_HIT = 8u };
+
+__global__ void __launch_bounds__(kTB) k_primary(PassCtx P, const uint32_t* pass_dev, uint32_t* hit_prim) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H) return;
+  uint32_t pass = *pass_dev;
+  float fx, fy;
+  camera_sample(P, pix, pass, &fx, &fy);
+  RayD r = camera_ray(P.S.cam, fx, fy);
+  hit_prim[pix] = trace_closest(P, r.o, r.d);
+}
+
+__global__ void __launch_bounds__(kTB) k_spawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
+                                               float4* state, float4* rays, float4* Lb, float2* pf) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H) return;
+  uint32_t pass = *pass_dev;
+  float fx, fy;
+  camera_sample(P, pix, pass, &fx, &fy);
+  pf[pix] = make_float2(fx, fy);
+  RayD r = camera_ray(P.S.cam, fx, fy);
+  uint32_t prim = hit_prim[pix];
+  float4* st = state + (size_t)pix * kStateF4;
+  float4* ry = rays + (size_t)pix * 4;
+  const float4 off = make_float4(0.0f, 0.0f, 0.0f, -1.0f);  // tmax < 0: nothing to trace
+  RGB3 L = rgb1(0.0f);
+  uint32_t flags = 0;
+  if (prim == kNoHit || P.S.nlights == 0) {
+    if (prim == kNoHit && P.S.has_env) L = radd(L, env_le(P.S.env, r.d));
+    ry[0] = off; ry[1] = off; ry[2] = off; ry[3] = off;
+    st[4] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(flags));
+    Lb[pix] = make_float4(L.r, L.g, L.b, 0.0f);
+    return;
+  }
+  flags |= SF_HIT;
+  SurfInt s = make_si(P.S, prim, r.o, r.d);
+  Frame fr = bsdf_frame(s);
+  uint32_t mid = prim_material(P.S, prim);
+  const wpbr_material& m = P.S.mats[mid];
+  V3 wo_l = to_local(fr, s.wo);
+  uint32_t li_idx = pick_light(P, pix, pass);
+  const wpbr_light& lt = P.S.lights[li_idx];
+  LightSample ls = sample_light(P, lt, s.p, pix, pass);
+  if (ls.ok && !rblack(ls.li)) {
+    flags |= SF_TRACE_L;
+    V3 o = add(s.p, mul(ls.wi, (float)0.1));
+    ry[0] = make_float4(o.x, o.y, o.z, 0.0f);
+    ry[1] = make_float4(ls.wi.x, ls.wi.y, ls.wi.z, inf_());
+  } else {
+    ry[0] = off;
+    ry[1] = off;
+  }
+  float u0, u1;
+  wpbr_rng::sample2d(P.rs, pix, pass, wpbr_rng::DIM_BSDF, &u0, &u1);
+  V3 bwi_l;
+  float bpdf;
+  bool valid;
+  RGB3 bf = bsdf_sample(m, wo_l, u0, u1, &bwi_l, &bpdf, &valid);
+  V3 bwi = to_world(fr, bwi_l);
+  if (valid) {
+    flags |= SF_VALID | SF_TRACE_B;
+    V3 o = add(s.p, mul(bwi, (float)0.01));
+    ry[2] = make_float4(o.x, o.y, o.z, 0.0f);
+    ry[3] = make_float4(bwi.x, bwi.y, bwi.z, inf_());
+  } else {
+    ry[2] = off;
+    ry[3] = off;
+  }
+  V3 wi_l = to_local(fr, ls.wi);
+  st[0] = make_float4(ls.li.r, ls.li.g, ls.li.b, ls.pdf);
+  st[1] = make_float4(wi_l.x, wi_l.y, wi_l.z, __uint_as_float(li_idx));
+  st[2] = make_float4(wo_l.x, wo_l.y, wo_l.z, __uint_as_float(mid));
+  st[3] = make_float4(bf.r, bf.g, bf.b, bpdf);
+  st[4] = make_float4(bwi.x, bwi.y, bwi.z, __uint_as_float(flags));
+  st[5] = make_float4(s.p.x, s.p.y, s.p.z, 0.0f);
+  Lb[pix] = make_float4(L.r, L.g, L.b, 0.0f);
+}
+
+__global__ void __launch_bounds__(kTB) k_trace_shadow(PassCtx P, const float4* rays, uint32_t n, uint32_t* out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 o = rays[2 * i], d = rays[2 * i + 1];
+  if (!(d.w > 0.0f)) {
+    out[i] = kNoHit;
+    return;
+  }
+  out[i] = trace_closest(P, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z});
+}
+
+__global__ void __launch_bounds__(kTB) k_finish(PassCtx P, const float4* state, const uint32_t* shadow, float4* Lb) {
+  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= P.W * P.H) return;
+  const float4* st = state + (size_t)pix * kStateF4;
+  float4 s4 = st[4];
+  uint32_t flags = __float_as_uint(s4.w);
+  if (!(flags & SF_HIT)) return;
+  float4 s0 = st[0], s1 = st[1], s2 = st[2], s3 = st[3], s5 = st[5];
+  uint32_t li_idx = __float_as_uint(s1.w);
+  const wpbr_light& lt = P.S.lights[li_idx];
+  uint32_t lp = light_prim(lt);
+  const wpbr_material& m = P.S.mats[__float_as_uint(s2.w)];
+  float4 l4 = Lb[pix];
+  RGB3 L{l4.x, l4.y, l4.z};
+  if (flags & SF_TRACE_L) {
+    uint32_t hp = shadow[2 * pix];
+    if (hp == kNoHit || hp == lp) {
+      float bpdf;
+      RGB3 f = bsdf_eval(m, V3{s2.x, s2.y, s2.z}, V3{s1.x, s1.y, s1.z}, &bpdf);
+      if (bpdf != 0.0f) {
+        float lpdf = s0.w;
+        float w = power_heuristic(lpdf, bpdf);
+        L = radd(L, rmuls(rmul(RGB3{s0.x, s0.y, s0.z}, f), w / lpdf));
+      }
+    }
+  }
+  if (flags & SF_TRACE_B) {
+    uint32_t hp = shadow[2 * pix + 1];
+    if (hp == kNoHit || hp == lp) {
+      RGB3 li;
+      float lpdf;
+      light_compute(P, lt, V3{s5.x, s5.y, s5.z}, V3{s4.x, s4.y, s4.z}, &li, &lpdf);
+      if (!rblack(li)) {
+        float bpdf = s3.w;
+        float w = (bpdf == 1.0f) ? 1.0f : power_heuristic(bpdf, lpdf);
+        L = radd(L, rmuls(rmul(li, RGB3{s3.x, s3.y, s3.z}), w / bpdf));
+      }
+    }
+  }
+  Lb[pix] = make_float4(L.r, L.g, L.b, 0.0f);
+}
+
+// ============================== environment =================================
+// JobLightInfiniteAreaPreprocessSampling (CLightInfiniteArea.cpp:113-139)
+__global__ void k_env_lum(EnvView e, float* data, uint32_t quirks) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t W = e.W, H = e.H;
+  if (i >= W * H) return;
+  uint32_t x, y;
+  if (quirks & WPBR_Q_ENV_DISTRIB_INDEX_BUG) {
+    // data[x + y*resY] written in row order: the last writer of index i is
+    // the one with the largest row.
+    uint32_t yy = min(H - 1, i / H);
+    uint32_t xx = i - yy * H;
+    if (xx >= W) {
+      data[i] = 0.0f;
+      return;
+    }
+    x = xx;
+    y = yy;
+  } else {
+    x = i % W;
+    y = i / W;
+  }
+  float yN = (float)y / (float)H;
+  float sin_t = (float)sin_d((kPI * (double)(float)((float)y + 0.5f)) / (double)(float)H);
+  float xN = (float)x / (float)W;
+  float v = env_bilerp(e, xN, yN).g;
+  data[i] = v * sin_t;
+}
+// Distribution1D rows: sequential prefix sums (same rounding as the
+// reference's serial loop), one thread per row.
+__global__ void k_distrib_rows(const float* func, uint32_t n, uint32_t rows, float* cdf, float* fint) {
+  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  const float* f = func + (size_t)r * n;
+  float* c = cdf + (size_t)r * (n + 1);
+  c[0] = 0.0f;
+  for (uint32_t i = 1; i < n + 1; ++i) c[i] = c[i - 1] + f[i - 1] / (float)n;
+  float fi = c[n];
+  fint[r] = fi;
+  if (fi == 0.0f) {
+    for (uint32_t i = 1; i < n + 1; ++i) c[i] = (float)i / (float)n;
+  } else {
+    for (uint32_t i = 1; i < n + 1; ++i) c[i] = c[i] / fi;
+  }
+}
+
+// JobOutputFilmTitles (CSFilm.cpp:129-170): /(w*800000), clamp, sRGB-like
+// curve with the reference's 12.98 linear slope, x255, truncated to bytes.
+__device__ float gamma_correct(float v) {
+  if (v <= 0.0031308f) return 12.98f * v;
+  return 1.055f * expf_(logf_(v) * (float)(1.0f / 2.4f)) - 0.055f;
+}
+__global__ void k_tonemap(uint32_t n, const float4* acc, uint8_t* out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 a = acc[i];
+  if (a.x == 0.0f && a.y == 0.0f && a.z == 0.0f) {
+    out[3 * i] = out[3 * i + 1] = out[3 * i + 2] = 0;
+    return;
+  }
+  float d = a.w * 800000.f;
+  float c[3] = {a.x / d, a.y / d, a.z / d};
+  for (int k = 0; k < 3; ++k) {
+    float v = clampf(c[k], 0.0f, 1.0f);
+    v = gamma_correct(v) * 255.0f;
+    out[3 * i + k] = (uint8_t)(int)v;
+  }
+}
+
+PassCtx make_pass_ctx(wpbr_ctx* ctx) {
+  PassCtx P;
+  P.S = scene_view(ctx);
+  P.Bv = ctx->bvh.view;
+  P.rs = wpbr_rng::Stream{ctx->rs.seed, ctx->rs.stream, ctx->rs.spp};
+  P.W = ctx->rs.W;
+  P.H = ctx->rs.H;
+  P.err = ctx->d_err.p;
+  return P;
+}
+
+Staged staged_view(wpbr_ctx* ctx) {
+  Staged G;
+  for (int i = 0; i < F_COUNT; ++i) G.f[i] = ctx->rs.f[i].p;
+  for (int i = 0; i < U_COUNT; ++i) G.u[i] = ctx->rs.u[i].p;
+  return G;
+}
+
+wpbr_status ensure_staged(wpbr_ctx* ctx) {
+  size_t n = (size_t)ctx->rs.W * ctx->rs.H;
+  for (int i = 0; i < F_COUNT; ++i) WPBR_CUDA(ctx->rs.f[i].ensure(n * kFW[i]));
+  for (int i = 0; i < U_COUNT; ++i) WPBR_CUDA(ctx->rs.u[i].ensure(n));
+  return WPBR_OK;
+}
+
+}  // namespace
+
+wpbr_status env_preprocess(wpbr_ctx* ctx) {
+  if (!ctx->has_env) return WPBR_OK;
+  SceneView S = scene_view(ctx);
+  uint32_t W = ctx->envW, H = ctx->envH;
+  cudaStream_t st = ctx->stream;
+  k_env_lum<<<div_up((uint64_t)W * H, 256), 256, 0, st>>>(S.env, ctx->cond_func.p, ctx->quirks);
+  k_distrib_rows<<<div_up(H, 64), 64, 0, st>>>(ctx->cond_func.p, W, H, ctx->cond_cdf.p, ctx->cond_int.p);
+  WPBR_CUDA(cudaMemcpyAsync(ctx->marg_func.p, ctx->cond_int.p, sizeof(float) * H, cudaMemcpyDeviceToDevice, st));
+  k_distrib_rows<<<1, 32, 0, st>>>(ctx->marg_func.p, H, 1, ctx->marg_cdf.p, ctx->marg_int.p);
+  WPBR_CUDA(cudaGetLastError());
+  float mi = 0.0f;
+  WPBR_CUDA(cudaMemcpyAsync(&mi, ctx->marg_int.p, 4, cudaMemcpyDeviceToHost, st));
+  WPBR_CUDA(cudaStreamSynchronize(st));
+  ctx->env_marg_int = mi;
+  return WPBR_OK;
+}
+
+wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t stream) {
+  if (!ctx->has_scene) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render_setup: no scene");
+  if (!ctx->bvh.built) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render_setup: BVH not built");
+  if (spp == 0) return set_err(ctx, WPBR_ERR_INVALID_ARG, "render_setup: spp must be > 0");
+  RenderState& R = ctx->rs;
+  R.spp = spp;
+  R.seed = seed;
+  R.stream = stream;
+  R.W = ctx->cam.W;
+  R.H = ctx->cam.H;
+  size_t n = (size_t)R.W * R.H;
+  WPBR_CUDA(R.acc.ensure(n * 4));
+  WPBR_CUDA(R.hit_prim.ensure(n));
+  WPBR_CUDA(R.shadow_rays.ensure(n * 4));
+  WPBR_CUDA(R.shadow_hit.ensure(n * 2));
+  WPBR_CUDA(R.pstate.ensure(n * kStateF4));
+  WPBR_CUDA(R.Lbuf.ensure(n));
+  WPBR_CUDA(R.pfilm.ensure(n));
+  WPBR_CUDA(R.pass_dev.ensure(1));
+  WPBR_CUDA(cudaMemsetAsync(R.acc.p, 0, n * 4 * sizeof(float), ctx->stream));
+  if (R.graph) {
+    cudaGraphExecDestroy(R.graph);
+    R.graph = nullptr;
+  }
+  R.graph_ok = false;
+  R.ready = true;
+  return WPBR_OK;
+}
+
+static wpbr_status launch_fused(wpbr_ctx* ctx) {
+  RenderState& R = ctx->rs;
+  PassCtx P = make_pass_ctx(ctx);
+  uint32_t n = R.W * R.H;
+  cudaStream_t st = ctx->stream;
+  k_primary<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pass_dev.p, R.hit_prim.p);
+  k_spawn<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pass_dev.p, R.hit_prim.p, R.pstate.p, R.shadow_rays.p, R.Lbuf.p,
+                                          R.pfilm.p);
+  k_trace_shadow<<<div_up(2 * n, kTB), kTB, 0, st>>>(P, R.shadow_rays.p, 2 * n, R.shadow_hit.p);
+  k_finish<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pstate.p, R.shadow_hit.p, R.Lbuf.p);
+  k_film<<<div_up(n, kTB), kTB, 0, st>>>(R.W, R.H, R.pfilm.p, R.Lbuf.p, (float4*)R.acc.p);
+  WPBR_CUDA(cudaGetLastError());
+  return WPBR_OK;
+}
+
+wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass) {
+  RenderState& R = ctx->rs;
+  if (!R.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render_pass: render_setup not called");
+  if (pass >= R.spp) return set_err(ctx, WPBR_ERR_INVALID_ARG, "render_pass: pass >= spp");
+  cudaStream_t st = ctx->stream;
+  WPBR_CUDA(cudaMemcpyAsync(R.pass_dev.p, &pass, 4, cudaMemcpyHostToDevice, st));
+  if (!R.graph_ok) {
+    // capture the five kernels once; later passes replay the graph
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      wpbr_status s = launch_fused(ctx);
+      cudaError_t e = cudaStreamEndCapture(st, &g);
+      if (s == WPBR_OK && e == cudaSuccess && g) {
+        if (cudaGraphInstantiate(&R.graph, g, 0) == cudaSuccess) R.graph_ok = true;
+      }
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+    }
+    if (!R.graph_ok) return launch_fused(ctx);
+  }
+  WPBR_CUDA(cudaGraphLaunch(R.graph, st));
+  return WPBR_OK;
+}
+
+wpbr_status job_run(wpbr_ctx* ctx, uint32_t job, uint32_t pass) {
+  RenderState& R = ctx->rs;
+  if (!R.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "job_run: render_setup not called");
+  if (job >= WPBR_JOB_COUNT) return set_err(ctx, WPBR_ERR_INVALID_ARG, "job_run: unknown job id");
+  if (pass >= R.spp) return set_err(ctx, WPBR_ERR_INVALID_ARG, "job_run: pass >= spp");
+  wpbr_status s = ensure_staged(ctx);
+  if (s != WPBR_OK) return s;
+  PassCtx P = make_pass_ctx(ctx);
+  Staged G = staged_view(ctx);
+  uint32_t n = R.W * R.H;
+  unsigned g = div_up(n, kTB);
+  cudaStream_t st = ctx->stream;
+  switch (job) {
+    case WPBR_JOB_CAMERA_RAYS: kj_camera<<<g, kTB, 0, st>>>(P, pass, G); break;
+    case WPBR_JOB_COLLIDE_PRIMARY: kj_collide<<<g, kTB, 0, st>>>(P, G); break;
+    case WPBR_JOB_EMITTED_LIGHT: kj_emitted<<<g, kTB, 0, st>>>(P, G); break;
+    case WPBR_JOB_BSDF_SETUP: kj_bsdf_setup<<<g, kTB, 0, st>>>(P, G); break;
+    case WPBR_JOB_SAMPLE_LIGHT: kj_sample_light<<<g, kTB, 0, st>>>(P, pass, G); break;
+    case WPBR_JOB_SHADOW_LIGHT: kj_shadow_light<<<g, kTB, 0, st>>>(P, G); break;
+    case WPBR_JOB_BSDF_COMPUTE: kj_bsdf_compute<<<g, kTB, 0, st>>>(P, G); break;
+    case WPBR_JOB_INTEGRATE_LIGHT: kj_integrate_light<<<g, kTB, 0, st>>>(P, G); break;
+    case WPBR_JOB_SAMPLE_BSDF: kj_sample_bsdf<<<g, kTB, 0, st>>>(P, pass, G); break;
+    case WPBR_JOB_SHADOW_BSDF: kj_shadow_bsdf<<<g, kTB, 0, st>>>(P, G); break;
+    case WPBR_JOB_LIGHT_COMPUTE: kj_light_compute<<<g, kTB, 0, st>>>(P, G); break;
+    case WPBR_JOB_INTEGRATE_BSDF: kj_integrate_bsdf<<<g, kTB, 0, st>>>(P, G); break;
+    case WPBR_JOB_FILM_ACCUMULATE:
+      kj_film_pack<<<g, kTB, 0, st>>>(P, G, R.pfilm.p, R.Lbuf.p);
+      k_film<<<g, kTB, 0, st>>>(R.W, R.H, R.pfilm.p, R.Lbuf.p, (float4*)R.acc.p);
+      break;
+  }
+  WPBR_CUDA(cudaGetLastError());
+  return WPBR_OK;
+}
+
+wpbr_status job_record(wpbr_ctx* ctx, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1, wpbr_pass_record* rec) {
+  RenderState& R = ctx->rs;
+  if (!R.ready || !R.f[0].p) return set_err(ctx, WPBR_ERR_NOT_BUILT, "job_record: no staged pass");
+  if (x1 > R.W || y1 > R.H || x0 >= x1 || y0 >= y1 || !rec)
+    return set_err(ctx, WPBR_ERR_INVALID_ARG, "job_record: bad rectangle");
+  float* fptr[F_COUNT] = {rec->pfilm, rec->ray_o, rec->ray_d, rec->ray_dx_d, rec->ray_dy_d, rec->hit_t,
+                          rec->si_p, rec->si_n, rec->si_wo, rec->si_sn, rec->si_sdpdu, rec->si_dpdu,
+                          rec->si_dpdv, rec->si_dndu, rec->si_dndv, rec->frame, rec->le, rec->l_wi,
+                          rec->l_li, rec->l_pdf, rec->l_f, rec->l_fpdf, rec->b_wi, rec->b_f,
+                          rec->b_pdf, rec->b_li, rec->b_lpdf, rec->L};
+  uint32_t* uptr[4] = {rec->hit_prim, rec->light_idx, rec->l_flags, rec->b_flags};
+  cudaStream_t st = ctx->stream;
+  uint32_t w = x1 - x0;
+  for (uint32_t y = y0; y < y1; ++y) {
+    size_t src = (size_t)y * R.W + x0;
+    size_t dst = (size_t)(y - y0) * w;
+    for (int f = 0; f < F_COUNT; ++f)
+      if (fptr[f])
+        WPBR_CUDA(cudaMemcpyAsync(fptr[f] + dst * kFW[f], R.f[f].p + src * kFW[f], sizeof(float) * w * kFW[f],
+                                  cudaMemcpyDeviceToHost, st));
+    for (int u = 0; u < 4; ++u)
+      if (uptr[u])
+        WPBR_CUDA(cudaMemcpyAsync(uptr[u] + dst, R.u[u].p + src, sizeof(uint32_t) * w, cudaMemcpyDeviceToHost, st));
+  }
+  WPBR_CUDA(cudaStreamSynchronize(st));
+  return WPBR_OK;
+}
+
+wpbr_status film_tonemap(wpbr_ctx* ctx, uint8_t* out) {
+  RenderState& R = ctx->rs;
+  if (!R.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "tonemap: render_setup not called");
+  uint32_t n = R.W * R.H;
+  DevBuf<uint8_t> tmp;
+  WPBR_CUDA(tmp.ensure((size_t)n * 3));
+  k_tonemap<<<div_up(n, 256), 256, 0, ctx->stream>>>(n, (const float4*)R.acc.p, tmp.p);
+  cudaError_t e = cudaMemcpyAsync(out, tmp.p, (size_t)n * 3, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  tmp.release();
+  if (e != cudaSuccess) return cuda_err(ctx, e, "tonemap");
+  return WPBR_OK;
+}
+
+}  // namespace wpbr

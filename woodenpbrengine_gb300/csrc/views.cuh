@@ -1,0 +1,58 @@
+// views.cuh — POD views of device-resident scene and BVH data, passed to
+// kernels by value.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "camera.cuh"
+#include "geom.cuh"
+#include "shade.cuh"
+#include "wpbr_scene.h"
+
+namespace wpbr {
+
+struct SceneView {
+  uint32_t ns, nt, N;
+  const Xf* sph_o2w;
+  const Xf* sph_w2o;
+  const float* sph_r;
+  const uint32_t* sph_mat;
+  const float* pos;        // nv*3
+  const uint32_t* idx;     // nt*3
+  const float* nrm;        // nv*3 or null
+  const float* tan;        // nv*3 or null
+  const float* uv;         // nv*2 or null
+  const uint32_t* tri_mat;
+  const uint32_t* tri_flags;
+  const wpbr_material* mats;
+  const wpbr_light* lights;
+  uint32_t nlights;
+  int has_env;
+  EnvView env;
+  CameraParams cam;
+  uint32_t quirks;
+};
+
+// Child-pair BVH node: the bounds of both children of one interior node of
+// the flattened CSceneTreeLBVH, so one 64-byte fetch tests two boxes.
+// ref >= 0: interior node index; ref < 0: leaf whose primitives start at
+// sorted position ~ref, count in cnt0 / (cnt1 & 0x3FFFFFFF). axis in the
+// top two bits of cnt1 (the parent's split axis, for near-first order).
+struct __align__(16) Node2 {
+  float4 b0;   // c0 lo.x hi.x lo.y hi.y
+  float4 b1;   // c1 lo.x hi.x lo.y hi.y
+  float4 bz;   // c0 lo.z hi.z, c1 lo.z hi.z
+  int4 meta;   // ref0, ref1, cnt0, (axis<<30)|cnt1
+};
+
+struct BvhView {
+  const Node2* nodes;
+  const float4* prims;   // 3 float4 per sorted primitive
+  int empty;
+  int root_ref;          // >=0 interior index, <0 leaf (~first)
+  uint32_t root_count;
+  float root_lo[3], root_hi[3];
+  uint32_t max_depth;
+};
+
+}  // namespace wpbr
