@@ -71,9 +71,34 @@ def test_fused_film_matches_oracle(W, O, ctx, config):
             ctx.job(s, p)
     Ls, ws = ctx.film(Wd, Hd)
     assert np.array_equal(Ls.view(np.uint32), Lo.view(np.uint32)) and np.array_equal(ws, wo)
-    img = ctx.tonemap(Wd, Hd)
-    assert img.shape == (Hd, Wd, 3) and img.max() > 0
     ctx.check_device_errors()
+
+
+def _tonemap_ref(L, w):
+    # JobOutputFilmTitles (CSFilm.cpp:129-170) restated in numpy
+    out = np.zeros(L.shape, np.uint8)
+    black = np.all(L == 0, axis=-1)
+    c = np.clip(L / (w[..., None] * np.float32(800000.0)), 0, 1).astype(np.float64)
+    g = np.where(c <= 0.0031308, 12.98 * c, 1.055 * np.power(c, 1 / 2.4) - 0.055) * 255.0
+    out[~black] = np.floor(g[~black]).astype(np.uint8)
+    return out
+
+
+def test_tonemap(W, ctx):
+    g = W.SceneGen(0, 0, (64, 64))
+    d = g.desc.contents
+    for c in range(3):
+        d.lights[0].Le[c] = 2.0e7  # the reference's exposure constant wants a bright light
+    ctx.set_quirks(0)
+    ctx.upload(g.desc)
+    ctx.build()
+    ctx.render_setup(2, seed=0)
+    ctx.render()
+    L, w = ctx.film(64, 64)
+    img = ctx.tonemap(64, 64)
+    ref = _tonemap_ref(L, w)
+    assert img.max() > 0
+    assert np.abs(img.astype(int) - ref.astype(int)).max() <= 1
 
 
 def test_env_distribution_matches_oracle(W, O, ctx):

@@ -898,7 +898,7 @@ __global__ void k_sah_sizes(uint32_t T, const uint32_t* troot, const uint32_t* p
 // ---------------------------------------------------------------------------
 // A9: flattenBVHTree — depth-first preorder index of every reference node
 // ---------------------------------------------------------------------------
-__global__ void k_flatten(uint32_t N, uint32_t nsah, uint32_t root, const uint32_t* skey, const uint32_t* tid,
+__global__ void k_flatten(uint32_t N, uint32_t nsah, uint32_t root, uint32_t M, const uint32_t* skey, const uint32_t* tid,
                           const uint32_t* tstart, const uint32_t* tsize, const uint32_t* rng_lo,
                           const uint32_t* rng_hi, const uint32_t* child0, const uint32_t* parent,
                           const uint32_t* size, const uint32_t* sah_axis, const float4* nb_lo, const float4* nb_hi,
@@ -941,6 +941,10 @@ __global__ void k_flatten(uint32_t N, uint32_t nsah, uint32_t root, const uint32
     idx += (pw & 1u) ? 1u + size[child0[p]] : 1u;
     cur = p;
   }
+  if (idx >= M) {
+    atomicOr(err, kErrBuild);
+    return;
+  }
   atomicMax(depth_max, depth);
   float4 bl = nb_lo[X], bh = nb_hi[X];
   float* B = lin_bounds + (size_t)idx * 6;
@@ -965,6 +969,7 @@ __global__ void k_node2(uint32_t M, const uint32_t* lin_node, const float* lin_b
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= M || !is_int[i]) return;
   uint32_t c[2] = {i + 1, lin_node[(size_t)i * 3]};
+  if (c[0] >= M || c[1] >= M) return;  // malformed tree: traversal guards report it
   int ref[2];
   uint32_t cnt[2];
   float b[2][6];
@@ -1237,7 +1242,7 @@ wpbr_status bvh_build(wpbr_ctx* ctx) {
   WPBR_CUDA(B.is_int.ensure(M));
   WPBR_CUDA(B.int_index.ensure(M));
   WPBR_CUDA(cudaMemsetAsync(B.depth_max.p, 0, 4, st));
-  k_flatten<<<div_up(N2 + nsah, kB), kB, 0, st>>>(N, nsah, root, B.skey, B.tid.p, B.tstart.p, B.tsize.p, B.rng_lo.p,
+  k_flatten<<<div_up(N2 + nsah, kB), kB, 0, st>>>(N, nsah, root, M, B.skey, B.tid.p, B.tstart.p, B.tsize.p, B.rng_lo.p,
                                                    B.rng_hi.p, B.child0.p, B.parent.p, B.size.p, B.sah_axis.p,
                                                    B.nb_lo.p, B.nb_hi.p, B.lin_node.p, B.lin_bounds.p, B.is_int.p,
                                                    B.depth_max.p, ctx->d_err.p);
@@ -1271,6 +1276,8 @@ wpbr_status bvh_build(wpbr_ctx* ctx) {
     v.root_hi[k] = b0[3 + k];
   }
   v.max_depth = depth;
+  v.n_prims = N;
+  v.n_int = B.n_int;
   B.view = v;
   uint32_t derr = 0;
   WPBR_CUDA(cudaMemcpyAsync(&derr, ctx->d_err.p, 4, cudaMemcpyDeviceToHost, st));

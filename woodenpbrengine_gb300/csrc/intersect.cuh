@@ -74,7 +74,14 @@ WPBR_HD float tri_intersect(V3 p0, V3 p1, V3 p2, V3 ro, V3 rd, uint32_t quirks, 
   float ts = (e0 * (z0 * sz) + e1 * (z1 * sz)) + e2 * (z2 * sz);
   if (det < 0.0f && ts >= 0.0f) return 0.0f;
   if (det > 0.0f && ts <= 0.0f) return 0.0f;
+  // float(1.0 / (double)det) as the reference writes it: a double quotient
+  // rounded to float equals the correctly rounded float reciprocal (53 >=
+  // 2*24 + 2 bits), which the device computes without double arithmetic.
+#if defined(__CUDA_ARCH__)
+  float inv_det = __frcp_rn(det);
+#else
   float inv_det = (float)(1.0 / (double)det);
+#endif
   *b0 = e0 * inv_det;
   *b1 = e1 * inv_det;
   *b2 = e2 * inv_det;

@@ -71,9 +71,18 @@ __device__ HitRec trace_ray(const SceneView& S, const BvhView& Bv, V3 o, V3 d, f
   int ref = Bv.root_ref;
   uint32_t cnt = Bv.root_count;
   float tb = inf_();
+  uint32_t iters = 0;
   while (true) {
     bool go = false;
+    if (++iters > (1u << 22)) {  // a well-formed tree never gets here
+      atomicOr(err, kErrLoopLimit);
+      break;
+    }
     if (ref >= 0) {
+      if ((uint32_t)ref >= Bv.n_int) {
+        atomicOr(err, kErrBuild);
+        break;
+      }
       const Node2* np_ = Bv.nodes + ref;
       float4 b0 = __ldg(&np_->b0), b1 = __ldg(&np_->b1), bz = __ldg(&np_->bz);
       int4 m = __ldg(&np_->meta);
@@ -107,6 +116,10 @@ __device__ HitRec trace_ray(const SceneView& S, const BvhView& Bv, V3 o, V3 d, f
       }
     } else {
       uint32_t first = (uint32_t)(~ref);
+      if (first >= Bv.n_prims || cnt > Bv.n_prims - first) {
+        atomicOr(err, kErrBuild);
+        break;
+      }
       for (uint32_t k = 0; k < cnt; ++k) {
         uint32_t prim;
         float b1, b2;

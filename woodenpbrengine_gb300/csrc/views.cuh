@@ -53,6 +53,7 @@ struct BvhView {
   uint32_t root_count;
   float root_lo[3], root_hi[3];
   uint32_t max_depth;
+  uint32_t n_prims, n_int;  // bounds for the index guards in traversal
 };
 
 }  // namespace wpbr
