@@ -36,4 +36,15 @@ constexpr int kScanTile = kScanBlock * kScanItems;  // 2048 elements per block
 
 inline unsigned div_up(uint64_t a, uint64_t b) { return (unsigned)((a + b - 1) / b); }
 
+// Grid for a persistent kernel: resident blocks per SM times the SM count.
+inline unsigned persistent_grid(const void* kernel, int block = 128) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+  if (per_sm < 1) per_sm = 1;
+  if (sms < 1) sms = 1;
+  return (unsigned)(sms * per_sm);
+}
+
 }  // namespace wpbr

@@ -139,8 +139,8 @@ WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
   B.nodes2.release(); B.prims.release();
   RenderState& R = ctx->rs;
   R.acc.release(); R.hit_prim.release(); R.shadow_rays.release(); R.shadow_hit.release(); R.pstate.release();
-  R.Lbuf.release(); R.pfilm.release(); R.pass_dev.release();
-  ctx->io_rays.release(); ctx->io_hits.release(); ctx->io_stats.release();
+  R.Lbuf.release(); R.pfilm.release(); R.pass_dev.release(); R.counters.release();
+  ctx->io_rays.release(); ctx->io_hits.release(); ctx->io_stats.release(); ctx->trace_counter.release();
   for (auto& f : R.f) f.release();
   for (auto& u : R.u) u.release();
   delete ctx;

@@ -85,6 +85,7 @@ struct RenderState {
   cudaGraphExec_t graph = nullptr;
   uint32_t graph_pass = 0xFFFFFFFFu;
   DevBuf<uint32_t> pass_dev;  // pass index read by the captured kernels
+  DevBuf<uint32_t> counters;  // ray-fetch counters of the pass's traversal launches
 };
 
 }  // namespace wpbr
@@ -120,6 +121,7 @@ struct wpbr_ctx {
   // staging for the host-buffer collide entry points
   wpbr::DevBuf<float4> io_rays, io_hits;
   wpbr::DevBuf<uint32_t> io_stats;
+  wpbr::DevBuf<uint32_t> trace_counter;  // ray-fetch counters of the persistent traversal
 };
 
 namespace wpbr {

@@ -14,6 +14,7 @@
 #include "ctx.hpp"
 #include "shade.cuh"
 #include "traverse.cuh"
+#include "traverse_persistent.cuh"
 #include "wpbr_sampling.h"
 
 namespace wpbr {
@@ -380,15 +381,18 @@ __global__ void k_film(uint32_t W, uint32_t H, const float2* pf, const float4* L
 constexpr int kStateF4 = 6;
 enum : uint32_t { SF_VALID = 1u, SF_TRACE_L = 2u, SF_TRACE_B = 4u, SF_HIT = 8u };
 
-__global__ void __launch_bounds__(kTB) k_primary(PassCtx P, const uint32_t* pass_dev, uint32_t* hit_prim) {
-  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= P.W * P.H) return;
-  uint32_t pass = *pass_dev;
-  float fx, fy;
-  camera_sample(P, pix, pass, &fx, &fy);
-  RayD r = camera_ray(P.S.cam, fx, fy);
-  hit_prim[pix] = trace_closest(P, r.o, r.d);
-}
+// Camera rays generated inside the persistent traversal's ray source.
+struct CameraSrc {
+  PassCtx P;
+  const uint32_t* pass_dev;
+  __device__ __forceinline__ void load(uint32_t pix, float4* o, float4* d) const {
+    float fx, fy;
+    camera_sample(P, pix, *pass_dev, &fx, &fy);
+    RayD r = camera_ray(P.S.cam, fx, fy);
+    *o = make_float4(r.o.x, r.o.y, r.o.z, 0.0f);
+    *d = make_float4(r.d.x, r.d.y, r.d.z, inf_());
+  }
+};
 
 __global__ void __launch_bounds__(kTB) k_spawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
                                                float4* state, float4* rays, float4* Lb, float2* pf) {
@@ -454,17 +458,6 @@ __global__ void __launch_bounds__(kTB) k_spawn(PassCtx P, const uint32_t* pass_d
   st[4] = make_float4(bwi.x, bwi.y, bwi.z, __uint_as_float(flags));
   st[5] = make_float4(s.p.x, s.p.y, s.p.z, 0.0f);
   Lb[pix] = make_float4(L.r, L.g, L.b, 0.0f);
-}
-
-__global__ void __launch_bounds__(kTB) k_trace_shadow(PassCtx P, const float4* rays, uint32_t n, uint32_t* out) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float4 o = rays[2 * i], d = rays[2 * i + 1];
-  if (!(d.w > 0.0f)) {
-    out[i] = kNoHit;
-    return;
-  }
-  out[i] = trace_closest(P, V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z});
 }
 
 __global__ void __launch_bounds__(kTB) k_finish(PassCtx P, const float4* state, const uint32_t* shadow, float4* Lb) {
@@ -641,6 +634,7 @@ wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t st
   WPBR_CUDA(R.Lbuf.ensure(n));
   WPBR_CUDA(R.pfilm.ensure(n));
   WPBR_CUDA(R.pass_dev.ensure(1));
+  WPBR_CUDA(R.counters.ensure(2));  // allocated before any graph capture
   WPBR_CUDA(cudaMemsetAsync(R.acc.p, 0, n * 4 * sizeof(float), ctx->stream));
   if (R.graph) {
     cudaGraphExecDestroy(R.graph);
@@ -656,10 +650,35 @@ static wpbr_status launch_fused(wpbr_ctx* ctx) {
   PassCtx P = make_pass_ctx(ctx);
   uint32_t n = R.W * R.H;
   cudaStream_t st = ctx->stream;
-  k_primary<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pass_dev.p, R.hit_prim.p);
+  WPBR_CUDA(R.counters.ensure(2));
+  WPBR_CUDA(cudaMemsetAsync(R.counters.p, 0, 2 * sizeof(uint32_t), st));
+  bool deep = P.Bv.max_depth >= 60;
+  {
+    CameraSrc src{P, R.pass_dev.p};
+    PrimSink sink{R.hit_prim.p};
+    if (deep) {
+      auto k = k_trace_persistent<false, 256, CameraSrc, PrimSink>;
+      k<<<persistent_grid((const void*)k), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, n, R.counters.p, P.err);
+    } else {
+      auto k = k_trace_persistent<false, 64, CameraSrc, PrimSink>;
+      k<<<persistent_grid((const void*)k), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, n, R.counters.p, P.err);
+    }
+  }
   k_spawn<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pass_dev.p, R.hit_prim.p, R.pstate.p, R.shadow_rays.p, R.Lbuf.p,
                                           R.pfilm.p);
-  k_trace_shadow<<<div_up(2 * n, kTB), kTB, 0, st>>>(P, R.shadow_rays.p, 2 * n, R.shadow_hit.p);
+  {
+    BufferSrc src{R.shadow_rays.p};
+    PrimSink sink{R.shadow_hit.p};
+    if (deep) {
+      auto k = k_trace_persistent<false, 256, BufferSrc, PrimSink>;
+      k<<<persistent_grid((const void*)k), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, 2 * n, R.counters.p + 1,
+                                                                    P.err);
+    } else {
+      auto k = k_trace_persistent<false, 64, BufferSrc, PrimSink>;
+      k<<<persistent_grid((const void*)k), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, 2 * n, R.counters.p + 1,
+                                                                    P.err);
+    }
+  }
   k_finish<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pstate.p, R.shadow_hit.p, R.Lbuf.p);
   k_film<<<div_up(n, kTB), kTB, 0, st>>>(R.W, R.H, R.pfilm.p, R.Lbuf.p, (float4*)R.acc.p);
   WPBR_CUDA(cudaGetLastError());

@@ -3,6 +3,7 @@
 #include "common.cuh"
 #include "ctx.hpp"
 #include "traverse.cuh"
+#include "traverse_persistent.cuh"
 
 namespace wpbr {
 
@@ -37,6 +38,17 @@ cudaError_t launch(const SceneView& S, const BvhView& Bv, const float4* rays, ui
   return cudaGetLastError();
 }
 
+template <bool ANY, int STACK>
+cudaError_t launch_persistent(const SceneView& S, const BvhView& Bv, const float4* rays, uint32_t n, float4* hits,
+                              uint32_t* counter, uint32_t* err, cudaStream_t st) {
+  auto kern = k_trace_persistent<ANY, STACK, BufferSrc, HitSink4>;
+  unsigned grid = persistent_grid((const void*)kern);
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, kPersistBlock, 0, st>>>(S, Bv, BufferSrc{rays}, HitSink4{hits}, n, counter, err);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* d_hits, uint32_t mode,
@@ -47,12 +59,23 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
   SceneView S = scene_view(ctx);
   const BvhView& Bv = ctx->bvh.view;
   cudaError_t e;
-  if (mode == WPBR_TRACE_ANY)
-    e = d_stats ? launch<true, true>(S, Bv, d_rays, n, d_hits, d_stats, ctx->d_err.p, ctx->stream)
-                : launch<true, false>(S, Bv, d_rays, n, d_hits, nullptr, ctx->d_err.p, ctx->stream);
-  else
-    e = d_stats ? launch<false, true>(S, Bv, d_rays, n, d_hits, d_stats, ctx->d_err.p, ctx->stream)
-                : launch<false, false>(S, Bv, d_rays, n, d_hits, nullptr, ctx->d_err.p, ctx->stream);
+  if (d_stats) {
+    e = (mode == WPBR_TRACE_ANY) ? launch<true, true>(S, Bv, d_rays, n, d_hits, d_stats, ctx->d_err.p, ctx->stream)
+                                 : launch<false, true>(S, Bv, d_rays, n, d_hits, d_stats, ctx->d_err.p, ctx->stream);
+  } else {
+    if (n >= 0xFFFFFFFFull) return set_err(ctx, WPBR_ERR_INVALID_ARG, "collide: more than 2^32-1 rays per call");
+    e = ctx->trace_counter.ensure(4);
+    if (e == cudaSuccess) {
+      uint32_t* c = ctx->trace_counter.p;
+      bool deep = Bv.max_depth >= 60;
+      if (mode == WPBR_TRACE_ANY)
+        e = deep ? launch_persistent<true, 256>(S, Bv, d_rays, (uint32_t)n, d_hits, c, ctx->d_err.p, ctx->stream)
+                 : launch_persistent<true, 64>(S, Bv, d_rays, (uint32_t)n, d_hits, c, ctx->d_err.p, ctx->stream);
+      else
+        e = deep ? launch_persistent<false, 256>(S, Bv, d_rays, (uint32_t)n, d_hits, c, ctx->d_err.p, ctx->stream)
+                 : launch_persistent<false, 64>(S, Bv, d_rays, (uint32_t)n, d_hits, c, ctx->d_err.p, ctx->stream);
+    }
+  }
   if (e != cudaSuccess) return cuda_err(ctx, e, "collide kernel");
   return WPBR_OK;
 }
