@@ -164,6 +164,26 @@ WPBR_API uint64_t wpbr_scenegen_ray_count(const wpbr_scenegen* g);
 WPBR_API const float* wpbr_scenegen_rays(const wpbr_scenegen* g);
 WPBR_API void wpbr_scenegen_destroy(wpbr_scenegen* g);
 
+/* ---- allocation-free Morton sort ----------------------------------------------
+ * No counterpart in the reference (its sort runs inside JobSortsShapesByMortonCode
+ * on the engine's temp allocator). For callers that cannot allocate device
+ * memory: hosts that hand out all device memory from their own arena and
+ * forbid allocation inside a job, loops that must not take cudaMalloc's
+ * device-wide synchronisation, and work recorded into a CUDA graph while a
+ * stream is being captured. Stable LSD radix sort of n Morton codes by their
+ * low key_bits bits (24: the order the reference builds over; 30: full), the
+ * same permutation as wpbr_bvh_build. Device buffers in and out (no aliasing),
+ * asynchronous on `stream`, no allocation: temporaries live in one file-scope
+ * device array of WPBR_SORT_NOALLOC_MAX_KEYS keys (about 8.5 MB per GPU that
+ * loads the library, held until exit). The first call on a device looks up the
+ * array's address and should come before any stream capture. All calls share
+ * the array; calls whose GPU work overlaps race. n above the maximum returns
+ * WPBR_ERR_INVALID_ARG; wpbr_sort_morton_noalloc_error() says why. */
+#define WPBR_SORT_NOALLOC_MAX_KEYS (1u << 20)
+WPBR_API wpbr_status wpbr_sort_morton_noalloc(const uint32_t* d_codes, uint32_t n, uint32_t key_bits,
+                                              uint32_t* d_sorted_codes, uint32_t* d_perm, void* stream);
+WPBR_API const char* wpbr_sort_morton_noalloc_error(void);
+
 /* Library build identification (host-only). */
 WPBR_API const char* wpbr_version(void);
 

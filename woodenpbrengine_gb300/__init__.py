@@ -66,7 +66,10 @@ _SIGS = {
     "wpbr_scenegen_ray_count": (C.c_uint64, [_VP]),
     "wpbr_scenegen_rays": (_FP, [_VP]),
     "wpbr_scenegen_destroy": (None, [_VP]),
+    "wpbr_sort_morton_noalloc": (C.c_int, [_VP, C.c_uint32, C.c_uint32, _VP, _VP, _VP]),
+    "wpbr_sort_morton_noalloc_error": (C.c_char_p, []),
 }
+SORT_NOALLOC_MAX_KEYS = 1 << 20
 EXPORTED = sorted(_SIGS)
 
 _lib = None
