@@ -44,6 +44,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-render", action="store_true")
     p.add_argument("--profile", action="store_true",
                    help="small case for ncu: 1,310,720 triangles, 1024x1024 + 1M incoherent rays, 5 launches")
     return p.parse_args()
@@ -132,6 +133,35 @@ def cpu_trace_rate(desc, rays, seconds, threads=None):
                 sample="%d rays (the first %d coherent and first %d incoherent of the set), prune-free "
                        "candidate traversal + min-t reduce as in JobProcessRayCasts/Results, %.1f s"
                        % (2 * m, m, m, dt)), o
+
+
+def render_rate(W, torch, config, res, spp, level=0, frames=1):
+    """Msamples/s of whole frames through the fused, graph-captured pass
+    (config 0: 64 spheres + quad + sphere light; config 2: the 1.31 M-triangle
+    mesh + 256 spheres + 1024x512 environment light)."""
+    g = W.SceneGen(config, 0, res, level=level)
+    ctx = W.Context(torch.cuda.current_device())
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload(g.desc)
+    ctx.build()
+    ctx.render_setup(spp, seed=0)
+    ctx.render()  # warm-up frame (captures the pass graph)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(frames):
+        ctx.render_setup(spp, seed=0)
+        ctx.render()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ctx.check_device_errors()
+    ms = e0.elapsed_time(e1) / frames
+    samples = res[0] * res[1] * spp
+    ctx.close()
+    return {"msamples_per_s": samples / ms / 1e3, "ms_per_frame": ms, "film": "%dx%d" % res, "spp": spp,
+            "kernel_launches_per_pass": 5}
 
 
 def run_reference(args):
@@ -335,6 +365,11 @@ def main():
     e2e_s = (time.perf_counter() - t) / e2e_steps
     e2e = world * n / e2e_s / 1e6
 
+    render = None
+    if rank == 0 and not args.no_render:
+        render = {"c0_plain_256x256_4spp": render_rate(W, torch, 0, (256, 256), 4, frames=3),
+                  "c2_fullframe_1080p_64spp": render_rate(W, torch, 2, (1920, 1080), 64, level=LEVEL)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu, _ = cpu_trace_rate(g.desc, rays, args.cpu_seconds)
@@ -356,6 +391,7 @@ def main():
         "clocks": ck,
         "build": {"mprims_per_s": info["n_prims"] / build_s / 1e6, "ms": build_s * 1e3},
         "anyhit_mrays_per_s": any_rate,
+        "render": render,
         "cpu_baseline": cpu,
     }
     if rank == 0:

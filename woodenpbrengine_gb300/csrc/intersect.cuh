@@ -88,6 +88,70 @@ WPBR_HD float tri_intersect(V3 p0, V3 p1, V3 p2, V3 ro, V3 rd, uint32_t quirks, 
   return ts * inv_det;
 }
 
+// The per-ray part of tri_intersect (axis permutation, shear, permuted
+// origin), evaluated once per ray: the same operations on the same operands,
+// so tri_intersect_pre returns exactly what tri_intersect returns.
+struct RayTri {
+  int kx, ky, kz;
+  float sx, sy, sz;
+  float ox, oy, oz;
+  bool miss_all;  // WPBR_Q_TRI_PERMUTATION_BUG with a y-dominant ray
+};
+WPBR_HD RayTri ray_tri_setup(V3 ro, V3 rd, uint32_t quirks) {
+  RayTri R;
+  float ax = fabs_(rd.x), ay = fabs_(rd.y), az = fabs_(rd.z);
+  R.kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
+  R.kx = (R.kz == 2) ? 0 : R.kz + 1;
+  R.ky = (R.kz == 2) ? 1 : R.kz + 2;
+  R.miss_all = false;
+  if (R.ky == 3) {
+    R.miss_all = (quirks & WPBR_Q_TRI_PERMUTATION_BUG) != 0;
+    R.ky = 0;
+  }
+  float dx = comp(rd, R.kx), dy = comp(rd, R.ky), dz = comp(rd, R.kz);
+  R.sx = -dx / dz;
+  R.sy = -dy / dz;
+  R.sz = 1.0f / dz;
+  R.ox = comp(ro, R.kx);
+  R.oy = comp(ro, R.ky);
+  R.oz = comp(ro, R.kz);
+  return R;
+}
+WPBR_HD float tri_intersect_pre(V3 p0, V3 p1, V3 p2, const RayTri& R, float* b0, float* b1, float* b2) {
+  if (R.miss_all) return 0.0f;
+  float x0 = comp(p0, R.kx) - R.ox, y0 = comp(p0, R.ky) - R.oy, z0 = comp(p0, R.kz) - R.oz;
+  float x1 = comp(p1, R.kx) - R.ox, y1 = comp(p1, R.ky) - R.oy, z1 = comp(p1, R.kz) - R.oz;
+  float x2 = comp(p2, R.kx) - R.ox, y2 = comp(p2, R.ky) - R.oy, z2 = comp(p2, R.kz) - R.oz;
+  x0 = x0 + R.sx * z0;
+  y0 = y0 + R.sy * z0;
+  x1 = x1 + R.sx * z1;
+  y1 = y1 + R.sy * z1;
+  x2 = x2 + R.sx * z2;
+  y2 = y2 + R.sy * z2;
+  z0 = z0 + 0.0f * z0;
+  z1 = z1 + 0.0f * z1;
+  z2 = z2 + 0.0f * z2;
+  float rx = x0 * y1 - x1 * y0;
+  float ry = x1 * y2 - x2 * y1;
+  float rz = x2 * y0 - x0 * y2;
+  if ((rx < 0.0f || ry < 0.0f || rz < 0.0f) && (rx > 0.0f || ry > 0.0f || rz > 0.0f)) return 0.0f;
+  float det = (rx + ry) + rz;
+  if (det == 0.0f) return 0.0f;
+  float e0 = ry, e1 = rz, e2 = rx;
+  float ts = (e0 * (z0 * R.sz) + e1 * (z1 * R.sz)) + e2 * (z2 * R.sz);
+  if (det < 0.0f && ts >= 0.0f) return 0.0f;
+  if (det > 0.0f && ts <= 0.0f) return 0.0f;
+#if defined(__CUDA_ARCH__)
+  float inv_det = __frcp_rn(det);
+#else
+  float inv_det = (float)(1.0 / (double)det);
+#endif
+  *b0 = e0 * inv_det;
+  *b1 = e1 * inv_det;
+  *b2 = e2 * inv_det;
+  return ts * inv_det;
+}
+
 // WoodenMath getRootsQuadraticEquation, restated as pbrt-v3's Quadratic
 // (double-precision discriminant and roots, rounded to float).
 WPBR_HD bool quadratic(float a, float b, float c, float* t0, float* t1) {

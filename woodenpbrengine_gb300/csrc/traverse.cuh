@@ -28,7 +28,7 @@ struct HitRec {
 };
 
 __device__ __forceinline__ float prim_test(const SceneView& S, const float4* prims, uint32_t pos, V3 o, V3 d,
-                                           uint32_t* prim_out, float* b1, float* b2) {
+                                           const RayTri& R, uint32_t* prim_out, float* b1, float* b2) {
   const float4* r = prims + (size_t)pos * 3;
   float4 r0 = __ldg(r), r1 = __ldg(r + 1);
   *prim_out = __float_as_uint(r0.w);
@@ -42,7 +42,7 @@ __device__ __forceinline__ float prim_test(const SceneView& S, const float4* pri
   }
   float4 r2 = __ldg(r + 2);
   float c0, c1, c2;
-  float t = tri_intersect(V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, V3{r2.x, r2.y, r2.z}, o, d, S.quirks, &c0, &c1, &c2);
+  float t = tri_intersect_pre(V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, V3{r2.x, r2.y, r2.z}, R, &c0, &c1, &c2);
   *b1 = c1;
   *b2 = c2;
   return t;
@@ -56,6 +56,7 @@ __device__ HitRec trace_ray(const SceneView& S, const BvhView& Bv, V3 o, V3 d, f
   if (Bv.empty) return h;
   V3 inv{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
   int neg[3] = {inv.x < 0.0f, inv.y < 0.0f, inv.z < 0.0f};
+  const RayTri R = ray_tri_setup(o, d, S.quirks);
   float te;
   ++nv;
   if (!slab_test(V3{Bv.root_lo[0], Bv.root_lo[1], Bv.root_lo[2]}, V3{Bv.root_hi[0], Bv.root_hi[1], Bv.root_hi[2]}, o,
@@ -124,7 +125,7 @@ __device__ HitRec trace_ray(const SceneView& S, const BvhView& Bv, V3 o, V3 d, f
         uint32_t prim;
         float b1, b2;
         ++np;
-        float t = prim_test(S, Bv.prims, first + k, o, d, &prim, &b1, &b2);
+        float t = prim_test(S, Bv.prims, first + k, o, d, R, &prim, &b1, &b2);
         if (t == 0.0f || !(t < tmax)) continue;
         if (tb > t) {
           tb = t;

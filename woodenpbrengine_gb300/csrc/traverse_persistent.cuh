@@ -27,6 +27,7 @@ __global__ void __launch_bounds__(kPersistBlock) k_trace_persistent(SceneView S,
   const uint32_t lt_mask = (1u << lane) - 1u;
   V3 o{0, 0, 0}, d{0, 0, 0}, inv{0, 0, 0};
   int neg[3] = {0, 0, 0};
+  RayTri R{};
   float tmax = 0.0f, tb = 0.0f;
   HitRec h{0.0f, kNoHit, 0.0f, 0.0f};
   int ref = kEnd;
@@ -66,6 +67,7 @@ __global__ void __launch_bounds__(kPersistBlock) k_trace_persistent(SceneView S,
           neg[0] = inv.x < 0.0f;
           neg[1] = inv.y < 0.0f;
           neg[2] = inv.z < 0.0f;
+          R = ray_tri_setup(o, d, S.quirks);
           tb = inf_();
           h = HitRec{inf_(), kNoHit, 0.0f, 0.0f};
           sp = 0;
@@ -179,7 +181,7 @@ __global__ void __launch_bounds__(kPersistBlock) k_trace_persistent(SceneView S,
         for (uint32_t k = 0; k < lcnt; ++k) {
           uint32_t prim;
           float b1, b2;
-          float t = prim_test(S, Bv.prims, first + k, o, d, &prim, &b1, &b2);
+          float t = prim_test(S, Bv.prims, first + k, o, d, R, &prim, &b1, &b2);
           if (t == 0.0f || !(t < tmax)) continue;
           if (tb > t) {
             tb = t;
