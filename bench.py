@@ -141,7 +141,7 @@ def render_rate(W, torch, config, res, spp, level=0, frames=1):
     mesh + 256 spheres + 1024x512 environment light)."""
     g = W.SceneGen(config, 0, res, level=level)
     ctx = W.Context(torch.cuda.current_device())
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()  # a capturable (non-default) stream for the pass graph
     ctx.set_stream(stream.cuda_stream)
     ctx.upload(g.desc)
     ctx.build()

@@ -701,8 +701,10 @@ wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass) {
         if (cudaGraphInstantiate(&R.graph, g, 0) == cudaSuccess) R.graph_ok = true;
       }
       if (g) cudaGraphDestroy(g);
-      cudaGetLastError();
     }
+    // capture is not possible on the legacy default stream: clear the error
+    // and launch the kernels directly
+    cudaGetLastError();
     if (!R.graph_ok) return launch_fused(ctx);
   }
   WPBR_CUDA(cudaGraphLaunch(R.graph, st));
