@@ -164,6 +164,74 @@ def render_rate(W, torch, config, res, spp, level=0, frames=1):
             "kernel_launches_per_pass": 5}
 
 
+def batch_rate(W, torch, n_scenes=32, spp=16, film_scale=1024, max_count=2000000):
+    """Aggregate Msamples/s of the batched-scenes set (32 scenes, triangle
+    counts log-uniform on [10k, 2M], films from {256..1024}^2, 16 spp): all
+    scenes through one wpbr_batch (pooled arena, one graph launch per pass,
+    autotuned traversal queue depth) against the same scenes rendered one
+    at a time through wpbr_ctx on the same stream."""
+    gens = [W.SceneGen(3, seed=3, res=(film_scale, max_count), level=k) for k in range(n_scenes)]
+    stream = torch.cuda.Stream()
+    dev = torch.cuda.current_device()
+    pixels = sum(g.desc.contents.camera.res_x * g.desc.contents.camera.res_y for g in gens)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    b = W.Batch(dev)
+    b.set_stream(stream.cuda_stream)
+    for g in gens:
+        b.add(g.desc)
+    t = time.perf_counter()
+    b.build()
+    build_s = time.perf_counter() - t
+    b.render_setup(spp, seed=0)
+    info = b.autotune(use_cache=True)
+    b.render()  # warm-up frame
+    b.render_setup(spp, seed=0)  # clear the films (and recapture) before the timed frame
+    b.synchronize()
+    e0.record(stream)
+    b.render()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    b.check_device_errors()
+    ms_batch = e0.elapsed_time(e1)
+    L0, w0 = b.film(0)
+    b.close()
+
+    ctxs = []
+    for g in gens:
+        c = W.Context(dev)
+        c.set_stream(stream.cuda_stream)
+        c.upload(g.desc)
+        c.build()
+        c.render_setup(spp, seed=0)
+        c.render()  # warm-up frame (captures the scene's pass graph)
+        ctxs.append(c)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for c in ctxs:
+        c.render_setup(spp, seed=0)
+        c.render()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_seq = e0.elapsed_time(e1)
+    cam = gens[0].desc.contents.camera
+    L1, w1 = ctxs[0].film(cam.res_x, cam.res_y)
+    for c in ctxs:
+        c.check_device_errors()
+        c.close()
+    same = bool((L0.view("u4") == L1.view("u4")).all() and (w0 == w1).all())
+    samples = pixels * spp
+    return {"scenes": n_scenes, "spp": spp, "total_pixels": pixels, "total_prims": info["total_prims"],
+            "arena_bytes": info["arena_bytes"], "rays_per_block": info["rays_per_block"],
+            "autotune_source": ["default", "measured", "cache", "caller"][info["autotune_source"]],
+            "msamples_per_s_batched": samples / ms_batch / 1e3, "ms_per_frame_batched": ms_batch,
+            "msamples_per_s_sequential": samples / ms_seq / 1e3, "ms_per_frame_sequential": ms_seq,
+            "speedup": ms_seq / ms_batch, "build_ms_all_scenes": build_s * 1e3,
+            "scene0_film_identical": same,
+            "graph_launches_per_frame": spp, "kernel_launches_per_frame": 5 * n_scenes * spp}
+
+
 def run_reference(args):
     import numpy as np
     import woodenpbrengine_gb300 as W
@@ -368,7 +436,8 @@ def main():
     render = None
     if rank == 0 and not args.no_render:
         render = {"c0_plain_256x256_4spp": render_rate(W, torch, 0, (256, 256), 4, frames=3),
-                  "c2_fullframe_1080p_64spp": render_rate(W, torch, 2, (1920, 1080), 64, level=LEVEL)}
+                  "c2_fullframe_1080p_64spp": render_rate(W, torch, 2, (1920, 1080), 64, level=LEVEL),
+                  "c3_batched_32_scenes_16spp": batch_rate(W, torch)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

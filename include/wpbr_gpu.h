@@ -156,7 +156,9 @@ typedef struct wpbr_scenegen wpbr_scenegen;
 enum { WPBR_SCENEGEN_RAYS = 1u };
 /* config 0 plain render, 1 LBVH microbench (level = icosphere subdivisions,
  * 0 -> 8; flag RAYS also builds res_x*res_y coherent + as many incoherent
- * rays), 2 full frame. Host-only, no GPU needed. */
+ * rays), 2 full frame, 3 scene `level` of the batched set (films scaled by
+ * res_x/1024, primitive counts capped at res_y; 1024 and 2000000 give the set
+ * as specified). Host-only, no GPU needed. */
 WPBR_API wpbr_status wpbr_scenegen_create(uint32_t config, uint32_t seed, uint32_t res_x, uint32_t res_y,
                                           uint32_t level, uint32_t flags, wpbr_scenegen** out);
 WPBR_API const wpbr_scene_desc* wpbr_scenegen_desc(const wpbr_scenegen* g);
@@ -183,6 +185,60 @@ WPBR_API void wpbr_scenegen_destroy(wpbr_scenegen* g);
 WPBR_API wpbr_status wpbr_sort_morton_noalloc(const uint32_t* d_codes, uint32_t n, uint32_t key_bits,
                                               uint32_t* d_sorted_codes, uint32_t* d_perm, void* stream);
 WPBR_API const char* wpbr_sort_morton_noalloc_error(void);
+
+/* ---- batched scenes ---------------------------------------------------------
+ * No counterpart in the reference, which renders one scene per engine
+ * (MEngine::render, MEngine.cpp:380-448). A batch holds many independent
+ * scenes of uneven size and film resolution; their traversal layouts live in
+ * one pooled device arena, and each sample pass of all scenes is one CUDA
+ * graph with one branch per scene (the five kernels of wpbr_render_pass), so a
+ * pass of every scene costs one graph launch. Each scene's film is bit-identical
+ * to rendering it alone with a wpbr_ctx and the same spp, seed and stream id.
+ * The persistent traversal grid per scene is picked by wpbr_batch_autotune. */
+typedef struct wpbr_batch wpbr_batch;
+typedef struct wpbr_batch_info {
+  uint32_t n_scenes;
+  uint32_t spp;
+  uint64_t total_pixels;      /* sum over scenes of film width x height */
+  uint64_t total_prims;
+  uint64_t arena_bytes;       /* pooled traversal arena (Node2 + primitive records) */
+  uint32_t rays_per_block;    /* traversal queue depth in effect (0 = one full wave) */
+  uint32_t autotune_source;   /* 0 default, 1 measured, 2 cache file, 3 set by caller */
+} wpbr_batch_info;
+WPBR_API wpbr_status wpbr_batch_create(int device, wpbr_batch** out);
+WPBR_API void wpbr_batch_destroy(wpbr_batch* b);
+WPBR_API const char* wpbr_batch_last_error(const wpbr_batch* b);
+/* Adds a scene (copied; same rules as wpbr_scene_upload) with its own quirk
+ * bits; *index receives its position. Only before wpbr_batch_build. */
+WPBR_API wpbr_status wpbr_batch_add_scene(wpbr_batch* b, const wpbr_scene_desc* scene, uint32_t quirks,
+                                          uint32_t* index);
+/* Builds every scene's BVH (one at a time, reusing one set of build scratch)
+ * and moves the traversal layouts into the pooled arena. */
+WPBR_API wpbr_status wpbr_batch_build(wpbr_batch* b);
+/* wpbr_render_setup for all scenes (stream id = first_stream + scene index)
+ * and captures the pass graph. */
+WPBR_API wpbr_status wpbr_batch_render_setup(wpbr_batch* b, uint32_t spp, uint32_t seed, uint32_t first_stream);
+/* Times the pass graph for each candidate traversal queue depth (rays per
+ * persistent block: one full wave, 4096, 1024, 256), keeps the fastest and
+ * records it in the cache file named by WPBR_AUTOTUNE_CACHE (default
+ * $HOME/.cache/wpbr_autotune.txt) under a key of device, scene count and film
+ * sizes; with use_cache a cached entry is taken without timing. Clears the
+ * films afterwards. */
+WPBR_API wpbr_status wpbr_batch_autotune(wpbr_batch* b, int use_cache);
+/* Sets the queue depth directly (0 = one full wave) and recaptures. */
+WPBR_API wpbr_status wpbr_batch_set_rays_per_block(wpbr_batch* b, uint32_t rays_per_block);
+/* One sample pass of every scene (one graph launch, asynchronous). */
+WPBR_API wpbr_status wpbr_batch_render_pass(wpbr_batch* b, uint32_t pass);
+/* All spp passes, asynchronous. */
+WPBR_API wpbr_status wpbr_batch_render(wpbr_batch* b);
+WPBR_API wpbr_status wpbr_batch_synchronize(wpbr_batch* b);
+WPBR_API wpbr_status wpbr_batch_info_get(const wpbr_batch* b, wpbr_batch_info* out);
+/* Film size and accumulated film of one scene (as wpbr_film_read). */
+WPBR_API wpbr_status wpbr_batch_film_size(const wpbr_batch* b, uint32_t scene, uint32_t* w, uint32_t* h);
+WPBR_API wpbr_status wpbr_batch_film_read(wpbr_batch* b, uint32_t scene, float* acc_L, float* acc_w);
+/* The stream the pass graph is launched on (default: one the batch creates). */
+WPBR_API wpbr_status wpbr_batch_set_stream(wpbr_batch* b, void* stream);
+WPBR_API wpbr_status wpbr_batch_check_device_errors(wpbr_batch* b);
 
 /* Library build identification (host-only). */
 WPBR_API const char* wpbr_version(void);

@@ -88,3 +88,32 @@ def test_camera_setup_matches_oracle(W, O, config, res, level):
     assert np.array_equal(rc.view(np.uint32), orc.view(np.uint32))
     assert np.array_equal(dx.view(np.uint32), odx.view(np.uint32))
     assert np.array_equal(dy.view(np.uint32), ody.view(np.uint32))
+
+
+def test_batched_scene_set(W):
+    # 32 scenes: primitive counts log-uniform on [10k, 2M] rounded to an
+    # icosphere level (or a sphere set), films from {256, 512, 768, 1024}^2
+    films, counts, spheres_sets = set(), [], 0
+    for k in range(32):
+        d = W.SceneGen(3, seed=3, res=(1024, 2000000), level=k).desc.contents
+        assert d.camera.res_x == d.camera.res_y
+        films.add(d.camera.res_x)
+        n = d.n_triangles + d.n_spheres - 1  # the light's sphere
+        counts.append(n)
+        spheres_sets += d.n_triangles == 0
+        assert d.n_lights == 2 and d.envmap and d.envmap.contents.width == 256  # sphere + environment
+    assert films <= {256, 512, 768, 1024} and len(films) >= 3
+    assert 10000 <= min(counts) and max(counts) <= 2000000 and len(set(counts)) >= 5
+    assert 0 < spheres_sets < 32
+    a = W.SceneGen(3, seed=3, res=(1024, 2000000), level=13).desc.contents
+    b = W.SceneGen(3, seed=3, res=(1024, 2000000), level=13).desc.contents
+    assert a.n_spheres == b.n_spheres and bytes(a.spheres[5]) == bytes(b.spheres[5])
+    small = W.SceneGen(3, seed=3, res=(128, 20000), level=1).desc.contents
+    assert small.camera.res_x in (32, 64, 96, 128) and small.n_spheres + small.n_triangles <= 20001 + 1
+
+
+def test_batch_entry_points_validate_arguments(W):
+    assert W.lib().wpbr_batch_create(0, None) == W.ERR_INVALID_ARG
+    assert W.lib().wpbr_batch_add_scene(None, None, 0, None) == W.ERR_INVALID_ARG
+    assert W.lib().wpbr_batch_info_get(None, None) == W.ERR_INVALID_ARG
+    assert W.lib().wpbr_batch_last_error(None) == b"null batch"

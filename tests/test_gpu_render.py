@@ -111,3 +111,33 @@ def test_env_distribution_matches_oracle(W, O, ctx):
         for a, b in zip(got, ref):
             assert _same(a, b)
     ctx.set_quirks(0)
+
+
+def test_pass_graph_reuse_and_invalidation(W, O, ctx):
+    # the captured pass graph survives render_setup with unchanged parameters
+    # and is recaptured when the seed, the scene or the BVH changes
+    g0 = W.SceneGen(0, 0, (48, 40))
+    g1 = W.SceneGen(2, 0, (40, 24), level=3)
+    ctx.set_quirks(0)
+    ctx.upload(g0.desc)
+    ctx.build()
+    ctx.render_setup(2, seed=0)
+    ctx.render()
+    a = ctx.film(48, 40)
+    ctx.render_setup(2, seed=0)
+    ctx.render()
+    b = ctx.film(48, 40)
+    assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32))
+    ctx.render_setup(2, seed=9)
+    ctx.render()
+    c = ctx.film(48, 40)
+    Lo, wo = O.OracleScene(g0.desc).render(48, 40, 2, 9, 0)
+    assert np.array_equal(c[0].view(np.uint32), Lo.view(np.uint32)) and np.array_equal(c[1], wo)
+    ctx.upload(g1.desc)
+    ctx.build()
+    ctx.render_setup(2, seed=9)
+    ctx.render()
+    d = ctx.film(40, 24)
+    Lo, wo = O.OracleScene(g1.desc).render(40, 24, 2, 9, 0)
+    assert np.array_equal(d[0].view(np.uint32), Lo.view(np.uint32)) and np.array_equal(d[1], wo)
+    ctx.check_device_errors()

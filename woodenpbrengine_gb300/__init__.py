@@ -68,6 +68,22 @@ _SIGS = {
     "wpbr_scenegen_destroy": (None, [_VP]),
     "wpbr_sort_morton_noalloc": (C.c_int, [_VP, C.c_uint32, C.c_uint32, _VP, _VP, _VP]),
     "wpbr_sort_morton_noalloc_error": (C.c_char_p, []),
+    "wpbr_batch_create": (C.c_int, [C.c_int, C.POINTER(_VP)]),
+    "wpbr_batch_destroy": (None, [_VP]),
+    "wpbr_batch_last_error": (C.c_char_p, [_VP]),
+    "wpbr_batch_add_scene": (C.c_int, [_VP, C.POINTER(A.SceneDesc), C.c_uint32, _UP]),
+    "wpbr_batch_build": (C.c_int, [_VP]),
+    "wpbr_batch_render_setup": (C.c_int, [_VP, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "wpbr_batch_autotune": (C.c_int, [_VP, C.c_int]),
+    "wpbr_batch_set_rays_per_block": (C.c_int, [_VP, C.c_uint32]),
+    "wpbr_batch_render_pass": (C.c_int, [_VP, C.c_uint32]),
+    "wpbr_batch_render": (C.c_int, [_VP]),
+    "wpbr_batch_synchronize": (C.c_int, [_VP]),
+    "wpbr_batch_info_get": (C.c_int, [_VP, C.POINTER(A.BatchInfo)]),
+    "wpbr_batch_film_size": (C.c_int, [_VP, C.c_uint32, _UP, _UP]),
+    "wpbr_batch_film_read": (C.c_int, [_VP, C.c_uint32, _FP, _FP]),
+    "wpbr_batch_set_stream": (C.c_int, [_VP, _VP]),
+    "wpbr_batch_check_device_errors": (C.c_int, [_VP]),
 }
 SORT_NOALLOC_MAX_KEYS = 1 << 20
 EXPORTED = sorted(_SIGS)
@@ -260,6 +276,89 @@ class Context:
         rec, arrays = A.make_record((x1 - x0) * (y1 - y0), fields)
         self._check(lib().wpbr_job_record(self._h, x0, y0, x1, y1, C.byref(rec)), "job_record")
         return arrays
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many scenes rendered together (wpbr_batch_*): pooled traversal arena,
+    one CUDA graph per sample pass, autotuned traversal queue depth."""
+
+    def __init__(self, device=0):
+        self._h = _VP()
+        st = lib().wpbr_batch_create(device, C.byref(self._h))
+        if st != OK:
+            raise WpbrError(st, "batch_create(device=%d)" % device)
+        self._keep = []
+
+    def _check(self, st, what):
+        if st != OK:
+            raise WpbrError(st, "%s: %s" % (what, lib().wpbr_batch_last_error(self._h).decode()))
+
+    def add(self, desc, quirks=0):
+        idx = C.c_uint32()
+        self._check(lib().wpbr_batch_add_scene(self._h, desc, quirks, C.byref(idx)), "batch_add_scene")
+        return idx.value
+
+    def build(self):
+        self._check(lib().wpbr_batch_build(self._h), "batch_build")
+
+    def render_setup(self, spp, seed=0, first_stream=0):
+        self._check(lib().wpbr_batch_render_setup(self._h, spp, seed, first_stream), "batch_render_setup")
+
+    def autotune(self, use_cache=True):
+        self._check(lib().wpbr_batch_autotune(self._h, 1 if use_cache else 0), "batch_autotune")
+        return self.info()
+
+    def set_rays_per_block(self, rpb):
+        self._check(lib().wpbr_batch_set_rays_per_block(self._h, rpb), "batch_set_rays_per_block")
+
+    def render_pass(self, p):
+        self._check(lib().wpbr_batch_render_pass(self._h, p), "batch_render_pass")
+
+    def render(self):
+        self._check(lib().wpbr_batch_render(self._h), "batch_render")
+
+    def synchronize(self):
+        self._check(lib().wpbr_batch_synchronize(self._h), "batch_synchronize")
+
+    def set_stream(self, stream_ptr):
+        self._check(lib().wpbr_batch_set_stream(self._h, stream_ptr), "batch_set_stream")
+
+    def check_device_errors(self):
+        self._check(lib().wpbr_batch_check_device_errors(self._h), "batch_check_device_errors")
+
+    def info(self):
+        bi = A.BatchInfo()
+        self._check(lib().wpbr_batch_info_get(self._h, C.byref(bi)), "batch_info")
+        return {f: getattr(bi, f) for f, _ in A.BatchInfo._fields_}
+
+    def film_size(self, k):
+        w, h = C.c_uint32(), C.c_uint32()
+        self._check(lib().wpbr_batch_film_size(self._h, k, C.byref(w), C.byref(h)), "batch_film_size")
+        return w.value, h.value
+
+    def film(self, k):
+        W, H = self.film_size(k)
+        L = np.zeros(W * H * 3, np.float32)
+        w = np.zeros(W * H, np.float32)
+        self._check(lib().wpbr_batch_film_read(self._h, k, _fp(L), _fp(w)), "batch_film_read")
+        return L.reshape(H, W, 3), w.reshape(H, W)
+
+    def close(self):
+        if self._h:
+            lib().wpbr_batch_destroy(self._h)
+            self._h = _VP()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
     def __del__(self):
         try:

@@ -127,3 +127,10 @@ def fptr(a):
 
 def uptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_uint32)) if a is not None else None
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [
+        ("n_scenes", C.c_uint32), ("spp", C.c_uint32), ("total_pixels", C.c_uint64), ("total_prims", C.c_uint64),
+        ("arena_bytes", C.c_uint64), ("rays_per_block", C.c_uint32), ("autotune_source", C.c_uint32),
+    ]

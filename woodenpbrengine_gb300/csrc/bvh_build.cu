@@ -1025,6 +1025,7 @@ wpbr_status bvh_build(wpbr_ctx* ctx) {
   cudaStream_t st = ctx->stream;
   const uint32_t N = ctx->N;
   B.built = false;
+  ++ctx->epoch;
   B.N = N;
   SceneView S = scene_view(ctx);
   if (N == 0) {

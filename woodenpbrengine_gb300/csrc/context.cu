@@ -79,6 +79,31 @@ cudaError_t upload(DevBuf<T>& d, const T* h, size_t n, cudaStream_t s) {
 
 }  // namespace
 
+namespace wpbr {
+// Frees the build scratch of the BVH; with keep_traversal the traversal
+// layout (Node2 array, primitive records) stays, else it goes too.
+void bvh_release(wpbr_ctx* ctx, bool keep_traversal) {
+  BvhState& B = ctx->bvh;
+  B.pb_lo.release(); B.pb_hi.release(); B.centroid.release(); B.codes.release(); B.cb_enc.release();
+  B.k0.release(); B.k1.release(); B.v0.release(); B.v1.release(); B.hist.release(); B.scan_tmp.release();
+  B.flags.release(); B.tid.release(); B.tstart.release(); B.tsize.release(); B.troot.release();
+  B.rng_lo.release(); B.rng_hi.release(); B.child0.release(); B.child1.release(); B.parent.release();
+  B.visits.release(); B.size.release(); B.nb_lo.release(); B.nb_hi.release();
+  B.cur.release(); B.nxt.release(); B.pos_seg.release(); B.bucket.release(); B.fl.release(); B.tr.release();
+  B.fscan.release(); B.tscan.release(); B.posF.release(); B.posT.release();
+  B.seg_a.release(); B.seg_b.release(); B.seg_start.release(); B.seg_end.release(); B.seg_node.release();
+  B.seg_k.release(); B.seg_mid.release(); B.seg_dim.release(); B.seg_benc.release(); B.seg_cenc.release();
+  B.seg_bucket_cnt.release(); B.seg_bucket_enc.release(); B.small_start.release(); B.small_end.release();
+  B.small_node.release(); B.counters.release(); B.sah_axis.release(); B.lin_node.release();
+  B.lin_bounds.release(); B.is_int.release(); B.int_index.release(); B.depth_max.release();
+  if (!keep_traversal) {
+    B.nodes2.release();
+    B.prims.release();
+  }
+}
+
+}  // namespace wpbr
+
 extern "C" {
 
 WPBR_API const char* wpbr_version(void) { return "wpbr-gb300 1.0 (sm_103a)"; }
@@ -123,20 +148,7 @@ WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
   ctx->tri_mat.release(); ctx->tri_flags.release(); ctx->mats.release(); ctx->lights.release();
   ctx->env_rgb.release(); ctx->cond_func.release(); ctx->cond_cdf.release(); ctx->cond_int.release();
   ctx->marg_func.release(); ctx->marg_cdf.release(); ctx->marg_int.release(); ctx->env_lum.release();
-  BvhState& B = ctx->bvh;
-  B.pb_lo.release(); B.pb_hi.release(); B.centroid.release(); B.codes.release(); B.cb_enc.release();
-  B.k0.release(); B.k1.release(); B.v0.release(); B.v1.release(); B.hist.release(); B.scan_tmp.release();
-  B.flags.release(); B.tid.release(); B.tstart.release(); B.tsize.release(); B.troot.release();
-  B.rng_lo.release(); B.rng_hi.release(); B.child0.release(); B.child1.release(); B.parent.release();
-  B.visits.release(); B.size.release(); B.nb_lo.release(); B.nb_hi.release();
-  B.cur.release(); B.nxt.release(); B.pos_seg.release(); B.bucket.release(); B.fl.release(); B.tr.release();
-  B.fscan.release(); B.tscan.release(); B.posF.release(); B.posT.release();
-  B.seg_a.release(); B.seg_b.release(); B.seg_start.release(); B.seg_end.release(); B.seg_node.release();
-  B.seg_k.release(); B.seg_mid.release(); B.seg_dim.release(); B.seg_benc.release(); B.seg_cenc.release();
-  B.seg_bucket_cnt.release(); B.seg_bucket_enc.release(); B.small_start.release(); B.small_end.release();
-  B.small_node.release(); B.counters.release(); B.sah_axis.release(); B.lin_node.release();
-  B.lin_bounds.release(); B.is_int.release(); B.int_index.release(); B.depth_max.release();
-  B.nodes2.release(); B.prims.release();
+  bvh_release(ctx, false);
   RenderState& R = ctx->rs;
   R.acc.release(); R.hit_prim.release(); R.shadow_rays.release(); R.shadow_hit.release(); R.pstate.release();
   R.Lbuf.release(); R.pfilm.release(); R.pass_dev.release(); R.counters.release();
@@ -171,6 +183,7 @@ WPBR_API wpbr_status wpbr_set_quirks(wpbr_ctx* ctx, uint32_t quirks) {
   if (quirks & ~0x1Fu) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_quirks: unknown bits");
   uint32_t changed = ctx->quirks ^ quirks;
   ctx->quirks = quirks;
+  ++ctx->epoch;
   // the sort order changes the tree; the index bug changes the env distribution
   if (changed & WPBR_Q_FULL_MORTON_SORT) ctx->bvh.built = false;
   if ((changed & WPBR_Q_ENV_DISTRIB_INDEX_BUG) && ctx->has_scene && ctx->has_env) {
@@ -250,6 +263,7 @@ WPBR_API wpbr_status wpbr_scene_upload(wpbr_ctx* ctx, const wpbr_scene_desc* d) 
 
   cudaStream_t st = ctx->stream;
   ctx->has_scene = false;
+  ++ctx->epoch;
   ctx->bvh.built = false;
   ctx->rs.ready = false;
   ctx->ns = d->n_spheres;

@@ -83,9 +83,11 @@ struct RenderState {
   DevBuf<uint32_t> u[8];
   bool graph_ok = false;
   cudaGraphExec_t graph = nullptr;
-  uint32_t graph_pass = 0xFFFFFFFFu;
+  uint64_t graph_key = 0;
   DevBuf<uint32_t> pass_dev;  // pass index read by the captured kernels
   DevBuf<uint32_t> counters;  // ray-fetch counters of the pass's traversal launches
+  const uint32_t* pass_ptr = nullptr;  // shared pass index (batches); null: pass_dev
+  uint32_t trace_grid = 0;             // persistent traversal grid cap (0: full)
 };
 
 }  // namespace wpbr
@@ -96,6 +98,7 @@ struct wpbr_ctx {
   bool own_stream = false;
   std::string err;
   uint32_t quirks = 0;
+  uint64_t epoch = 0;  // bumped by every scene upload, BVH build and quirk change
   wpbr::DevBuf<uint32_t> d_err;
   // scene
   bool has_scene = false;
@@ -134,6 +137,9 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
 wpbr_status env_preprocess(wpbr_ctx* ctx);
 wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t stream);
 wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass);
+wpbr_status render_pass_launch(wpbr_ctx* ctx);
+uint32_t persistent_full_grid();
+void bvh_release(wpbr_ctx* ctx, bool keep_traversal);
 wpbr_status job_run(wpbr_ctx* ctx, uint32_t job, uint32_t pass);
 wpbr_status job_record(wpbr_ctx* ctx, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1, wpbr_pass_record* rec);
 wpbr_status film_tonemap(wpbr_ctx* ctx, uint8_t* out);

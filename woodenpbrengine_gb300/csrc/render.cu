@@ -636,47 +636,52 @@ wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t st
   WPBR_CUDA(R.pass_dev.ensure(1));
   WPBR_CUDA(R.counters.ensure(2));  // allocated before any graph capture
   WPBR_CUDA(cudaMemsetAsync(R.acc.p, 0, n * 4 * sizeof(float), ctx->stream));
-  if (R.graph) {
-    cudaGraphExecDestroy(R.graph);
-    R.graph = nullptr;
-  }
-  R.graph_ok = false;
-  R.ready = true;
+  R.ready = true;  // a captured pass graph stays valid while pass_graph_key is unchanged
   return WPBR_OK;
 }
 
-static wpbr_status launch_fused(wpbr_ctx* ctx) {
+static uint32_t grid_for(const void* kernel, uint32_t override_grid) {
+  uint32_t full = persistent_grid(kernel);
+  return (override_grid && override_grid < full) ? override_grid : full;
+}
+
+// Launches the five kernels of one sample pass on the context's stream. The
+// pass index is read from device memory (R.pass_ptr, shared across the scenes
+// of a batch, else R.pass_dev); R.trace_grid caps the persistent traversal
+// grids (0: one full wave of resident blocks).
+wpbr_status render_pass_launch(wpbr_ctx* ctx) {
   RenderState& R = ctx->rs;
   PassCtx P = make_pass_ctx(ctx);
   uint32_t n = R.W * R.H;
   cudaStream_t st = ctx->stream;
+  const uint32_t* pass_ptr = R.pass_ptr ? R.pass_ptr : R.pass_dev.p;
   WPBR_CUDA(R.counters.ensure(2));
   WPBR_CUDA(cudaMemsetAsync(R.counters.p, 0, 2 * sizeof(uint32_t), st));
   bool deep = P.Bv.max_depth >= 60;
   {
-    CameraSrc src{P, R.pass_dev.p};
+    CameraSrc src{P, pass_ptr};
     PrimSink sink{R.hit_prim.p};
     if (deep) {
       auto k = k_trace_persistent<false, 256, CameraSrc, PrimSink>;
-      k<<<persistent_grid((const void*)k), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, n, R.counters.p, P.err);
+      k<<<grid_for((const void*)k, R.trace_grid), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, n, R.counters.p, P.err);
     } else {
       auto k = k_trace_persistent<false, 64, CameraSrc, PrimSink>;
-      k<<<persistent_grid((const void*)k), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, n, R.counters.p, P.err);
+      k<<<grid_for((const void*)k, R.trace_grid), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, n, R.counters.p, P.err);
     }
   }
-  k_spawn<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pass_dev.p, R.hit_prim.p, R.pstate.p, R.shadow_rays.p, R.Lbuf.p,
+  k_spawn<<<div_up(n, kTB), kTB, 0, st>>>(P, pass_ptr, R.hit_prim.p, R.pstate.p, R.shadow_rays.p, R.Lbuf.p,
                                           R.pfilm.p);
   {
     BufferSrc src{R.shadow_rays.p};
     PrimSink sink{R.shadow_hit.p};
     if (deep) {
       auto k = k_trace_persistent<false, 256, BufferSrc, PrimSink>;
-      k<<<persistent_grid((const void*)k), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, 2 * n, R.counters.p + 1,
-                                                                    P.err);
+      k<<<grid_for((const void*)k, R.trace_grid), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, 2 * n,
+                                                                           R.counters.p + 1, P.err);
     } else {
       auto k = k_trace_persistent<false, 64, BufferSrc, PrimSink>;
-      k<<<persistent_grid((const void*)k), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, 2 * n, R.counters.p + 1,
-                                                                    P.err);
+      k<<<grid_for((const void*)k, R.trace_grid), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, 2 * n,
+                                                                           R.counters.p + 1, P.err);
     }
   }
   k_finish<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pstate.p, R.shadow_hit.p, R.Lbuf.p);
@@ -685,17 +690,53 @@ static wpbr_status launch_fused(wpbr_ctx* ctx) {
   return WPBR_OK;
 }
 
+uint32_t persistent_full_grid() {
+  return persistent_grid((const void*)k_trace_persistent<false, 64, CameraSrc, PrimSink>);
+}
+
+// Everything the captured pass graph bakes into its kernel arguments: the
+// scene/BVH epoch, the sample-stream parameters, the film size and every
+// device pointer the five kernels receive.
+static uint64_t pass_graph_key(const wpbr_ctx* ctx) {
+  const RenderState& R = ctx->rs;
+  uint64_t h = 0xCBF29CE484222325ull;
+  auto mix = [&h](uint64_t v) {
+    for (int i = 0; i < 8; ++i) {
+      h ^= (v >> (8 * i)) & 0xFFu;
+      h *= 0x100000001B3ull;
+    }
+  };
+  mix(ctx->epoch);
+  mix(R.spp);
+  mix(R.seed);
+  mix(R.stream);
+  mix(((uint64_t)R.W << 32) | R.H);
+  mix((uint64_t)R.trace_grid);
+  const void* ptrs[] = {R.acc.p,    R.hit_prim.p, R.shadow_rays.p,     R.shadow_hit.p,      R.pstate.p,
+                        R.Lbuf.p,   R.pfilm.p,    R.pass_dev.p,        R.counters.p,        R.pass_ptr,
+                        ctx->d_err.p, ctx->bvh.view.nodes, ctx->bvh.view.prims};
+  for (const void* q : ptrs) mix((uint64_t)(uintptr_t)q);
+  return h;
+}
+
 wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass) {
   RenderState& R = ctx->rs;
   if (!R.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render_pass: render_setup not called");
   if (pass >= R.spp) return set_err(ctx, WPBR_ERR_INVALID_ARG, "render_pass: pass >= spp");
   cudaStream_t st = ctx->stream;
   WPBR_CUDA(cudaMemcpyAsync(R.pass_dev.p, &pass, 4, cudaMemcpyHostToDevice, st));
+  uint64_t key = pass_graph_key(ctx);
+  if (R.graph && R.graph_key != key) {
+    cudaGraphExecDestroy(R.graph);
+    R.graph = nullptr;
+    R.graph_ok = false;
+  }
   if (!R.graph_ok) {
+    R.graph_key = key;
     // capture the five kernels once; later passes replay the graph
     cudaGraph_t g = nullptr;
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      wpbr_status s = launch_fused(ctx);
+      wpbr_status s = render_pass_launch(ctx);
       cudaError_t e = cudaStreamEndCapture(st, &g);
       if (s == WPBR_OK && e == cudaSuccess && g) {
         if (cudaGraphInstantiate(&R.graph, g, 0) == cudaSuccess) R.graph_ok = true;
@@ -705,7 +746,7 @@ wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass) {
     // capture is not possible on the legacy default stream: clear the error
     // and launch the kernels directly
     cudaGetLastError();
-    if (!R.graph_ok) return launch_fused(ctx);
+    if (!R.graph_ok) return render_pass_launch(ctx);
   }
   WPBR_CUDA(cudaGraphLaunch(R.graph, st));
   return WPBR_OK;

@@ -480,6 +480,62 @@ void gen_config2(wpbr_scenegen* g, uint32_t seed, uint32_t W, uint32_t H, uint32
   g->set_camera(V3{0.0f, 4.0f, -16.0f}, V3{0.0f, 0.0f, 0.0f}, 60.0f, W, H);
 }
 
+// Config 3, scene k of the batched-scenes set: primitive counts log-uniform in
+// [10k, 2M] (seed 3); even scenes and counts of at least 100k are displaced
+// icospheres at the nearest subdivision level, the others random sphere sets;
+// films uniform over {256, 512, 768, 1024}^2; one sphere light and a
+// 256x128 procedural environment light. Film sides are scaled by
+// film_scale/1024 and counts capped at max_count (1024 and 2M give the set as
+// specified; smaller values give a quick test set of the same shape).
+void gen_config3(wpbr_scenegen* g, uint32_t k, uint32_t seed, uint32_t film_scale, uint32_t max_count) {
+  Rng pick(seed, 0xC3000u + k);
+  double lo = std::log(10000.0), hi = std::log(2000000.0);
+  double count = std::exp(lo + (hi - lo) * (double)pick.u01());
+  if (count > (double)max_count) count = (double)max_count;
+  static const uint32_t films[4] = {256, 512, 768, 1024};
+  uint32_t res = (uint32_t)(((uint64_t)films[pick.next_u32() % 4] * film_scale) / 1024u);
+  if (res < 8) res = 8;
+  float ce[3] = {0.9f, 0.6f, 0.3f}, ck[3] = {2.0f, 2.5f, 3.0f};
+  uint32_t m_cond = g->add_material(WPBR_MAT_CONDUCTOR, 0.2f, ce, ck);
+  float de[3] = {1.5f, 1.5f, 1.5f}, dk[3] = {0, 0, 0};
+  uint32_t m_diel = g->add_material(WPBR_MAT_DIELECTRIC, 0.3f, de, dk);
+  bool mesh = (k % 2 == 0) || count >= 100000.0;
+  if (mesh) {
+    uint32_t level = 0;
+    double best = 1e30;
+    for (uint32_t L = 3; L <= 9; ++L) {
+      double c = 20.0 * std::pow(4.0, (double)L);
+      double dlog = std::fabs(std::log(c) - std::log(count));
+      if (dlog < best) {
+        best = dlog;
+        level = L;
+      }
+    }
+    if (level > 8) level = 8;
+    g->add_icosphere(level, 3.0, 0.1, seed + k, V3{0, 0, 0}, m_cond);
+  } else {
+    uint32_t ns = (uint32_t)count;
+    Rng rs(seed + k, 0x5F5u);
+    float extent = 4.0f * std::cbrt((float)ns / 10000.0f);
+    for (uint32_t i = 0; i < ns; ++i) {
+      V3 c{rs.uni(-extent, extent), rs.uni(-extent, extent), rs.uni(-extent, extent)};
+      g->add_sphere(c, rs.uni(0.02f, 0.12f), (i & 1) ? m_diel : m_cond);
+    }
+  }
+  float le[3] = {1.5f, 1.5f, 1.5f}, lk[3] = {1.0f, 1.0f, 1.0f};
+  uint32_t ml = g->add_material(WPBR_MAT_CONDUCTOR, 0.3f, le, lk);
+  g->add_sphere(V3{0.0f, 9.0f, -3.0f}, 1.0f, ml);
+  wpbr_light L;
+  memset(&L, 0, sizeof(L));
+  L.type = WPBR_LIGHT_SPHERE;
+  L.sphere_index = (uint32_t)g->spheres.size() - 1;
+  L.Le[0] = L.Le[1] = L.Le[2] = 40.0f;
+  g->lights.push_back(L);
+  g->make_env(256, 128, seed + k);
+  float dist = mesh ? 9.0f : 3.2f * (4.0f * std::cbrt((float)count / 10000.0f));
+  g->set_camera(V3{0.0f, 0.35f * dist, -dist}, V3{0.0f, 0.0f, 0.0f}, 50.0f, res, res);
+}
+
 }  // namespace
 
 extern "C" {
@@ -498,6 +554,10 @@ WPBR_API wpbr_status wpbr_scenegen_create(uint32_t config, uint32_t seed, uint32
       gen_config1(g, seed, res_x, res_y, level ? level : 8, (flags & WPBR_SCENEGEN_RAYS) != 0);
     } else if (config == 2) {
       gen_config2(g, seed, res_x, res_y, level ? level : 8, 1024, 512);
+      g->finish();
+    } else if (config == 3) {
+      // `level` selects the scene of the set; res_x scales the films, res_y caps the counts
+      gen_config3(g, level, seed, res_x, res_y);
       g->finish();
     } else {
       delete g;
