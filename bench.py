@@ -232,6 +232,119 @@ def batch_rate(W, torch, n_scenes=32, spp=16, film_scale=1024, max_count=2000000
             "graph_launches_per_frame": spp, "kernel_launches_per_frame": 5 * n_scenes * spp}
 
 
+def _c4_params(desc):
+    import numpy as np
+
+    d = desc.contents
+    mats = [d.materials[i] for i in range(d.n_materials)]
+    mat = np.array([[m.alpha_x, *m.R, *m.eta_t, *m.k] for m in mats], np.float32).reshape(-1)
+    e = d.envmap.contents
+    env = np.ctypeslib.as_array(e.rgb, shape=(e.width * e.height * 3,)).astype(np.float32)
+    return mat, env
+
+
+def adjoint_rate(W, torch, res=(512, 512), spp=16, n_fd=64, n_fp64=64, fp64=True):
+    """Differentiable estimator on the config-4 scene (512x512, 16 spp, 64
+    materials x 10 parameters + a 256x128 RGB environment = 98,944
+    parameters): forward + backward time, gradient parameters/s, the rate of
+    central differences (h = 1e-3) through the same forward, their agreement,
+    and the FP64 oracle's dual-number gradient on a subset."""
+    import numpy as np
+
+    g0 = W.SceneGen(4, 0, res, level=0)
+    g1 = W.SceneGen(4, 0, res, level=1)
+    dev = torch.cuda.current_device()
+    stream = torch.cuda.Stream()
+    ctx = W.Context(dev)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload(g0.desc)
+    ctx.build()
+    nm, ne = ctx.adjoint_setup(spp, seed=0, stream=0)
+    m0, e0 = _c4_params(g0.desc)
+    mh, eh = _c4_params(g1.desc)
+    ctx.adjoint_set_params(mh, eh)
+    ctx.adjoint_freeze()
+    target, _ = ctx.adjoint_forward(*res)
+    ctx.adjoint_set_params(m0, e0)
+    ctx.adjoint_freeze()
+    n = res[0] * res[1]
+    with torch.cuda.stream(stream):
+        d_target = torch.from_numpy(target.reshape(-1).copy()).to("cuda")
+        d_gm = torch.zeros(nm, device="cuda")
+        d_ge = torch.zeros(ne, device="cuda")
+    torch.cuda.synchronize()
+    e0_ = torch.cuda.Event(enable_timing=True)
+    e1_ = torch.cuda.Event(enable_timing=True)
+    e2_ = torch.cuda.Event(enable_timing=True)
+    for _ in range(2):  # warm-up
+        ctx.adjoint_forward_device(d_target.data_ptr())
+        ctx.adjoint_backward_device(d_gm.data_ptr(), d_ge.data_ptr())
+    reps = 3
+    fwd_ms = bwd_ms = 0.0
+    for _ in range(reps):
+        e0_.record(stream)
+        loss = ctx.adjoint_forward_device(d_target.data_ptr())
+        e1_.record(stream)
+        ctx.adjoint_backward_device(d_gm.data_ptr(), d_ge.data_ptr())
+        e2_.record(stream)
+        torch.cuda.synchronize()
+        fwd_ms += e0_.elapsed_time(e1_) / reps
+        bwd_ms += e1_.elapsed_time(e2_) / reps
+    grad = np.concatenate([d_gm.cpu().numpy(), d_ge.cpu().numpy()])
+    # end to end through the host-buffer entry points
+    t = time.perf_counter()
+    img, _ = ctx.adjoint_forward(*res, target)
+    gm_h, ge_h = ctx.adjoint_backward()
+    e2e_s = time.perf_counter() - t
+    # central differences through the same forward
+    rng = np.random.default_rng(4)
+    sel = np.concatenate([rng.choice(nm, n_fd // 2, replace=False),
+                          nm + rng.choice(np.nonzero(grad[nm:])[0], n_fd // 2, replace=False)])
+    h = 1e-3
+    fd = np.zeros(n_fd)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for k, i in enumerate(sel):
+        vals = []
+        for s in (+1, -1):
+            m, e = m0.copy(), e0.copy()
+            if i < nm:
+                m[i] += s * h
+            else:
+                e[i - nm] += s * h
+            ctx.adjoint_set_params(m, e)
+            vals.append(ctx.adjoint_forward_device(d_target.data_ptr()))
+        fd[k] = (vals[0] - vals[1]) / (2 * h)
+    fd_s = time.perf_counter() - t
+    ctx.adjoint_set_params(m0, e0)
+    ctx.check_device_errors()
+    ctx.close()
+    g_sel = grad[sel]
+    out = {"film": "%dx%d" % res, "spp": spp, "params": int(nm + ne), "loss": loss,
+           "forward_ms": fwd_ms, "backward_ms": bwd_ms,
+           "gradient_params_per_s": (nm + ne) / ((fwd_ms + bwd_ms) / 1e3),
+           "fd_params_per_s": n_fd / fd_s, "fd_h": h,
+           "speedup_vs_fd": ((nm + ne) / ((fwd_ms + bwd_ms) / 1e3)) / (n_fd / fd_s),
+           "rel_err_vs_fd32_norm": float(np.linalg.norm(g_sel - fd) / np.linalg.norm(fd)),
+           "e2e_forward_backward_s": e2e_s, "msamples_per_s_forward": n * spp / fwd_ms / 1e3,
+           "kernel_launches": {"forward_per_pass": 5, "backward_per_pass": 4}}
+    if fp64:
+        from oracle import binding as O
+
+        o = O.OracleScene(g0.desc)
+        sub = np.concatenate([sel[: n_fp64 // 2], sel[n_fd // 2: n_fd // 2 + n_fp64 // 2]])
+        t = time.perf_counter()
+        _, _, g64 = o.adjoint_eval(res[0], res[1], spp, 0, 0, m0.astype(np.float64), e0.astype(np.float64),
+                                   target, sub)
+        gs = grad[sub]
+        floor = 1e-2 * np.abs(g64).max()
+        out["fp64"] = {"params": int(len(sub)), "seconds": time.perf_counter() - t,
+                       "rel_err_max": float(np.max(np.abs(gs - g64) / np.maximum(np.abs(g64), floor))),
+                       "rel_err_norm": float(np.linalg.norm(gs - g64) / np.linalg.norm(g64)),
+                       "cores": O.lib().orc_num_threads()}
+    return out
+
+
 def run_reference(args):
     import numpy as np
     import woodenpbrengine_gb300 as W
@@ -437,7 +550,8 @@ def main():
     if rank == 0 and not args.no_render:
         render = {"c0_plain_256x256_4spp": render_rate(W, torch, 0, (256, 256), 4, frames=3),
                   "c2_fullframe_1080p_64spp": render_rate(W, torch, 2, (1920, 1080), 64, level=LEVEL),
-                  "c3_batched_32_scenes_16spp": batch_rate(W, torch)}
+                  "c3_batched_32_scenes_16spp": batch_rate(W, torch),
+                  "c4_adjoint_512x512_16spp": adjoint_rate(W, torch, fp64=not args.no_cpu)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -158,7 +158,9 @@ enum { WPBR_SCENEGEN_RAYS = 1u };
  * 0 -> 8; flag RAYS also builds res_x*res_y coherent + as many incoherent
  * rays), 2 full frame, 3 scene `level` of the batched set (films scaled by
  * res_x/1024, primitive counts capped at res_y; 1024 and 2000000 give the set
- * as specified). Host-only, no GPU needed. */
+ * as specified), 4 the differentiable scene (config 0's geometry, 64
+ * materials, sphere + 256x128 environment light; `level` seeds the material
+ * parameters and the environment). Host-only, no GPU needed. */
 WPBR_API wpbr_status wpbr_scenegen_create(uint32_t config, uint32_t seed, uint32_t res_x, uint32_t res_y,
                                           uint32_t level, uint32_t flags, wpbr_scenegen** out);
 WPBR_API const wpbr_scene_desc* wpbr_scenegen_desc(const wpbr_scenegen* g);
@@ -239,6 +241,36 @@ WPBR_API wpbr_status wpbr_batch_film_read(wpbr_batch* b, uint32_t scene, float* 
 /* The stream the pass graph is launched on (default: one the batch creates). */
 WPBR_API wpbr_status wpbr_batch_set_stream(wpbr_batch* b, void* stream);
 WPBR_API wpbr_status wpbr_batch_check_device_errors(wpbr_batch* b);
+
+/* ---- differentiable estimator (forward / backward) -----------------------------
+ * No counterpart in the reference (it renders forward only). Gradients of the
+ * image loss  sum_pixels sum_rgb (I - T)^2 / (3 W H),  I = filtered film
+ * radiance of wpbr_adjoint_setup's spp passes, with respect to
+ *  - per material m, 10 floats at mat_params[10 m]: alpha (sets alpha_x and
+ *    alpha_y), albedo R[3], eta_t[3] (a dielectric uses eta_t[0]), k[3];
+ *  - the environment texels, 3 floats per texel in row order (env_params).
+ * The differentiated function is the frozen-direction estimator: directions,
+ * hits and visibility come from the sampling parameters captured by
+ * wpbr_adjoint_freeze; BSDF values, pdfs, MIS weights and emitted / incident
+ * radiance are evaluated at the current parameters (wpbr_adjoint_set_params).
+ * At equal parameters its image is MEngine::render's (MEngine.cpp:393-442)
+ * up to rounding. wpbr_adjoint_backward replays the sample passes (no stored
+ * paths) and needs a wpbr_adjoint_forward with a target at the current
+ * parameters. Samples whose radiance is not finite contribute zero. */
+WPBR_API wpbr_status wpbr_adjoint_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t stream);
+WPBR_API wpbr_status wpbr_adjoint_param_counts(wpbr_ctx* ctx, uint32_t* n_mat_params, uint32_t* n_env_params);
+WPBR_API wpbr_status wpbr_adjoint_get_params(wpbr_ctx* ctx, float* mat_params, float* env_params);
+/* NULL keeps the current values of that group. */
+WPBR_API wpbr_status wpbr_adjoint_set_params(wpbr_ctx* ctx, const float* mat_params, const float* env_params);
+WPBR_API wpbr_status wpbr_adjoint_set_params_device(wpbr_ctx* ctx, const float* d_mat_params,
+                                                    const float* d_env_params);
+WPBR_API wpbr_status wpbr_adjoint_freeze(wpbr_ctx* ctx);
+/* target and image: W*H*3 floats (NULL: no loss / no image); *loss receives
+ * the loss when a target is given. */
+WPBR_API wpbr_status wpbr_adjoint_forward(wpbr_ctx* ctx, const float* target, float* image, double* loss);
+WPBR_API wpbr_status wpbr_adjoint_forward_device(wpbr_ctx* ctx, const float* d_target, float* d_image, double* loss);
+WPBR_API wpbr_status wpbr_adjoint_backward(wpbr_ctx* ctx, float* grad_mat, float* grad_env);
+WPBR_API wpbr_status wpbr_adjoint_backward_device(wpbr_ctx* ctx, float* d_grad_mat, float* d_grad_env);
 
 /* Library build identification (host-only). */
 WPBR_API const char* wpbr_version(void);

@@ -35,6 +35,9 @@ _SIGS = {
     "orc_philox": (None, [_UP, _UP, _UP]),
     "orc_fmath": (None, [C.c_int, _FP, _FP, _FP, C.c_uint64]),
     "orc_fmath_d": (None, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint64]),
+    "orc_adjoint_eval": (C.c_double, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double), _FP, C.POINTER(C.c_double), C.c_uint32, _UP,
+                                      C.POINTER(C.c_double)]),
 }
 _lib = None
 
@@ -124,6 +127,21 @@ class OracleScene:
         rec, arrays = A.make_record((x1 - x0) * (y1 - y0), fields)
         lib().orc_render_pass(self._h, p, spp, seed, stream, x0, y0, x1, y1, C.byref(rec))
         return arrays
+
+    def adjoint_eval(self, W, H, spp, seed, stream, mat, env, target=None, sel=None, image=False):
+        """FP64 frozen-direction estimator at parameters (mat, env): returns
+        (loss, image or None, gradient at the indices `sel` or None)."""
+        dp = C.POINTER(C.c_double)
+        mat = np.ascontiguousarray(mat, np.float64)
+        env = np.ascontiguousarray(env if env is not None else np.zeros(0), np.float64)
+        tgt = np.ascontiguousarray(target, np.float32) if target is not None else None
+        img = np.zeros(W * H * 3, np.float64) if image else None
+        sel_a = np.ascontiguousarray(sel, np.uint32) if sel is not None else np.zeros(0, np.uint32)
+        g = np.zeros(len(sel_a), np.float64)
+        loss = lib().orc_adjoint_eval(self._h, spp, seed, stream, mat.ctypes.data_as(dp), env.ctypes.data_as(dp),
+                                      _fp(tgt), img.ctypes.data_as(dp) if img is not None else None, len(sel_a),
+                                      _up(sel_a), g.ctypes.data_as(dp))
+        return loss, (img.reshape(H, W, 3) if img is not None else None), (g if sel is not None else None)
 
     def render(self, W, H, spp, seed=0, stream=0):
         L = np.zeros(W * H * 3, np.float32)

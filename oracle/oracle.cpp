@@ -11,6 +11,7 @@
  * golden vectors and cannot be built here.
  */
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -1111,6 +1112,8 @@ static Scene* scene_from_desc(const wpbr_scene_desc* d, uint32_t quirks) {
   return sc;
 }
 
+#include "oracle_adjoint.inc"
+
 }  // namespace orc
 
 /* ------------------------------------------------------------------------ */
@@ -1301,5 +1304,36 @@ void orc_fmath_d(int fn, const double* x, double* out, uint64_t n) {
 float orc_sample1d(uint32_t seed, uint32_t stream, uint32_t spp, uint32_t pixel, uint32_t pass, uint32_t dim) {
   wpbr_rng::Stream rs{seed, stream, spp};
   return wpbr_rng::sample1d(rs, pixel, pass, dim);
+}
+/* The FP64 frozen-direction estimator: sampling parameters are the scene's
+ * own; mat (nmat*10) and env (W*H*3) are the evaluation parameters. Returns
+ * the loss against target (0 without); image (W*H*3) optional; grad receives
+ * dLoss/dparam for the n_sel parameter indices in sel (materials first, then
+ * texels), by dual numbers. */
+double orc_adjoint_eval(void* h, uint32_t spp, uint32_t seed, uint32_t stream, const double* mat, const double* env,
+                        const float* target, double* image, uint32_t n_sel, const uint32_t* sel, double* grad) {
+  const Scene& sc = *(const Scene*)h;
+  std::vector<Frozen> fz = freeze_all(sc, spp, seed, stream);
+  EvalParams<double> P;
+  load_params(sc, mat, env, P);
+  if (sc.has_env) eval_env_distribution(sc.env, sc.quirks, P);
+  double loss = eval_loss(sc, fz, spp, P, target, image);
+  const size_t nm = sc.mats.size() * 10;
+  constexpr int K = 8;
+  for (uint32_t b = 0; b < n_sel; b += K) {
+    EvalParams<Dual<K>> D;
+    load_params(sc, mat, env, D);
+    for (int k = 0; k < K && b + k < n_sel; ++k) {
+      uint32_t idx = sel[b + k];
+      if (idx < nm)
+        D.mat[idx].d[k] = 1.0;
+      else
+        D.env[idx - nm].d[k] = 1.0;
+    }
+    if (sc.has_env) eval_env_distribution(sc.env, sc.quirks, D);
+    Dual<K> l = eval_loss(sc, fz, spp, D, target, nullptr);
+    for (int k = 0; k < K && b + k < n_sel; ++k) grad[b + k] = l.d[k];
+  }
+  return loss;
 }
 }

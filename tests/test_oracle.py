@@ -85,3 +85,45 @@ def test_golden_fixtures(W, O):
     assert set(ref.files) == set(now)
     for k in ref.files:
         assert np.array_equal(ref[k].view(np.uint8), np.asarray(now[k]).view(np.uint8)), k
+
+
+def test_fp64_estimator_dual_gradient_matches_central_differences(W, O):
+    # the oracle's FP64 frozen-direction estimator: its image at the scene's
+    # own parameters is the oracle render's, and its dual-number gradient
+    # matches central differences of its own loss
+    g0 = W.SceneGen(4, 0, (40, 32), level=0)
+    g1 = W.SceneGen(4, 0, (40, 32), level=1)
+
+    def params(g):
+        d = g.desc.contents
+        m = np.array([[x.alpha_x, *x.R, *x.eta_t, *x.k] for x in [d.materials[i] for i in range(d.n_materials)]],
+                     np.float64).reshape(-1)
+        e = np.ctypeslib.as_array(d.envmap.contents.rgb, shape=(256 * 128 * 3,)).astype(np.float64)
+        return m, e
+
+    m0, e0 = params(g0)
+    m1, e1 = params(g1)
+    o = O.OracleScene(g0.desc)
+    _, img0, _ = o.adjoint_eval(40, 32, 2, 0, 0, m0, e0, None, None, image=True)
+    L, w = o.render(40, 32, 2, 0, 0)
+    I = L / w[..., None]
+    ok = np.isfinite(I)
+    assert np.max(np.abs(img0 - I)[ok] / np.maximum(np.abs(I[ok]), 1e-6)) < 1e-4
+    _, target, _ = O.OracleScene(g1.desc).adjoint_eval(40, 32, 2, 0, 0, m1, e1, None, None, image=True)
+    target = target.astype(np.float32)
+    rng = np.random.default_rng(4)
+    sel = np.concatenate([rng.choice(m0.size, 6, replace=False), m0.size + rng.choice(e0.size, 2000, replace=False)])
+    loss, _, grad = o.adjoint_eval(40, 32, 2, 0, 0, m0, e0, target, sel)
+    keep = np.concatenate([np.arange(6), 6 + np.nonzero(grad[6:])[0][:4]])
+    h = 1e-4
+    for k in keep:
+        i = sel[k]
+        mp, ep, mm, em = m0.copy(), e0.copy(), m0.copy(), e0.copy()
+        if i < m0.size:
+            mp[i] += h
+            mm[i] -= h
+        else:
+            ep[i - m0.size] += h
+            em[i - m0.size] -= h
+        fd = (o.adjoint_eval(40, 32, 2, 0, 0, mp, ep, target)[0] - o.adjoint_eval(40, 32, 2, 0, 0, mm, em, target)[0]) / (2 * h)
+        assert abs(grad[k] - fd) <= 1e-4 * max(abs(fd), 1e-3 * np.abs(grad).max()), (i, grad[k], fd)

@@ -68,6 +68,16 @@ _SIGS = {
     "wpbr_scenegen_destroy": (None, [_VP]),
     "wpbr_sort_morton_noalloc": (C.c_int, [_VP, C.c_uint32, C.c_uint32, _VP, _VP, _VP]),
     "wpbr_sort_morton_noalloc_error": (C.c_char_p, []),
+    "wpbr_adjoint_setup": (C.c_int, [_VP, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "wpbr_adjoint_param_counts": (C.c_int, [_VP, _UP, _UP]),
+    "wpbr_adjoint_get_params": (C.c_int, [_VP, _FP, _FP]),
+    "wpbr_adjoint_set_params": (C.c_int, [_VP, _FP, _FP]),
+    "wpbr_adjoint_set_params_device": (C.c_int, [_VP, _VP, _VP]),
+    "wpbr_adjoint_freeze": (C.c_int, [_VP]),
+    "wpbr_adjoint_forward": (C.c_int, [_VP, _FP, _FP, C.POINTER(C.c_double)]),
+    "wpbr_adjoint_forward_device": (C.c_int, [_VP, _VP, _VP, C.POINTER(C.c_double)]),
+    "wpbr_adjoint_backward": (C.c_int, [_VP, _FP, _FP]),
+    "wpbr_adjoint_backward_device": (C.c_int, [_VP, _VP, _VP]),
     "wpbr_batch_create": (C.c_int, [C.c_int, C.POINTER(_VP)]),
     "wpbr_batch_destroy": (None, [_VP]),
     "wpbr_batch_last_error": (C.c_char_p, [_VP]),
@@ -276,6 +286,57 @@ class Context:
         rec, arrays = A.make_record((x1 - x0) * (y1 - y0), fields)
         self._check(lib().wpbr_job_record(self._h, x0, y0, x1, y1, C.byref(rec)), "job_record")
         return arrays
+
+    # ---- differentiable estimator (wpbr_adjoint_*) ----
+    def adjoint_setup(self, spp, seed=0, stream=0):
+        self._check(lib().wpbr_adjoint_setup(self._h, spp, seed, stream), "adjoint_setup")
+        nm, ne = C.c_uint32(), C.c_uint32()
+        self._check(lib().wpbr_adjoint_param_counts(self._h, C.byref(nm), C.byref(ne)), "adjoint_param_counts")
+        self._adj_counts = (nm.value, ne.value)
+        return self._adj_counts
+
+    def adjoint_params(self):
+        nm, ne = self._adj_counts
+        m = np.zeros(nm, np.float32)
+        e = np.zeros(ne, np.float32)
+        self._check(lib().wpbr_adjoint_get_params(self._h, _fp(m), _fp(e) if ne else None), "adjoint_get_params")
+        return m, e
+
+    def adjoint_set_params(self, mat=None, env=None):
+        m = np.ascontiguousarray(mat, np.float32) if mat is not None else None
+        e = np.ascontiguousarray(env, np.float32) if env is not None else None
+        self._check(lib().wpbr_adjoint_set_params(self._h, _fp(m), _fp(e)), "adjoint_set_params")
+
+    def adjoint_set_params_device(self, d_mat=None, d_env=None):
+        self._check(lib().wpbr_adjoint_set_params_device(self._h, d_mat, d_env), "adjoint_set_params_device")
+
+    def adjoint_freeze(self):
+        self._check(lib().wpbr_adjoint_freeze(self._h), "adjoint_freeze")
+
+    def adjoint_forward(self, W, H, target=None):
+        """Returns (image (H, W, 3), loss or None)."""
+        img = np.zeros(W * H * 3, np.float32)
+        t = np.ascontiguousarray(target, np.float32).reshape(-1) if target is not None else None
+        loss = C.c_double(0.0)
+        self._check(lib().wpbr_adjoint_forward(self._h, _fp(t), _fp(img), C.byref(loss)), "adjoint_forward")
+        return img.reshape(H, W, 3), (loss.value if target is not None else None)
+
+    def adjoint_forward_device(self, d_target, d_image=None):
+        loss = C.c_double(0.0)
+        self._check(lib().wpbr_adjoint_forward_device(self._h, d_target, d_image, C.byref(loss)),
+                    "adjoint_forward_device")
+        return loss.value
+
+    def adjoint_backward(self):
+        """Returns (material gradient (n_mat_params,), environment gradient (n_env_params,))."""
+        nm, ne = self._adj_counts
+        gm = np.zeros(nm, np.float32)
+        ge = np.zeros(ne, np.float32)
+        self._check(lib().wpbr_adjoint_backward(self._h, _fp(gm), _fp(ge) if ne else None), "adjoint_backward")
+        return gm, ge
+
+    def adjoint_backward_device(self, d_grad_mat, d_grad_env):
+        self._check(lib().wpbr_adjoint_backward_device(self._h, d_grad_mat, d_grad_env), "adjoint_backward_device")
 
     def __del__(self):
         try:

@@ -155,6 +155,7 @@ WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
   ctx->io_rays.release(); ctx->io_hits.release(); ctx->io_stats.release(); ctx->trace_counter.release();
   for (auto& f : R.f) f.release();
   for (auto& u : R.u) u.release();
+  ctx->adj.release();
   delete ctx;
 }
 

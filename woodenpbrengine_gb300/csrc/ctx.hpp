@@ -90,6 +90,35 @@ struct RenderState {
   uint32_t trace_grid = 0;             // persistent traversal grid cap (0: full)
 };
 
+// State of the differentiable estimator (adjoint.cu): sampling (_s) and
+// evaluation (_e) parameters, per-pixel replay state, gradients.
+struct AdjState {
+  bool ready = false;
+  uint32_t spp = 0, seed = 0, stream = 0, W = 0, H = 0, nmat = 0;
+  size_t n_texels = 0;
+  uint64_t param_gen = 0, fwd_gen = 0;
+  float Z_s = 0.0f, Z_e = 0.0f;
+  std::vector<wpbr_material> h_mats;
+  DevBuf<wpbr_material> mats_s, mats_e;
+  DevBuf<float4> rgb_s, rgb_e;
+  DevBuf<float> s_func, s_cdf, s_int, s_mfunc, s_mcdf, s_mint;
+  DevBuf<float> e_func, e_cdf, e_int, e_mfunc, e_mcdf, e_mint;
+  DevBuf<float> mat_prm, env_prm, target, image, g_env, g_func;
+  DevBuf<double> g_mat, g_scalar;
+  DevBuf<float4> state, rays, Lb, acc, gpix;
+  DevBuf<float2> pf;
+  DevBuf<uint32_t> hit_prim, shadow_hit, pass_dev, counters;
+  void release() {
+    mats_s.release(); mats_e.release(); rgb_s.release(); rgb_e.release();
+    s_func.release(); s_cdf.release(); s_int.release(); s_mfunc.release(); s_mcdf.release(); s_mint.release();
+    e_func.release(); e_cdf.release(); e_int.release(); e_mfunc.release(); e_mcdf.release(); e_mint.release();
+    mat_prm.release(); env_prm.release(); target.release(); image.release(); g_env.release(); g_func.release();
+    g_mat.release(); g_scalar.release(); state.release(); rays.release(); Lb.release(); acc.release();
+    gpix.release(); pf.release(); hit_prim.release(); shadow_hit.release(); pass_dev.release(); counters.release();
+    ready = false;
+  }
+};
+
 }  // namespace wpbr
 
 struct wpbr_ctx {
@@ -121,6 +150,7 @@ struct wpbr_ctx {
   wpbr::CameraParams cam{};
   wpbr::BvhState bvh;
   wpbr::RenderState rs;
+  wpbr::AdjState adj;
   // staging for the host-buffer collide entry points
   wpbr::DevBuf<float4> io_rays, io_hits;
   wpbr::DevBuf<uint32_t> io_stats;
@@ -135,6 +165,12 @@ wpbr_status bvh_build(wpbr_ctx* ctx);
 wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* d_hits, uint32_t mode,
                        uint32_t* d_stats);
 wpbr_status env_preprocess(wpbr_ctx* ctx);
+// Distribution2D of an environment image (JobLightInfiniteAreaPreprocessSampling)
+// into caller-owned arrays: cond_func/cond_cdf/cond_int of H rows of W, marg_* of H.
+struct EnvDist {
+  float *cond_func, *cond_cdf, *cond_int, *marg_func, *marg_cdf, *marg_int;
+};
+wpbr_status env_distribution_build(wpbr_ctx* ctx, const float4* rgb, const EnvDist& out, float* marg_int_host);
 wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t stream);
 wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass);
 wpbr_status render_pass_launch(wpbr_ctx* ctx);
@@ -143,6 +179,12 @@ void bvh_release(wpbr_ctx* ctx, bool keep_traversal);
 wpbr_status job_run(wpbr_ctx* ctx, uint32_t job, uint32_t pass);
 wpbr_status job_record(wpbr_ctx* ctx, uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1, wpbr_pass_record* rec);
 wpbr_status film_tonemap(wpbr_ctx* ctx, uint8_t* out);
+wpbr_status adjoint_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t stream);
+wpbr_status adjoint_get_params(wpbr_ctx* ctx, float* mat, float* env);
+wpbr_status adjoint_set_params(wpbr_ctx* ctx, const float* mat, const float* env, bool device);
+wpbr_status adjoint_freeze(wpbr_ctx* ctx);
+wpbr_status adjoint_forward(wpbr_ctx* ctx, const float* target, float* image, double* loss, bool device);
+wpbr_status adjoint_backward(wpbr_ctx* ctx, float* grad_mat, float* grad_env, bool device);
 // scan helper (exclusive, in place allowed): out[i] = sum in[0..i); returns total in *total_dev (device, may be null)
 cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, DevBuf<uint32_t>& tmp, cudaStream_t s);
 }  // namespace wpbr

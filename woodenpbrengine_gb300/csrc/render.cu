@@ -12,16 +12,13 @@
 
 #include "common.cuh"
 #include "ctx.hpp"
-#include "shade.cuh"
+#include "pass.cuh"
 #include "traverse.cuh"
 #include "traverse_persistent.cuh"
-#include "wpbr_sampling.h"
 
 namespace wpbr {
 
 namespace {
-
-constexpr int kTB = 128;
 
 // Staged-path field slots (float and uint buffers in RenderState).
 enum FF {
@@ -42,117 +39,6 @@ struct Staged {
   float* f[F_COUNT];
   uint32_t* u[U_COUNT];
 };
-
-struct PassCtx {
-  SceneView S;
-  BvhView Bv;
-  wpbr_rng::Stream rs;
-  uint32_t W, H;
-  uint32_t* err;
-};
-
-__device__ __forceinline__ V3 ld3(const float* f, uint32_t i) { return V3{f[3 * i], f[3 * i + 1], f[3 * i + 2]}; }
-__device__ __forceinline__ void st3(float* f, uint32_t i, V3 v) {
-  f[3 * i] = v.x;
-  f[3 * i + 1] = v.y;
-  f[3 * i + 2] = v.z;
-}
-__device__ __forceinline__ RGB3 ldc(const float* f, uint32_t i) { return RGB3{f[3 * i], f[3 * i + 1], f[3 * i + 2]}; }
-__device__ __forceinline__ void stc(float* f, uint32_t i, RGB3 c) {
-  f[3 * i] = c.r;
-  f[3 * i + 1] = c.g;
-  f[3 * i + 2] = c.b;
-}
-
-__device__ __forceinline__ uint32_t prim_material(const SceneView& S, uint32_t prim) {
-  return prim < S.ns ? S.sph_mat[prim] : S.tri_mat[prim - S.ns];
-}
-
-// Full interaction for the winning primitive: re-runs its intersection test
-// (identical bits) and builds the surface interaction.
-__device__ SurfInt make_si(const SceneView& S, uint32_t prim, V3 o, V3 d) {
-  if (prim < S.ns) {
-    V3 rlo, rld, ph;
-    sphere_intersect(S.sph_w2o[prim], S.sph_r[prim], o, d, &rlo, &rld, &ph);
-    return sphere_si(S.sph_o2w[prim], S.sph_w2o[prim], S.sph_r[prim], rld, ph);
-  }
-  uint32_t t = prim - S.ns;
-  const uint32_t* ix = S.idx + 3 * (size_t)t;
-  TriData td;
-  uint32_t fl = S.tri_flags[t];
-  td.has_ns = (fl & WPBR_MESH_NORMALS_TANGENTS) != 0;
-  td.has_uv = (fl & WPBR_MESH_UVS) != 0;
-  for (int k = 0; k < 3; ++k) {
-    uint32_t v = ix[k];
-    td.p[k] = V3{S.pos[3 * v], S.pos[3 * v + 1], S.pos[3 * v + 2]};
-    td.n[k] = td.has_ns ? V3{S.nrm[3 * v], S.nrm[3 * v + 1], S.nrm[3 * v + 2]} : V3{0, 0, 0};
-    td.s[k] = td.has_ns ? V3{S.tan[3 * v], S.tan[3 * v + 1], S.tan[3 * v + 2]} : V3{0, 0, 0};
-    td.uv[k] = td.has_uv ? V2{S.uv[2 * v], S.uv[2 * v + 1]} : V2{0, 0};
-  }
-  float b0, b1, b2;
-  tri_intersect(td.p[0], td.p[1], td.p[2], o, d, S.quirks, &b0, &b1, &b2);
-  return triangle_si(td, d, b0, b1, b2);
-}
-
-__device__ __forceinline__ void pixel_xy(uint32_t pix, uint32_t W, uint32_t* x, uint32_t* y) {
-  *x = pix % W;
-  *y = pix / W;
-}
-
-// JobSamplerUpdateCameraSamples (CSSampler.cpp:7-23): pFilm = pixel + u2
-__device__ __forceinline__ void camera_sample(const PassCtx& P, uint32_t pix, uint32_t pass, float* fx, float* fy) {
-  uint32_t x, y;
-  pixel_xy(pix, P.W, &x, &y);
-  float u0, u1;
-  wpbr_rng::sample2d(P.rs, pix, pass, wpbr_rng::DIM_CAMERA, &u0, &u1);
-  *fx = (float)x + u0;
-  *fy = (float)y + u1;
-}
-
-// JobScatteringSampleLight (SScattering.cpp:82-88), index clamped
-__device__ __forceinline__ uint32_t pick_light(const PassCtx& P, uint32_t pix, uint32_t pass) {
-  uint32_t nl = P.S.nlights;
-  float ul = wpbr_rng::sample1d(P.rs, pix, pass, wpbr_rng::DIM_LIGHT_PICK);
-  float fl = (ul + 0.5f) * (float)(nl - 1);
-  uint32_t li = (uint32_t)fl;
-  return li > nl - 1 ? nl - 1 : li;
-}
-
-struct LightSample {
-  V3 wi;
-  RGB3 li;
-  float pdf;
-  bool ok;
-};
-__device__ LightSample sample_light(const PassCtx& P, const wpbr_light& lt, V3 p, uint32_t pix, uint32_t pass) {
-  float u0, u1;
-  wpbr_rng::sample2d(P.rs, pix, pass, wpbr_rng::DIM_LIGHT, &u0, &u1);
-  LightSample s;
-  s.wi = V3{0, 0, 0};
-  s.li = rgb1(0.0f);
-  s.pdf = 0.0f;
-  s.ok = true;
-  if (lt.type == WPBR_LIGHT_SPHERE) {
-    sphere_light_sample(P.S.sph_o2w[lt.sphere_index], P.S.sph_r[lt.sphere_index], p, u0, u1, &s.wi, &s.pdf);
-    s.li = RGB3{lt.Le[0], lt.Le[1], lt.Le[2]};
-  } else {
-    env_li_sample(P.S.env, P.S.quirks, u0, u1, &s.wi, &s.li, &s.pdf, &s.ok);
-  }
-  return s;
-}
-
-__device__ void light_compute(const PassCtx& P, const wpbr_light& lt, V3 p, V3 wi, RGB3* li, float* pdf) {
-  if (lt.type == WPBR_LIGHT_SPHERE) {
-    *pdf = sphere_light_pdf(P.S.sph_o2w[lt.sphere_index], P.S.sph_r[lt.sphere_index], p, P.S.quirks);
-    *li = RGB3{lt.Le[0], lt.Le[1], lt.Le[2]};
-  } else {
-    env_li_compute(P.S.env, wi, li, pdf);
-  }
-}
-
-__device__ __forceinline__ uint32_t light_prim(const wpbr_light& lt) {
-  return lt.type == WPBR_LIGHT_SPHERE ? lt.sphere_index : 0xFFFFFFFEu;
-}
 
 __device__ __forceinline__ uint32_t trace_closest(const PassCtx& P, V3 o, V3 d) {
   HitRec h = P.Bv.max_depth < 60 ? trace_ray<false, 64>(P.S, P.Bv, o, d, inf_(), nullptr, nullptr, P.err)
@@ -329,39 +215,6 @@ __global__ void kj_integrate_bsdf(PassCtx P, Staged G) {
   stc(G.f[F_L], pix, radd(ldc(G.f[F_L], pix), c));
 }
 
-// JobAccumalateLIFromSamples (CSFilm.cpp:70-122) as a gather: each pixel
-// sums, in the reference's row-major sample order, the Mitchell-weighted
-// samples of its 32x32 tile whose splat footprint covers it.
-__device__ void film_gather(uint32_t W, uint32_t H, uint32_t x, uint32_t y, const float2* pf, const float4* Lb,
-                            float4* acc) {
-  uint32_t tx0 = (x / 32) * 32, ty0 = (y / 32) * 32;
-  uint32_t tx1 = min(tx0 + 31, W - 1), ty1 = min(ty0 + 31, H - 1);
-  float4 a = acc[(size_t)y * W + x];
-  RGB3 L{a.x, a.y, a.z};
-  float ws = a.w;
-  int sy0 = max((int)ty0, (int)y - 2), sy1 = min((int)ty1, (int)y + 2);
-  int sx0 = max((int)tx0, (int)x - 2), sx1 = min((int)tx1, (int)x + 2);
-  for (int sy = sy0; sy <= sy1; ++sy)
-    for (int sx = sx0; sx <= sx1; ++sx) {
-      size_t sp = (size_t)sy * W + sx;
-      float2 f = pf[sp];
-      float dx0 = f.x - 0.5f, dy0 = f.y - 0.5f;
-      int pminx = (int)ceilf(dx0 - 2.0f), pmaxx = (int)floorf(dx0 + 2.0f);
-      int pminy = (int)ceilf(dy0 - 2.0f), pmaxy = (int)floorf(dy0 + 2.0f);
-      pminx = max(pminx, (int)tx0);
-      pminy = max(pminy, (int)ty0);
-      pmaxx = min(pmaxx, (int)tx1);
-      pmaxy = min(pmaxy, (int)ty1);
-      if ((int)x < pminx || (int)x > pmaxx || (int)y < pminy || (int)y > pmaxy) continue;
-      float w = mitchell1(((float)x - f.x) / 2.0f) * mitchell1(((float)y - f.y) / 2.0f);
-      float4 s = Lb[sp];
-      RGB3 c{s.x, s.y, s.z};
-      if (!rblack(c)) L = radd(L, rmuls(c, w));
-      ws = ws + w;
-    }
-  acc[(size_t)y * W + x] = make_float4(L.r, L.g, L.b, ws);
-}
-
 __global__ void kj_film_pack(PassCtx P, Staged G, float2* pf, float4* Lb) {
   uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= P.W * P.H) return;
@@ -380,19 +233,6 @@ __global__ void k_film(uint32_t W, uint32_t H, const float2* pf, const float4* L
 // Compact per-pixel state written by k_spawn and read by k_finish.
 constexpr int kStateF4 = 6;
 enum : uint32_t { SF_VALID = 1u, SF_TRACE_L = 2u, SF_TRACE_B = 4u, SF_HIT = 8u };
-
-// Camera rays generated inside the persistent traversal's ray source.
-struct CameraSrc {
-  PassCtx P;
-  const uint32_t* pass_dev;
-  __device__ __forceinline__ void load(uint32_t pix, float4* o, float4* d) const {
-    float fx, fy;
-    camera_sample(P, pix, *pass_dev, &fx, &fy);
-    RayD r = camera_ray(P.S.cam, fx, fy);
-    *o = make_float4(r.o.x, r.o.y, r.o.z, 0.0f);
-    *d = make_float4(r.d.x, r.d.y, r.d.z, inf_());
-  }
-};
 
 __global__ void __launch_bounds__(kTB) k_spawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
                                                float4* state, float4* rays, float4* Lb, float2* pf) {
@@ -598,21 +438,27 @@ wpbr_status ensure_staged(wpbr_ctx* ctx) {
 
 }  // namespace
 
-wpbr_status env_preprocess(wpbr_ctx* ctx) {
-  if (!ctx->has_env) return WPBR_OK;
+wpbr_status env_distribution_build(wpbr_ctx* ctx, const float4* rgb, const EnvDist& out, float* marg_int_host) {
   SceneView S = scene_view(ctx);
+  S.env.rgb = rgb;
   uint32_t W = ctx->envW, H = ctx->envH;
   cudaStream_t st = ctx->stream;
-  k_env_lum<<<div_up((uint64_t)W * H, 256), 256, 0, st>>>(S.env, ctx->cond_func.p, ctx->quirks);
-  k_distrib_rows<<<div_up(H, 64), 64, 0, st>>>(ctx->cond_func.p, W, H, ctx->cond_cdf.p, ctx->cond_int.p);
-  WPBR_CUDA(cudaMemcpyAsync(ctx->marg_func.p, ctx->cond_int.p, sizeof(float) * H, cudaMemcpyDeviceToDevice, st));
-  k_distrib_rows<<<1, 32, 0, st>>>(ctx->marg_func.p, H, 1, ctx->marg_cdf.p, ctx->marg_int.p);
+  k_env_lum<<<div_up((uint64_t)W * H, 256), 256, 0, st>>>(S.env, out.cond_func, ctx->quirks);
+  k_distrib_rows<<<div_up(H, 64), 64, 0, st>>>(out.cond_func, W, H, out.cond_cdf, out.cond_int);
+  WPBR_CUDA(cudaMemcpyAsync(out.marg_func, out.cond_int, sizeof(float) * H, cudaMemcpyDeviceToDevice, st));
+  k_distrib_rows<<<1, 32, 0, st>>>(out.marg_func, H, 1, out.marg_cdf, out.marg_int);
   WPBR_CUDA(cudaGetLastError());
   float mi = 0.0f;
-  WPBR_CUDA(cudaMemcpyAsync(&mi, ctx->marg_int.p, 4, cudaMemcpyDeviceToHost, st));
+  WPBR_CUDA(cudaMemcpyAsync(&mi, out.marg_int, 4, cudaMemcpyDeviceToHost, st));
   WPBR_CUDA(cudaStreamSynchronize(st));
-  ctx->env_marg_int = mi;
+  *marg_int_host = mi;
   return WPBR_OK;
+}
+
+wpbr_status env_preprocess(wpbr_ctx* ctx) {
+  if (!ctx->has_env) return WPBR_OK;
+  EnvDist d{ctx->cond_func.p, ctx->cond_cdf.p, ctx->cond_int.p, ctx->marg_func.p, ctx->marg_cdf.p, ctx->marg_int.p};
+  return env_distribution_build(ctx, ctx->env_rgb.p, d, &ctx->env_marg_int);
 }
 
 wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t stream) {

@@ -375,6 +375,45 @@ void gen_config0(wpbr_scenegen* g, uint32_t seed, uint32_t W, uint32_t H) {
   g->set_camera(V3{0.0f, 3.0f, -30.0f}, V3{0.0f, -2.0f, 0.0f}, 60.0f, W, H);
 }
 
+// Config 4, the differentiable-rendering scene: config 0's geometry (seed
+// `seed`), one material per sphere (64; the ground quad and the light sphere
+// share material 0) and a 256x128 environment light beside the sphere light.
+// The material parameters and the environment come from `param_seed`:
+// alternating conductor (alpha U[.05,.5], R U[.4,1]^3, eta, k U[.2,3]^3) and
+// dielectric microfacet (alpha U[.05,.5], R U[.4,1]^3, eta U[1.3,1.7]).
+void gen_config4(wpbr_scenegen* g, uint32_t seed, uint32_t param_seed, uint32_t W, uint32_t H) {
+  Rng rng(seed, 0xC0u);
+  Rng prm(param_seed, 0xC4u);
+  for (int i = 0; i < 64; ++i) {
+    V3 c{rng.uni(-10.0f, 10.0f), rng.uni(-10.0f, 10.0f), rng.uni(-10.0f, 10.0f)};
+    float r = rng.uni(0.2f, 1.0f);
+    float alpha = prm.uni(0.05f, 0.5f);
+    float R[3] = {prm.uni(0.4f, 1.0f), prm.uni(0.4f, 1.0f), prm.uni(0.4f, 1.0f)};
+    uint32_t m;
+    if ((i & 1) == 0) {
+      float eta[3] = {prm.uni(0.2f, 3.0f), prm.uni(0.2f, 3.0f), prm.uni(0.2f, 3.0f)};
+      float k[3] = {prm.uni(0.2f, 3.0f), prm.uni(0.2f, 3.0f), prm.uni(0.2f, 3.0f)};
+      m = g->add_material(WPBR_MAT_CONDUCTOR, alpha, eta, k);
+    } else {
+      float e = prm.uni(1.3f, 1.7f);
+      float eta[3] = {e, e, e}, k[3] = {0, 0, 0};
+      m = g->add_material(WPBR_MAT_DIELECTRIC, alpha, eta, k);
+    }
+    for (int ch = 0; ch < 3; ++ch) g->mats[m].R[ch] = R[ch];
+    g->add_sphere(c, r, m);
+  }
+  g->add_sphere(V3{0.0f, 15.0f, 0.0f}, 1.0f, 0);
+  wpbr_light L;
+  memset(&L, 0, sizeof(L));
+  L.type = WPBR_LIGHT_SPHERE;
+  L.sphere_index = (uint32_t)g->spheres.size() - 1;
+  L.Le[0] = L.Le[1] = L.Le[2] = 10.0f;
+  g->lights.push_back(L);
+  g->add_quad(40.0f, 40.0f, V3{0.0f, -11.0f, 0.0f}, 0);
+  g->make_env(256, 128, 0xC4E0u + param_seed);
+  g->set_camera(V3{0.0f, 3.0f, -30.0f}, V3{0.0f, -2.0f, 0.0f}, 60.0f, W, H);
+}
+
 void gen_config1(wpbr_scenegen* g, uint32_t seed, uint32_t W, uint32_t H, uint32_t level, bool with_rays) {
   float e[3] = {1.5f, 1.5f, 1.5f}, k[3] = {1, 1, 1};
   uint32_t m = g->add_material(WPBR_MAT_CONDUCTOR, 0.2f, e, k);
@@ -554,6 +593,9 @@ WPBR_API wpbr_status wpbr_scenegen_create(uint32_t config, uint32_t seed, uint32
       gen_config1(g, seed, res_x, res_y, level ? level : 8, (flags & WPBR_SCENEGEN_RAYS) != 0);
     } else if (config == 2) {
       gen_config2(g, seed, res_x, res_y, level ? level : 8, 1024, 512);
+      g->finish();
+    } else if (config == 4) {
+      gen_config4(g, seed, level, res_x, res_y);  // `level` is the parameter seed
       g->finish();
     } else if (config == 3) {
       // `level` selects the scene of the set; res_x scales the films, res_y caps the counts

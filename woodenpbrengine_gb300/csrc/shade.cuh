@@ -420,21 +420,29 @@ WPBR_HD RGB3 env_le(const EnvView& e, V3 d) {
 }
 // JobLightInfiniteAreaLiSample (CLightInfiniteArea.cpp:163-204): the looked-up
 // radiance is discarded unless WPBR_Q_ENV_LI_SAMPLE_FIX.
+// uv_st (optional) receives the sampled map coordinates and sin(theta).
 WPBR_HD void env_li_sample(const EnvView& e, uint32_t quirks, float u0, float u1, V3* wi, RGB3* li, float* pdf,
-                           bool* ok) {
+                           bool* ok, float* uv_st = nullptr) {
   float uv0, uv1, map_pdf;
   env_sample_uv(e, u0, u1, &uv0, &uv1, &map_pdf);
   *li = rgb1(0.0f);
   *ok = false;
+  float st = 0.0f;
   if (map_pdf != 0.0f) {
     float theta = (float)((double)uv1 * kPI);
     float phi = (float)((double)(uv0 * 2.0f) * kPI);
-    float ct = cosf_(theta), st = sinf_(theta);
+    float ct = cosf_(theta);
+    st = sinf_(theta);
     *wi = xvector(e.l2w, sph_dir(st, ct, phi));
     *pdf = (st != 0.0f) ? (float)((double)map_pdf / (((2.0 * kPI) * kPI) * (double)st)) : 0.0f;
     *ok = true;
   }
   if (quirks & WPBR_Q_ENV_LI_SAMPLE_FIX) *li = rmul(env_bilerp(e, uv0, uv1), e.le);
+  if (uv_st) {
+    uv_st[0] = uv0;
+    uv_st[1] = uv1;
+    uv_st[2] = st;
+  }
 }
 // JobLightInfiniteAreaLiCompute (CLightInfiniteArea.cpp:206-237)
 WPBR_HD void env_li_compute(const EnvView& e, V3 wi, RGB3* li, float* pdf) {
