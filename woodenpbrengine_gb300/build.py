@@ -91,6 +91,25 @@ def build_library(force=False, verbose=False, extra_nvcc=()):
     return LIB
 
 
+HOST_SRC = os.path.join(PKG, "host", "wpbr_host.cpp")
+HOST_BIN = os.path.join(PKG, "wpbr_host")
+
+
+def build_host(force=False):
+    """Compile the C++17 host runner (host/wpbr_host.cpp) against libwpbr_gpu.so."""
+    lib = build_library()
+    deps = [HOST_SRC, os.path.join(PKG, "host", "scene_io.hpp"), os.path.join(INC, "wpbr_gpu.h"), lib]
+    if not force and not _stale(HOST_BIN, deps):
+        return HOST_BIN
+    cxx = os.environ.get("CXX", "g++")
+    tmp = HOST_BIN + ".tmp"
+    _run([cxx, "-O2", "-std=c++17", "-Wall", "-I" + INC, HOST_SRC, "-o", tmp, "-L" + PKG, "-lwpbr_gpu",
+          "-Wl,-rpath,$ORIGIN"])
+    os.replace(tmp, HOST_BIN)
+    return HOST_BIN
+
+
 if __name__ == "__main__":
     path = build_library(force="--force" in sys.argv, verbose="-v" in sys.argv)
     print(path)
+    print(build_host(force="--force" in sys.argv))
