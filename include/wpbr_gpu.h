@@ -64,6 +64,12 @@ WPBR_API void* wpbr_get_stream(const wpbr_ctx* ctx);
 /* wpbr_quirk bits (wpbr_scene.h); applies to later builds and renders. */
 WPBR_API wpbr_status wpbr_set_quirks(wpbr_ctx* ctx, uint32_t quirks);
 WPBR_API wpbr_status wpbr_synchronize(wpbr_ctx* ctx);
+/* Traversal layout (an implementation choice of this library; the results
+ * are the same): BINARY (default) traverses the child-pair layout of the
+ * reference's tree; WIDE a four-wide collapse of it, built by the next
+ * wpbr_bvh_build after the mode is set. */
+enum wpbr_traversal { WPBR_TRAVERSAL_BINARY = 0, WPBR_TRAVERSAL_WIDE = 1 };
+WPBR_API wpbr_status wpbr_set_traversal(wpbr_ctx* ctx, uint32_t mode);
 /* Device error word (traversal limits etc.) since the last call; cleared. */
 WPBR_API wpbr_status wpbr_check_device_errors(wpbr_ctx* ctx);
 

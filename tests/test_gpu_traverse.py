@@ -66,3 +66,33 @@ def test_degenerate_rays_and_quirk(W, O, ctx):
         ho = O.OracleScene(g.desc, q).trace(rays, mode=0)
         _check(hg, ho)
     ctx.set_quirks(0)
+
+
+@pytest.mark.parametrize("config,level,res", [(1, 6, (128, 128)), (0, 0, (64, 64)), (2, 4, (64, 36))])
+def test_wide_and_binary_traversals_agree(W, O, ctx, config, level, res):
+    # the four-wide layout is collapsed from the same binary tree and visits
+    # leaves in the binary near-first order: identical hits, ties included
+    g = W.SceneGen(config, 0, res, level=level, rays=(config == 1))
+    ctx.set_quirks(0)
+    ctx.set_traversal(W.TRAVERSAL_WIDE)
+    ctx.upload(g.desc)
+    ctx.build()
+    if config == 1:
+        rays = g.rays()
+    else:
+        rng = np.random.default_rng(3)
+        n = 30000
+        rays = np.zeros((n, 8), np.float32)
+        rays[:, :3] = rng.uniform(-12, 12, (n, 3))
+        d = rng.normal(size=(n, 3))
+        rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+        rays[:, 7] = np.inf
+    hw = ctx.collide(rays)
+    aw = ctx.collide(rays, mode=W.TRACE_ANY)
+    ctx.set_traversal(W.TRAVERSAL_BINARY)
+    hb = ctx.collide(rays)
+    ab = ctx.collide(rays, mode=W.TRACE_ANY)
+    assert np.array_equal(hw.view(np.uint32), hb.view(np.uint32))
+    assert np.array_equal(aw[:, 1].view(np.uint32) == 0xFFFFFFFF, ab[:, 1].view(np.uint32) == 0xFFFFFFFF)
+    _check(hw, O.OracleScene(g.desc).trace(rays, mode=0))
+    ctx.check_device_errors()

@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(_HERE, "libwpbr_gpu.so")
 
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TRAVERSAL_LIMIT, ERR_NOT_BUILT, ERR_NO_DEVICE = range(7)
 TRACE_CLOSEST, TRACE_ANY = 0, 1
+TRAVERSAL_BINARY, TRAVERSAL_WIDE = 0, 1
 Q_TRI_PERMUTATION_BUG, Q_ENV_LI_SAMPLE_FIX, Q_SPHERE_PDF_FIX, Q_ENV_DISTRIB_INDEX_BUG, Q_FULL_MORTON_SORT = (
     1, 2, 4, 8, 16)
 MAT_CONDUCTOR, MAT_DIELECTRIC, MAT_SPECULAR = 0, 1, 2
@@ -43,6 +44,7 @@ _SIGS = {
     "wpbr_get_stream": (_VP, [_VP]),
     "wpbr_set_quirks": (C.c_int, [_VP, C.c_uint32]),
     "wpbr_synchronize": (C.c_int, [_VP]),
+    "wpbr_set_traversal": (C.c_int, [_VP, C.c_uint32]),
     "wpbr_check_device_errors": (C.c_int, [_VP]),
     "wpbr_scene_upload": (C.c_int, [_VP, C.POINTER(A.SceneDesc)]),
     "wpbr_camera_info": (C.c_int, [_VP, _FP, _FP, _FP]),
@@ -196,6 +198,9 @@ class Context:
 
     def set_quirks(self, q):
         self._check(lib().wpbr_set_quirks(self._h, q), "set_quirks")
+
+    def set_traversal(self, mode):
+        self._check(lib().wpbr_set_traversal(self._h, mode), "set_traversal")
 
     def synchronize(self):
         self._check(lib().wpbr_synchronize(self._h), "synchronize")

@@ -558,7 +558,7 @@ AdjView adj_view(const wpbr_ctx* ctx) {
 PassCtx adj_pass_ctx(wpbr_ctx* ctx) {
   PassCtx P;
   P.S = scene_view(ctx);
-  P.Bv = ctx->bvh.view;
+  P.Bv = traversal_view(ctx);
   P.rs = wpbr_rng::Stream{ctx->adj.seed, ctx->adj.stream, ctx->adj.spp};
   P.W = ctx->adj.W;
   P.H = ctx->adj.H;
@@ -580,32 +580,10 @@ wpbr_status replay_pass(wpbr_ctx* ctx, const PassCtx& P, const AdjView& A, uint3
   uint32_t n = J.W * J.H;
   WPBR_CUDA(cudaMemcpyAsync(J.pass_dev.p, &pass, 4, cudaMemcpyHostToDevice, st));
   WPBR_CUDA(cudaMemsetAsync(J.counters.p, 0, 2 * sizeof(uint32_t), st));
-  bool deep = P.Bv.max_depth >= 60;
-  {
-    CameraSrc src{P, J.pass_dev.p};
-    PrimSink sink{J.hit_prim.p};
-    if (deep) {
-      auto k = k_trace_persistent<false, 256, CameraSrc, PrimSink>;
-      k<<<persistent_grid((const void*)k), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, n, J.counters.p, P.err);
-    } else {
-      auto k = k_trace_persistent<false, 64, CameraSrc, PrimSink>;
-      k<<<persistent_grid((const void*)k), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, n, J.counters.p, P.err);
-    }
-  }
+  launch_traversal<false>(P.S, P.Bv, CameraSrc{P, J.pass_dev.p}, PrimSink{J.hit_prim.p}, n, J.counters.p, P.err, st);
   k_adj_spawn<<<div_up(n, kTB), kTB, 0, st>>>(P, A, J.pass_dev.p, J.hit_prim.p, J.state.p, J.rays.p, J.pf.p);
-  {
-    BufferSrc src{J.rays.p};
-    PrimSink sink{J.shadow_hit.p};
-    if (deep) {
-      auto k = k_trace_persistent<false, 256, BufferSrc, PrimSink>;
-      k<<<persistent_grid((const void*)k), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, 2 * n, J.counters.p + 1,
-                                                                    P.err);
-    } else {
-      auto k = k_trace_persistent<false, 64, BufferSrc, PrimSink>;
-      k<<<persistent_grid((const void*)k), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, 2 * n, J.counters.p + 1,
-                                                                    P.err);
-    }
-  }
+  launch_traversal<false>(P.S, P.Bv, BufferSrc{J.rays.p}, PrimSink{J.shadow_hit.p}, 2 * n, J.counters.p + 1, P.err,
+                          st);
   WPBR_CUDA(cudaGetLastError());
   return WPBR_OK;
 }

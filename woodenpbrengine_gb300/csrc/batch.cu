@@ -2,7 +2,7 @@
 //
 // A batch owns one wpbr_ctx per scene (scene buffers, per-pixel render state,
 // film) and one pooled device arena holding every scene's traversal layout
-// (Node2 array followed by the primitive records, each block 256-byte
+// (Node2 array, Node4 array and primitive records, each block 256-byte
 // aligned). A sample pass of all scenes is one CUDA graph: a fork event on the
 // batch stream, one branch per scene with the five kernels of the fused pass
 // (render_pass_launch) on that scene's stream, and a join back. All branches
@@ -284,20 +284,22 @@ WPBR_API wpbr_status wpbr_batch_build(wpbr_batch* b) {
   if (b->scenes.empty()) return berr(b, WPBR_ERR_INVALID_ARG, "batch_build: no scenes");
   cudaSetDevice(b->device);
   // build one scene at a time; each frees its build scratch before the next
-  std::vector<uint64_t> off_nodes(b->scenes.size()), off_prims(b->scenes.size());
+  std::vector<uint64_t> off_nodes(b->scenes.size()), off_wide(b->scenes.size()), off_prims(b->scenes.size());
   uint64_t total = 0, prims = 0;
+  auto block = [&total](uint64_t bytes) {
+    uint64_t at = total;
+    total += (bytes + 255) & ~(uint64_t)255;
+    return at;
+  };
   for (size_t k = 0; k < b->scenes.size(); ++k) {
     wpbr_ctx* c = b->scenes[k];
     wpbr_status st = bvh_build(c);
     if (st != WPBR_OK) return from_scene(b, k, st);
     bvh_release(c, true);
     const BvhView& v = c->bvh.view;
-    uint64_t nb = v.empty ? 0 : (uint64_t)v.n_int * sizeof(Node2);
-    uint64_t pb = v.empty ? 0 : (uint64_t)3 * v.n_prims * sizeof(float4);
-    off_nodes[k] = total;
-    total += (nb + 255) & ~(uint64_t)255;
-    off_prims[k] = total;
-    total += (pb + 255) & ~(uint64_t)255;
+    off_nodes[k] = block(v.empty ? 0 : (uint64_t)v.n_int * sizeof(Node2));
+    off_wide[k] = block(v.nodes4 ? (uint64_t)v.n_wide * sizeof(Node4) : 0);
+    off_prims[k] = block(v.empty ? 0 : (uint64_t)3 * v.n_prims * sizeof(float4));
     prims += c->N;
   }
   // one arena for every traversal layout
@@ -306,18 +308,24 @@ WPBR_API wpbr_status wpbr_batch_build(wpbr_batch* b) {
     wpbr_ctx* c = b->scenes[k];
     BvhView& v = c->bvh.view;
     Node2* nd = (Node2*)(b->arena.p + off_nodes[k]);
+    Node4* wd = (Node4*)(b->arena.p + off_wide[k]);
     float4* pd = (float4*)(b->arena.p + off_prims[k]);
     if (!v.empty) {
       if (v.n_int)
         BATCH_CUDA(cudaMemcpyAsync(nd, v.nodes, (size_t)v.n_int * sizeof(Node2), cudaMemcpyDeviceToDevice,
+                                   c->stream));
+      if (v.nodes4)
+        BATCH_CUDA(cudaMemcpyAsync(wd, v.nodes4, (size_t)v.n_wide * sizeof(Node4), cudaMemcpyDeviceToDevice,
                                    c->stream));
       BATCH_CUDA(cudaMemcpyAsync(pd, v.prims, (size_t)3 * v.n_prims * sizeof(float4), cudaMemcpyDeviceToDevice,
                                  c->stream));
     }
     BATCH_CUDA(cudaStreamSynchronize(c->stream));
     c->bvh.nodes2.release();
+    c->bvh.nodes4.release();
     c->bvh.prims.release();
     v.nodes = nd;
+    if (v.nodes4) v.nodes4 = wd;
     v.prims = pd;
   }
   b->arena_bytes = total;

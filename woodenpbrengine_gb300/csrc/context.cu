@@ -96,8 +96,11 @@ void bvh_release(wpbr_ctx* ctx, bool keep_traversal) {
   B.seg_bucket_cnt.release(); B.seg_bucket_enc.release(); B.small_start.release(); B.small_end.release();
   B.small_node.release(); B.counters.release(); B.sah_axis.release(); B.lin_node.release();
   B.lin_bounds.release(); B.is_int.release(); B.int_index.release(); B.depth_max.release();
+  B.wq_bin0.release(); B.wq_bin1.release(); B.wq_wide0.release(); B.wq_wide1.release();
+  B.wcnt.release(); B.woff.release();
   if (!keep_traversal) {
     B.nodes2.release();
+    B.nodes4.release();
     B.prims.release();
   }
 }
@@ -196,6 +199,14 @@ WPBR_API wpbr_status wpbr_set_quirks(wpbr_ctx* ctx, uint32_t quirks) {
     cudaGraphExecDestroy(ctx->rs.graph);
     ctx->rs.graph = nullptr;
   }
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_set_traversal(wpbr_ctx* ctx, uint32_t mode) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  if (mode > WPBR_TRAVERSAL_WIDE) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_traversal: unknown mode");
+  ctx->traversal = mode;
+  ++ctx->epoch;
   return WPBR_OK;
 }
 

@@ -62,6 +62,8 @@ struct BvhState {
   DevBuf<float> lin_bounds;   // M*6
   DevBuf<uint32_t> is_int, int_index, depth_max;
   DevBuf<Node2> nodes2;
+  DevBuf<Node4> nodes4;
+  DevBuf<uint32_t> wq_bin0, wq_bin1, wq_wide0, wq_wide1, wcnt, woff;  // wide collapse queues
   DevBuf<float4> prims;
   BvhView view{};
 };
@@ -127,7 +129,8 @@ struct wpbr_ctx {
   bool own_stream = false;
   std::string err;
   uint32_t quirks = 0;
-  uint64_t epoch = 0;  // bumped by every scene upload, BVH build and quirk change
+  uint64_t epoch = 0;  // bumped by every scene upload, BVH build, quirk or traversal change
+  uint32_t traversal = 0;  // wpbr_traversal: 0 binary, 1 wide (collapsed at build time)
   wpbr::DevBuf<uint32_t> d_err;
   // scene
   bool has_scene = false;
@@ -158,6 +161,13 @@ struct wpbr_ctx {
 };
 
 namespace wpbr {
+// The BVH view the traversal kernels receive (the wide layout only when the
+// context asks for the wide traversal).
+inline BvhView traversal_view(const wpbr_ctx* ctx) {
+  BvhView v = ctx->bvh.view;
+  if (ctx->traversal != 1) v.nodes4 = nullptr;
+  return v;
+}
 wpbr_status set_err(wpbr_ctx* ctx, wpbr_status st, const std::string& msg);
 wpbr_status cuda_err(wpbr_ctx* ctx, cudaError_t e, const char* what);
 SceneView scene_view(const wpbr_ctx* ctx);

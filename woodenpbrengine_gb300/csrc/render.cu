@@ -414,7 +414,7 @@ __global__ void k_tonemap(uint32_t n, const float4* acc, uint8_t* out) {
 PassCtx make_pass_ctx(wpbr_ctx* ctx) {
   PassCtx P;
   P.S = scene_view(ctx);
-  P.Bv = ctx->bvh.view;
+  P.Bv = traversal_view(ctx);
   P.rs = wpbr_rng::Stream{ctx->rs.seed, ctx->rs.stream, ctx->rs.spp};
   P.W = ctx->rs.W;
   P.H = ctx->rs.H;
@@ -486,10 +486,6 @@ wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t st
   return WPBR_OK;
 }
 
-static uint32_t grid_for(const void* kernel, uint32_t override_grid) {
-  uint32_t full = persistent_grid(kernel);
-  return (override_grid && override_grid < full) ? override_grid : full;
-}
 
 // Launches the five kernels of one sample pass on the context's stream. The
 // pass index is read from device memory (R.pass_ptr, shared across the scenes
@@ -503,33 +499,12 @@ wpbr_status render_pass_launch(wpbr_ctx* ctx) {
   const uint32_t* pass_ptr = R.pass_ptr ? R.pass_ptr : R.pass_dev.p;
   WPBR_CUDA(R.counters.ensure(2));
   WPBR_CUDA(cudaMemsetAsync(R.counters.p, 0, 2 * sizeof(uint32_t), st));
-  bool deep = P.Bv.max_depth >= 60;
-  {
-    CameraSrc src{P, pass_ptr};
-    PrimSink sink{R.hit_prim.p};
-    if (deep) {
-      auto k = k_trace_persistent<false, 256, CameraSrc, PrimSink>;
-      k<<<grid_for((const void*)k, R.trace_grid), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, n, R.counters.p, P.err);
-    } else {
-      auto k = k_trace_persistent<false, 64, CameraSrc, PrimSink>;
-      k<<<grid_for((const void*)k, R.trace_grid), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, n, R.counters.p, P.err);
-    }
-  }
+  launch_traversal<false>(P.S, P.Bv, CameraSrc{P, pass_ptr}, PrimSink{R.hit_prim.p}, n, R.counters.p, P.err, st,
+                          R.trace_grid);
   k_spawn<<<div_up(n, kTB), kTB, 0, st>>>(P, pass_ptr, R.hit_prim.p, R.pstate.p, R.shadow_rays.p, R.Lbuf.p,
                                           R.pfilm.p);
-  {
-    BufferSrc src{R.shadow_rays.p};
-    PrimSink sink{R.shadow_hit.p};
-    if (deep) {
-      auto k = k_trace_persistent<false, 256, BufferSrc, PrimSink>;
-      k<<<grid_for((const void*)k, R.trace_grid), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, 2 * n,
-                                                                           R.counters.p + 1, P.err);
-    } else {
-      auto k = k_trace_persistent<false, 64, BufferSrc, PrimSink>;
-      k<<<grid_for((const void*)k, R.trace_grid), kPersistBlock, 0, st>>>(P.S, P.Bv, src, sink, 2 * n,
-                                                                           R.counters.p + 1, P.err);
-    }
-  }
+  launch_traversal<false>(P.S, P.Bv, BufferSrc{R.shadow_rays.p}, PrimSink{R.shadow_hit.p}, 2 * n, R.counters.p + 1,
+                          P.err, st, R.trace_grid);
   k_finish<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pstate.p, R.shadow_hit.p, R.Lbuf.p);
   k_film<<<div_up(n, kTB), kTB, 0, st>>>(R.W, R.H, R.pfilm.p, R.Lbuf.p, (float4*)R.acc.p);
   WPBR_CUDA(cudaGetLastError());
@@ -560,7 +535,8 @@ static uint64_t pass_graph_key(const wpbr_ctx* ctx) {
   mix((uint64_t)R.trace_grid);
   const void* ptrs[] = {R.acc.p,    R.hit_prim.p, R.shadow_rays.p,     R.shadow_hit.p,      R.pstate.p,
                         R.Lbuf.p,   R.pfilm.p,    R.pass_dev.p,        R.counters.p,        R.pass_ptr,
-                        ctx->d_err.p, ctx->bvh.view.nodes, ctx->bvh.view.prims};
+                        ctx->d_err.p, ctx->bvh.view.nodes, ctx->bvh.view.nodes4,
+                        ctx->bvh.view.prims};
   for (const void* q : ptrs) mix((uint64_t)(uintptr_t)q);
   return h;
 }

@@ -38,17 +38,6 @@ cudaError_t launch(const SceneView& S, const BvhView& Bv, const float4* rays, ui
   return cudaGetLastError();
 }
 
-template <bool ANY, int STACK>
-cudaError_t launch_persistent(const SceneView& S, const BvhView& Bv, const float4* rays, uint32_t n, float4* hits,
-                              uint32_t* counter, uint32_t* err, cudaStream_t st) {
-  auto kern = k_trace_persistent<ANY, STACK, BufferSrc, HitSink4>;
-  unsigned grid = persistent_grid((const void*)kern);
-  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), st);
-  if (e != cudaSuccess) return e;
-  kern<<<grid, kPersistBlock, 0, st>>>(S, Bv, BufferSrc{rays}, HitSink4{hits}, n, counter, err);
-  return cudaGetLastError();
-}
-
 }  // namespace
 
 wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* d_hits, uint32_t mode,
@@ -57,7 +46,7 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
   if (ctx->bvh.view.max_depth >= 250) return set_err(ctx, WPBR_ERR_TRAVERSAL_LIMIT, "collide: BVH deeper than 250");
   if (n == 0) return WPBR_OK;
   SceneView S = scene_view(ctx);
-  const BvhView& Bv = ctx->bvh.view;
+  const BvhView Bv = traversal_view(ctx);
   cudaError_t e;
   if (d_stats) {
     e = (mode == WPBR_TRACE_ANY) ? launch<true, true>(S, Bv, d_rays, n, d_hits, d_stats, ctx->d_err.p, ctx->stream)
@@ -67,13 +56,16 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
     e = ctx->trace_counter.ensure(4);
     if (e == cudaSuccess) {
       uint32_t* c = ctx->trace_counter.p;
-      bool deep = Bv.max_depth >= 60;
-      if (mode == WPBR_TRACE_ANY)
-        e = deep ? launch_persistent<true, 256>(S, Bv, d_rays, (uint32_t)n, d_hits, c, ctx->d_err.p, ctx->stream)
-                 : launch_persistent<true, 64>(S, Bv, d_rays, (uint32_t)n, d_hits, c, ctx->d_err.p, ctx->stream);
-      else
-        e = deep ? launch_persistent<false, 256>(S, Bv, d_rays, (uint32_t)n, d_hits, c, ctx->d_err.p, ctx->stream)
-                 : launch_persistent<false, 64>(S, Bv, d_rays, (uint32_t)n, d_hits, c, ctx->d_err.p, ctx->stream);
+      e = cudaMemsetAsync(c, 0, sizeof(uint32_t), ctx->stream);
+      if (e == cudaSuccess) {
+        BufferSrc src{d_rays};
+        HitSink4 sink{d_hits};
+        if (mode == WPBR_TRACE_ANY)
+          launch_traversal<true>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, ctx->stream);
+        else
+          launch_traversal<false>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, ctx->stream);
+        e = cudaGetLastError();
+      }
     }
   }
   if (e != cudaSuccess) return cuda_err(ctx, e, "collide kernel");
