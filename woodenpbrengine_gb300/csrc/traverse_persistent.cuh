@@ -19,6 +19,9 @@ namespace wpbr {
 
 constexpr int kEnd = (int)0x80000000;  // no node (empty stack)
 constexpr int kPersistBlock = 128;
+#ifndef WPBR_TRACE_MIN_BLOCKS
+#define WPBR_TRACE_MIN_BLOCKS 8
+#endif
 
 // Ray data the warp's lanes read when they test primitives for another lane.
 struct SharedRay {
@@ -28,7 +31,8 @@ struct SharedRay {
 };
 
 template <bool ANY, int STACK, class Src, class Sink>
-__global__ void __launch_bounds__(kPersistBlock) k_trace_persistent(SceneView S, BvhView Bv, Src src, Sink sink,
+__global__ void __launch_bounds__(kPersistBlock, WPBR_TRACE_MIN_BLOCKS) k_trace_persistent(SceneView S, BvhView Bv,
+                                                                                           Src src, Sink sink,
                                                                     uint32_t n, uint32_t* counter, uint32_t* err) {
   __shared__ SharedRay s_ray[kPersistBlock / 32][32];
   __shared__ unsigned long long s_key[kPersistBlock / 32][32];
