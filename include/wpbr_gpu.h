@@ -70,6 +70,16 @@ WPBR_API wpbr_status wpbr_synchronize(wpbr_ctx* ctx);
  * wpbr_bvh_build after the mode is set. */
 enum wpbr_traversal { WPBR_TRAVERSAL_BINARY = 0, WPBR_TRAVERSAL_WIDE = 1 };
 WPBR_API wpbr_status wpbr_set_traversal(wpbr_ctx* ctx, uint32_t mode);
+/* Spectral representation of the render passes. RGB (default) carries three
+ * channels; SAMPLED64 is the reference's Spectrum (SampledSpectrum, 64 bins
+ * over 400-700 nm, CSpectrum.h:8): scene RGB values become spectra (grey
+ * values constant, others through the RGB-to-spectrum bases; environment
+ * texels as illuminants), shading runs per bin, and the film accumulates
+ * spectra that wpbr_film_read / wpbr_film_tonemap see through toRGB. A
+ * parity mode: one thread per sample, no staged jobs, no adjoint. Takes
+ * effect at the next wpbr_render_setup. */
+enum wpbr_spectrum { WPBR_SPECTRUM_RGB = 0, WPBR_SPECTRUM_SAMPLED64 = 1 };
+WPBR_API wpbr_status wpbr_set_spectrum(wpbr_ctx* ctx, uint32_t mode);
 /* Device error word (traversal limits etc.) since the last call; cleared. */
 WPBR_API wpbr_status wpbr_check_device_errors(wpbr_ctx* ctx);
 

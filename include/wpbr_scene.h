@@ -140,7 +140,11 @@ enum wpbr_quirk {
    * (SLBVH.cpp:250-283), so the treelet split, the bounds gather and
    * emitLBVH all read the array after the fourth pass: codes sorted by their
    * low 24 bits. Default keeps that order. */
-  WPBR_Q_FULL_MORTON_SORT = 1u << 4
+  WPBR_Q_FULL_MORTON_SORT = 1u << 4,
+  /* Sampled64 mode only: xyzToRGB's stored matrix has 0.041556 where the
+   * standard XYZ-to-sRGB matrix has 0.055648 (blue from X,
+   * CoefficientSpectrum.h:17-19). Set to use the standard value. */
+  WPBR_Q_XYZ_MATRIX_FIX = 1u << 5
 };
 
 #ifdef __cplusplus

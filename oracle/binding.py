@@ -35,6 +35,8 @@ _SIGS = {
     "orc_philox": (None, [_UP, _UP, _UP]),
     "orc_fmath": (None, [C.c_int, _FP, _FP, _FP, C.c_uint64]),
     "orc_fmath_d": (None, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint64]),
+    "orc_render_spectral": (None, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, _FP, _FP]),
+    "orc_spectral_tables": (None, [_FP]),
     "orc_adjoint_eval": (C.c_double, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_double),
                                       C.POINTER(C.c_double), _FP, C.POINTER(C.c_double), C.c_uint32, _UP,
                                       C.POINTER(C.c_double)]),
@@ -143,11 +145,23 @@ class OracleScene:
                                       _up(sel_a), g.ctypes.data_as(dp))
         return loss, (img.reshape(H, W, 3) if img is not None else None), (g if sel is not None else None)
 
+    def render_spectral(self, W, H, spp, seed=0, stream=0):
+        L = np.zeros(W * H * 3, np.float32)
+        w = np.zeros(W * H, np.float32)
+        lib().orc_render_spectral(self._h, spp, seed, stream, _fp(L), _fp(w))
+        return L.reshape(H, W, 3), w.reshape(H, W)
+
     def render(self, W, H, spp, seed=0, stream=0):
         L = np.zeros(W * H * 3, np.float32)
         w = np.zeros(W * H, np.float32)
         lib().orc_render(self._h, spp, seed, stream, _fp(L), _fp(w))
         return L.reshape(H, W, 3), w.reshape(H, W)
+
+
+def spectral_tables():
+    t = np.zeros(17 * 64, np.float32)
+    lib().orc_spectral_tables(_fp(t))
+    return t.reshape(17, 64)
 
 
 def philox(ctr, key):

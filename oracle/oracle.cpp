@@ -13,11 +13,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <cstdlib>
 #include <vector>
 
 #include "oracle_math.hpp"
 #include "wpbr_record.h"
+#include "wpbr_spectrum_data.h"
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -1113,6 +1115,7 @@ static Scene* scene_from_desc(const wpbr_scene_desc* d, uint32_t quirks) {
 }
 
 #include "oracle_adjoint.inc"
+#include "oracle_spectral.inc"
 
 }  // namespace orc
 
@@ -1335,5 +1338,16 @@ double orc_adjoint_eval(void* h, uint32_t spp, uint32_t seed, uint32_t stream, c
     for (int k = 0; k < K && b + k < n_sel; ++k) grad[b + k] = l.d[k];
   }
   return loss;
+}
+/* Sampled64 render: spp passes of the spectral per-sample job list; the
+ * film's spectra resolved with toRGB (acc_L[W*H*3]) and the weights. */
+void orc_render_spectral(void* h, uint32_t spp, uint32_t seed, uint32_t stream, float* acc_L, float* acc_w) {
+  spec_render(*(const Scene*)h, spp, seed, stream, acc_L, acc_w);
+}
+/* The binned spectral tables (64 floats each): X, Y, Z, 7 reflectance and
+ * 7 illuminant bases, in that order (17 * 64 floats). */
+void orc_spectral_tables(float* out) {
+  const SpecTab& T = spec_tables();
+  memcpy(out, &T, sizeof(T));
 }
 }

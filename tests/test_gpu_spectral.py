@@ -1,0 +1,49 @@
+"""Sampled64 mode (wpbr_set_spectrum): the spectral render pass against the
+oracle's spectral restatement, bit for bit, on the plain scene and on the
+full-frame scene (environment light, specular material) with quirks."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _same_nan_aware(a, b):
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    return bool(np.all((a.view(np.uint32) == b.view(np.uint32)) | (np.isnan(a) & np.isnan(b))))
+
+
+@pytest.mark.parametrize("config,res,level,quirks", [(0, (64, 48), 0, 0), (2, (48, 32), 4, 2), (2, (48, 32), 4, 32)])
+def test_spectral_film_matches_oracle(W, O, ctx, config, res, level, quirks):
+    g = W.SceneGen(config, 0, res, level=level)
+    ctx.set_quirks(quirks)
+    ctx.set_spectrum(W.SPECTRUM_SAMPLED64)
+    ctx.upload(g.desc)
+    ctx.build()
+    ctx.render_setup(2, seed=3, stream=1)
+    ctx.render()
+    L, w = ctx.film(*res)
+    Lo, wo = O.OracleScene(g.desc, quirks).render_spectral(res[0], res[1], 2, 3, 1)
+    assert np.array_equal(w, wo)
+    assert _same_nan_aware(L, Lo)
+    assert np.isfinite(L).mean() > 0.99 and np.nanmax(L) > 0
+    with pytest.raises(W.WpbrError):
+        ctx.job("CAMERA_RAYS", 0)  # the staged jobs are RGB only
+    ctx.check_device_errors()
+    ctx.set_spectrum(W.SPECTRUM_RGB)
+    ctx.set_quirks(0)
+
+
+def test_back_to_rgb_after_spectral(W, O, ctx):
+    g = W.SceneGen(0, 0, (32, 32))
+    ctx.set_quirks(0)
+    ctx.set_spectrum(W.SPECTRUM_SAMPLED64)
+    ctx.upload(g.desc)
+    ctx.build()
+    ctx.render_setup(1, seed=0)
+    ctx.render()
+    ctx.set_spectrum(W.SPECTRUM_RGB)
+    ctx.render_setup(2, seed=0)
+    ctx.render()
+    L, w = ctx.film(32, 32)
+    Lo, wo = O.OracleScene(g.desc).render(32, 32, 2)
+    assert np.array_equal(L.view(np.uint32), Lo.view(np.uint32)) and np.array_equal(w, wo)

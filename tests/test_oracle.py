@@ -127,3 +127,30 @@ def test_fp64_estimator_dual_gradient_matches_central_differences(W, O):
             em[i - m0.size] -= h
         fd = (o.adjoint_eval(40, 32, 2, 0, 0, mp, ep, target)[0] - o.adjoint_eval(40, 32, 2, 0, 0, mm, em, target)[0]) / (2 * h)
         assert abs(grad[k] - fd) <= 1e-4 * max(abs(fd), 1e-3 * np.abs(grad).max()), (i, grad[k], fd)
+
+
+def test_spectral_tables_and_conversions(W, O):
+    # binned CIE matching functions and RGB-to-spectrum bases of the
+    # Sampled64 mode (64 bins over 400-700 nm)
+    t = O.spectral_tables()
+    X, Y, Z = t[0], t[1], t[2]
+    white_refl, white_illum = t[3], t[10]
+    assert np.all(Y >= 0) and np.all(X >= 0) and np.all(Z >= 0)
+    dl = 300.0 / 64
+    # the visible part of the Y integral (106.857 over 360-830 nm)
+    assert 100.0 < Y.sum() * dl < 106.857
+    assert np.argmax(Y) in range(25, 35)          # peak near 555 nm
+    assert abs(white_refl.mean() - 1.0) < 0.1 and abs(white_illum.mean() - 1.0) < 0.1
+    # a spectral render of the plain scene is finite and, up to the
+    # unnormalised toXYZ scale, close in chromaticity to the RGB render
+    g = W.SceneGen(0, 0, (48, 40))
+    o = O.OracleScene(g.desc)
+    Ls, ws = o.render_spectral(48, 40, 2, 0, 0)
+    Lr, wr = o.render(48, 40, 2, 0, 0)
+    assert np.array_equal(ws, wr)
+    ok = np.isfinite(Ls).all(axis=-1) & (Lr.sum(-1) > 1e-3)
+    assert ok.sum() > 100
+    lum_s, lum_r = Ls[ok].sum(-1), Lr[ok].sum(-1)
+    ratio = lum_s / lum_r
+    # toXYZ is not divided by CIE_Y_integral: the spectral film is ~107x the RGB one
+    assert 100 < np.median(ratio) < 115 and np.std(np.log(ratio)) < 0.1

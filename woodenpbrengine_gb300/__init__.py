@@ -19,6 +19,8 @@ LIB_PATH = os.path.join(_HERE, "libwpbr_gpu.so")
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TRAVERSAL_LIMIT, ERR_NOT_BUILT, ERR_NO_DEVICE = range(7)
 TRACE_CLOSEST, TRACE_ANY = 0, 1
 TRAVERSAL_BINARY, TRAVERSAL_WIDE = 0, 1
+SPECTRUM_RGB, SPECTRUM_SAMPLED64 = 0, 1
+Q_XYZ_MATRIX_FIX = 32
 Q_TRI_PERMUTATION_BUG, Q_ENV_LI_SAMPLE_FIX, Q_SPHERE_PDF_FIX, Q_ENV_DISTRIB_INDEX_BUG, Q_FULL_MORTON_SORT = (
     1, 2, 4, 8, 16)
 MAT_CONDUCTOR, MAT_DIELECTRIC, MAT_SPECULAR = 0, 1, 2
@@ -45,6 +47,7 @@ _SIGS = {
     "wpbr_set_quirks": (C.c_int, [_VP, C.c_uint32]),
     "wpbr_synchronize": (C.c_int, [_VP]),
     "wpbr_set_traversal": (C.c_int, [_VP, C.c_uint32]),
+    "wpbr_set_spectrum": (C.c_int, [_VP, C.c_uint32]),
     "wpbr_check_device_errors": (C.c_int, [_VP]),
     "wpbr_scene_upload": (C.c_int, [_VP, C.POINTER(A.SceneDesc)]),
     "wpbr_camera_info": (C.c_int, [_VP, _FP, _FP, _FP]),
@@ -201,6 +204,9 @@ class Context:
 
     def set_traversal(self, mode):
         self._check(lib().wpbr_set_traversal(self._h, mode), "set_traversal")
+
+    def set_spectrum(self, mode):
+        self._check(lib().wpbr_set_spectrum(self._h, mode), "set_spectrum")
 
     def synchronize(self):
         self._check(lib().wpbr_synchronize(self._h), "synchronize")

@@ -14,7 +14,7 @@ INC = os.path.join(ROOT, "include")
 OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libwpbr_gpu.so")
 
-CU_SOURCES = ["context.cu", "bvh_build.cu", "trace.cu", "render.cu", "sort_noalloc.cu", "batch.cu", "adjoint.cu"]
+CU_SOURCES = ["context.cu", "bvh_build.cu", "trace.cu", "render.cu", "sort_noalloc.cu", "batch.cu", "adjoint.cu", "spectral.cu"]
 CPP_SOURCES = ["scene_gen.cpp"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

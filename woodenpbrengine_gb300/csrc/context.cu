@@ -155,6 +155,7 @@ WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
   RenderState& R = ctx->rs;
   R.acc.release(); R.hit_prim.release(); R.shadow_rays.release(); R.shadow_hit.release(); R.pstate.release();
   R.Lbuf.release(); R.pfilm.release(); R.pass_dev.release(); R.counters.release();
+  R.spec_mats.release(); R.spec_le.release(); R.spec_L.release(); R.spec_acc.release();
   ctx->io_rays.release(); ctx->io_hits.release(); ctx->io_stats.release(); ctx->trace_counter.release();
   for (auto& f : R.f) f.release();
   for (auto& u : R.u) u.release();
@@ -184,7 +185,7 @@ WPBR_API void* wpbr_get_stream(const wpbr_ctx* ctx) { return ctx ? (void*)ctx->s
 
 WPBR_API wpbr_status wpbr_set_quirks(wpbr_ctx* ctx, uint32_t quirks) {
   if (!ctx) return WPBR_ERR_INVALID_ARG;
-  if (quirks & ~0x1Fu) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_quirks: unknown bits");
+  if (quirks & ~0x3Fu) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_quirks: unknown bits");
   uint32_t changed = ctx->quirks ^ quirks;
   ctx->quirks = quirks;
   ++ctx->epoch;
@@ -206,6 +207,15 @@ WPBR_API wpbr_status wpbr_set_traversal(wpbr_ctx* ctx, uint32_t mode) {
   if (!ctx) return WPBR_ERR_INVALID_ARG;
   if (mode > WPBR_TRAVERSAL_WIDE) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_traversal: unknown mode");
   ctx->traversal = mode;
+  ++ctx->epoch;
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_set_spectrum(wpbr_ctx* ctx, uint32_t mode) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  if (mode > WPBR_SPECTRUM_SAMPLED64) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_spectrum: unknown mode");
+  ctx->spectrum = mode;
+  ctx->rs.ready = false;  // render_setup allocates the mode's buffers
   ++ctx->epoch;
   return WPBR_OK;
 }

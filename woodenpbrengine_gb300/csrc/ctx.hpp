@@ -88,6 +88,8 @@ struct RenderState {
   uint64_t graph_key = 0;
   DevBuf<uint32_t> pass_dev;  // pass index read by the captured kernels
   DevBuf<uint32_t> counters;  // ray-fetch counters of the pass's traversal launches
+  // Sampled64 mode: material / light spectra, per-pixel sample spectra, film spectra
+  DevBuf<float> spec_mats, spec_le, spec_L, spec_acc;
   const uint32_t* pass_ptr = nullptr;  // shared pass index (batches); null: pass_dev
   uint32_t trace_grid = 0;             // persistent traversal grid cap (0: full)
 };
@@ -131,6 +133,7 @@ struct wpbr_ctx {
   uint32_t quirks = 0;
   uint64_t epoch = 0;  // bumped by every scene upload, BVH build, quirk or traversal change
   uint32_t traversal = 0;  // wpbr_traversal: 0 binary, 1 wide (collapsed at build time)
+  uint32_t spectrum = 0;   // wpbr_spectrum: 0 RGB, 1 Sampled64
   wpbr::DevBuf<uint32_t> d_err;
   // scene
   bool has_scene = false;
@@ -184,6 +187,8 @@ wpbr_status env_distribution_build(wpbr_ctx* ctx, const float4* rgb, const EnvDi
 wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t stream);
 wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass);
 wpbr_status render_pass_launch(wpbr_ctx* ctx);
+wpbr_status spectral_setup(wpbr_ctx* ctx);
+wpbr_status spectral_pass(wpbr_ctx* ctx, uint32_t pass);
 uint32_t persistent_full_grid();
 void bvh_release(wpbr_ctx* ctx, bool keep_traversal);
 wpbr_status job_run(wpbr_ctx* ctx, uint32_t job, uint32_t pass);

@@ -482,6 +482,10 @@ wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t st
   WPBR_CUDA(R.pass_dev.ensure(1));
   WPBR_CUDA(R.counters.ensure(2));  // allocated before any graph capture
   WPBR_CUDA(cudaMemsetAsync(R.acc.p, 0, n * 4 * sizeof(float), ctx->stream));
+  if (ctx->spectrum == WPBR_SPECTRUM_SAMPLED64) {
+    wpbr_status sst = spectral_setup(ctx);
+    if (sst != WPBR_OK) return sst;
+  }
   R.ready = true;  // a captured pass graph stays valid while pass_graph_key is unchanged
   return WPBR_OK;
 }
@@ -542,6 +546,7 @@ static uint64_t pass_graph_key(const wpbr_ctx* ctx) {
 }
 
 wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass) {
+  if (ctx->spectrum == WPBR_SPECTRUM_SAMPLED64) return spectral_pass(ctx, pass);
   RenderState& R = ctx->rs;
   if (!R.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render_pass: render_setup not called");
   if (pass >= R.spp) return set_err(ctx, WPBR_ERR_INVALID_ARG, "render_pass: pass >= spp");
@@ -576,6 +581,8 @@ wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass) {
 
 wpbr_status job_run(wpbr_ctx* ctx, uint32_t job, uint32_t pass) {
   RenderState& R = ctx->rs;
+  if (ctx->spectrum != WPBR_SPECTRUM_RGB)
+    return set_err(ctx, WPBR_ERR_INVALID_ARG, "job_run: the staged jobs run in RGB mode only");
   if (!R.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "job_run: render_setup not called");
   if (job >= WPBR_JOB_COUNT) return set_err(ctx, WPBR_ERR_INVALID_ARG, "job_run: unknown job id");
   if (pass >= R.spp) return set_err(ctx, WPBR_ERR_INVALID_ARG, "job_run: pass >= spp");
