@@ -47,6 +47,9 @@ def parse():
     p.add_argument("--no-render", action="store_true")
     p.add_argument("--profile", action="store_true",
                    help="small case for ncu: 1,310,720 triangles, 1024x1024 + 1M incoherent rays, 5 launches")
+    p.add_argument("--profile-render", action="store_true",
+                   help="small render cases for ncu: full frame 640x360 x 2 spp, adjoint 256x256 x 2 spp "
+                        "forward + backward, 8 batched scenes x 2 spp")
     return p.parse_args()
 
 
@@ -424,8 +427,27 @@ def run_profile_case():
     ctx.close()
 
 
+def run_render_profile_case():
+    """Small render cases sized for ncu captures of the render, adjoint and
+    batched kernels (each a few hundred MB on the device at most)."""
+    import torch
+
+    from __graft_entry__ import build
+
+    build()
+    import woodenpbrengine_gb300 as W
+
+    out = {"full_frame": render_rate(W, torch, 2, (640, 360), 2, level=LEVEL),
+           "adjoint": adjoint_rate(W, torch, res=(256, 256), spp=2, n_fd=4, fp64=False),
+           "batched": batch_rate(W, torch, n_scenes=8, spp=2, film_scale=512, max_count=200000)}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
+    if args.profile_render:
+        run_render_profile_case()
+        return
     if args.profile:
         run_profile_case()
         return
