@@ -445,10 +445,21 @@ __global__ void k_fill(uint32_t* p, uint32_t n, uint32_t v) {
   if (i < n) p[i] = v;
 }
 
-__global__ void k_pos_seg(uint32_t nseg, const uint32_t* seg_start, const uint32_t* seg_end, uint32_t* pos_seg) {
-  uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (s >= nseg) return;
-  for (uint32_t p = seg_start[s] + lane_id(); p <= seg_end[s]; p += 32) pos_seg[p] = s;
+// Segment of every position (kNone outside the level's large segments): a
+// binary search over the segment starts, which are in ascending order.
+__global__ void k_pos_seg(uint32_t T, uint32_t nseg, const uint32_t* seg_start, const uint32_t* seg_end,
+                          uint32_t* pos_seg) {
+  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= T) return;
+  uint32_t lo = 0, hi = nseg;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(seg_start + mid) <= p)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  pos_seg[p] = (lo > 0 && p <= __ldg(seg_end + lo - 1)) ? lo - 1 : kNone;
 }
 
 __global__ void k_seg_init(uint32_t nseg, uint32_t* benc, uint32_t* cenc, uint32_t* bcnt, uint32_t* bkenc) {
@@ -727,7 +738,11 @@ __global__ void k_seg_children(uint32_t nseg, SegLevel L, const uint32_t* seg_mi
   }
 }
 
-// Segments of 2..32 roots: the whole SAH recursion inside one warp.
+// Segments of 2..32 roots: the whole SAH recursion inside one warp. Bounds
+// by warp reductions, buckets by shared-memory atomics, the 11 split costs
+// one per lane (the same float operations as sah_decide) and the sequential
+// first-minimum rule by a lexicographic (cost, split) reduction. The
+// segment's n - 2 new SAH node ids are reserved with one atomic.
 __global__ void k_small_sah(SahArgs A, uint32_t nsmall, const uint32_t* sm_start, const uint32_t* sm_end,
                             const uint32_t* sm_node, uint32_t* cur, uint32_t* counters, uint32_t* sah_axis,
                             float4* nb_lo, float4* nb_hi, uint32_t* child0, uint32_t* child1, uint32_t* parent,
@@ -735,6 +750,7 @@ __global__ void k_small_sah(SahArgs A, uint32_t nsmall, const uint32_t* sm_start
   __shared__ uint32_t sh_bcnt[kB / 32][12];
   __shared__ uint32_t sh_benc[kB / 32][12 * 6];
   __shared__ uint32_t sh_stack[kB / 32][3 * 64];
+  const uint32_t FULL = 0xFFFFFFFFu;
   const uint32_t w = threadIdx.x >> 5, lane = lane_id();
   uint32_t seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (seg >= nsmall) return;
@@ -743,6 +759,9 @@ __global__ void k_small_sah(SahArgs A, uint32_t nsmall, const uint32_t* sm_start
   uint32_t item = lane < n ? cur[base + lane] : 0u;
   V3 lo{0, 0, 0}, hi{0, 0, 0};
   if (lane < n) item_bounds(A, item, &lo, &hi);
+  uint32_t id_base = 0, id_next = 0;
+  if (lane == 0 && n > 2) id_base = atomicAdd(&counters[0], n - 2);
+  id_base = __shfl_sync(FULL, id_base, 0);
   uint32_t* stk = sh_stack[w];
   int sp = 0;
   if (lane == 0) {
@@ -763,21 +782,17 @@ __global__ void k_small_sah(SahArgs A, uint32_t nsmall, const uint32_t* sm_start
     __syncwarp();
     bool act = lane >= a && lane <= b;
     uint32_t cnt = b - a + 1;
-    // bounds + centroid bounds over active lanes
     V3 c = mul(add(lo, hi), 0.5f);
-    uint32_t e[12];
-    e[0] = act ? fenc(lo.x) : 0xFFFFFFFFu; e[1] = act ? fenc(lo.y) : 0xFFFFFFFFu; e[2] = act ? fenc(lo.z) : 0xFFFFFFFFu;
-    e[3] = act ? fenc(hi.x) : 0u; e[4] = act ? fenc(hi.y) : 0u; e[5] = act ? fenc(hi.z) : 0u;
-    e[6] = act ? fenc(c.x) : 0xFFFFFFFFu; e[7] = act ? fenc(c.y) : 0xFFFFFFFFu; e[8] = act ? fenc(c.z) : 0xFFFFFFFFu;
-    e[9] = act ? fenc(c.x) : 0u; e[10] = act ? fenc(c.y) : 0u; e[11] = act ? fenc(c.z) : 0u;
-    for (int o = 16; o > 0; o >>= 1)
-      for (int k = 0; k < 12; ++k) {
-        uint32_t y = __shfl_xor_sync(0xFFFFFFFFu, e[k], o);
-        bool mn = (k < 3) || (k >= 6 && k < 9);
-        e[k] = mn ? min(e[k], y) : max(e[k], y);
-      }
-    Bounds bb{V3{fdec(e[0]), fdec(e[1]), fdec(e[2])}, V3{fdec(e[3]), fdec(e[4]), fdec(e[5])}};
-    Bounds cb{V3{fdec(e[6]), fdec(e[7]), fdec(e[8])}, V3{fdec(e[9]), fdec(e[10]), fdec(e[11])}};
+    Bounds bb{V3{fdec(__reduce_min_sync(FULL, act ? fenc(lo.x) : 0xFFFFFFFFu)),
+                 fdec(__reduce_min_sync(FULL, act ? fenc(lo.y) : 0xFFFFFFFFu)),
+                 fdec(__reduce_min_sync(FULL, act ? fenc(lo.z) : 0xFFFFFFFFu))},
+              V3{fdec(__reduce_max_sync(FULL, act ? fenc(hi.x) : 0u)), fdec(__reduce_max_sync(FULL, act ? fenc(hi.y) : 0u)),
+                 fdec(__reduce_max_sync(FULL, act ? fenc(hi.z) : 0u))}};
+    Bounds cb{V3{fdec(__reduce_min_sync(FULL, act ? fenc(c.x) : 0xFFFFFFFFu)),
+                 fdec(__reduce_min_sync(FULL, act ? fenc(c.y) : 0xFFFFFFFFu)),
+                 fdec(__reduce_min_sync(FULL, act ? fenc(c.z) : 0xFFFFFFFFu))},
+              V3{fdec(__reduce_max_sync(FULL, act ? fenc(c.x) : 0u)), fdec(__reduce_max_sync(FULL, act ? fenc(c.y) : 0u)),
+                 fdec(__reduce_max_sync(FULL, act ? fenc(c.z) : 0u))}};
     int dim = bmax_extent(cb);
     float dist = comp(cb.hi, dim) - comp(cb.lo, dim);
     uint32_t ib = 0;
@@ -788,35 +803,65 @@ __global__ void k_small_sah(SahArgs A, uint32_t nsmall, const uint32_t* sm_start
       ib = (bt >= 0.0f) ? (uint32_t)bt : 0u;
       if (ib >= 12u) ib = 11u;
     }
-    // per-bucket counts and bounds: lane j < 12 accumulates bucket j
-    uint32_t fe[6] = {fenc(lo.x), fenc(lo.y), fenc(lo.z), fenc(hi.x), fenc(hi.y), fenc(hi.z)};
-    uint32_t bc = 0;
-    uint32_t be[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
-    for (uint32_t q = a; q <= b; ++q) {
-      uint32_t qb = __shfl_sync(0xFFFFFFFFu, ib, q);
-      uint32_t qe[6];
-      for (int k = 0; k < 6; ++k) qe[k] = __shfl_sync(0xFFFFFFFFu, fe[k], q);
-      if (lane < 12 && qb == lane) {
-        ++bc;
-        for (int k = 0; k < 3; ++k) be[k] = min(be[k], qe[k]);
-        for (int k = 3; k < 6; ++k) be[k] = max(be[k], qe[k]);
-      }
-    }
+    // per-bucket counts and bounds
+    uint32_t* bcnt = sh_bcnt[w];
+    uint32_t* benc = sh_benc[w];
     if (lane < 12) {
-      sh_bcnt[w][lane] = bc;
-      for (int k = 0; k < 6; ++k) sh_benc[w][lane * 6 + k] = be[k];
+      bcnt[lane] = 0;
+      for (int k = 0; k < 6; ++k) benc[lane * 6 + k] = k < 3 ? 0xFFFFFFFFu : 0u;
     }
     __syncwarp();
-    int best = 0;
+    if (act) {
+      atomicAdd(&bcnt[ib], 1u);
+      uint32_t* be = benc + ib * 6;
+      atomicMin(be + 0, fenc(lo.x));
+      atomicMin(be + 1, fenc(lo.y));
+      atomicMin(be + 2, fenc(lo.z));
+      atomicMax(be + 3, fenc(hi.x));
+      atomicMax(be + 4, fenc(hi.y));
+      atomicMax(be + 5, fenc(hi.z));
+    }
+    __syncwarp();
+    // SAH cost of split `lane` (sah_decide's loop body)
+    float cost = 0.0f;
+    if (lane < 11) {
+      Bounds b0 = bempty(), b1 = bempty();
+      uint32_t n0 = 0, n1 = 0;
+      for (int j = 0; j < 12; ++j) {
+        uint32_t cj = bcnt[j];
+        if (!cj) continue;
+        if (j <= (int)lane) {
+          b0 = bunion(b0, dec_bounds(benc + j * 6));
+          n0 += cj;
+        } else {
+          b1 = bunion(b1, dec_bounds(benc + j * 6));
+          n1 += cj;
+        }
+      }
+      float l = (n0 == 0) ? 0.0f : (float)n0 * barea(b0);
+      float r = (n1 == 0) ? 0.0f : (float)n1 * barea(b1);
+      cost = (float)(0.125 + (double)((l + r) / barea(bb)));
+    }
+    // first index of the minimum; a NaN never wins, and a NaN at split 0 keeps split 0
+    float c0 = __shfl_sync(FULL, cost, 0);
+    float bc = (lane < 11 && !isnan(cost)) ? cost : __int_as_float(0x7f800000);
+    uint32_t bi = lane;
+    for (int o = 16; o > 0; o >>= 1) {
+      float oc = __shfl_xor_sync(FULL, bc, o);
+      uint32_t oi = __shfl_xor_sync(FULL, bi, o);
+      if (oc < bc || (oc == bc && oi < bi)) {
+        bc = oc;
+        bi = oi;
+      }
+    }
+    int best = isnan(c0) ? 0 : (int)bi;
     uint32_t k = 0;
-    if (lane == 0) sah_decide(sh_bcnt[w], sh_benc[w], bb, cnt, &best, &k);
-    best = __shfl_sync(0xFFFFFFFFu, best, 0);
-    k = __shfl_sync(0xFFFFFFFFu, k, 0);
+    for (int j = 0; j <= best; ++j) k += bcnt[j];
     // two-pointer partition of [a, b] by ib <= best
     uint32_t spt = a + k;
     bool pred = ib <= (uint32_t)best;
-    uint32_t fmask = __ballot_sync(0xFFFFFFFFu, act && lane < spt && !pred);
-    uint32_t tmask = __ballot_sync(0xFFFFFFFFu, act && lane >= spt && pred);
+    uint32_t fmask = __ballot_sync(FULL, act && lane < spt && !pred);
+    uint32_t tmask = __ballot_sync(FULL, act && lane >= spt && pred);
     uint32_t src = lane;
     if (act && lane < spt && !pred) {
       uint32_t r = __popc(fmask & ((1u << lane) - 1u));
@@ -830,10 +875,10 @@ __global__ void k_small_sah(SahArgs A, uint32_t nsmall, const uint32_t* sm_start
       for (uint32_t q = 0; q < r; ++q) m &= m - 1u;
       src = (uint32_t)(__ffs(m) - 1);
     }
-    item = __shfl_sync(0xFFFFFFFFu, item, src);
-    lo.x = __shfl_sync(0xFFFFFFFFu, lo.x, src); lo.y = __shfl_sync(0xFFFFFFFFu, lo.y, src);
-    lo.z = __shfl_sync(0xFFFFFFFFu, lo.z, src); hi.x = __shfl_sync(0xFFFFFFFFu, hi.x, src);
-    hi.y = __shfl_sync(0xFFFFFFFFu, hi.y, src); hi.z = __shfl_sync(0xFFFFFFFFu, hi.z, src);
+    item = __shfl_sync(FULL, item, src);
+    lo.x = __shfl_sync(FULL, lo.x, src); lo.y = __shfl_sync(FULL, lo.y, src);
+    lo.z = __shfl_sync(FULL, lo.z, src); hi.x = __shfl_sync(FULL, hi.x, src);
+    hi.y = __shfl_sync(FULL, hi.y, src); hi.z = __shfl_sync(FULL, hi.z, src);
     uint32_t mid = (k == cnt) ? a + cnt / 2 : a + k;
     uint32_t me = N2 + nd;
     if (lane == 0) {
@@ -842,15 +887,15 @@ __global__ void k_small_sah(SahArgs A, uint32_t nsmall, const uint32_t* sm_start
       nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
     }
     uint32_t ln = mid - a, rn = b - mid + 1;
-    uint32_t litem = __shfl_sync(0xFFFFFFFFu, item, a);
-    uint32_t ritem = __shfl_sync(0xFFFFFFFFu, item, b);
+    uint32_t litem = __shfl_sync(FULL, item, a);
+    uint32_t ritem = __shfl_sync(FULL, item, b);
     if (lane == 0) {
       if (ln == 1) {
         uint32_t r = A.troot[litem];
         child0[me] = r;
         parent[r] = (me << 1) | 0u;
       } else {
-        uint32_t cl = atomicAdd(&counters[0], 1u);
+        uint32_t cl = id_base + id_next++;
         child0[me] = N2 + cl;
         parent[N2 + cl] = (me << 1) | 0u;
         stk[3 * sp] = a; stk[3 * sp + 1] = mid - 1; stk[3 * sp + 2] = cl;
@@ -861,14 +906,14 @@ __global__ void k_small_sah(SahArgs A, uint32_t nsmall, const uint32_t* sm_start
         child1[me] = r;
         parent[r] = (me << 1) | 1u;
       } else {
-        uint32_t cr = atomicAdd(&counters[0], 1u);
+        uint32_t cr = id_base + id_next++;
         child1[me] = N2 + cr;
         parent[N2 + cr] = (me << 1) | 1u;
         stk[3 * sp] = mid; stk[3 * sp + 1] = b; stk[3 * sp + 2] = cr;
         ++sp;
       }
     }
-    sp = __shfl_sync(0xFFFFFFFFu, sp, 0);
+    sp = __shfl_sync(FULL, sp, 0);
     __syncwarp();
   }
   if (lane < n) cur[base + lane] = item;
@@ -1358,8 +1403,7 @@ wpbr_status bvh_build(wpbr_ctx* ctx) {
     while (nlarge > 0) {
       if (++level > 100000) return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: SAH level limit");
       SegLevel L{L_start, L_end, L_node};
-      k_fill<<<gT, kB, 0, st>>>(B.pos_seg.p, T, kNone);
-      k_pos_seg<<<div_up((uint64_t)nlarge * 32, kB), kB, 0, st>>>(nlarge, L_start, L_end, B.pos_seg.p);
+      k_pos_seg<<<gT, kB, 0, st>>>(T, nlarge, L_start, L_end, B.pos_seg.p);
       k_seg_init<<<div_up(nlarge, kB), kB, 0, st>>>(nlarge, B.seg_benc.p, B.seg_cenc.p, B.seg_bucket_cnt.p,
                                                     B.seg_bucket_enc.p);
       k_seg_reduce<<<gT, kB, 0, st>>>(A, B.cur.p, B.pos_seg.p, B.seg_benc.p, B.seg_cenc.p);
