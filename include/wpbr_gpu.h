@@ -125,6 +125,11 @@ WPBR_API wpbr_status wpbr_collide(wpbr_ctx* ctx, const float* rays, uint64_t n, 
 WPBR_API wpbr_status wpbr_collide_device(wpbr_ctx* ctx, const void* d_rays, uint64_t n, void* d_hits,
                                          uint32_t mode);
 /* Per-ray node visits and primitive tests (u32 pairs), for the byte model. */
+/* Large batches (256k rays and more) are traced in the order of their
+ * origins' Morton cells on a 2^b per axis grid over the scene bounds
+ * (b = bits_per_axis, default 8, at most 10) and written back at their input
+ * positions; the hits do not depend on the order. 0 traces in input order. */
+WPBR_API wpbr_status wpbr_set_ray_sort(wpbr_ctx* ctx, uint32_t bits_per_axis);
 WPBR_API wpbr_status wpbr_collide_stats(wpbr_ctx* ctx, const float* rays, uint64_t n, float* hits,
                                         uint32_t* stats, uint32_t mode);
 

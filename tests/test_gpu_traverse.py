@@ -96,3 +96,26 @@ def test_wide_and_binary_traversals_agree(W, O, ctx, config, level, res):
     assert np.array_equal(aw[:, 1].view(np.uint32) == 0xFFFFFFFF, ab[:, 1].view(np.uint32) == 0xFFFFFFFF)
     _check(hw, O.OracleScene(g.desc).trace(rays, mode=0))
     ctx.check_device_errors()
+
+
+def test_ray_reordering_keeps_hits(W, ctx):
+    # batches of 256k rays and more are traced in Morton order of their
+    # origins; every hit is written back to its input position unchanged
+    g = W.SceneGen(1, 0, (512, 512), level=6, rays=True)
+    ctx.set_quirks(0)
+    ctx.upload(g.desc)
+    ctx.build()
+    rays = g.rays()
+    assert rays.shape[0] >= 1 << 18
+    hs = ctx.collide(rays)
+    as_ = ctx.collide(rays, mode=W.TRACE_ANY)
+    ctx.set_ray_sort(0)
+    hu = ctx.collide(rays)
+    au = ctx.collide(rays, mode=W.TRACE_ANY)
+    ctx.set_ray_sort(5)
+    h5 = ctx.collide(rays)
+    ctx.set_ray_sort(8)
+    assert np.array_equal(hs.view(np.uint32), h5.view(np.uint32))
+    assert np.array_equal(hs.view(np.uint32), hu.view(np.uint32))
+    assert np.array_equal(as_[:, 1].view(np.uint32) == 0xFFFFFFFF, au[:, 1].view(np.uint32) == 0xFFFFFFFF)
+    ctx.check_device_errors()

@@ -48,6 +48,7 @@ _SIGS = {
     "wpbr_synchronize": (C.c_int, [_VP]),
     "wpbr_set_traversal": (C.c_int, [_VP, C.c_uint32]),
     "wpbr_set_spectrum": (C.c_int, [_VP, C.c_uint32]),
+    "wpbr_set_ray_sort": (C.c_int, [_VP, C.c_uint32]),
     "wpbr_check_device_errors": (C.c_int, [_VP]),
     "wpbr_scene_upload": (C.c_int, [_VP, C.POINTER(A.SceneDesc)]),
     "wpbr_camera_info": (C.c_int, [_VP, _FP, _FP, _FP]),
@@ -204,6 +205,10 @@ class Context:
 
     def set_traversal(self, mode):
         self._check(lib().wpbr_set_traversal(self._h, mode), "set_traversal")
+
+    def set_ray_sort(self, bits_per_axis):
+        """Origin-grid bits per axis for reordering large collide batches (0: input order)."""
+        self._check(lib().wpbr_set_ray_sort(self._h, int(bits_per_axis)), "set_ray_sort")
 
     def set_spectrum(self, mode):
         self._check(lib().wpbr_set_spectrum(self._h, mode), "set_spectrum")

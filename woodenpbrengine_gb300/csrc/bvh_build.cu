@@ -1232,6 +1232,31 @@ __global__ void k_wide_emit(uint32_t nq, uint32_t base, const uint32_t* q_bin, c
 
 }  // namespace
 
+// Stable LSD radix sort of (key, value) pairs by key bits [0, bits), 8 bits
+// per pass (the build's sort kernels); *kres / *vres point at the buffer
+// pair that holds the result.
+cudaError_t radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t n, int bits,
+                             DevBuf<uint32_t>& hist, DevBuf<uint32_t>& scan_tmp, cudaStream_t st, uint32_t** kres,
+                             uint32_t** vres) {
+  uint32_t nblk = div_up(n, kRadixTile);
+  cudaError_t e = hist.ensure((size_t)256 * nblk);
+  if (e != cudaSuccess) return e;
+  uint32_t *kin = k0, *vin = v0, *kout = k1, *vout = v1;
+  for (int shift = 0; shift < bits && n > 1; shift += 8) {
+    int w = bits - shift < 8 ? bits - shift : 8;
+    uint32_t dmask = (1u << w) - 1u;
+    k_radix_hist<<<nblk, kB, 0, st>>>(kin, n, shift, dmask, hist.p, nblk);
+    e = scan_exclusive(hist.p, hist.p, 256 * nblk, scan_tmp, st);
+    if (e != cudaSuccess) return e;
+    k_radix_scatter<<<nblk, kB, 0, st>>>(kin, vin, kout, vout, n, shift, dmask, hist.p, nblk);
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+  }
+  *kres = kin;
+  *vres = vin;
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // host orchestration
 // ---------------------------------------------------------------------------

@@ -157,6 +157,8 @@ WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
   R.Lbuf.release(); R.pfilm.release(); R.pass_dev.release(); R.counters.release();
   R.spec_mats.release(); R.spec_le.release(); R.spec_L.release(); R.spec_acc.release();
   ctx->io_rays.release(); ctx->io_hits.release(); ctx->io_stats.release(); ctx->trace_counter.release();
+  ctx->rs_k0.release(); ctx->rs_v0.release(); ctx->rs_k1.release(); ctx->rs_v1.release();
+  ctx->rs_hist.release(); ctx->rs_scan.release();
   for (auto& f : R.f) f.release();
   for (auto& u : R.u) u.release();
   ctx->adj.release();
@@ -208,6 +210,13 @@ WPBR_API wpbr_status wpbr_set_traversal(wpbr_ctx* ctx, uint32_t mode) {
   if (mode > WPBR_TRAVERSAL_WIDE) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_traversal: unknown mode");
   ctx->traversal = mode;
   ++ctx->epoch;
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_set_ray_sort(wpbr_ctx* ctx, uint32_t bits_per_axis) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  if (bits_per_axis > 10) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_ray_sort: at most 10 bits per axis");
+  ctx->ray_sort = bits_per_axis;
   return WPBR_OK;
 }
 

@@ -161,6 +161,9 @@ struct wpbr_ctx {
   wpbr::DevBuf<float4> io_rays, io_hits;
   wpbr::DevBuf<uint32_t> io_stats;
   wpbr::DevBuf<uint32_t> trace_counter;  // ray-fetch counters of the persistent traversal
+  // ray reordering of large collide batches (keys, permutation, radix scratch)
+  uint32_t ray_sort = 8;  // bits per axis of the origin grid (0: input order)
+  wpbr::DevBuf<uint32_t> rs_k0, rs_v0, rs_k1, rs_v1, rs_hist, rs_scan;
 };
 
 namespace wpbr {
@@ -175,6 +178,9 @@ wpbr_status set_err(wpbr_ctx* ctx, wpbr_status st, const std::string& msg);
 wpbr_status cuda_err(wpbr_ctx* ctx, cudaError_t e, const char* what);
 SceneView scene_view(const wpbr_ctx* ctx);
 wpbr_status bvh_build(wpbr_ctx* ctx);
+cudaError_t radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t n, int bits,
+                             DevBuf<uint32_t>& hist, DevBuf<uint32_t>& scan_tmp, cudaStream_t st, uint32_t** kres,
+                             uint32_t** vres);
 wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* d_hits, uint32_t mode,
                        uint32_t* d_stats);
 wpbr_status env_preprocess(wpbr_ctx* ctx);

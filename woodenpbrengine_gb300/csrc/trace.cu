@@ -9,6 +9,8 @@ namespace wpbr {
 
 namespace {
 
+constexpr uint64_t kRaySortMin = 1u << 18;  // batches below this are traced in input order
+
 template <bool ANY, bool STATS, int STACK>
 __global__ void __launch_bounds__(128) k_trace(SceneView S, BvhView Bv, const float4* __restrict__ rays, uint64_t n,
                                                float4* __restrict__ hits, uint32_t* __restrict__ stats,
@@ -25,6 +27,29 @@ __global__ void __launch_bounds__(128) k_trace(SceneView S, BvhView Bv, const fl
     stats[2 * i] = nv;
     stats[2 * i + 1] = np;
   }
+}
+
+// Sort key of a ray: Morton code of its origin on a 2^b grid per axis over
+// the scene bounds (clamped), 3b bits; the index is the payload.
+__device__ __forceinline__ uint32_t spread10(uint32_t v) {
+  v &= 0x3FFu;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+__global__ void k_ray_keys(const float4* rays, uint32_t n, float3 lo, float3 scale, uint32_t cells, uint32_t* keys,
+                           uint32_t* idx) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 o = __ldg(&rays[2 * (size_t)i]);
+  float q[3] = {(o.x - lo.x) * scale.x, (o.y - lo.y) * scale.y, (o.z - lo.z) * scale.z};
+  float top = (float)(cells - 1);
+  uint32_t c[3];
+  for (int k = 0; k < 3; ++k) c[k] = q[k] > 0.0f ? (q[k] < top ? (uint32_t)q[k] : cells - 1) : 0u;
+  keys[i] = spread10(c[0]) | (spread10(c[1]) << 1) | (spread10(c[2]) << 2);
+  idx[i] = i;
 }
 
 template <bool ANY, bool STATS>
@@ -57,13 +82,44 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
     if (e == cudaSuccess) {
       uint32_t* c = ctx->trace_counter.p;
       e = cudaMemsetAsync(c, 0, sizeof(uint32_t), ctx->stream);
+      // large batches are traced in the order of their origins' Morton cells:
+      // neighbouring rays of a warp then share nodes (hits are per ray, so the
+      // order does not change them)
+      const uint32_t* perm = nullptr;
+      if (e == cudaSuccess && ctx->ray_sort && n >= kRaySortMin && !Bv.empty) {
+        for (DevBuf<uint32_t>* b : {&ctx->rs_k0, &ctx->rs_v0, &ctx->rs_k1, &ctx->rs_v1})
+          if (e == cudaSuccess) e = b->ensure(n);
+        if (e == cudaSuccess) {
+          float3 lo = make_float3(Bv.root_lo[0], Bv.root_lo[1], Bv.root_lo[2]);
+          float ex[3] = {Bv.root_hi[0] - Bv.root_lo[0], Bv.root_hi[1] - Bv.root_lo[1], Bv.root_hi[2] - Bv.root_lo[2]};
+          uint32_t b = ctx->ray_sort;  // bits per axis
+          float cells = (float)(1u << b);
+          float3 sc = make_float3(ex[0] > 0.0f ? cells / ex[0] : 0.0f, ex[1] > 0.0f ? cells / ex[1] : 0.0f,
+                                  ex[2] > 0.0f ? cells / ex[2] : 0.0f);
+          k_ray_keys<<<div_up(n, 256), 256, 0, ctx->stream>>>(d_rays, (uint32_t)n, lo, sc, 1u << b, ctx->rs_k0.p,
+                                                              ctx->rs_v0.p);
+          uint32_t *kr = nullptr, *vr = nullptr;
+          e = radix_sort_pairs(ctx->rs_k0.p, ctx->rs_v0.p, ctx->rs_k1.p, ctx->rs_v1.p, (uint32_t)n, 3 * (int)b,
+                               ctx->rs_hist, ctx->rs_scan, ctx->stream, &kr, &vr);
+          perm = vr;
+        }
+      }
       if (e == cudaSuccess) {
-        BufferSrc src{d_rays};
-        HitSink4 sink{d_hits};
-        if (mode == WPBR_TRACE_ANY)
-          launch_traversal<true>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, ctx->stream);
-        else
-          launch_traversal<false>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, ctx->stream);
+        if (perm) {
+          PermSrc src{d_rays, perm};
+          PermHitSink4 sink{d_hits, perm};
+          if (mode == WPBR_TRACE_ANY)
+            launch_traversal<true>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, ctx->stream);
+          else
+            launch_traversal<false>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, ctx->stream);
+        } else {
+          BufferSrc src{d_rays};
+          HitSink4 sink{d_hits};
+          if (mode == WPBR_TRACE_ANY)
+            launch_traversal<true>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, ctx->stream);
+          else
+            launch_traversal<false>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, ctx->stream);
+        }
         e = cudaGetLastError();
       }
     }

@@ -535,6 +535,24 @@ struct HitSink4 {
     hits[i] = make_float4(h.t, __uint_as_float(h.prim), h.b1, h.b2);
   }
 };
+// Rays visited in the order of a permutation (sorted position -> input
+// index); hits land at the input index.
+struct PermSrc {
+  const float4* rays;
+  const uint32_t* perm;
+  __device__ __forceinline__ void load(uint32_t i, float4* o, float4* d) const {
+    size_t j = __ldg(&perm[i]);
+    *o = __ldg(&rays[2 * j]);
+    *d = __ldg(&rays[2 * j + 1]);
+  }
+};
+struct PermHitSink4 {
+  float4* hits;
+  const uint32_t* perm;
+  __device__ __forceinline__ void store(uint32_t i, const HitRec& h) const {
+    hits[__ldg(&perm[i])] = make_float4(h.t, __uint_as_float(h.prim), h.b1, h.b2);
+  }
+};
 struct PrimSink {
   uint32_t* prims;
   __device__ __forceinline__ void store(uint32_t i, const HitRec& h) const { prims[i] = h.prim; }
