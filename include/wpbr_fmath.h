@@ -280,6 +280,9 @@ WPBR_HD float logf_(float x) {
   return (k * 0x1.62ep-1f + lm) + k * 0x1.0bfbe8p-15f;
 }
 
+// log2 through logf_: log(x) / log(2) with the quotient taken in double.
+WPBR_HD float log2f_(float x) { return (float)((double)logf_(x) * 1.4426950408889634); }
+
 /* ---- double-precision sin / cos ------------------------------------------ */
 WPBR_HD double sin_kernel_d(double r) {
   double x = r * r;

@@ -181,7 +181,9 @@ enum { WPBR_SCENEGEN_RAYS = 1u };
  * res_x/1024, primitive counts capped at res_y; 1024 and 2000000 give the set
  * as specified), 4 the differentiable scene (config 0's geometry, 64
  * materials, sphere + 256x128 environment light; `level` seeds the material
- * parameters and the environment). Host-only, no GPU needed. */
+ * parameters and the environment), 5 the textured-metal scene (config 0's
+ * spheres, every third one and the ground CMaterialMetal with four procedural
+ * textures, grazing camera). Host-only, no GPU needed. */
 WPBR_API wpbr_status wpbr_scenegen_create(uint32_t config, uint32_t seed, uint32_t res_x, uint32_t res_y,
                                           uint32_t level, uint32_t flags, wpbr_scenegen** out);
 WPBR_API const wpbr_scene_desc* wpbr_scenegen_desc(const wpbr_scenegen* g);

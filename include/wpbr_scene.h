@@ -38,7 +38,13 @@ typedef struct wpbr_mat4 {
 enum wpbr_material_type {
   WPBR_MAT_CONDUCTOR = 0,  /* SBSDFConductorMicroface (Trowbridge-Reitz + conductor Fresnel) */
   WPBR_MAT_DIELECTRIC = 1, /* SBSDFDielectricMicroface (reflection lobe, dielectric Fresnel) */
-  WPBR_MAT_SPECULAR = 2    /* SBXDFSpecularReflectance (perfect glass material) */
+  WPBR_MAT_SPECULAR = 2,   /* SBXDFSpecularReflectance (perfect glass material) */
+  /* CMaterialMetal (CMaterialMetal.cpp:8-58): a conductor whose k is the
+   * metallic texture and whose alpha is roughnessToAlpha(clamp(90 * r, 0, 90))
+   * of the roughness texture's red channel, both looked up with anisotropic
+   * EWA filtering at the hit's texture footprint; R = 1, eta_i = 1,
+   * eta_t = 1.5. Texture indices in wpbr_material::tex. */
+  WPBR_MAT_METAL = 3
 };
 
 typedef struct wpbr_material {
@@ -49,7 +55,7 @@ typedef struct wpbr_material {
   float eta_i[3];    /* conductor: per channel; dielectric/specular: [0] */
   float eta_t[3];
   float k[3];        /* conductor absorption */
-  float pad;
+  uint16_t tex[2];   /* WPBR_MAT_METAL: metallic and roughness texture indices */
 } wpbr_material;     /* 64 bytes */
 
 typedef struct wpbr_sphere {
@@ -87,6 +93,13 @@ typedef struct wpbr_envmap {
   wpbr_mat4 world_to_light;
 } wpbr_envmap;
 
+/* An RGB texture (linear values, row 0 at t = 0), MIP-mapped at upload as
+ * SLoadTexture::generateMIPS does (CSTextureProcess.h:352-400). At least 4x4. */
+typedef struct wpbr_texture {
+  uint32_t width, height;
+  const float* rgb;          /* width*height*3 floats, row-major */
+} wpbr_texture;
+
 typedef struct wpbr_camera {
   wpbr_mat4 camera_to_world;
   wpbr_mat4 world_to_camera;
@@ -114,6 +127,8 @@ typedef struct wpbr_scene_desc {
   uint32_t n_lights;
   const wpbr_envmap* envmap; /* NULL when the scene has no infinite light */
   wpbr_camera camera;
+  const wpbr_texture* textures; /* referenced by WPBR_MAT_METAL materials */
+  uint32_t n_textures;
 } wpbr_scene_desc;
 
 /* Behaviour switches shared by the GPU pipeline and the CPU oracle.

@@ -37,6 +37,8 @@ _SIGS = {
     "orc_fmath_d": (None, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint64]),
     "orc_render_spectral": (None, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, _FP, _FP]),
     "orc_spectral_tables": (None, [_FP]),
+    "orc_texture_level": (C.c_uint32, [C.c_void_p, C.c_uint32, _FP, _UP]),
+    "orc_texture_eval": (None, [C.c_void_p, _FP, _FP]),
     "orc_adjoint_eval": (C.c_double, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_double),
                                       C.POINTER(C.c_double), _FP, C.POINTER(C.c_double), C.c_uint32, _UP,
                                       C.POINTER(C.c_double)]),
@@ -162,6 +164,38 @@ def spectral_tables():
     t = np.zeros(17 * 64, np.float32)
     lib().orc_spectral_tables(_fp(t))
     return t.reshape(17, 64)
+
+
+def _texture(rgb):
+    """A wpbr_texture over an (h, w, 3) float32 array (kept alive by the caller)."""
+    h, w, _ = rgb.shape
+    return A.Texture(w, h, rgb.ctypes.data_as(_FP))
+
+
+def texture_levels(rgb):
+    """The MIP pyramid the oracle builds for an (h, w, 3) texture: a list of
+    (h_l, w_l, 3) arrays, level 0 first."""
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    t = _texture(rgb)
+    n = lib().orc_texture_level(C.byref(t), 0, None, None)
+    out = []
+    for lvl in range(n):
+        wh = np.zeros(2, np.uint32)
+        buf = np.zeros(rgb.size, np.float32)
+        lib().orc_texture_level(C.byref(t), lvl, _fp(buf), _up(wh))
+        out.append(buf[: wh[0] * wh[1] * 3].reshape(wh[1], wh[0], 3))
+    return out
+
+
+def texture_eval(rgb, fp):
+    """Anisotropic EWA lookup of an (h, w, 3) texture at the footprint
+    fp = (s, t, ds/dx, dt/dx, ds/dy, dt/dy)."""
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    t = _texture(rgb)
+    f = np.asarray(fp, np.float32)
+    o = np.zeros(3, np.float32)
+    lib().orc_texture_eval(C.byref(t), _fp(f), _fp(o))
+    return o
 
 
 def philox(ctr, key):

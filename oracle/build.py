@@ -9,7 +9,8 @@ ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_build", "liboracle.so")
 SRC = [os.path.join(HERE, "oracle.cpp")]
 DEPS = SRC + [os.path.join(HERE, "oracle_math.hpp"), os.path.join(HERE, "oracle_adjoint.inc"),
-                                                      os.path.join(HERE, "oracle_spectral.inc")] + [
+                                                      os.path.join(HERE, "oracle_spectral.inc"),
+                                                      os.path.join(HERE, "oracle_texture.inc")] + [
     os.path.join(ROOT, "include", f) for f in ("wpbr_fmath.h", "wpbr_sampling.h", "wpbr_scene.h", "wpbr_record.h", "wpbr_spectrum_data.h")]
 FLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-I" + os.path.join(ROOT, "include")]
 

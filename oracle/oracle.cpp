@@ -155,6 +155,12 @@ struct Mat {
   float ax, ay;
   RGB R;
   float eta_i[3], eta_t[3], k[3];
+  uint32_t tex[2];
+};
+
+struct TexLevelO {
+  uint32_t w = 0, h = 0;
+  std::vector<RGB> t;
 };
 
 struct Light {
@@ -187,6 +193,8 @@ struct Scene {
   bool has_env = false;
   Env env;
   Camera cam;
+  std::vector<std::vector<TexLevelO>> textures;  /* MIP levels per texture */
+  float gauss[64];
   /* BVH (CSceneTreeLBVH, R/SLBVH.h:28-40) */
   std::vector<LinearNode> nodes;
   std::vector<Bounds> node_bounds;
@@ -758,6 +766,8 @@ static void env_li_compute(const Env& e, V3 wi, RGB* li, float* pdf) {
   }
 }
 
+#include "oracle_texture.inc"
+
 /* ------------------------------------------------------------------------ */
 /* BSDF Compute / Sample jobs                                                  */
 /* ------------------------------------------------------------------------ */
@@ -900,7 +910,7 @@ static SampleOut shade_sample(const Scene& sc, const wpbr_rng::Stream& rs, uint3
     f[3] = fr.ts.x; f[4] = fr.ts.y; f[5] = fr.ts.z;
     f[6] = fr.ns.x; f[7] = fr.ns.y; f[8] = fr.ns.z;
   }
-  const Mat& mat = sc.mats[prim_material(sc, h.prim)];
+  const Mat mat = hit_mat(sc, h.prim, si, rd);
   V3 wo_l = to_local(fr, si.wo);
   uint32_t nl = (uint32_t)sc.lights.size();
   if (nl == 0) {
@@ -1091,6 +1101,8 @@ static Scene* scene_from_desc(const wpbr_scene_desc* d, uint32_t quirks) {
       o.eta_t[c] = m.eta_t[c];
       o.k[c] = m.k[c];
     }
+    o.tex[0] = m.tex[0];
+    o.tex[1] = m.tex[1];
     sc->mats.push_back(o);
   }
   for (uint32_t i = 0; i < d->n_lights; ++i)
@@ -1109,6 +1121,11 @@ static Scene* scene_from_desc(const wpbr_scene_desc* d, uint32_t quirks) {
       if (d->lights[i].type == WPBR_LIGHT_ENV) e.le = RGB{d->lights[i].Le[0], d->lights[i].Le[1], d->lights[i].Le[2]};
     env_preprocess(e, quirks);
   }
+  for (uint32_t i = 0; i < d->n_textures; ++i) {
+    sc->textures.emplace_back();
+    build_texture(d->textures[i], sc->textures.back());
+  }
+  build_gauss(sc->gauss);
   camera_setup(d->camera, &sc->cam);
   build_bvh(*sc);
   return sc;
@@ -1349,5 +1366,39 @@ void orc_render_spectral(void* h, uint32_t spp, uint32_t seed, uint32_t stream, 
 void orc_spectral_tables(float* out) {
   const SpecTab& T = spec_tables();
   memcpy(out, &T, sizeof(T));
+}
+/* The MIP pyramid of one texture (SLoadTexture::generateMIPS): returns the
+ * level count; with out != NULL copies level `level` (w*h*3 floats) and
+ * writes its size to wh[2]. */
+uint32_t orc_texture_level(const wpbr_texture* t, uint32_t level, float* out, uint32_t* wh) {
+  std::vector<TexLevelO> lv;
+  build_texture(*t, lv);
+  if (out && level < lv.size()) {
+    const TexLevelO& L = lv[level];
+    for (size_t i = 0; i < L.t.size(); ++i) {
+      out[3 * i] = L.t[i].r;
+      out[3 * i + 1] = L.t[i].g;
+      out[3 * i + 2] = L.t[i].b;
+    }
+    wh[0] = L.w;
+    wh[1] = L.h;
+  }
+  return (uint32_t)lv.size();
+}
+/* STexture2DSamplerAnisotropic::eval of one texture at the footprint
+ * fp = (s, t, ds/dx, dt/dx, ds/dy, dt/dy); rgb to out[3]. */
+void orc_texture_eval(const wpbr_texture* t, const float* fp, float* out) {
+  std::vector<TexLevelO> lv;
+  build_texture(*t, lv);
+  float gauss[64];
+  build_gauss(gauss);
+  Footprint f;
+  f.p = V2{fp[0], fp[1]};
+  f.dx = V2{fp[2], fp[3]};
+  f.dy = V2{fp[4], fp[5]};
+  RGB c = tx_aniso(lv, gauss, f);
+  out[0] = c.r;
+  out[1] = c.g;
+  out[2] = c.b;
 }
 }

@@ -37,6 +37,8 @@ def test_struct_layouts(W):
     assert C.sizeof(A.Mesh) == 16
     assert C.sizeof(A.Light) == 20
     assert C.sizeof(A.PassRecord) == 32 * 8
+    assert C.sizeof(A.Texture) == 16
+    assert A.Material.tex.offset == 60 and A.SceneDesc.n_textures.offset == A.SceneDesc.textures.offset + 8
 
 
 def test_host_entry_points_validate_arguments(W):
@@ -64,9 +66,12 @@ def test_scenegen_counts_and_determinism(W):
     assert np.array_equal(pos, np.ctypeslib.as_array(d2.positions, shape=(d2.n_vertices * 3,)))
     r = np.linalg.norm(pos.reshape(-1, 3), axis=1)
     assert 0.89 < r.min() and r.max() < 1.11
-    c0 = W.SceneGen(0, 0, (256, 256)).desc.contents
+    # the desc points into its generator: keep each generator alive while it is read
+    g0 = W.SceneGen(0, 0, (256, 256))
+    c0 = g0.desc.contents
     assert c0.n_spheres == 65 and c0.n_triangles == 2 and c0.n_lights == 1
-    c2 = W.SceneGen(2, 0, (64, 36), level=4).desc.contents
+    g2 = W.SceneGen(2, 0, (64, 36), level=4)
+    c2 = g2.desc.contents
     assert c2.n_spheres == 256 and c2.envmap.contents.width == 1024 and c2.envmap.contents.height == 512
 
 
@@ -95,7 +100,8 @@ def test_batched_scene_set(W):
     # icosphere level (or a sphere set), films from {256, 512, 768, 1024}^2
     films, counts, spheres_sets = set(), [], 0
     for k in range(32):
-        d = W.SceneGen(3, seed=3, res=(1024, 2000000), level=k).desc.contents
+        gk = W.SceneGen(3, seed=3, res=(1024, 2000000), level=k)
+        d = gk.desc.contents
         assert d.camera.res_x == d.camera.res_y
         films.add(d.camera.res_x)
         n = d.n_triangles + d.n_spheres - 1  # the light's sphere
@@ -105,10 +111,11 @@ def test_batched_scene_set(W):
     assert films <= {256, 512, 768, 1024} and len(films) >= 3
     assert 10000 <= min(counts) and max(counts) <= 2000000 and len(set(counts)) >= 5
     assert 0 < spheres_sets < 32
-    a = W.SceneGen(3, seed=3, res=(1024, 2000000), level=13).desc.contents
-    b = W.SceneGen(3, seed=3, res=(1024, 2000000), level=13).desc.contents
+    ga, gb = (W.SceneGen(3, seed=3, res=(1024, 2000000), level=13) for _ in range(2))
+    a, b = ga.desc.contents, gb.desc.contents
     assert a.n_spheres == b.n_spheres and bytes(a.spheres[5]) == bytes(b.spheres[5])
-    small = W.SceneGen(3, seed=3, res=(128, 20000), level=1).desc.contents
+    gs = W.SceneGen(3, seed=3, res=(128, 20000), level=1)
+    small = gs.desc.contents
     assert small.camera.res_x in (32, 64, 96, 128) and small.n_spheres + small.n_triangles <= 20001 + 1
 
 
@@ -117,3 +124,30 @@ def test_batch_entry_points_validate_arguments(W):
     assert W.lib().wpbr_batch_add_scene(None, None, 0, None) == W.ERR_INVALID_ARG
     assert W.lib().wpbr_batch_info_get(None, None) == W.ERR_INVALID_ARG
     assert W.lib().wpbr_batch_last_error(None) == b"null batch"
+
+
+def test_textured_scene_generation(W):
+    g = W.SceneGen(5, 3, (64, 48))
+    d = g.desc.contents
+    assert d.n_textures == 4 and d.n_spheres == 65 and d.n_triangles == 2
+    metal = [m for m in range(d.n_materials) if d.materials[m].type == 3]
+    assert len(metal) == 2
+    for m in metal:
+        assert all(t < d.n_textures for t in d.materials[m].tex)
+    # ground and every third sphere are textured metal
+    assert d.meshes[0].material in metal
+    assert sum(d.spheres[i].material in metal for i in range(64)) == 22
+
+    def texels(desc, i):
+        t = desc.textures[i]
+        return np.ctypeslib.as_array(t.rgb, shape=(t.width * t.height * 3,)).copy()
+
+    g2, g3 = W.SceneGen(5, 3, (64, 48)), W.SceneGen(5, 4, (64, 48))  # keep the generators alive
+    d2, d3 = g2.desc.contents, g3.desc.contents
+    for i in range(4):
+        a = texels(d, i)
+        assert np.isfinite(a).all() and (a >= 0).all()
+        assert np.array_equal(a, texels(d2, i))
+        assert not np.array_equal(a, texels(d3, i))
+    rough = texels(d, 1).reshape(64, 64, 3)[..., 0]
+    assert 1e-6 < rough.min() and rough.max() <= 1e-2

@@ -18,7 +18,7 @@ class Material(C.Structure):
         ("eta_i", C.c_float * 3),
         ("eta_t", C.c_float * 3),
         ("k", C.c_float * 3),
-        ("pad", C.c_float),
+        ("tex", C.c_uint16 * 2),
     ]
 
 
@@ -63,6 +63,10 @@ class Camera(C.Structure):
     ]
 
 
+class Texture(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("rgb", C.POINTER(C.c_float))]
+
+
 class SceneDesc(C.Structure):
     _fields_ = [
         ("spheres", C.POINTER(Sphere)),
@@ -82,6 +86,8 @@ class SceneDesc(C.Structure):
         ("n_lights", C.c_uint32),
         ("envmap", C.POINTER(EnvMap)),
         ("camera", Camera),
+        ("textures", C.POINTER(Texture)),
+        ("n_textures", C.c_uint32),
     ]
 
 

@@ -596,6 +596,8 @@ wpbr_status adjoint_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t s
   if (spp == 0) return set_err(ctx, WPBR_ERR_INVALID_ARG, "adjoint_setup: spp must be > 0");
   if (ctx->spectrum != WPBR_SPECTRUM_RGB)
     return set_err(ctx, WPBR_ERR_INVALID_ARG, "adjoint_setup: the differentiable estimator runs in RGB mode only");
+  if (ctx->has_metal)
+    return set_err(ctx, WPBR_ERR_INVALID_ARG, "adjoint_setup: textured metal materials have no material parameters");
   if (ctx->nmat > kMaxAdjMaterials)
     return set_err(ctx, WPBR_ERR_INVALID_ARG, "adjoint_setup: more than 1024 materials");
   AdjState& J = ctx->adj;

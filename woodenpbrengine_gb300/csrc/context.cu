@@ -2,6 +2,8 @@
 // upload, BVH build/export, collision, rendering entry points.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -61,6 +63,7 @@ SceneView scene_view(const wpbr_ctx* ctx) {
   e.le = ctx->env_le;
   S.cam = ctx->cam;
   S.quirks = ctx->quirks;
+  S.tex = TexView{ctx->tex_texels.p, ctx->tex_levels.p, ctx->tex_info.p, ctx->tex_gauss.p, ctx->ntex};
   return S;
 }
 
@@ -69,6 +72,51 @@ SceneView scene_view(const wpbr_ctx* ctx) {
 using namespace wpbr;
 
 namespace {
+
+// SLoadTexture::generateMIPS (CSTextureProcess.h:352-400): floor(log2(max
+// side)) - 1 levels, each the 2x2 box average of the previous one; the last
+// column and row average the previous level's last column / row only, the
+// corner copies its last texel.
+void build_mips(const wpbr_texture& t, std::vector<float4>& tx, std::vector<TexLevel>& lv, std::vector<TexInfo>& ti) {
+  uint32_t n = (uint32_t)(uint16_t)(std::log2((double)std::max(t.width, t.height)) - 1.0);
+  if (n < 1) n = 1;
+  TexInfo info{(uint32_t)lv.size(), n};
+  uint32_t W = t.width, H = t.height;
+  uint32_t base = (uint32_t)tx.size();
+  lv.push_back(TexLevel{base, W, H, 0});
+  for (size_t i = 0; i < (size_t)W * H; ++i) tx.push_back(make_float4(t.rgb[3 * i], t.rgb[3 * i + 1], t.rgb[3 * i + 2], 0.0f));
+  for (uint32_t l = 1; l < n; ++l) {
+    TexLevel pv = lv.back();
+    uint32_t w = std::max(1u, pv.w / 2), h = std::max(1u, pv.h / 2);
+    uint32_t off = (uint32_t)tx.size();
+    tx.resize(tx.size() + (size_t)w * h);
+    auto P = [&](uint32_t x, uint32_t y) { return tx[pv.offset + (size_t)y * pv.w + x]; };
+    auto avg4 = [](float4 a, float4 b, float4 c, float4 d) {
+      return make_float4((((a.x + b.x) + c.x) + d.x) * 0.25f, (((a.y + b.y) + c.y) + d.y) * 0.25f,
+                         (((a.z + b.z) + c.z) + d.z) * 0.25f, 0.0f);
+    };
+    auto avg2 = [](float4 a, float4 b) {
+      return make_float4((a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f, 0.0f);
+    };
+    for (uint32_t y = 0; y + 1 < h; ++y) {
+      for (uint32_t x = 0; x + 1 < w; ++x)
+        tx[off + (size_t)y * w + x] = avg4(P(2 * x, 2 * y), P(2 * x + 1, 2 * y), P(2 * x, 2 * y + 1), P(2 * x + 1, 2 * y + 1));
+      tx[off + (size_t)y * w + (w - 1)] = avg2(P(pv.w - 1, 2 * y), P(pv.w - 1, 2 * y + 1));
+    }
+    for (uint32_t x = 0; x + 1 < w; ++x) tx[off + (size_t)(h - 1) * w + x] = avg2(P(2 * x, pv.h - 1), P(2 * x + 1, pv.h - 1));
+    tx[off + (size_t)(h - 1) * w + (w - 1)] = P(pv.w - 1, pv.h - 1);
+    lv.push_back(TexLevel{off, w, h, 0});
+  }
+  ti.push_back(info);
+}
+
+// JobFilterTableGaussing (CSTextureProcess.cpp:16-32): exp(-2 r2) - exp(-2)
+void gauss_table(float* w) {
+  for (int i = 0; i < kGaussTable; ++i) {
+    float r2 = (float)i / (float)(kGaussTable - 1);
+    w[i] = wpbr_fm::expf_(-2.0f * r2) - wpbr_fm::expf_(-2.0f);
+  }
+}
 
 template <typename T>
 cudaError_t upload(DevBuf<T>& d, const T* h, size_t n, cudaStream_t s) {
@@ -151,6 +199,7 @@ WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
   ctx->tri_mat.release(); ctx->tri_flags.release(); ctx->mats.release(); ctx->lights.release();
   ctx->env_rgb.release(); ctx->cond_func.release(); ctx->cond_cdf.release(); ctx->cond_int.release();
   ctx->marg_func.release(); ctx->marg_cdf.release(); ctx->marg_int.release(); ctx->env_lum.release();
+  ctx->tex_texels.release(); ctx->tex_levels.release(); ctx->tex_info.release(); ctx->tex_gauss.release();
   bvh_release(ctx, false);
   RenderState& R = ctx->rs;
   R.acc.release(); R.hit_prim.release(); R.shadow_rays.release(); R.shadow_hit.release(); R.pstate.release();
@@ -291,6 +340,20 @@ WPBR_API wpbr_status wpbr_scene_upload(wpbr_ctx* ctx, const wpbr_scene_desc* d) 
     return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: camera resolution is zero");
   if (d->n_spheres + (uint64_t)d->n_triangles >= (1ull << 29))
     return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: more than 2^29 primitives");
+  if (d->n_textures && !d->textures) return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: textures pointer is null");
+  for (uint32_t i = 0; i < d->n_textures; ++i)
+    if (d->textures[i].width < 4 || d->textures[i].height < 4 || !d->textures[i].rgb)
+      return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: textures must be at least 4x4");
+  bool has_metal = false;
+  for (uint32_t m = 0; m < d->n_materials; ++m) {
+    const wpbr_material& mt = d->materials[m];
+    if (mt.type > WPBR_MAT_METAL) return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: unknown material type");
+    if (mt.type == WPBR_MAT_METAL) {
+      if (mt.tex[0] >= d->n_textures || mt.tex[1] >= d->n_textures)
+        return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: metal material texture index out of range");
+      has_metal = true;
+    }
+  }
 
   cudaStream_t st = ctx->stream;
   ctx->has_scene = false;
@@ -350,6 +413,20 @@ WPBR_API wpbr_status wpbr_scene_upload(wpbr_ctx* ctx, const wpbr_scene_desc* d) 
     for (uint32_t i = 0; i < d->n_lights; ++i)
       if (d->lights[i].type == WPBR_LIGHT_ENV) ctx->env_le = RGB3{d->lights[i].Le[0], d->lights[i].Le[1], d->lights[i].Le[2]};
   }
+  // textures: MIP pyramids on the host (SLoadTexture::generateMIPS), one
+  // float4 array for every level of every texture, and the EWA filter table
+  std::vector<float4> tx;
+  std::vector<TexLevel> lv;
+  std::vector<TexInfo> ti;
+  for (uint32_t i = 0; i < d->n_textures; ++i) build_mips(d->textures[i], tx, lv, ti);
+  ctx->ntex = d->n_textures;
+  ctx->has_metal = has_metal;
+  WPBR_CUDA(upload(ctx->tex_texels, tx.empty() ? nullptr : tx.data(), tx.size(), st));
+  WPBR_CUDA(upload(ctx->tex_levels, lv.empty() ? nullptr : lv.data(), lv.size(), st));
+  WPBR_CUDA(upload(ctx->tex_info, ti.empty() ? nullptr : ti.data(), ti.size(), st));
+  float gauss[kGaussTable];
+  gauss_table(gauss);
+  WPBR_CUDA(upload(ctx->tex_gauss, gauss, kGaussTable, st));
   ctx->cam = camera_setup(d->camera);
   WPBR_CUDA(cudaStreamSynchronize(st));
   ctx->has_scene = true;

@@ -144,6 +144,13 @@ struct wpbr_ctx {
   bool has_nrm = false, has_uv = false;
   wpbr::DevBuf<wpbr_material> mats;
   uint32_t nmat = 0;
+  // MIP-mapped textures (all levels of all textures) and the EWA filter table
+  wpbr::DevBuf<float4> tex_texels;
+  wpbr::DevBuf<wpbr::TexLevel> tex_levels;
+  wpbr::DevBuf<wpbr::TexInfo> tex_info;
+  wpbr::DevBuf<float> tex_gauss;
+  uint32_t ntex = 0;
+  bool has_metal = false;
   wpbr::DevBuf<wpbr_light> lights;
   std::vector<wpbr_light> h_lights;
   bool has_env = false;

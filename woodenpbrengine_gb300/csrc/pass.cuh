@@ -67,6 +67,39 @@ __device__ SurfInt make_si(const SceneView& S, uint32_t prim, V3 o, V3 d) {
   return triangle_si(td, d, b0, b1, b2);
 }
 
+// The material of a hit: the scene's, or for WPBR_MAT_METAL the conductor
+// built from its textures at the hit's footprint (camera-ray differentials,
+// sphere or uv mapping).
+__device__ wpbr_material hit_material(const SceneView& S, uint32_t prim, uint32_t mid, const SurfInt& s,
+                                      const RayD& r) {
+  wpbr_material m = S.mats[mid];
+  if (m.type != WPBR_MAT_METAL) return m;
+  SurfDiff D = surf_differentials(s, r);
+  TexFootprint fp = prim < S.ns ? sphere_footprint(S.sph_w2o[prim], s, D) : uv_footprint(s, D);
+  return metal_material(S.tex, m, fp);
+}
+// The part of a textured-metal material that varies per hit, packed in a
+// float4 (alpha, k.rgb), and its inverse.
+__device__ __forceinline__ float4 metal_pack(const wpbr_material& m) {
+  return make_float4(m.alpha_x, m.k[0], m.k[1], m.k[2]);
+}
+__device__ __forceinline__ wpbr_material metal_unpack(float4 v) {
+  wpbr_material e;
+  e.type = WPBR_MAT_CONDUCTOR;
+  e.alpha_x = v.x;
+  e.alpha_y = v.x;
+  for (int c = 0; c < 3; ++c) {
+    e.R[c] = 1.0f;
+    e.eta_i[c] = 1.0f;
+    e.eta_t[c] = 1.5f;
+  }
+  e.k[0] = v.y;
+  e.k[1] = v.z;
+  e.k[2] = v.w;
+  e.tex[0] = e.tex[1] = 0;
+  return e;
+}
+
 __device__ __forceinline__ void pixel_xy(uint32_t pix, uint32_t W, uint32_t* x, uint32_t* y) {
   *x = pix % W;
   *y = pix / W;

@@ -24,10 +24,10 @@ namespace {
 enum FF {
   F_PFILM, F_RAY_O, F_RAY_D, F_RAY_DX, F_RAY_DY, F_HIT_T, F_SI_P, F_SI_N, F_SI_WO, F_SI_SN, F_SI_SDPDU, F_SI_DPDU,
   F_SI_DPDV, F_SI_DNDU, F_SI_DNDV, F_FRAME, F_LE, F_L_WI, F_L_LI, F_L_PDF, F_L_F, F_L_FPDF, F_B_WI, F_B_F, F_B_PDF,
-  F_B_LI, F_B_LPDF, F_L, F_COUNT
+  F_B_LI, F_B_LPDF, F_L, F_MAT, F_COUNT
 };
-constexpr int kFW_h[F_COUNT] = {2, 3, 3, 3, 3, 1, 3, 3, 3, 3, 3, 3, 3, 3, 3, 9, 3, 3, 3, 1, 3, 1, 3, 3, 1, 3, 1, 3};
-__constant__ int kFW_d[F_COUNT] = {2, 3, 3, 3, 3, 1, 3, 3, 3, 3, 3, 3, 3, 3, 3, 9, 3, 3, 3, 1, 3, 1, 3, 3, 1, 3, 1, 3};
+constexpr int kFW_h[F_COUNT] = {2, 3, 3, 3, 3, 1, 3, 3, 3, 3, 3, 3, 3, 3, 3, 9, 3, 3, 3, 1, 3, 1, 3, 3, 1, 3, 1, 3, 4};
+__constant__ int kFW_d[F_COUNT] = {2, 3, 3, 3, 3, 1, 3, 3, 3, 3, 3, 3, 3, 3, 3, 9, 3, 3, 3, 1, 3, 1, 3, 3, 1, 3, 1, 3, 4};
 #ifdef __CUDA_ARCH__
 #define kFW kFW_d
 #else
@@ -105,6 +105,17 @@ __device__ __forceinline__ Frame load_frame(const float* f, uint32_t pix) {
 __global__ void kj_bsdf_setup(PassCtx P, Staged G) {
   uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= P.W * P.H || G.u[U_HIT_PRIM][pix] == kNoHit) return;
+  uint32_t prim = G.u[U_HIT_PRIM][pix];
+  uint32_t mid = prim_material(P.S, prim);
+  if (P.S.mats[mid].type == WPBR_MAT_METAL) {
+    // JobComputeDifferentialsForSurfInter + the uv mapping jobs +
+    // JobGenerateBSDFMaterialMetal (MEngine.cpp:399-403)
+    RayD r = camera_ray(P.S.cam, G.f[F_PFILM][2 * pix], G.f[F_PFILM][2 * pix + 1]);
+    SurfInt hs = make_si(P.S, prim, r.o, r.d);
+    float4 v = metal_pack(hit_material(P.S, prim, mid, hs, r));
+    float* q = G.f[F_MAT] + 4 * (size_t)pix;
+    q[0] = v.x; q[1] = v.y; q[2] = v.z; q[3] = v.w;
+  }
   SurfInt s;
   s.sdpdu = ld3(G.f[F_SI_SDPDU], pix);
   s.sn = ld3(G.f[F_SI_SN], pix);
@@ -139,12 +150,19 @@ __global__ void kj_shadow_light(PassCtx P, Staged G) {
   G.u[U_L_FLAGS][pix] = 1u | ((hp == kNoHit || hp == lp) ? 2u : 0u);
 }
 
+__device__ __forceinline__ wpbr_material staged_material(const PassCtx& P, const Staged& G, uint32_t pix) {
+  const wpbr_material& m = P.S.mats[prim_material(P.S, G.u[U_HIT_PRIM][pix])];
+  if (m.type != WPBR_MAT_METAL) return m;
+  const float* q = G.f[F_MAT] + 4 * (size_t)pix;
+  return metal_unpack(make_float4(q[0], q[1], q[2], q[3]));
+}
+
 __global__ void kj_bsdf_compute(PassCtx P, Staged G) {
   uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= P.W * P.H || G.u[U_HIT_PRIM][pix] == kNoHit || P.S.nlights == 0) return;
   if (!(G.u[U_L_FLAGS][pix] & 2u)) return;
   Frame fr = load_frame(G.f[F_FRAME], pix);
-  const wpbr_material& m = P.S.mats[prim_material(P.S, G.u[U_HIT_PRIM][pix])];
+  wpbr_material m = staged_material(P, G, pix);
   float pdf;
   RGB3 f = bsdf_eval(m, to_local(fr, ld3(G.f[F_SI_WO], pix)), to_local(fr, ld3(G.f[F_L_WI], pix)), &pdf);
   stc(G.f[F_L_F], pix, f);
@@ -167,7 +185,7 @@ __global__ void kj_sample_bsdf(PassCtx P, uint32_t pass, Staged G) {
   uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= P.W * P.H || G.u[U_HIT_PRIM][pix] == kNoHit || P.S.nlights == 0) return;
   Frame fr = load_frame(G.f[F_FRAME], pix);
-  const wpbr_material& m = P.S.mats[prim_material(P.S, G.u[U_HIT_PRIM][pix])];
+  wpbr_material m = staged_material(P, G, pix);
   float u0, u1;
   wpbr_rng::sample2d(P.rs, pix, pass, wpbr_rng::DIM_BSDF, &u0, &u1);
   V3 wi_l;
@@ -231,8 +249,8 @@ __global__ void k_film(uint32_t W, uint32_t H, const float2* pf, const float4* L
 
 // ============================== fused pass ==================================
 // Compact per-pixel state written by k_spawn and read by k_finish.
-constexpr int kStateF4 = 6;
-enum : uint32_t { SF_VALID = 1u, SF_TRACE_L = 2u, SF_TRACE_B = 4u, SF_HIT = 8u };
+constexpr int kStateF4 = 7;
+enum : uint32_t { SF_VALID = 1u, SF_TRACE_L = 2u, SF_TRACE_B = 4u, SF_HIT = 8u, SF_METAL = 16u };
 
 __global__ void __launch_bounds__(kTB) k_spawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
                                                float4* state, float4* rays, float4* Lb, float2* pf) {
@@ -260,7 +278,11 @@ __global__ void __launch_bounds__(kTB) k_spawn(PassCtx P, const uint32_t* pass_d
   SurfInt s = make_si(P.S, prim, r.o, r.d);
   Frame fr = bsdf_frame(s);
   uint32_t mid = prim_material(P.S, prim);
-  const wpbr_material& m = P.S.mats[mid];
+  const wpbr_material m = hit_material(P.S, prim, mid, s, r);
+  if (P.S.mats[mid].type == WPBR_MAT_METAL) {
+    flags |= SF_METAL;
+    st[6] = metal_pack(m);
+  }
   V3 wo_l = to_local(fr, s.wo);
   uint32_t li_idx = pick_light(P, pix, pass);
   const wpbr_light& lt = P.S.lights[li_idx];
@@ -311,7 +333,7 @@ __global__ void __launch_bounds__(kTB) k_finish(PassCtx P, const float4* state, 
   uint32_t li_idx = __float_as_uint(s1.w);
   const wpbr_light& lt = P.S.lights[li_idx];
   uint32_t lp = light_prim(lt);
-  const wpbr_material& m = P.S.mats[__float_as_uint(s2.w)];
+  const wpbr_material m = (flags & SF_METAL) ? metal_unpack(st[6]) : P.S.mats[__float_as_uint(s2.w)];
   float4 l4 = Lb[pix];
   RGB3 L{l4.x, l4.y, l4.z};
   if (flags & SF_TRACE_L) {
@@ -624,7 +646,7 @@ wpbr_status job_record(wpbr_ctx* ctx, uint32_t x0, uint32_t y0, uint32_t x1, uin
                           rec->si_p, rec->si_n, rec->si_wo, rec->si_sn, rec->si_sdpdu, rec->si_dpdu,
                           rec->si_dpdv, rec->si_dndu, rec->si_dndv, rec->frame, rec->le, rec->l_wi,
                           rec->l_li, rec->l_pdf, rec->l_f, rec->l_fpdf, rec->b_wi, rec->b_f,
-                          rec->b_pdf, rec->b_li, rec->b_lpdf, rec->L};
+                          rec->b_pdf, rec->b_li, rec->b_lpdf, rec->L, nullptr};
   uint32_t* uptr[4] = {rec->hit_prim, rec->light_idx, rec->l_flags, rec->b_flags};
   cudaStream_t st = ctx->stream;
   uint32_t w = x1 - x0;

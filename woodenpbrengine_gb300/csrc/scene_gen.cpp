@@ -108,6 +108,9 @@ struct wpbr_scenegen {
   wpbr_envmap env;
   bool has_env = false;
   wpbr_camera cam;
+  std::vector<std::vector<float>> tex_rgb;  // one rgb array per texture
+  std::vector<uint32_t> tex_wh;             // width, height per texture
+  std::vector<wpbr_texture> texs;
   wpbr_scene_desc desc;
   std::vector<float> rays;  // n * 8
 
@@ -280,6 +283,30 @@ struct wpbr_scenegen {
     desc.n_lights = (uint32_t)lights.size();
     desc.envmap = has_env ? &env : nullptr;
     desc.camera = cam;
+    texs.clear();
+    for (size_t i = 0; i < tex_rgb.size(); ++i) texs.push_back(wpbr_texture{tex_wh[2 * i], tex_wh[2 * i + 1], tex_rgb[i].data()});
+    desc.textures = texs.empty() ? nullptr : texs.data();
+    desc.n_textures = (uint32_t)texs.size();
+  }
+  // A procedural texture: `fn(x, y, rgb)` fills texel (x, y).
+  template <typename F>
+  uint16_t add_texture(uint32_t W, uint32_t H, F fn) {
+    std::vector<float> t((size_t)W * H * 3);
+    for (uint32_t y = 0; y < H; ++y)
+      for (uint32_t x = 0; x < W; ++x) fn(x, y, &t[3 * ((size_t)y * W + x)]);
+    tex_rgb.push_back(std::move(t));
+    tex_wh.push_back(W);
+    tex_wh.push_back(H);
+    return (uint16_t)(tex_rgb.size() - 1);
+  }
+  uint32_t add_metal(uint16_t metallic, uint16_t roughness) {
+    wpbr_material m;
+    memset(&m, 0, sizeof(m));
+    m.type = WPBR_MAT_METAL;
+    m.tex[0] = metallic;
+    m.tex[1] = roughness;
+    mats.push_back(m);
+    return (uint32_t)mats.size() - 1;
   }
   void make_env(uint32_t W, uint32_t H, uint32_t seed) {
     Rng rng(seed, 0xE417u);
@@ -412,6 +439,67 @@ void gen_config4(wpbr_scenegen* g, uint32_t seed, uint32_t param_seed, uint32_t 
   g->add_quad(40.0f, 40.0f, V3{0.0f, -11.0f, 0.0f}, 0);
   g->make_env(256, 128, 0xC4E0u + param_seed);
   g->set_camera(V3{0.0f, 3.0f, -30.0f}, V3{0.0f, -2.0f, 0.0f}, 60.0f, W, H);
+}
+
+// Config 5, the textured-metal scene: config 0's spheres and light with every
+// third sphere and the ground quad made of CMaterialMetal. Four procedural
+// textures: a 256x256 checker of two metallic k colours with seeded texel
+// noise (ground k), a 64x64 diagonal roughness ramp from 1e-5 to 1e-2 (log
+// scale, with noise; roughnessToAlpha(90 r) then spans alpha ~0.04 to ~1.6)
+// for the ground, a 100x60 striped metallic (sphere k; odd sizes exercise
+// the MIP edge rules) and a 32x16 log-uniform roughness for the spheres. The camera looks
+// along the ground at a grazing angle, so the footprints are anisotropic.
+void gen_config5(wpbr_scenegen* g, uint32_t seed, uint32_t W, uint32_t H) {
+  Rng tr(seed, 0xC5u);
+  float ka[3] = {tr.uni(0.2f, 3.0f), tr.uni(0.2f, 3.0f), tr.uni(0.2f, 3.0f)};
+  float kb[3] = {tr.uni(0.2f, 3.0f), tr.uni(0.2f, 3.0f), tr.uni(0.2f, 3.0f)};
+  uint16_t t_km = g->add_texture(256, 256, [&](uint32_t x, uint32_t y, float* c) {
+    const float* k = (((x >> 5) ^ (y >> 5)) & 1) ? ka : kb;
+    for (int ch = 0; ch < 3; ++ch) c[ch] = k[ch] * tr.uni(0.9f, 1.1f);
+  });
+  uint16_t t_kr = g->add_texture(64, 64, [&](uint32_t x, uint32_t y, float* c) {
+    c[0] = wpbr_fm::expf_(2.3025851f * (-5.0f + 3.0f * (float)((x + y) & 63) / 63.0f)) * tr.uni(0.5f, 1.0f);
+    c[1] = tr.u01();
+    c[2] = 0.0f;
+  });
+  uint16_t t_sm = g->add_texture(100, 60, [&](uint32_t x, uint32_t y, float* c) {
+    const float* k = ((x / 7 + y / 11) & 1) ? ka : kb;
+    for (int ch = 0; ch < 3; ++ch) c[ch] = k[ch] * tr.uni(0.8f, 1.2f);
+  });
+  uint16_t t_sr = g->add_texture(32, 16, [&](uint32_t, uint32_t, float* c) {
+    c[0] = wpbr_fm::expf_(2.3025851f * tr.uni(-5.0f, -2.0f));
+    c[1] = c[2] = 0.5f;
+  });
+  uint32_t m_ground = g->add_metal(t_km, t_kr);
+  uint32_t m_sphere = g->add_metal(t_sm, t_sr);
+  Rng rng(seed, 0xC0u);
+  for (int i = 0; i < 64; ++i) {
+    V3 c{rng.uni(-10.0f, 10.0f), rng.uni(-10.0f, 10.0f), rng.uni(-10.0f, 10.0f)};
+    float r = rng.uni(0.2f, 1.0f);
+    float alpha = rng.uni(0.05f, 0.5f);
+    uint32_t m;
+    if ((i & 1) == 0) {
+      float eta[3] = {rng.uni(0.2f, 3.0f), rng.uni(0.2f, 3.0f), rng.uni(0.2f, 3.0f)};
+      float k[3] = {rng.uni(0.2f, 3.0f), rng.uni(0.2f, 3.0f), rng.uni(0.2f, 3.0f)};
+      m = g->add_material(WPBR_MAT_CONDUCTOR, alpha, eta, k);
+    } else {
+      float e = rng.uni(1.3f, 1.7f);
+      float eta[3] = {e, e, e}, k[3] = {0, 0, 0};
+      m = g->add_material(WPBR_MAT_DIELECTRIC, alpha, eta, k);
+    }
+    g->add_sphere(c, r, i % 3 == 0 ? m_sphere : m);
+  }
+  float le[3] = {1.5f, 1.5f, 1.5f}, lk[3] = {1.0f, 1.0f, 1.0f};
+  uint32_t ml = g->add_material(WPBR_MAT_CONDUCTOR, 0.3f, le, lk);
+  g->add_sphere(V3{0.0f, 15.0f, 0.0f}, 1.0f, ml);
+  wpbr_light L;
+  memset(&L, 0, sizeof(L));
+  L.type = WPBR_LIGHT_SPHERE;
+  L.sphere_index = (uint32_t)g->spheres.size() - 1;
+  L.Le[0] = L.Le[1] = L.Le[2] = 10.0f;
+  g->lights.push_back(L);
+  g->add_quad(40.0f, 40.0f, V3{0.0f, -11.0f, 0.0f}, m_ground);
+  g->set_camera(V3{0.0f, -9.5f, -24.0f}, V3{0.0f, -10.5f, 0.0f}, 60.0f, W, H);
 }
 
 void gen_config1(wpbr_scenegen* g, uint32_t seed, uint32_t W, uint32_t H, uint32_t level, bool with_rays) {
@@ -600,6 +688,9 @@ WPBR_API wpbr_status wpbr_scenegen_create(uint32_t config, uint32_t seed, uint32
     } else if (config == 3) {
       // `level` selects the scene of the set; res_x scales the films, res_y caps the counts
       gen_config3(g, level, seed, res_x, res_y);
+      g->finish();
+    } else if (config == 5) {
+      gen_config5(g, seed, res_x, res_y);
       g->finish();
     } else {
       delete g;

@@ -16,6 +16,7 @@ struct SurfInt {
   V3 p, n, wo;
   V3 dpdu, dpdv, dndu, dndv;
   V3 sn, sdpdu;
+  V2 uv;  // triangles: interpolated uv; spheres: (0, 0), the world transform drops it
 };
 
 // SSphere::computeSurfInteraction (CSSphere.cpp:122-186) then
@@ -38,6 +39,7 @@ WPBR_HD SurfInt sphere_si(const Xf& o2w, const Xf& w2o, float radius, V3 rld, V3
   V3 dndv = add(mul(dpdu, (g * F - f * G) * inv), mul(dpdv, (f * F - g * E) * inv));
   V3 n = normalize(cross(dpdu, dpdv));
   SurfInt s;
+  s.uv = V2{0.0f, 0.0f};
   s.p = xpoint(o2w, ph);
   s.n = normalize(xnormal(w2o, n));
   s.wo = normalize(xvector(o2w, neg(rld)));
@@ -86,6 +88,7 @@ WPBR_HD SurfInt triangle_si(const TriData& tv, V3 rd, float b0, float b1, float 
   V3 dpdv = mul(add(mul(neg(dp02), duv12.x), mul(dp12, duv02.x)), det_inv);
   SurfInt s;
   s.p = add(add(mul(tv.p[0], b0), mul(tv.p[1], b1)), mul(tv.p[2], b2));
+  s.uv = V2{(uv0.x * b0 + uv1.x * b1) + uv2.x * b2, (uv0.y * b0 + uv1.y * b1) + uv2.y * b2};
   s.wo = neg(rd);
   s.dpdu = dpdu;
   s.dpdv = dpdv;

@@ -7,6 +7,7 @@
 #include "camera.cuh"
 #include "geom.cuh"
 #include "shade.cuh"
+#include "texture.cuh"
 #include "wpbr_scene.h"
 
 namespace wpbr {
@@ -31,6 +32,7 @@ struct SceneView {
   EnvView env;
   CameraParams cam;
   uint32_t quirks;
+  TexView tex;  // textures of WPBR_MAT_METAL materials
 };
 
 // Child-pair BVH node: the bounds of both children of one interior node of
