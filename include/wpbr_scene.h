@@ -44,8 +44,13 @@ enum wpbr_material_type {
    * of the roughness texture's red channel, both looked up with anisotropic
    * EWA filtering at the hit's texture footprint; R = 1, eta_i = 1,
    * eta_t = 1.5. Texture indices in wpbr_material::tex. */
-  WPBR_MAT_METAL = 3
+  WPBR_MAT_METAL = 3,
+  /* The same material looked up with the isotropic trilinear sampler
+   * (STexture2DSamplerIsotropic, CSTextureProcess.h:259-289), the
+   * alternative left commented out in CMaterialMetal.cpp:34-35. */
+  WPBR_MAT_METAL_ISOTROPIC = 4
 };
+#define WPBR_MAT_TEXTURED(type) ((type) == WPBR_MAT_METAL || (type) == WPBR_MAT_METAL_ISOTROPIC)
 
 typedef struct wpbr_material {
   uint32_t type;     /* wpbr_material_type */
@@ -55,7 +60,7 @@ typedef struct wpbr_material {
   float eta_i[3];    /* conductor: per channel; dielectric/specular: [0] */
   float eta_t[3];
   float k[3];        /* conductor absorption */
-  uint16_t tex[2];   /* WPBR_MAT_METAL: metallic and roughness texture indices */
+  uint16_t tex[2];   /* textured metal: metallic and roughness texture indices */
 } wpbr_material;     /* 64 bytes */
 
 typedef struct wpbr_sphere {
@@ -127,7 +132,7 @@ typedef struct wpbr_scene_desc {
   uint32_t n_lights;
   const wpbr_envmap* envmap; /* NULL when the scene has no infinite light */
   wpbr_camera camera;
-  const wpbr_texture* textures; /* referenced by WPBR_MAT_METAL materials */
+  const wpbr_texture* textures; /* referenced by textured-metal materials */
   uint32_t n_textures;
 } wpbr_scene_desc;
 

@@ -38,7 +38,7 @@ _SIGS = {
     "orc_render_spectral": (None, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, _FP, _FP]),
     "orc_spectral_tables": (None, [_FP]),
     "orc_texture_level": (C.c_uint32, [C.c_void_p, C.c_uint32, _FP, _UP]),
-    "orc_texture_eval": (None, [C.c_void_p, _FP, _FP]),
+    "orc_texture_eval": (None, [C.c_void_p, _FP, C.c_uint32, _FP]),
     "orc_adjoint_eval": (C.c_double, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_double),
                                       C.POINTER(C.c_double), _FP, C.POINTER(C.c_double), C.c_uint32, _UP,
                                       C.POINTER(C.c_double)]),
@@ -187,14 +187,14 @@ def texture_levels(rgb):
     return out
 
 
-def texture_eval(rgb, fp):
-    """Anisotropic EWA lookup of an (h, w, 3) texture at the footprint
-    fp = (s, t, ds/dx, dt/dx, ds/dy, dt/dy)."""
+def texture_eval(rgb, fp, isotropic=False):
+    """Anisotropic EWA (or, with isotropic, trilinear) lookup of an (h, w, 3)
+    texture at the footprint fp = (s, t, ds/dx, dt/dx, ds/dy, dt/dy)."""
     rgb = np.ascontiguousarray(rgb, np.float32)
     t = _texture(rgb)
     f = np.asarray(fp, np.float32)
     o = np.zeros(3, np.float32)
-    lib().orc_texture_eval(C.byref(t), _fp(f), _fp(o))
+    lib().orc_texture_eval(C.byref(t), _fp(f), 1 if isotropic else 0, _fp(o))
     return o
 
 

@@ -1385,9 +1385,10 @@ uint32_t orc_texture_level(const wpbr_texture* t, uint32_t level, float* out, ui
   }
   return (uint32_t)lv.size();
 }
-/* STexture2DSamplerAnisotropic::eval of one texture at the footprint
- * fp = (s, t, ds/dx, dt/dx, ds/dy, dt/dy); rgb to out[3]. */
-void orc_texture_eval(const wpbr_texture* t, const float* fp, float* out) {
+/* STexture2DSamplerAnisotropic::eval (isotropic = 0) or
+ * STexture2DSamplerIsotropic::eval (isotropic = 1) of one texture at the
+ * footprint fp = (s, t, ds/dx, dt/dx, ds/dy, dt/dy); rgb to out[3]. */
+void orc_texture_eval(const wpbr_texture* t, const float* fp, uint32_t isotropic, float* out) {
   std::vector<TexLevelO> lv;
   build_texture(*t, lv);
   float gauss[64];
@@ -1396,7 +1397,7 @@ void orc_texture_eval(const wpbr_texture* t, const float* fp, float* out) {
   f.p = V2{fp[0], fp[1]};
   f.dx = V2{fp[2], fp[3]};
   f.dy = V2{fp[4], fp[5]};
-  RGB c = tx_aniso(lv, gauss, f);
+  RGB c = isotropic ? tx_iso(lv, f) : tx_aniso(lv, gauss, f);
   out[0] = c.r;
   out[1] = c.g;
   out[2] = c.b;

@@ -130,8 +130,8 @@ def test_textured_scene_generation(W):
     g = W.SceneGen(5, 3, (64, 48))
     d = g.desc.contents
     assert d.n_textures == 4 and d.n_spheres == 65 and d.n_triangles == 2
-    metal = [m for m in range(d.n_materials) if d.materials[m].type == 3]
-    assert len(metal) == 2
+    metal = [m for m in range(d.n_materials) if d.materials[m].type in (3, 4)]
+    assert len(metal) == 3 and sum(d.materials[m].type == 4 for m in metal) == 1
     for m in metal:
         assert all(t < d.n_textures for t in d.materials[m].tex)
     # ground and every third sphere are textured metal

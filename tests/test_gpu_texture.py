@@ -1,6 +1,7 @@
-"""Textured metal (WPBR_MAT_METAL, CMaterialMetal.cpp:8-58) on the GPU against
-the oracle: camera-ray differentials at the hit, uv and sphere mappings,
-MIP-mapped anisotropic EWA lookups and the conductor built from them, through
+"""Textured metal (WPBR_MAT_METAL and WPBR_MAT_METAL_ISOTROPIC,
+CMaterialMetal.cpp:8-58) on the GPU against the oracle: camera-ray
+differentials at the hit, uv and sphere mappings, MIP-mapped anisotropic EWA
+and isotropic trilinear lookups and the conductor built from them, through
 the staged jobs (per-pixel records), the fused graph-captured pass, the
 Sampled64 pass and a batch. Films are bit-identical up to NaN payloads (the
 reference's sphere parameterisation makes a few NaN samples; device and host
@@ -25,7 +26,8 @@ def _same_nan_aware(a, b):
 
 
 def _metal_pixels(g, hit_prim):
-    """Which pixels hit a WPBR_MAT_METAL primitive."""
+    """Which pixels hit a textured-metal primitive, which of them use the
+    isotropic sampler, and which pixels hit a sphere."""
     d = g.desc.contents
     ns = d.n_spheres
     mat_of = np.zeros(ns + d.n_triangles, np.int64)
@@ -34,12 +36,12 @@ def _metal_pixels(g, hit_prim):
     for m in range(d.n_meshes):
         me = d.meshes[m]
         mat_of[ns + me.tri_begin: ns + me.tri_begin + me.tri_count] = me.material
-    metal = np.array([d.materials[i].type == 3 for i in range(d.n_materials)])
+    types = np.array([d.materials[i].type for i in range(d.n_materials)])
     hp = np.asarray(hit_prim).astype(np.int64)
     hit = hp != 0xFFFFFFFF
-    out = np.zeros(hp.shape, bool)
-    out[hit] = metal[mat_of[hp[hit]]]
-    return out, hit & (hp < ns)
+    t = np.full(hp.shape, -1)
+    t[hit] = types[mat_of[hp[hit]]]
+    return (t == 3) | (t == 4), t == 4, hit & (hp < ns)
 
 
 @pytest.fixture(scope="module")
@@ -52,6 +54,7 @@ def test_scene_has_textured_spheres_and_ground(W, scene):
     assert d.n_textures == 4
     assert [(d.textures[i].width, d.textures[i].height) for i in range(4)] == [(256, 256), (64, 64), (100, 60), (32, 16)]
     assert sum(d.materials[i].type == 3 for i in range(d.n_materials)) == 2
+    assert sum(d.materials[i].type == 4 for i in range(d.n_materials)) == 1
 
 
 def test_staged_jobs_match_oracle(W, O, ctx, scene):
@@ -69,9 +72,10 @@ def test_staged_jobs_match_oracle(W, O, ctx, scene):
         ro = o.render_pass(p, spp, 0, 0, (0, 0, Wd, Hd))
         for k in ro:
             assert _same_nan_aware(rg[k], ro[k]), (k, p)
-        metal, sph = _metal_pixels(scene, ro["hit_prim"])
-        # both mappings are exercised: textured ground and textured spheres
-        assert metal.sum() > 0.2 * Wd * Hd and (metal & sph).sum() > 20
+        metal, iso, sph = _metal_pixels(scene, ro["hit_prim"])
+        # both mappings and both samplers are exercised: textured ground,
+        # anisotropic and isotropic textured spheres
+        assert metal.sum() > 0.2 * Wd * Hd and (metal & sph & ~iso).sum() > 10 and iso.sum() > 10
     ctx.check_device_errors()
 
 
@@ -105,7 +109,7 @@ def test_textures_change_the_image(W, O, ctx, scene):
     d = scene.desc.contents
     mats = (type(d.materials[0]) * d.n_materials)()
     C.memmove(mats, d.materials, C.sizeof(mats))
-    ground = [i for i in range(d.n_materials) if mats[i].type == 3][0]
+    ground = d.meshes[0].material
     mats[ground].tex[1] = 3
     d2 = type(d).from_buffer_copy(d)
     d2.materials = C.cast(mats, type(d.materials))
@@ -166,7 +170,7 @@ def test_upload_rejects_bad_textures(W, ctx, scene):
     d = scene.desc.contents
     mats = (type(d.materials[0]) * d.n_materials)()
     C.memmove(mats, d.materials, C.sizeof(mats))
-    metal = [i for i in range(d.n_materials) if mats[i].type == 3][0]
+    metal = [i for i in range(d.n_materials) if mats[i].type in (3, 4)][0]
     mats[metal].tex[0] = d.n_textures
     bad = type(d).from_buffer_copy(d)
     bad.materials = C.cast(mats, type(d.materials))

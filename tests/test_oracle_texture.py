@@ -1,7 +1,8 @@
 """The oracle's texture restatement on the CPU: MIP pyramids built as
-SLoadTexture::generateMIPS does (CSTextureProcess.h:352-400) and the
+SLoadTexture::generateMIPS does (CSTextureProcess.h:352-400), the
 anisotropic EWA lookup (STexture2DSamplerAnisotropic, CSTextureProcess.h:
-150-239) on textures whose filtered values are known."""
+138-239) and the isotropic trilinear one (STexture2DSamplerIsotropic,
+CSTextureProcess.h:259-289) on textures whose filtered values are known."""
 import numpy as np
 import pytest
 
@@ -111,3 +112,32 @@ def test_major_axis_is_never_swapped(O):
     dy_long = O.texture_eval(t, (s_mid, 0.5, 0.5 / 256, 0.0, 0.0, 40.0 / 256))
     assert dx_long[0] < 0.05
     assert dy_long[0] > 0.45
+
+
+def test_isotropic_sampler_levels(O):
+    rng = np.random.default_rng(13)
+    t = rng.random((64, 64, 3), dtype=np.float32)
+    lv = O.texture_levels(t)
+    p = (0.37, 0.61)
+    fine = O.texture_eval(t, (p[0], p[1], 0, 0, 0, 0), isotropic=True)
+    assert np.array_equal(fine, O.texture_eval(t, (p[0], p[1], 0, 0, 0, 0)))  # both: bilinear on level 0
+    # negative components never widen the footprint: still the finest level
+    neg = O.texture_eval(t, (p[0], p[1], -0.3, -0.2, -0.1, -0.4), isotropic=True)
+    assert np.array_equal(neg, fine)
+    # a footprint at or past the coarsest level reads its texel (0, 0)
+    coarse = O.texture_eval(t, (p[0], p[1], 0.5, 0.0, 0.0, 0.0), isotropic=True)
+    assert np.array_equal(coarse, lv[-1][0, 0])
+    # constant texture: every level blends to the constant
+    c = np.full((64, 64, 3), 0.75, np.float32)
+    for w in (1e-3, 1e-2, 3e-2, 0.1):
+        np.testing.assert_allclose(O.texture_eval(c, (0.5, 0.5, w, 0.0, 0.0, w / 2), isotropic=True), 0.75, rtol=1e-6)
+
+
+def test_isotropic_sampler_blurs_with_width(O):
+    y, x = np.mgrid[0:128, 0:128]
+    t = np.repeat(((x + y) & 1).astype(np.float32)[..., None], 3, axis=2)
+    vals = [O.texture_eval(t, (0.5 + 0.3 / 128, 0.5 + 0.2 / 128, w, 0.0, 0.0, w), isotropic=True)[0]
+            for w in (0.1 / 128, 3.0 / 128, 8.0 / 128)]
+    # width 2w: below one texel of level 0 -> level 0; 6/128 -> between levels 0 and 1
+    assert abs(vals[0] - 0.5) > abs(vals[1] - 0.5) > abs(vals[2] - 0.5)
+    assert abs(vals[2] - 0.5) < 0.05

@@ -347,8 +347,8 @@ WPBR_API wpbr_status wpbr_scene_upload(wpbr_ctx* ctx, const wpbr_scene_desc* d) 
   bool has_metal = false;
   for (uint32_t m = 0; m < d->n_materials; ++m) {
     const wpbr_material& mt = d->materials[m];
-    if (mt.type > WPBR_MAT_METAL) return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: unknown material type");
-    if (mt.type == WPBR_MAT_METAL) {
+    if (mt.type > WPBR_MAT_METAL_ISOTROPIC) return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: unknown material type");
+    if (WPBR_MAT_TEXTURED(mt.type)) {
       if (mt.tex[0] >= d->n_textures || mt.tex[1] >= d->n_textures)
         return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: metal material texture index out of range");
       has_metal = true;

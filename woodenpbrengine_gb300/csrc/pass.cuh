@@ -67,13 +67,13 @@ __device__ SurfInt make_si(const SceneView& S, uint32_t prim, V3 o, V3 d) {
   return triangle_si(td, d, b0, b1, b2);
 }
 
-// The material of a hit: the scene's, or for WPBR_MAT_METAL the conductor
+// The material of a hit: the scene's, or for textured metal the conductor
 // built from its textures at the hit's footprint (camera-ray differentials,
 // sphere or uv mapping).
 __device__ wpbr_material hit_material(const SceneView& S, uint32_t prim, uint32_t mid, const SurfInt& s,
                                       const RayD& r) {
   wpbr_material m = S.mats[mid];
-  if (m.type != WPBR_MAT_METAL) return m;
+  if (!WPBR_MAT_TEXTURED(m.type)) return m;
   SurfDiff D = surf_differentials(s, r);
   TexFootprint fp = prim < S.ns ? sphere_footprint(S.sph_w2o[prim], s, D) : uv_footprint(s, D);
   return metal_material(S.tex, m, fp);

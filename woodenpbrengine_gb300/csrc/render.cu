@@ -107,7 +107,7 @@ __global__ void kj_bsdf_setup(PassCtx P, Staged G) {
   if (pix >= P.W * P.H || G.u[U_HIT_PRIM][pix] == kNoHit) return;
   uint32_t prim = G.u[U_HIT_PRIM][pix];
   uint32_t mid = prim_material(P.S, prim);
-  if (P.S.mats[mid].type == WPBR_MAT_METAL) {
+  if (WPBR_MAT_TEXTURED(P.S.mats[mid].type)) {
     // JobComputeDifferentialsForSurfInter + the uv mapping jobs +
     // JobGenerateBSDFMaterialMetal (MEngine.cpp:399-403)
     RayD r = camera_ray(P.S.cam, G.f[F_PFILM][2 * pix], G.f[F_PFILM][2 * pix + 1]);
@@ -152,7 +152,7 @@ __global__ void kj_shadow_light(PassCtx P, Staged G) {
 
 __device__ __forceinline__ wpbr_material staged_material(const PassCtx& P, const Staged& G, uint32_t pix) {
   const wpbr_material& m = P.S.mats[prim_material(P.S, G.u[U_HIT_PRIM][pix])];
-  if (m.type != WPBR_MAT_METAL) return m;
+  if (!WPBR_MAT_TEXTURED(m.type)) return m;
   const float* q = G.f[F_MAT] + 4 * (size_t)pix;
   return metal_unpack(make_float4(q[0], q[1], q[2], q[3]));
 }
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(kTB) k_spawn(PassCtx P, const uint32_t* pass_d
   Frame fr = bsdf_frame(s);
   uint32_t mid = prim_material(P.S, prim);
   const wpbr_material m = hit_material(P.S, prim, mid, s, r);
-  if (P.S.mats[mid].type == WPBR_MAT_METAL) {
+  if (WPBR_MAT_TEXTURED(P.S.mats[mid].type)) {
     flags |= SF_METAL;
     st[6] = metal_pack(m);
   }

@@ -299,10 +299,10 @@ struct wpbr_scenegen {
     tex_wh.push_back(H);
     return (uint16_t)(tex_rgb.size() - 1);
   }
-  uint32_t add_metal(uint16_t metallic, uint16_t roughness) {
+  uint32_t add_metal(uint16_t metallic, uint16_t roughness, uint32_t type = WPBR_MAT_METAL) {
     wpbr_material m;
     memset(&m, 0, sizeof(m));
-    m.type = WPBR_MAT_METAL;
+    m.type = type;
     m.tex[0] = metallic;
     m.tex[1] = roughness;
     mats.push_back(m);
@@ -442,7 +442,9 @@ void gen_config4(wpbr_scenegen* g, uint32_t seed, uint32_t param_seed, uint32_t 
 }
 
 // Config 5, the textured-metal scene: config 0's spheres and light with every
-// third sphere and the ground quad made of CMaterialMetal. Four procedural
+// third sphere and the ground quad made of CMaterialMetal (spheres 0, 6, 12,
+// ... and the ground with the anisotropic sampler, spheres 3, 9, 15, ... with
+// the isotropic one). Four procedural
 // textures: a 256x256 checker of two metallic k colours with seeded texel
 // noise (ground k), a 64x64 diagonal roughness ramp from 1e-5 to 1e-2 (log
 // scale, with noise; roughnessToAlpha(90 r) then spans alpha ~0.04 to ~1.6)
@@ -472,6 +474,7 @@ void gen_config5(wpbr_scenegen* g, uint32_t seed, uint32_t W, uint32_t H) {
   });
   uint32_t m_ground = g->add_metal(t_km, t_kr);
   uint32_t m_sphere = g->add_metal(t_sm, t_sr);
+  uint32_t m_sphere_iso = g->add_metal(t_sm, t_sr, WPBR_MAT_METAL_ISOTROPIC);
   Rng rng(seed, 0xC0u);
   for (int i = 0; i < 64; ++i) {
     V3 c{rng.uni(-10.0f, 10.0f), rng.uni(-10.0f, 10.0f), rng.uni(-10.0f, 10.0f)};
@@ -487,7 +490,7 @@ void gen_config5(wpbr_scenegen* g, uint32_t seed, uint32_t W, uint32_t H) {
       float eta[3] = {e, e, e}, k[3] = {0, 0, 0};
       m = g->add_material(WPBR_MAT_DIELECTRIC, alpha, eta, k);
     }
-    g->add_sphere(c, r, i % 3 == 0 ? m_sphere : m);
+    g->add_sphere(c, r, i % 6 == 0 ? m_sphere : i % 6 == 3 ? m_sphere_iso : m);
   }
   float le[3] = {1.5f, 1.5f, 1.5f}, lk[3] = {1.0f, 1.0f, 1.0f};
   uint32_t ml = g->add_material(WPBR_MAT_CONDUCTOR, 0.3f, le, lk);

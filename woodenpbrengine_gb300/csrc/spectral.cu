@@ -190,7 +190,7 @@ __global__ void k_spec_pass(PassCtx P, SpecCtx C, uint32_t pass, float2* pf) {
     uint32_t mid = prim_material(P.S, prim);
     const wpbr_material m = hit_material(P.S, prim, mid, si, r);
     SpecMat tsm;
-    if (P.S.mats[mid].type == WPBR_MAT_METAL) {
+    if (WPBR_MAT_TEXTURED(P.S.mats[mid].type)) {
       // R = Spectrum(1.0), etaI = Spectrum(1.0f), etaT = Spectrum(1.5f),
       // k = (Spectrum)metallic (CMaterialMetal.cpp:44-48)
       tsm.R = s64_const(1.0f);
@@ -198,7 +198,7 @@ __global__ void k_spec_pass(PassCtx P, SpecCtx C, uint32_t pass, float2* pf) {
       tsm.eta_t = s64_const(1.5f);
       tsm.k = s64_from_rgb(c_spec, RGB3{m.k[0], m.k[1], m.k[2]}, false);
     }
-    const SpecMat& sm = (P.S.mats[mid].type == WPBR_MAT_METAL) ? tsm : C.mats[mid];
+    const SpecMat& sm = (WPBR_MAT_TEXTURED(P.S.mats[mid].type)) ? tsm : C.mats[mid];
     V3 wo_l = to_local(fr, si.wo);
     uint32_t li_idx = pick_light(P, pix, pass);
     const wpbr_light& lt = P.S.lights[li_idx];

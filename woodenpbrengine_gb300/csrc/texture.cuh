@@ -131,6 +131,25 @@ WPBR_HD RGB3 tex_aniso(const TexView& T, uint32_t texid, const TexFootprint& fp)
   return rlerp(lod - (float)ilod, tex_ewa(T, ti, fp, (uint32_t)ilod), tex_ewa(T, ti, fp, (uint32_t)ilod + 1));
 }
 
+// STexture2DSamplerIsotropic::eval: the width is twice the largest signed
+// derivative component (negative components never widen it); a width <= 0
+// reads the finest level bilinearly, a level at or past the coarsest reads
+// texel (0, 0) of the coarsest level, otherwise two bilinear levels are
+// blended.
+WPBR_HD RGB3 tex_iso(const TexView& T, uint32_t texid, const TexFootprint& fp) {
+  const TexInfo& ti = T.tex[texid];
+  float a = fp.dstdx.x < fp.dstdx.y ? fp.dstdx.y : fp.dstdx.x;
+  float b = fp.dstdy.x < fp.dstdy.y ? fp.dstdy.y : fp.dstdy.x;
+  float width = 2.0f * (a < b ? b : a);
+  if (!(width > 0.0f)) return tex_triangle(T, ti, fp.p, 0);
+  uint32_t n = ti.n_levels;
+  float level = (float)(n - 1) + log2f_(width);
+  if (level < 0.0f) return tex_triangle(T, ti, fp.p, 0);
+  if (level >= (float)(n - 1)) return tex_texel(T, T.levels[ti.first_level + n - 1], 0, 0);
+  int il = (int)floorf(level);
+  return rlerp(level - (float)il, tex_triangle(T, ti, fp.p, (uint32_t)il), tex_triangle(T, ti, fp.p, (uint32_t)il + 1));
+}
+
 // pbrt's SolveLinearSystem2x2 (WoodenMath solveLinearSystem2x2).
 WPBR_HD bool solve2x2(const float A[2][2], const float B[2], float* x0, float* x1) {
   float det = A[0][0] * A[1][1] - A[0][1] * A[1][0];
@@ -222,8 +241,9 @@ WPBR_HD float roughness_to_alpha(float r) {
 
 // JobGenerateBSDFMaterialMetal: the conductor of one hit.
 WPBR_HD wpbr_material metal_material(const TexView& T, const wpbr_material& m, const TexFootprint& fp) {
-  RGB3 metallic = tex_aniso(T, m.tex[0], fp);
-  RGB3 rough = tex_aniso(T, m.tex[1], fp);
+  bool iso = m.type == WPBR_MAT_METAL_ISOTROPIC;
+  RGB3 metallic = iso ? tex_iso(T, m.tex[0], fp) : tex_aniso(T, m.tex[0], fp);
+  RGB3 rough = iso ? tex_iso(T, m.tex[1], fp) : tex_aniso(T, m.tex[1], fp);
   float sv = clampf(rough.r * 90.0f, 0.0f, 90.0f);
   float alpha = roughness_to_alpha(sv);
   wpbr_material e;

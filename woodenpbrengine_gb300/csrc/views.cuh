@@ -32,7 +32,7 @@ struct SceneView {
   EnvView env;
   CameraParams cam;
   uint32_t quirks;
-  TexView tex;  // textures of WPBR_MAT_METAL materials
+  TexView tex;  // textures of the textured-metal materials
 };
 
 // Child-pair BVH node: the bounds of both children of one interior node of
