@@ -138,14 +138,17 @@ def cpu_trace_rate(desc, rays, seconds, threads=None):
                        % (2 * m, m, m, dt)), o
 
 
-def render_rate(W, torch, config, res, spp, level=0, frames=1):
+def render_rate(W, torch, config, res, spp, level=0, frames=1, spectrum=None):
     """Msamples/s of whole frames through the fused, graph-captured pass
     (config 0: 64 spheres + quad + sphere light; config 2: the 1.31 M-triangle
-    mesh + 256 spheres + 1024x512 environment light)."""
+    mesh + 256 spheres + 1024x512 environment light; config 5: config 0 with
+    textured metal). spectrum=W.SPECTRUM_SAMPLED64 times the 64-bin pass."""
     g = W.SceneGen(config, 0, res, level=level)
     ctx = W.Context(torch.cuda.current_device())
     stream = torch.cuda.Stream()  # a capturable (non-default) stream for the pass graph
     ctx.set_stream(stream.cuda_stream)
+    if spectrum is not None:
+        ctx.set_spectrum(spectrum)
     ctx.upload(g.desc)
     ctx.build()
     ctx.render_setup(spp, seed=0)

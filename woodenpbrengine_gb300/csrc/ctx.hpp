@@ -201,7 +201,13 @@ wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t st
 wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass);
 wpbr_status render_pass_launch(wpbr_ctx* ctx);
 wpbr_status spectral_setup(wpbr_ctx* ctx);
-wpbr_status spectral_pass(wpbr_ctx* ctx, uint32_t pass);
+// Sampled64 pieces of render_pass_launch: the scalar spawn (replaces the
+// RGB spawn) and the per-bin finish + film (replace the RGB finish + film).
+cudaError_t spectral_spawn_launch(wpbr_ctx* ctx, const uint32_t* pass_ptr);
+cudaError_t spectral_finish_launch(wpbr_ctx* ctx);
+// float4 per pixel of the fused pass's state buffer (RenderState::pstate);
+// the RGB and the Sampled64 spawn records both fit in it.
+constexpr int kPassStateF4 = 7;
 uint32_t persistent_full_grid();
 void bvh_release(wpbr_ctx* ctx, bool keep_traversal);
 wpbr_status job_run(wpbr_ctx* ctx, uint32_t job, uint32_t pass);

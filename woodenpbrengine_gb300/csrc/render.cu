@@ -249,7 +249,7 @@ __global__ void k_film(uint32_t W, uint32_t H, const float2* pf, const float4* L
 
 // ============================== fused pass ==================================
 // Compact per-pixel state written by k_spawn and read by k_finish.
-constexpr int kStateF4 = 7;
+constexpr int kStateF4 = kPassStateF4;
 enum : uint32_t { SF_VALID = 1u, SF_TRACE_L = 2u, SF_TRACE_B = 4u, SF_HIT = 8u, SF_METAL = 16u };
 
 __global__ void __launch_bounds__(kTB) k_spawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
@@ -525,14 +525,22 @@ wpbr_status render_pass_launch(wpbr_ctx* ctx) {
   const uint32_t* pass_ptr = R.pass_ptr ? R.pass_ptr : R.pass_dev.p;
   WPBR_CUDA(R.counters.ensure(2));
   WPBR_CUDA(cudaMemsetAsync(R.counters.p, 0, 2 * sizeof(uint32_t), st));
+  bool spectral = ctx->spectrum == WPBR_SPECTRUM_SAMPLED64;
   launch_traversal<false>(P.S, P.Bv, CameraSrc{P, pass_ptr}, PrimSink{R.hit_prim.p}, n, R.counters.p, P.err, st,
                           R.trace_grid);
-  k_spawn<<<div_up(n, kTB), kTB, 0, st>>>(P, pass_ptr, R.hit_prim.p, R.pstate.p, R.shadow_rays.p, R.Lbuf.p,
-                                          R.pfilm.p);
+  if (spectral)
+    WPBR_CUDA(spectral_spawn_launch(ctx, pass_ptr));
+  else
+    k_spawn<<<div_up(n, kTB), kTB, 0, st>>>(P, pass_ptr, R.hit_prim.p, R.pstate.p, R.shadow_rays.p, R.Lbuf.p,
+                                            R.pfilm.p);
   launch_traversal<false>(P.S, P.Bv, BufferSrc{R.shadow_rays.p}, PrimSink{R.shadow_hit.p}, 2 * n, R.counters.p + 1,
                           P.err, st, R.trace_grid);
-  k_finish<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pstate.p, R.shadow_hit.p, R.Lbuf.p);
-  k_film<<<div_up(n, kTB), kTB, 0, st>>>(R.W, R.H, R.pfilm.p, R.Lbuf.p, (float4*)R.acc.p);
+  if (spectral) {
+    WPBR_CUDA(spectral_finish_launch(ctx));
+  } else {
+    k_finish<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pstate.p, R.shadow_hit.p, R.Lbuf.p);
+    k_film<<<div_up(n, kTB), kTB, 0, st>>>(R.W, R.H, R.pfilm.p, R.Lbuf.p, (float4*)R.acc.p);
+  }
   WPBR_CUDA(cudaGetLastError());
   return WPBR_OK;
 }
@@ -559,16 +567,16 @@ static uint64_t pass_graph_key(const wpbr_ctx* ctx) {
   mix(R.stream);
   mix(((uint64_t)R.W << 32) | R.H);
   mix((uint64_t)R.trace_grid);
+  mix((uint64_t)ctx->spectrum | ((uint64_t)ctx->quirks << 8));
   const void* ptrs[] = {R.acc.p,    R.hit_prim.p, R.shadow_rays.p,     R.shadow_hit.p,      R.pstate.p,
                         R.Lbuf.p,   R.pfilm.p,    R.pass_dev.p,        R.counters.p,        R.pass_ptr,
                         ctx->d_err.p, ctx->bvh.view.nodes, ctx->bvh.view.nodes4,
-                        ctx->bvh.view.prims};
+                        ctx->bvh.view.prims, R.spec_mats.p, R.spec_le.p, R.spec_L.p, R.spec_acc.p};
   for (const void* q : ptrs) mix((uint64_t)(uintptr_t)q);
   return h;
 }
 
 wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass) {
-  if (ctx->spectrum == WPBR_SPECTRUM_SAMPLED64) return spectral_pass(ctx, pass);
   RenderState& R = ctx->rs;
   if (!R.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render_pass: render_setup not called");
   if (pass >= R.spp) return set_err(ctx, WPBR_ERR_INVALID_ARG, "render_pass: pass >= spp");

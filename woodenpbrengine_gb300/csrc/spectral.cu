@@ -1,11 +1,18 @@
-// spectral.cu — the Sampled64 parity mode of the render pass: the same
-// per-sample job list as the RGB path (MEngine::render, MEngine.cpp:393-442)
-// with every radiance, reflectance and Fresnel value a 64-bin
-// SampledSpectrum, as the reference computes it (Spectrum = SampledSpectrum,
-// CSpectrum.h:8). One thread per pixel and sample (per-thread traversal);
-// the film accumulates spectra and is resolved to RGB with toRGB after every
-// pass, so wpbr_film_read and wpbr_film_tonemap read it as in RGB mode
-// (JobOutputFilmTitles converts with toRGB, CSFilm.cpp:159).
+// spectral.cu — the Sampled64 mode of the render pass: the same per-sample
+// job list as the RGB path (MEngine::render, MEngine.cpp:393-442) with every
+// radiance, reflectance and Fresnel value a 64-bin SampledSpectrum, as the
+// reference computes it (Spectrum = SampledSpectrum, CSpectrum.h:8).
+//
+// Wavefront layout: the pass shares the RGB path's camera and shadow-ray
+// persistent traversals (render.cu); k_sspawn (one thread per pixel) does
+// the scalar part of shading and sampling and records, per pixel, the
+// scalar factors every spectral term needs; k_sfinish and k_sfilm give each
+// pixel a half-warp, 16 lanes x 4 bins, for the per-bin products, the
+// Fresnel terms, the Mitchell film gather and toRGB. Every per-bin value is
+// computed with the same operations in the same order as the one-thread
+// restatement, so the film is bit-identical to it; sums over bins (toXYZ)
+// stay sequential in bin order.
+
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -14,13 +21,14 @@
 #include "ctx.hpp"
 #include "pass.cuh"
 #include "spectral.cuh"
-#include "traverse.cuh"
 
 namespace wpbr {
 
 namespace {
 
-__constant__ SpecTables c_spec;
+// The binned tables in global memory: the lanes of a pixel read different
+// bins, which the constant cache would serialise.
+__device__ __align__(16) SpecTables g_spec;
 
 // Per material: R, eta_i, eta_t, k as spectra.
 struct SpecMat {
@@ -32,6 +40,27 @@ struct SpecCtx {
   const S64* light_le;  // per light: sphere Le, or the environment's LEmit
   float* L;             // per pixel, 64 floats
 };
+
+// Per-pixel record of k_sspawn (kSpecStateF4 float4):
+//  [0] flags, light index (environment light on a miss), material id, w/lpdf
+//  [1] light branch: cos(wi, wh), scalar BSDF factor, |cos wi|;  w/bpdf
+//  [2] BSDF branch:  cos(wi, wh), scalar BSDF factor, |cos wi|;  -
+//  [3] environment (s, t) of the light sample (or of the camera miss), of the BSDF sample
+//  [4] textured metal: k (RGB)
+constexpr int kSpecStateF4 = 5;
+enum : uint32_t {
+  SS_HIT = 1u,        // the camera ray hit and the scene has lights
+  SS_MISS_ENV = 2u,   // the camera ray missed into the environment
+  SS_LB = 4u,         // light branch: shadow ray traced, contribution if unoccluded and Li not black
+  SS_BB = 8u,         // BSDF branch: likewise
+  SS_COND = 16u,      // conductor Fresnel per bin (else the scalar dielectric form)
+  SS_TEX = 32u,       // textured metal: eta 1 / 1.5, k from RGB
+  SS_LZERO = 64u,     // light-branch f is 0 (grazing wi or wo, or wh = 0)
+  SS_BZERO = 128u,    // BSDF-branch f is 0
+  SS_LENV = 256u,     // light-branch Li is the environment lookup (WPBR_Q_ENV_LI_SAMPLE_FIX)
+  SS_BENV = 512u      // BSDF-branch Li is the environment lookup
+};
+constexpr int kBinLanes = 16;  // lanes per pixel in the spectral kernels; 4 bins each
 
 // averageSpectrumSamples (CSpectrumSampled.h:45-87): piecewise-linear average
 // over [l0, l1], the trapezoid of each segment times 0.5 in double as the
@@ -76,207 +105,328 @@ void build_tables(SpecTables* T) {
   }
 }
 
-__device__ __forceinline__ void s64_mul(S64& a, const S64& b) {
-  for (int i = 0; i < kSpecN; ++i) a.v[i] = a.v[i] * b.v[i];
-}
+// ---- scalar part (one thread per pixel) -----------------------------------
 
-// Spectrum(Spectrum(RGB texel lookup, Illuminant) * LEmit)
-__device__ S64 env_spectrum(const EnvView& e, float s, float t, const S64& lemit) {
-  S64 r = s64_from_rgb(c_spec, env_bilerp(e, s, t), true);
-  s64_mul(r, lemit);
-  return r;
-}
-
-// mf_f_impl per bin: conductor Fresnel per bin from the eta/k spectra,
-// dielectric Fresnel scalar (CFresnelDielectric keeps float etaI/etaT).
-__device__ S64 mf_f_spec(const wpbr_material& m, const SpecMat& sm, float d_wh, V3 wh, V3 wo, V3 wi) {
-  S64 f = s64_const(0.0f);
+// Scalar factors of mf_f_impl for (wo, wi, wh, D): the per-bin value is
+// ((F_conductor(c) * R) * kf) * fcos for a conductor and (R * kf) * fcos
+// otherwise; zero when either cosine or wh is zero (then 0 * fcos).
+struct FScalars {
+  float c, kf, fcos;
+  bool zero;
+};
+__device__ __forceinline__ FScalars f_scalars(const wpbr_material& m, float d_wh, V3 wh, V3 wo, V3 wi) {
+  FScalars F;
+  F.fcos = abs_cos(wi);
+  F.c = 0.0f;
+  F.kf = 0.0f;
   float co = abs_cos(wo), ci = abs_cos(wi);
-  if (ci == 0.0f || co == 0.0f) return f;
-  if (wh.x == 0.0f && wh.y == 0.0f && wh.z == 0.0f) return f;
-  float c = dot(wi, wh);
+  F.zero = ci == 0.0f || co == 0.0f || (wh.x == 0.0f && wh.y == 0.0f && wh.z == 0.0f);
+  if (F.zero) return F;
+  F.c = dot(wi, wh);
   if (m.type == WPBR_MAT_CONDUCTOR) {
-    float k = d_wh / ((4.0f * ci) * co);
-    for (int i = 0; i < kSpecN; ++i)
-      f.v[i] = (fresnel_conductor(c, sm.eta_i.v[i], sm.eta_t.v[i], sm.k.v[i]) * sm.R.v[i]) * k;
-    return f;
+    F.kf = d_wh / ((4.0f * ci) * co);
+  } else {
+    float fr = fresnel_dielectric(F.c, m.eta_i[0], m.eta_t[0]);
+    F.kf = (fr * d_wh) / ((4.0f * ci) * co);
   }
-  float fr = fresnel_dielectric(c, m.eta_i[0], m.eta_t[0]);
-  float k = (fr * d_wh) / ((4.0f * ci) * co);
-  for (int i = 0; i < kSpecN; ++i) f.v[i] = sm.R.v[i] * k;
-  return f;
+  return F;
 }
 
-__device__ S64 bsdf_eval_spec(const wpbr_material& m, const SpecMat& sm, V3 wo, V3 wi, float* pdf) {
-  if (m.type == WPBR_MAT_SPECULAR) {
-    *pdf = 0.0f;
-    return s64_const(0.0f);
-  }
-  V3 wh = normalize(add(wo, wi));
-  float d = tr_d(m.alpha_x, m.alpha_y, wh);
-  *pdf = (d * abs_cos(wh)) / (4.0f * dot(wo, wh));
-  S64 f = mf_f_spec(m, sm, d, wh, wo, wi);
-  float c = abs_cos(wi);
-  for (int i = 0; i < kSpecN; ++i) f.v[i] = f.v[i] * c;
-  return f;
-}
-
-__device__ S64 bsdf_sample_spec(const wpbr_material& m, const SpecMat& sm, V3 wo, float u0, float u1, V3* wi,
-                                float* pdf, bool* valid) {
-  if (m.type == WPBR_MAT_SPECULAR) {
-    *wi = V3{-wo.x, -wo.y, wo.z};
-    *pdf = 1.0f;
-    *valid = true;
-    S64 f = s64_const(0.0f);
-    float c = abs_cos(*wi);
-    if (c != 0.0f) {
-      float fr = fresnel_dielectric(wi->z, m.eta_i[0], m.eta_t[0]);
-      for (int i = 0; i < kSpecN; ++i) f.v[i] = sm.R.v[i] * (fr / c);
-    }
-    for (int i = 0; i < kSpecN; ++i) f.v[i] = f.v[i] * c;
-    return f;
-  }
-  float d;
-  V3 wh = tr_sample(m.alpha_x, m.alpha_y, wo, u0, u1, &d);
-  *wi = reflect(wo, wh);
-  if (!same_hemi(*wi, wo)) {
-    *valid = false;
-    *pdf = 0.0f;
-    return s64_const(0.0f);
-  }
-  *valid = true;
-  *pdf = (d * abs_cos(wh)) / (4.0f * dot(wo, wh));
-  S64 f = mf_f_spec(m, sm, d, wh, wo, *wi);
-  float c = abs_cos(*wi);
-  for (int i = 0; i < kSpecN; ++i) f.v[i] = f.v[i] * c;
-  return f;
-}
-
-__device__ __forceinline__ uint32_t trace_closest_s(const PassCtx& P, V3 o, V3 d) {
-  HitRec h = P.Bv.max_depth < 60 ? trace_ray<false, 64>(P.S, P.Bv, o, d, inf_(), nullptr, nullptr, P.err)
-                                 : trace_ray<false, 256>(P.S, P.Bv, o, d, inf_(), nullptr, nullptr, P.err);
-  return h.prim;
-}
-
-// L += a * b * k, per bin in the RGB path's order ((li * f) * k)
-__device__ __forceinline__ void s64_acc(S64& L, const S64& a, const S64& b, float k) {
-  for (int i = 0; i < kSpecN; ++i) L.v[i] = L.v[i] + (a.v[i] * b.v[i]) * k;
-}
-
-__global__ void k_spec_pass(PassCtx P, SpecCtx C, uint32_t pass, float2* pf) {
+__global__ void __launch_bounds__(kTB) k_sspawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
+                                                float4* state, float4* rays, float2* pf) {
   uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= P.W * P.H) return;
+  uint32_t pass = *pass_dev;
   float fx, fy;
   camera_sample(P, pix, pass, &fx, &fy);
   pf[pix] = make_float2(fx, fy);
   RayD r = camera_ray(P.S.cam, fx, fy);
-  S64 L = s64_const(0.0f);
-  uint32_t prim = trace_closest_s(P, r.o, r.d);
+  uint32_t prim = hit_prim[pix];
+  float4* st = state + (size_t)pix * kSpecStateF4;
+  float4* ry = rays + (size_t)pix * 4;
+  const float4 off = make_float4(0.0f, 0.0f, 0.0f, -1.0f);  // tmax < 0: nothing to trace
+  ry[0] = off; ry[1] = off; ry[2] = off; ry[3] = off;
   uint32_t nl = P.S.nlights;
-  if (prim == kNoHit) {
-    if (P.S.has_env) {
-      uint32_t env_light = 0;
+  if (prim == kNoHit || nl == 0) {
+    uint32_t flags = 0, env_light = 0;
+    if (prim == kNoHit && P.S.has_env) {
+      flags = SS_MISS_ENV;
       for (uint32_t i = 0; i < nl; ++i)
         if (P.S.lights[i].type == WPBR_LIGHT_ENV) env_light = i;
       V3 dl = xvector(P.S.env.w2l, r.d);
       float s = (float)((double)sph_phi(dl) / (2.0 * kPI));
       float t = (float)((double)sph_theta(dl) / kPI);
-      S64 le = env_spectrum(P.S.env, s, t, C.light_le[env_light]);
-      for (int i = 0; i < kSpecN; ++i) L.v[i] = L.v[i] + le.v[i];
+      st[3] = make_float4(s, t, 0.0f, 0.0f);
     }
-  } else if (nl > 0) {
-    SurfInt si = make_si(P.S, prim, r.o, r.d);
-    Frame fr = bsdf_frame(si);
-    uint32_t mid = prim_material(P.S, prim);
-    const wpbr_material m = hit_material(P.S, prim, mid, si, r);
-    SpecMat tsm;
-    if (WPBR_MAT_TEXTURED(P.S.mats[mid].type)) {
-      // R = Spectrum(1.0), etaI = Spectrum(1.0f), etaT = Spectrum(1.5f),
-      // k = (Spectrum)metallic (CMaterialMetal.cpp:44-48)
-      tsm.R = s64_const(1.0f);
-      tsm.eta_i = s64_const(1.0f);
-      tsm.eta_t = s64_const(1.5f);
-      tsm.k = s64_from_rgb(c_spec, RGB3{m.k[0], m.k[1], m.k[2]}, false);
+    st[0] = make_float4(__uint_as_float(flags), __uint_as_float(env_light), 0.0f, 0.0f);
+    return;
+  }
+  uint32_t flags = SS_HIT;
+  SurfInt si = make_si(P.S, prim, r.o, r.d);
+  Frame fr = bsdf_frame(si);
+  uint32_t mid = prim_material(P.S, prim);
+  const wpbr_material m = hit_material(P.S, prim, mid, si, r);
+  if (WPBR_MAT_TEXTURED(P.S.mats[mid].type)) {
+    flags |= SS_TEX;
+    st[4] = make_float4(m.k[0], m.k[1], m.k[2], 0.0f);
+  }
+  if (m.type == WPBR_MAT_CONDUCTOR) flags |= SS_COND;
+  V3 wo_l = to_local(fr, si.wo);
+  uint32_t li_idx = pick_light(P, pix, pass);
+  const wpbr_light& lt = P.S.lights[li_idx];
+  float4 s0 = make_float4(0.0f, __uint_as_float(li_idx), __uint_as_float(mid), 0.0f);
+  float4 s1 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), s2 = s1, s3 = s1;
+  // ---- light-sampling branch: Li is the sphere's LEmit, or (quirk fixed)
+  // the environment lookup at the sampled (s, t); without the fix the
+  // environment branch's Li is black and nothing is traced
+  float u0, u1;
+  wpbr_rng::sample2d(P.rs, pix, pass, wpbr_rng::DIM_LIGHT, &u0, &u1);
+  V3 wi{0, 0, 0};
+  float lpdf = 0.0f;
+  bool ok = true, li_possible = true;
+  if (lt.type == WPBR_LIGHT_SPHERE) {
+    sphere_light_sample(P.S.sph_o2w[lt.sphere_index], P.S.sph_r[lt.sphere_index], si.p, u0, u1, &wi, &lpdf);
+  } else {
+    RGB3 li_rgb;
+    float uv[3];
+    env_li_sample(P.S.env, P.S.quirks, u0, u1, &wi, &li_rgb, &lpdf, &ok, uv);
+    li_possible = (P.S.quirks & WPBR_Q_ENV_LI_SAMPLE_FIX) != 0;
+    flags |= SS_LENV;
+    s3.x = uv[0];
+    s3.y = uv[1];
+  }
+  if (ok && li_possible && m.type != WPBR_MAT_SPECULAR) {
+    // bsdf_eval: the specular lobe evaluates to pdf 0, which contributes nothing
+    V3 wi_l = to_local(fr, wi);
+    V3 wh = normalize(add(wo_l, wi_l));
+    float d = tr_d(m.alpha_x, m.alpha_y, wh);
+    float bpdf = (d * abs_cos(wh)) / (4.0f * dot(wo_l, wh));
+    if (bpdf != 0.0f) {
+      flags |= SS_LB;
+      FScalars F = f_scalars(m, d, wh, wo_l, wi_l);
+      if (F.zero) flags |= SS_LZERO;
+      float w = power_heuristic(lpdf, bpdf);
+      s0.w = w / lpdf;
+      s1 = make_float4(F.c, F.kf, F.fcos, 0.0f);
+      V3 o = add(si.p, mul(wi, (float)0.1));
+      ry[0] = make_float4(o.x, o.y, o.z, 0.0f);
+      ry[1] = make_float4(wi.x, wi.y, wi.z, inf_());
     }
-    const SpecMat& sm = (WPBR_MAT_TEXTURED(P.S.mats[mid].type)) ? tsm : C.mats[mid];
-    V3 wo_l = to_local(fr, si.wo);
-    uint32_t li_idx = pick_light(P, pix, pass);
+  }
+  // ---- BSDF-sampling branch
+  wpbr_rng::sample2d(P.rs, pix, pass, wpbr_rng::DIM_BSDF, &u0, &u1);
+  V3 wi_l;
+  float bpdf = 0.0f;
+  bool valid;
+  FScalars F;
+  if (m.type == WPBR_MAT_SPECULAR) {
+    // SBXDFSpecularReflectance::sample_f: f = R * (Fr / |cos|) * |cos|
+    wi_l = V3{-wo_l.x, -wo_l.y, wo_l.z};
+    bpdf = 1.0f;
+    valid = true;
+    F.fcos = abs_cos(wi_l);
+    F.c = 0.0f;
+    F.zero = !(F.fcos != 0.0f);
+    F.kf = F.zero ? 0.0f : fresnel_dielectric(wi_l.z, m.eta_i[0], m.eta_t[0]) / F.fcos;
+  } else {
+    float d;
+    V3 wh = tr_sample(m.alpha_x, m.alpha_y, wo_l, u0, u1, &d);
+    wi_l = reflect(wo_l, wh);
+    valid = same_hemi(wi_l, wo_l);
+    if (valid) {
+      bpdf = (d * abs_cos(wh)) / (4.0f * dot(wo_l, wh));
+      F = f_scalars(m, d, wh, wo_l, wi_l);
+    }
+  }
+  if (valid) {
+    V3 wi_w = to_world(fr, wi_l);
+    bool contributes = true;
+    float blpdf = 0.0f;
+    if (lt.type == WPBR_LIGHT_SPHERE) {
+      blpdf = sphere_light_pdf(P.S.sph_o2w[lt.sphere_index], P.S.sph_r[lt.sphere_index], si.p, P.S.quirks);
+    } else {
+      flags |= SS_BENV;
+      V3 wl = xvector(P.S.env.w2l, wi_w);
+      float theta = sph_theta(wl);
+      float phi = sph_phi(wl);
+      float uu = (float)((double)phi / (2.0 * kPI));
+      float vv = (float)((double)theta / kPI);
+      float stt = sinf_(theta);
+      contributes = stt != 0.0f;  // else Li stays black
+      if (contributes) blpdf = (float)((double)env_pdf_uv(P.S.env, uu, vv) / (((2.0 * kPI) * kPI) * (double)stt));
+      s3.z = uu;
+      s3.w = vv;
+    }
+    if (contributes) {
+      flags |= SS_BB;
+      if (F.zero) flags |= SS_BZERO;
+      float w = (bpdf == 1.0f) ? 1.0f : power_heuristic(bpdf, blpdf);
+      s1.w = w / bpdf;
+      s2 = make_float4(F.c, F.kf, F.fcos, 0.0f);
+      V3 o = add(si.p, mul(wi_w, (float)0.01));
+      ry[2] = make_float4(o.x, o.y, o.z, 0.0f);
+      ry[3] = make_float4(wi_w.x, wi_w.y, wi_w.z, inf_());
+    }
+  }
+  s0.x = __uint_as_float(flags);
+  st[0] = s0;
+  st[1] = s1;
+  st[2] = s2;
+  st[3] = s3;
+}
+
+// ---- per-bin part (a half-warp per pixel, 4 bins per lane) -----------------
+
+struct Bins4 {
+  float v[4];
+};
+__device__ __forceinline__ Bins4 ld_bins(const float* p) {
+  float4 q = *reinterpret_cast<const float4*>(p);
+  return Bins4{{q.x, q.y, q.z, q.w}};
+}
+__device__ __forceinline__ void st_bins(float* p, const Bins4& b) {
+  *reinterpret_cast<float4*>(p) = make_float4(b.v[0], b.v[1], b.v[2], b.v[3]);
+}
+__device__ __forceinline__ Bins4 bins_const(float v) { return Bins4{{v, v, v, v}}; }
+__device__ __forceinline__ bool bins_nonzero(const Bins4& b) {
+  return b.v[0] != 0.0f || b.v[1] != 0.0f || b.v[2] != 0.0f || b.v[3] != 0.0f;
+}
+// s64_from_rgb at bins b0..b0+3: the same three accumulation steps per bin.
+__device__ __forceinline__ Bins4 bins_from_rgb(RGB3 c, bool illuminant, int b0) {
+  const float(*B)[kSpecN] = illuminant ? g_spec.illum : g_spec.refl;
+  float r = c.r, g = c.g, b = c.b;
+  int k0, k1, k2;
+  float a0, a1, a2;
+  if (r <= g && r <= b) {
+    k0 = kSpWhite; a0 = r;
+    if (g <= b) { k1 = kSpCyan; a1 = g - r; k2 = kSpBlue; a2 = b - g; }
+    else { k1 = kSpCyan; a1 = b - r; k2 = kSpGreen; a2 = g - b; }
+  } else if (g <= r && g <= b) {
+    k0 = kSpWhite; a0 = g;
+    if (r <= b) { k1 = kSpMagenta; a1 = r - g; k2 = kSpBlue; a2 = b - r; }
+    else { k1 = kSpMagenta; a1 = b - g; k2 = kSpRed; a2 = r - b; }
+  } else {
+    k0 = kSpWhite; a0 = b;
+    if (r <= g) { k1 = kSpYellow; a1 = r - b; k2 = kSpGreen; a2 = g - r; }
+    else { k1 = kSpYellow; a1 = g - b; k2 = kSpRed; a2 = r - g; }
+  }
+  Bins4 s;
+  for (int j = 0; j < 4; ++j) {
+    float v = 0.0f + B[k0][b0 + j] * a0;
+    v = v + B[k1][b0 + j] * a1;
+    s.v[j] = v + B[k2][b0 + j] * a2;
+  }
+  return s;
+}
+// Spectrum(Spectrum(RGB texel lookup, Illuminant) * LEmit), bins b0..b0+3
+__device__ __forceinline__ Bins4 bins_env(const EnvView& e, float s, float t, const float* lemit, int b0) {
+  Bins4 r = bins_from_rgb(env_bilerp(e, s, t), true, b0);
+  Bins4 le = ld_bins(lemit + b0);
+  for (int j = 0; j < 4; ++j) r.v[j] = r.v[j] * le.v[j];
+  return r;
+}
+
+struct MatBins {
+  Bins4 R, eta_i, eta_t, k;
+};
+
+__device__ __forceinline__ Bins4 bins_f(bool cond, bool zero, float c, float kf, float fcos, const MatBins& M) {
+  Bins4 f;
+  for (int j = 0; j < 4; ++j) {
+    float v;
+    if (zero)
+      v = 0.0f;
+    else if (cond)
+      v = (fresnel_conductor(c, M.eta_i.v[j], M.eta_t.v[j], M.k.v[j]) * M.R.v[j]) * kf;
+    else
+      v = M.R.v[j] * kf;
+    f.v[j] = v * fcos;
+  }
+  return f;
+}
+
+__global__ void __launch_bounds__(128) k_sfinish(PassCtx P, SpecCtx C, const float4* state, const uint32_t* shadow) {
+  uint32_t pix = (blockIdx.x * blockDim.x + threadIdx.x) / kBinLanes;
+  if (pix >= P.W * P.H) return;  // the whole half-warp leaves together
+  uint32_t lane = threadIdx.x & 31u;
+  uint32_t hmask = 0xFFFFu << (lane & 16u);
+  int b0 = 4 * (int)(lane & 15u);
+  const float4* st = state + (size_t)pix * kSpecStateF4;
+  float4 s0 = st[0];
+  uint32_t flags = __float_as_uint(s0.x);
+  uint32_t li_idx = __float_as_uint(s0.y);
+  Bins4 L = bins_const(0.0f);
+  if (flags & SS_MISS_ENV) {
+    float4 s3 = st[3];
+    Bins4 le = bins_env(P.S.env, s3.x, s3.y, C.light_le[li_idx].v, b0);
+    for (int j = 0; j < 4; ++j) L.v[j] = L.v[j] + le.v[j];
+  } else if (flags & (SS_LB | SS_BB)) {
     const wpbr_light& lt = P.S.lights[li_idx];
     uint32_t lp = light_prim(lt);
-    const S64& lemit = C.light_le[li_idx];
-    // ---- light-sampling branch
-    float u0, u1;
-    wpbr_rng::sample2d(P.rs, pix, pass, wpbr_rng::DIM_LIGHT, &u0, &u1);
-    V3 wi{0, 0, 0};
-    float lpdf = 0.0f;
-    bool ok = true;
-    S64 li = s64_const(0.0f);
-    if (lt.type == WPBR_LIGHT_SPHERE) {
-      sphere_light_sample(P.S.sph_o2w[lt.sphere_index], P.S.sph_r[lt.sphere_index], si.p, u0, u1, &wi, &lpdf);
-      li = lemit;
+    const float* lemit = C.light_le[li_idx].v;
+    MatBins M;
+    if (flags & SS_TEX) {
+      // R = Spectrum(1.0), etaI = Spectrum(1.0f), etaT = Spectrum(1.5f),
+      // k = (Spectrum)metallic (CMaterialMetal.cpp:44-48)
+      float4 kr = st[4];
+      M.R = bins_const(1.0f);
+      M.eta_i = bins_const(1.0f);
+      M.eta_t = bins_const(1.5f);
+      M.k = bins_from_rgb(RGB3{kr.x, kr.y, kr.z}, false, b0);
     } else {
-      RGB3 li_rgb;
-      float uv[3];
-      env_li_sample(P.S.env, P.S.quirks, u0, u1, &wi, &li_rgb, &lpdf, &ok, uv);
-      if (P.S.quirks & WPBR_Q_ENV_LI_SAMPLE_FIX) li = env_spectrum(P.S.env, uv[0], uv[1], lemit);
+      const SpecMat& sm = C.mats[__float_as_uint(s0.z)];
+      M.R = ld_bins(sm.R.v + b0);
+      M.eta_i = ld_bins(sm.eta_i.v + b0);
+      M.eta_t = ld_bins(sm.eta_t.v + b0);
+      M.k = ld_bins(sm.k.v + b0);
     }
-    if (ok && !s64_black(li)) {
-      uint32_t hp = trace_closest_s(P, add(si.p, mul(wi, (float)0.1)), wi);
+    float4 s1 = st[1], s3 = st[3];
+    bool cond = (flags & SS_COND) != 0;
+    if (flags & SS_LB) {
+      uint32_t hp = shadow[2 * pix];
       if (hp == kNoHit || hp == lp) {
-        float bpdf;
-        S64 f = bsdf_eval_spec(m, sm, wo_l, to_local(fr, wi), &bpdf);
-        if (bpdf != 0.0f) {
-          float w = power_heuristic(lpdf, bpdf);
-          s64_acc(L, li, f, w / lpdf);
+        Bins4 li = (flags & SS_LENV) ? bins_env(P.S.env, s3.x, s3.y, lemit, b0) : ld_bins(lemit + b0);
+        if (__ballot_sync(hmask, bins_nonzero(li)) & hmask) {
+          Bins4 f = bins_f(cond, (flags & SS_LZERO) != 0, s1.x, s1.y, s1.z, M);
+          for (int j = 0; j < 4; ++j) L.v[j] = L.v[j] + (li.v[j] * f.v[j]) * s0.w;
         }
       }
     }
-    // ---- BSDF-sampling branch
-    wpbr_rng::sample2d(P.rs, pix, pass, wpbr_rng::DIM_BSDF, &u0, &u1);
-    V3 wi_l;
-    float bpdf;
-    bool valid;
-    S64 bf = bsdf_sample_spec(m, sm, wo_l, u0, u1, &wi_l, &bpdf, &valid);
-    if (valid) {
-      V3 wi_w = to_world(fr, wi_l);
-      uint32_t hp = trace_closest_s(P, add(si.p, mul(wi_w, (float)0.01)), wi_w);
+    if (flags & SS_BB) {
+      uint32_t hp = shadow[2 * pix + 1];
       if (hp == kNoHit || hp == lp) {
-        S64 bli = s64_const(0.0f);
-        float blpdf = 0.0f;
-        if (lt.type == WPBR_LIGHT_SPHERE) {
-          blpdf = sphere_light_pdf(P.S.sph_o2w[lt.sphere_index], P.S.sph_r[lt.sphere_index], si.p, P.S.quirks);
-          bli = lemit;
-        } else {
-          V3 wl = xvector(P.S.env.w2l, wi_w);
-          float theta = sph_theta(wl);
-          float phi = sph_phi(wl);
-          float uu = (float)((double)phi / (2.0 * kPI));
-          float vv = (float)((double)theta / kPI);
-          float st = sinf_(theta);
-          if (st != 0.0f) {
-            blpdf = (float)((double)env_pdf_uv(P.S.env, uu, vv) / (((2.0 * kPI) * kPI) * (double)st));
-            bli = env_spectrum(P.S.env, uu, vv, lemit);
-          }
-        }
-        if (!s64_black(bli)) {
-          float w = (bpdf == 1.0f) ? 1.0f : power_heuristic(bpdf, blpdf);
-          s64_acc(L, bli, bf, w / bpdf);
+        Bins4 bli = (flags & SS_BENV) ? bins_env(P.S.env, s3.z, s3.w, lemit, b0) : ld_bins(lemit + b0);
+        if (__ballot_sync(hmask, bins_nonzero(bli)) & hmask) {
+          float4 s2 = st[2];
+          Bins4 f = bins_f(cond, (flags & SS_BZERO) != 0, s2.x, s2.y, s2.z, M);
+          for (int j = 0; j < 4; ++j) L.v[j] = L.v[j] + (bli.v[j] * f.v[j]) * s1.w;
         }
       }
     }
   }
-  float* out = C.L + (size_t)pix * kSpecN;
-  for (int i = 0; i < kSpecN; ++i) out[i] = L.v[i];
+  st_bins(C.L + (size_t)pix * kSpecN + b0, L);
 }
 
-// Tile-clipped Mitchell gather of film_gather, 64 bins per sample.
-__global__ void k_spec_film(uint32_t W, uint32_t H, const float2* pf, const float* L, float* acc, float4* accw) {
-  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+// Tile-clipped Mitchell gather of film_gather, 64 bins per sample, then
+// toRGB of the accumulated spectrum (s64_to_rgb: products per bin, the three
+// sums taken sequentially in bin order by lanes 0-2 of the half-warp).
+constexpr int kSumStride = 68;  // floats per channel row in shared memory (float4-aligned, bank-skewed)
+__global__ void __launch_bounds__(128) k_sfilm(uint32_t W, uint32_t H, const float2* pf, const float* L, float* acc,
+                                               float4* accw, uint32_t quirks) {
+  __shared__ __align__(16) float prod[128 / kBinLanes][3][kSumStride];
+  __shared__ float xyz[128 / kBinLanes][3];
+  uint32_t pix = (blockIdx.x * blockDim.x + threadIdx.x) / kBinLanes;
   if (pix >= W * H) return;
+  uint32_t lane = threadIdx.x & 31u;
+  uint32_t hmask = 0xFFFFu << (lane & 16u);
+  uint32_t l16 = lane & 15u;
+  int b0 = 4 * (int)l16;
+  uint32_t slot = threadIdx.x / kBinLanes;
   uint32_t x = pix % W, y = pix / W;
   uint32_t tx0 = (x / 32) * 32, ty0 = (y / 32) * 32;
   uint32_t tx1 = min(tx0 + 31, W - 1), ty1 = min(ty0 + 31, H - 1);
-  float* a = acc + (size_t)pix * kSpecN;
+  float* ap = acc + (size_t)pix * kSpecN + b0;
+  Bins4 a = ld_bins(ap);
   float ws = accw[pix].w;
   int sy0 = max((int)ty0, (int)y - 2), sy1 = min((int)ty1, (int)y + 2);
   int sx0 = max((int)tx0, (int)x - 2), sx1 = min((int)tx1, (int)x + 2);
@@ -293,23 +443,38 @@ __global__ void k_spec_film(uint32_t W, uint32_t H, const float2* pf, const floa
       pmaxy = min(pmaxy, (int)ty1);
       if ((int)x < pminx || (int)x > pmaxx || (int)y < pminy || (int)y > pmaxy) continue;
       float w = mitchell1(((float)x - f.x) / 2.0f) * mitchell1(((float)y - f.y) / 2.0f);
-      const float* s = L + sp * kSpecN;
-      bool black = true;
-      for (int i = 0; i < kSpecN; ++i) black = black && s[i] == 0.0f;
-      if (!black)
-        for (int i = 0; i < kSpecN; ++i) a[i] = a[i] + s[i] * w;
+      Bins4 s = ld_bins(L + sp * kSpecN + b0);
+      if (__ballot_sync(hmask, bins_nonzero(s)) & hmask)
+        for (int j = 0; j < 4; ++j) a.v[j] = a.v[j] + s.v[j] * w;
       ws = ws + w;
     }
-  accw[pix].w = ws;
-}
-
-// toRGB of the accumulated spectra with the context's quirks (film output).
-__global__ void k_spec_resolve(uint32_t n, const float* acc, float4* accw, uint32_t quirks) {
-  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= n) return;
-  RGB3 c = s64_to_rgb(c_spec, acc + (size_t)pix * kSpecN, quirks);
-  float4 a = accw[pix];
-  accw[pix] = make_float4(c.r, c.g, c.b, a.w);
+  st_bins(ap, a);
+  // toXYZ products, then sequential sums
+  float* px = prod[slot][0];
+  float* py = prod[slot][1];
+  float* pz = prod[slot][2];
+  for (int j = 0; j < 4; ++j) {
+    px[b0 + j] = a.v[j] * g_spec.X[b0 + j];
+    py[b0 + j] = a.v[j] * g_spec.Y[b0 + j];
+    pz[b0 + j] = a.v[j] * g_spec.Z[b0 + j];
+  }
+  __syncwarp(hmask);
+  if (l16 < 3) {
+    const float* p = prod[slot][l16];
+    float sum = 0.0f;
+    for (int i = 0; i < kSpecN; ++i) sum = sum + p[i];
+    xyz[slot][l16] = sum;
+  }
+  __syncwarp(hmask);
+  if (l16 == 0) {
+    float dl = (float)(wpbr_spec::kLambdaEnd - wpbr_spec::kLambdaStart) / (float)kSpecN;
+    float X = xyz[slot][0] * dl, Y = xyz[slot][1] * dl, Z = xyz[slot][2] * dl;
+    float m20 = (quirks & WPBR_Q_XYZ_MATRIX_FIX) ? 0.055648f : 0.041556f;
+    float r = (X * 3.240479f + Y * -1.537150f) + Z * -0.498535f;
+    float g = (X * -0.969256f + Y * 1.875991f) + Z * 0.041556f;
+    float b = (X * m20 + Y * -0.204043f) + Z * 1.057311f;
+    accw[pix] = make_float4(r, g, b, ws);
+  }
 }
 
 }  // namespace
@@ -319,7 +484,7 @@ wpbr_status spectral_setup(wpbr_ctx* ctx) {
   size_t n = (size_t)R.W * R.H;
   SpecTables T;
   build_tables(&T);
-  WPBR_CUDA(cudaMemcpyToSymbolAsync(c_spec, &T, sizeof(T), 0, cudaMemcpyHostToDevice, ctx->stream));
+  WPBR_CUDA(cudaMemcpyToSymbolAsync(g_spec, &T, sizeof(T), 0, cudaMemcpyHostToDevice, ctx->stream));
   // material and light spectra from the scene's RGB parameters
   std::vector<wpbr_material> mats(ctx->nmat);
   WPBR_CUDA(cudaMemcpyAsync(mats.data(), ctx->mats.p, sizeof(wpbr_material) * ctx->nmat, cudaMemcpyDeviceToHost,
@@ -351,25 +516,36 @@ wpbr_status spectral_setup(wpbr_ctx* ctx) {
   return WPBR_OK;
 }
 
-wpbr_status spectral_pass(wpbr_ctx* ctx, uint32_t pass) {
-  RenderState& R = ctx->rs;
-  if (!R.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render_pass: render_setup not called");
-  if (pass >= R.spp) return set_err(ctx, WPBR_ERR_INVALID_ARG, "render_pass: pass >= spp");
+static PassCtx spec_pass_ctx(wpbr_ctx* ctx) {
   PassCtx P;
   P.S = scene_view(ctx);
-  P.Bv = ctx->bvh.view;
-  P.rs = wpbr_rng::Stream{R.seed, R.stream, R.spp};
-  P.W = R.W;
-  P.H = R.H;
+  P.Bv = traversal_view(ctx);
+  P.rs = wpbr_rng::Stream{ctx->rs.seed, ctx->rs.stream, ctx->rs.spp};
+  P.W = ctx->rs.W;
+  P.H = ctx->rs.H;
   P.err = ctx->d_err.p;
+  return P;
+}
+
+// The scalar spawn of the Sampled64 pass, between the camera traversal and
+// the shadow-ray traversal (render_pass_launch).
+cudaError_t spectral_spawn_launch(wpbr_ctx* ctx, const uint32_t* pass_ptr) {
+  RenderState& R = ctx->rs;
+  uint32_t n = R.W * R.H;
+  k_sspawn<<<div_up(n, kTB), kTB, 0, ctx->stream>>>(spec_pass_ctx(ctx), pass_ptr, R.hit_prim.p, R.pstate.p,
+                                                     R.shadow_rays.p, R.pfilm.p);
+  return cudaGetLastError();
+}
+
+// The per-bin finish, film gather and toRGB after the shadow-ray traversal.
+cudaError_t spectral_finish_launch(wpbr_ctx* ctx) {
+  RenderState& R = ctx->rs;
   uint32_t n = R.W * R.H;
   SpecCtx C{(const SpecMat*)R.spec_mats.p, (const S64*)R.spec_le.p, R.spec_L.p};
-  cudaStream_t st = ctx->stream;
-  k_spec_pass<<<div_up(n, 64), 64, 0, st>>>(P, C, pass, R.pfilm.p);
-  k_spec_film<<<div_up(n, 128), 128, 0, st>>>(R.W, R.H, R.pfilm.p, R.spec_L.p, R.spec_acc.p, (float4*)R.acc.p);
-  k_spec_resolve<<<div_up(n, 128), 128, 0, st>>>(n, R.spec_acc.p, (float4*)R.acc.p, ctx->quirks);
-  WPBR_CUDA(cudaGetLastError());
-  return WPBR_OK;
+  unsigned g = div_up((uint64_t)n * kBinLanes, 128);
+  k_sfinish<<<g, 128, 0, ctx->stream>>>(spec_pass_ctx(ctx), C, R.pstate.p, R.shadow_hit.p);
+  k_sfilm<<<g, 128, 0, ctx->stream>>>(R.W, R.H, R.pfilm.p, R.spec_L.p, R.spec_acc.p, (float4*)R.acc.p, ctx->quirks);
+  return cudaGetLastError();
 }
 
 }  // namespace wpbr
