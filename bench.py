@@ -575,6 +575,9 @@ def main():
     if rank == 0 and not args.no_render:
         render = {"c0_plain_256x256_4spp": render_rate(W, torch, 0, (256, 256), 4, frames=3),
                   "c2_fullframe_1080p_64spp": render_rate(W, torch, 2, (1920, 1080), 64, level=LEVEL),
+                  "c2_fullframe_1080p_16spp_sampled64": render_rate(W, torch, 2, (1920, 1080), 16, level=LEVEL,
+                                                                    spectrum=W.SPECTRUM_SAMPLED64),
+                  "c5_textured_metal_1080p_16spp": render_rate(W, torch, 5, (1920, 1080), 16),
                   "c3_batched_32_scenes_16spp": batch_rate(W, torch),
                   "c4_adjoint_512x512_16spp": adjoint_rate(W, torch, fp64=not args.no_cpu)}
 
@@ -591,7 +594,7 @@ def main():
                    "hit_fraction": hit_frac, "l2": "inputs larger than L2 (268 MB of rays), no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 16 * n},
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * ctx.collide_launches(n),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind,
                      "traffic": (tpr * n) if tpr else None,

@@ -121,17 +121,25 @@ WPBR_API wpbr_status wpbr_bvh_export(wpbr_ctx* ctx, float* prim_bounds, float* c
  * CLOSEST returns the reference's hit (closest non-zero t, first candidate in
  * near-first order on ties); ANY stops at the first hit (occlusion only). */
 enum wpbr_trace_mode { WPBR_TRACE_CLOSEST = 0, WPBR_TRACE_ANY = 1 };
+/* Host buffers (rays: n x 8 floats o.xyz, 0, d.xyz, tmax; hits: n x 4 floats
+ * t, prim id bits, b1, b2). Batches of 2^22 rays and more are copied and
+ * traced in up to 4 chunks, the copies of one chunk overlapping the
+ * traversal of its neighbours (page-locked host buffers let them overlap). */
 WPBR_API wpbr_status wpbr_collide(wpbr_ctx* ctx, const float* rays, uint64_t n, float* hits, uint32_t mode);
 WPBR_API wpbr_status wpbr_collide_device(wpbr_ctx* ctx, const void* d_rays, uint64_t n, void* d_hits,
                                          uint32_t mode);
-/* Per-ray node visits and primitive tests (u32 pairs), for the byte model. */
 /* Large batches (256k rays and more) are traced in the order of their
  * origins' Morton cells on a 2^b per axis grid over the scene bounds
  * (b = bits_per_axis, default 8, at most 10) and written back at their input
  * positions; the hits do not depend on the order. 0 traces in input order. */
 WPBR_API wpbr_status wpbr_set_ray_sort(wpbr_ctx* ctx, uint32_t bits_per_axis);
+/* Per-ray node visits and primitive tests (u32 pairs), for the byte model. */
 WPBR_API wpbr_status wpbr_collide_stats(wpbr_ctx* ctx, const float* rays, uint64_t n, float* hits,
                                         uint32_t* stats, uint32_t mode);
+/* Number of kernels one wpbr_collide_device call of n rays launches with the
+ * context's current settings (the traversal, plus the ray-order key and
+ * radix-sort kernels for large batches). */
+WPBR_API wpbr_status wpbr_collide_launches(const wpbr_ctx* ctx, uint64_t n, uint32_t* launches);
 
 /* ---- rendering -------------------------------------------------------------- */
 /* Film + sample streams for spp passes (JobGenerateFilmTiles,

@@ -112,10 +112,44 @@ def test_ray_reordering_keeps_hits(W, ctx):
     ctx.set_ray_sort(0)
     hu = ctx.collide(rays)
     au = ctx.collide(rays, mode=W.TRACE_ANY)
+    assert ctx.collide_launches(rays.shape[0]) == 1  # traversal only
     ctx.set_ray_sort(5)
     h5 = ctx.collide(rays)
+    # key kernel + 2 radix passes (15 bits) x (histogram, scan, scatter) + traversal
+    assert ctx.collide_launches(rays.shape[0]) > 4
+    assert ctx.collide_launches(1000) == 1
     ctx.set_ray_sort(8)
     assert np.array_equal(hs.view(np.uint32), h5.view(np.uint32))
     assert np.array_equal(hs.view(np.uint32), hu.view(np.uint32))
     assert np.array_equal(as_[:, 1].view(np.uint32) == 0xFFFFFFFF, au[:, 1].view(np.uint32) == 0xFFFFFFFF)
+    ctx.check_device_errors()
+
+
+def test_chunked_host_collide_matches_device_collide(W, ctx):
+    # host-buffer batches of 2^22 rays and more are copied and traced in
+    # chunks whose copies overlap the neighbouring chunks' traversal; the
+    # hits must equal one device-resident call over the whole batch (each
+    # chunk is reordered on its own, and reordering never changes a hit)
+    torch = pytest.importorskip("torch")
+    g = W.SceneGen(1, 0, (1024, 1024), level=7, rays=True)
+    ctx.set_quirks(0)
+    ctx.upload(g.desc)
+    ctx.build()
+    rays = g.rays()
+    rays = np.concatenate([rays, rays, rays])
+    n = (1 << 22) + (1 << 21) + 777  # 4 chunks, the last one short
+    rays = np.concatenate([rays, rays[: n - rays.shape[0]]])
+    assert rays.shape[0] == n
+    d_rays = torch.from_numpy(rays).cuda()
+    d_hits = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()  # the context's stream does not wait for torch's
+    for mode in (W.TRACE_CLOSEST, W.TRACE_ANY):
+        ctx.collide_device(d_rays.data_ptr(), n, d_hits.data_ptr(), mode)
+        ctx.synchronize()
+        hd = d_hits.cpu().numpy()
+        hh = ctx.collide(rays, mode=mode)
+        if mode == W.TRACE_CLOSEST:
+            assert np.array_equal(hh.view(np.uint32), hd.view(np.uint32))
+        else:
+            assert np.array_equal(hh[:, 1].view(np.uint32) == 0xFFFFFFFF, hd[:, 1].view(np.uint32) == 0xFFFFFFFF)
     ctx.check_device_errors()

@@ -60,6 +60,7 @@ _SIGS = {
     "wpbr_collide": (C.c_int, [_VP, _FP, C.c_uint64, _FP, C.c_uint32]),
     "wpbr_collide_device": (C.c_int, [_VP, _VP, C.c_uint64, _VP, C.c_uint32]),
     "wpbr_collide_stats": (C.c_int, [_VP, _FP, C.c_uint64, _FP, _UP, C.c_uint32]),
+    "wpbr_collide_launches": (C.c_int, [_VP, C.c_uint64, _UP]),
     "wpbr_render_setup": (C.c_int, [_VP, C.c_uint32, C.c_uint32, C.c_uint32]),
     "wpbr_render_pass": (C.c_int, [_VP, C.c_uint32]),
     "wpbr_render": (C.c_int, [_VP]),
@@ -271,6 +272,12 @@ class Context:
             return hits, st
         self._check(lib().wpbr_collide(self._h, _fp(rays), n, _fp(hits), mode), "collide")
         return hits
+
+    def collide_launches(self, n):
+        """Kernels one collide_device call of n rays launches."""
+        c = C.c_uint32()
+        self._check(lib().wpbr_collide_launches(self._h, n, C.byref(c)), "collide_launches")
+        return c.value
 
     def collide_device(self, d_rays, n, d_hits, mode=TRACE_CLOSEST):
         self._check(lib().wpbr_collide_device(self._h, d_rays, n, d_hits, mode), "collide_device")

@@ -99,6 +99,15 @@ __global__ void k_scan_add(uint32_t* out, uint32_t n, const uint32_t* boff) {
 
 }  // namespace
 
+// Kernel launches of scan_exclusive over n elements: one tile scan per
+// level, one add per level but the last.
+uint32_t scan_launches(uint32_t n) {
+  if (n == 0) return 0;
+  uint32_t levels = 1;
+  for (uint32_t m = n; m > (uint32_t)kScanTile; m = div_up(m, kScanTile)) ++levels;
+  return 2 * levels - 1;
+}
+
 cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, DevBuf<uint32_t>& tmp, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   // tmp layout: level-1 sums, level-2 sums, ...
@@ -1231,6 +1240,14 @@ __global__ void k_wide_emit(uint32_t nq, uint32_t base, const uint32_t* q_bin, c
 }
 
 }  // namespace
+
+// Kernel launches of radix_sort_pairs: per 8-bit pass a histogram, the
+// scan of the block histograms and a scatter.
+uint32_t radix_sort_launches(uint32_t n, int bits) {
+  if (n <= 1) return 0;
+  uint32_t passes = (uint32_t)((bits + 7) / 8);
+  return passes * (2 + scan_launches(256 * div_up(n, kRadixTile)));
+}
 
 // Stable LSD radix sort of (key, value) pairs by key bits [0, bits), 8 bits
 // per pass (the build's sort kernels); *kres / *vres point at the buffer

@@ -90,6 +90,7 @@ struct RenderState {
   DevBuf<uint32_t> counters;  // ray-fetch counters of the pass's traversal launches
   // Sampled64 mode: material / light spectra, per-pixel sample spectra, film spectra
   DevBuf<float> spec_mats, spec_le, spec_L, spec_acc;
+  bool spec_dirty = false;  // Sampled64 passes ran since the last toRGB of the film
   const uint32_t* pass_ptr = nullptr;  // shared pass index (batches); null: pass_dev
   uint32_t trace_grid = 0;             // persistent traversal grid cap (0: full)
 };
@@ -167,6 +168,11 @@ struct wpbr_ctx {
   // staging for the host-buffer collide entry points
   wpbr::DevBuf<float4> io_rays, io_hits;
   wpbr::DevBuf<uint32_t> io_stats;
+  // copy streams and events of the chunked host-buffer collide (created on
+  // first use): rays of chunk i+1 go up and hits of chunk i-1 come down while
+  // chunk i is traced on the context's stream
+  cudaStream_t io_h2d = nullptr, io_d2h = nullptr;
+  cudaEvent_t io_ev[3] = {nullptr, nullptr, nullptr};
   wpbr::DevBuf<uint32_t> trace_counter;  // ray-fetch counters of the persistent traversal
   // ray reordering of large collide batches (keys, permutation, radix scratch)
   uint32_t ray_sort = 8;  // bits per axis of the origin grid (0: input order)
@@ -205,6 +211,7 @@ wpbr_status spectral_setup(wpbr_ctx* ctx);
 // RGB spawn) and the per-bin finish + film (replace the RGB finish + film).
 cudaError_t spectral_spawn_launch(wpbr_ctx* ctx, const uint32_t* pass_ptr);
 cudaError_t spectral_finish_launch(wpbr_ctx* ctx);
+wpbr_status spectral_resolve(wpbr_ctx* ctx);
 // float4 per pixel of the fused pass's state buffer (RenderState::pstate);
 // the RGB and the Sampled64 spawn records both fit in it.
 constexpr int kPassStateF4 = 7;
@@ -221,6 +228,9 @@ wpbr_status adjoint_forward(wpbr_ctx* ctx, const float* target, float* image, do
 wpbr_status adjoint_backward(wpbr_ctx* ctx, float* grad_mat, float* grad_env, bool device);
 // scan helper (exclusive, in place allowed): out[i] = sum in[0..i); returns total in *total_dev (device, may be null)
 cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, DevBuf<uint32_t>& tmp, cudaStream_t s);
+uint32_t scan_launches(uint32_t n);
+uint32_t radix_sort_launches(uint32_t n, int bits);
+uint32_t trace_launches(const wpbr_ctx* ctx, uint64_t n, bool stats);
 }  // namespace wpbr
 
 #define WPBR_CUDA(call)                                          \

@@ -582,6 +582,7 @@ wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass) {
   if (pass >= R.spp) return set_err(ctx, WPBR_ERR_INVALID_ARG, "render_pass: pass >= spp");
   cudaStream_t st = ctx->stream;
   WPBR_CUDA(cudaMemcpyAsync(R.pass_dev.p, &pass, 4, cudaMemcpyHostToDevice, st));
+  if (ctx->spectrum == WPBR_SPECTRUM_SAMPLED64) R.spec_dirty = true;
   uint64_t key = pass_graph_key(ctx);
   if (R.graph && R.graph_key != key) {
     cudaGraphExecDestroy(R.graph);
@@ -676,6 +677,8 @@ wpbr_status job_record(wpbr_ctx* ctx, uint32_t x0, uint32_t y0, uint32_t x1, uin
 wpbr_status film_tonemap(wpbr_ctx* ctx, uint8_t* out) {
   RenderState& R = ctx->rs;
   if (!R.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "tonemap: render_setup not called");
+  wpbr_status rs = spectral_resolve(ctx);
+  if (rs != WPBR_OK) return rs;
   uint32_t n = R.W * R.H;
   DevBuf<uint8_t> tmp;
   WPBR_CUDA(tmp.ensure((size_t)n * 3));

@@ -6,9 +6,10 @@
 // Wavefront layout: the pass shares the RGB path's camera and shadow-ray
 // persistent traversals (render.cu); k_sspawn (one thread per pixel) does
 // the scalar part of shading and sampling and records, per pixel, the
-// scalar factors every spectral term needs; k_sfinish and k_sfilm give each
-// pixel a half-warp, 16 lanes x 4 bins, for the per-bin products, the
-// Fresnel terms, the Mitchell film gather and toRGB. Every per-bin value is
+// scalar factors every spectral term needs; k_sfinish gives each pixel a
+// half-warp, 16 lanes x 4 bins, for the per-bin Fresnel terms and products,
+// k_sfilm 8 lanes x 8 bins for the Mitchell film gather; k_sresolve
+// converts the film to RGB once per frame (or before a film read). Every per-bin value is
 // computed with the same operations in the same order as the one-thread
 // restatement, so the film is bit-identical to it; sums over bins (toXYZ)
 // stay sequential in bin order.
@@ -407,33 +408,38 @@ __global__ void __launch_bounds__(128) k_sfinish(PassCtx P, SpecCtx C, const flo
   st_bins(C.L + (size_t)pix * kSpecN + b0, L);
 }
 
-// Tile-clipped Mitchell gather of film_gather, 64 bins per sample, then
-// toRGB of the accumulated spectrum (s64_to_rgb: products per bin, the three
-// sums taken sequentially in bin order by lanes 0-2 of the half-warp).
-constexpr int kSumStride = 68;  // floats per channel row in shared memory (float4-aligned, bank-skewed)
+// Tile-clipped Mitchell gather of film_gather, 64 bins per sample, with 8
+// lanes per pixel and 8 bins per lane (the per-neighbour bookkeeping is
+// shared by 8 bins). The lanes of a pixel first evaluate the footprint test
+// and filter weight of the up to 25 neighbouring samples in parallel (lane
+// l: neighbours l, l + 8, l + 16, l + 24 in row-major order); the
+// accumulation then walks the neighbours in the reference's order,
+// broadcasting each weight.
+constexpr int kFilmLanes = 8;
 __global__ void __launch_bounds__(128) k_sfilm(uint32_t W, uint32_t H, const float2* pf, const float* L, float* acc,
-                                               float4* accw, uint32_t quirks) {
-  __shared__ __align__(16) float prod[128 / kBinLanes][3][kSumStride];
-  __shared__ float xyz[128 / kBinLanes][3];
-  uint32_t pix = (blockIdx.x * blockDim.x + threadIdx.x) / kBinLanes;
-  if (pix >= W * H) return;
+                                               float4* accw) {
+  uint32_t pix = (blockIdx.x * blockDim.x + threadIdx.x) / kFilmLanes;
+  if (pix >= W * H) return;  // the pixel's lanes leave together
   uint32_t lane = threadIdx.x & 31u;
-  uint32_t hmask = 0xFFFFu << (lane & 16u);
-  uint32_t l16 = lane & 15u;
-  int b0 = 4 * (int)l16;
-  uint32_t slot = threadIdx.x / kBinLanes;
+  uint32_t gbase = lane & ~(uint32_t)(kFilmLanes - 1);
+  uint32_t gmask = 0xFFu << gbase;
+  uint32_t l8 = lane - gbase;
+  int b0 = 8 * (int)l8;
   uint32_t x = pix % W, y = pix / W;
   uint32_t tx0 = (x / 32) * 32, ty0 = (y / 32) * 32;
   uint32_t tx1 = min(tx0 + 31, W - 1), ty1 = min(ty0 + 31, H - 1);
-  float* ap = acc + (size_t)pix * kSpecN + b0;
-  Bins4 a = ld_bins(ap);
-  float ws = accw[pix].w;
   int sy0 = max((int)ty0, (int)y - 2), sy1 = min((int)ty1, (int)y + 2);
   int sx0 = max((int)tx0, (int)x - 2), sx1 = min((int)tx1, (int)x + 2);
-  for (int sy = sy0; sy <= sy1; ++sy)
-    for (int sx = sx0; sx <= sx1; ++sx) {
-      size_t sp = (size_t)sy * W + sx;
-      float2 f = pf[sp];
+  int nsx = sx1 - sx0 + 1, cnt = nsx * (sy1 - sy0 + 1);
+  float wk[4];
+  uint32_t vbits = 0;  // bit r: neighbour l8 + 8 r lies in the sample's clipped footprint
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    int k = (int)l8 + kFilmLanes * r;
+    wk[r] = 0.0f;
+    if (k < cnt) {
+      int sy = sy0 + k / nsx, sx = sx0 + k % nsx;
+      float2 f = pf[(size_t)sy * W + sx];
       float dx0 = f.x - 0.5f, dy0 = f.y - 0.5f;
       int pminx = (int)ceilf(dx0 - 2.0f), pmaxx = (int)floorf(dx0 + 2.0f);
       int pminy = (int)ceilf(dy0 - 2.0f), pmaxy = (int)floorf(dy0 + 2.0f);
@@ -441,40 +447,74 @@ __global__ void __launch_bounds__(128) k_sfilm(uint32_t W, uint32_t H, const flo
       pminy = max(pminy, (int)ty0);
       pmaxx = min(pmaxx, (int)tx1);
       pmaxy = min(pmaxy, (int)ty1);
-      if ((int)x < pminx || (int)x > pmaxx || (int)y < pminy || (int)y > pmaxy) continue;
-      float w = mitchell1(((float)x - f.x) / 2.0f) * mitchell1(((float)y - f.y) / 2.0f);
-      Bins4 s = ld_bins(L + sp * kSpecN + b0);
-      if (__ballot_sync(hmask, bins_nonzero(s)) & hmask)
-        for (int j = 0; j < 4; ++j) a.v[j] = a.v[j] + s.v[j] * w;
+      if (!((int)x < pminx || (int)x > pmaxx || (int)y < pminy || (int)y > pmaxy)) {
+        vbits |= 1u << r;
+        wk[r] = mitchell1(((float)x - f.x) / 2.0f) * mitchell1(((float)y - f.y) / 2.0f);
+      }
+    }
+  }
+  float* ap = acc + (size_t)pix * kSpecN + b0;
+  Bins4 a0 = ld_bins(ap), a1 = ld_bins(ap + 4);
+  float ws = accw[pix].w;
+  int k = 0;
+  for (int sy = sy0; sy <= sy1; ++sy)
+    for (int sx = sx0; sx <= sx1; ++sx, ++k) {
+      uint32_t src = gbase | (uint32_t)(k & (kFilmLanes - 1));
+      int r = k / kFilmLanes;
+      float mine = r == 0 ? wk[0] : r == 1 ? wk[1] : r == 2 ? wk[2] : wk[3];
+      float w = __shfl_sync(gmask, mine, src);
+      uint32_t vb = __shfl_sync(gmask, vbits, src);
+      if (!((vb >> r) & 1u)) continue;
+      const float* sp = L + ((size_t)sy * W + sx) * kSpecN + b0;
+      Bins4 s0 = ld_bins(sp), s1 = ld_bins(sp + 4);
+      if (__ballot_sync(gmask, bins_nonzero(s0) || bins_nonzero(s1)) & gmask) {
+        for (int j = 0; j < 4; ++j) a0.v[j] = a0.v[j] + s0.v[j] * w;
+        for (int j = 0; j < 4; ++j) a1.v[j] = a1.v[j] + s1.v[j] * w;
+      }
       ws = ws + w;
     }
-  st_bins(ap, a);
-  // toXYZ products, then sequential sums
-  float* px = prod[slot][0];
-  float* py = prod[slot][1];
-  float* pz = prod[slot][2];
-  for (int j = 0; j < 4; ++j) {
-    px[b0 + j] = a.v[j] * g_spec.X[b0 + j];
-    py[b0 + j] = a.v[j] * g_spec.Y[b0 + j];
-    pz[b0 + j] = a.v[j] * g_spec.Z[b0 + j];
+  st_bins(ap, a0);
+  st_bins(ap + 4, a1);
+  if (l8 == 0) accw[pix].w = ws;
+}
+
+// toRGB of the accumulated spectra (s64_to_rgb: per bin products, the three
+// sums taken sequentially in bin order, bin width, XYZ to RGB matrix). A
+// warp stages 32 pixels' spectra in shared memory with coalesced loads, then
+// each lane sums one pixel.
+constexpr int kResolveRow = kSpecN + 1;  // padded row: lane l reads bank (l + i) mod 32
+__global__ void __launch_bounds__(128) k_sresolve(uint32_t n, const float* acc, float4* accw, uint32_t quirks) {
+  __shared__ float sh[4][32 * kResolveRow];
+  uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31u;
+  uint64_t base = ((uint64_t)blockIdx.x * 4 + warp) * 32;
+  if (base >= n) return;
+  float* row = sh[warp];
+  for (int i = 0; i < kSpecN; ++i) {
+    uint32_t k = (uint32_t)i * 32 + lane;  // element k of the warp's 32 x 64 block
+    uint64_t p = base + k / kSpecN;
+    if (p < n) row[(k / kSpecN) * kResolveRow + k % kSpecN] = acc[p * kSpecN + k % kSpecN];
   }
-  __syncwarp(hmask);
-  if (l16 < 3) {
-    const float* p = prod[slot][l16];
-    float sum = 0.0f;
-    for (int i = 0; i < kSpecN; ++i) sum = sum + p[i];
-    xyz[slot][l16] = sum;
+  __syncwarp();
+  uint64_t p = base + lane;
+  if (p >= n) return;
+  const float* s = row + lane * kResolveRow;
+  float X = 0.0f, Y = 0.0f, Z = 0.0f;
+  for (int i = 0; i < kSpecN; ++i) {
+    float v = s[i];
+    X = X + v * g_spec.X[i];
+    Y = Y + v * g_spec.Y[i];
+    Z = Z + v * g_spec.Z[i];
   }
-  __syncwarp(hmask);
-  if (l16 == 0) {
-    float dl = (float)(wpbr_spec::kLambdaEnd - wpbr_spec::kLambdaStart) / (float)kSpecN;
-    float X = xyz[slot][0] * dl, Y = xyz[slot][1] * dl, Z = xyz[slot][2] * dl;
-    float m20 = (quirks & WPBR_Q_XYZ_MATRIX_FIX) ? 0.055648f : 0.041556f;
-    float r = (X * 3.240479f + Y * -1.537150f) + Z * -0.498535f;
-    float g = (X * -0.969256f + Y * 1.875991f) + Z * 0.041556f;
-    float b = (X * m20 + Y * -0.204043f) + Z * 1.057311f;
-    accw[pix] = make_float4(r, g, b, ws);
-  }
+  float dl = (float)(wpbr_spec::kLambdaEnd - wpbr_spec::kLambdaStart) / (float)kSpecN;
+  X = X * dl;
+  Y = Y * dl;
+  Z = Z * dl;
+  float m20 = (quirks & WPBR_Q_XYZ_MATRIX_FIX) ? 0.055648f : 0.041556f;
+  float r = (X * 3.240479f + Y * -1.537150f) + Z * -0.498535f;
+  float g = (X * -0.969256f + Y * 1.875991f) + Z * 0.041556f;
+  float b = (X * m20 + Y * -0.204043f) + Z * 1.057311f;
+  float4 a = accw[p];
+  accw[p] = make_float4(r, g, b, a.w);
 }
 
 }  // namespace
@@ -542,10 +582,22 @@ cudaError_t spectral_finish_launch(wpbr_ctx* ctx) {
   RenderState& R = ctx->rs;
   uint32_t n = R.W * R.H;
   SpecCtx C{(const SpecMat*)R.spec_mats.p, (const S64*)R.spec_le.p, R.spec_L.p};
-  unsigned g = div_up((uint64_t)n * kBinLanes, 128);
-  k_sfinish<<<g, 128, 0, ctx->stream>>>(spec_pass_ctx(ctx), C, R.pstate.p, R.shadow_hit.p);
-  k_sfilm<<<g, 128, 0, ctx->stream>>>(R.W, R.H, R.pfilm.p, R.spec_L.p, R.spec_acc.p, (float4*)R.acc.p, ctx->quirks);
+  k_sfinish<<<div_up((uint64_t)n * kBinLanes, 128), 128, 0, ctx->stream>>>(spec_pass_ctx(ctx), C, R.pstate.p,
+                                                                            R.shadow_hit.p);
+  k_sfilm<<<div_up((uint64_t)n * kFilmLanes, 128), 128, 0, ctx->stream>>>(R.W, R.H, R.pfilm.p, R.spec_L.p, R.spec_acc.p, (float4*)R.acc.p);
   return cudaGetLastError();
+}
+
+// Converts the accumulated spectra to the RGB film (wpbr_film_read and
+// wpbr_film_tonemap read it) when passes ran since the last conversion.
+wpbr_status spectral_resolve(wpbr_ctx* ctx) {
+  RenderState& R = ctx->rs;
+  if (ctx->spectrum != WPBR_SPECTRUM_SAMPLED64 || !R.spec_dirty) return WPBR_OK;
+  uint32_t n = R.W * R.H;
+  k_sresolve<<<div_up(n, 128), 128, 0, ctx->stream>>>(n, R.spec_acc.p, (float4*)R.acc.p, ctx->quirks);
+  WPBR_CUDA(cudaGetLastError());
+  R.spec_dirty = false;
+  return WPBR_OK;
 }
 
 }  // namespace wpbr

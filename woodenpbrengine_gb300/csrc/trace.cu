@@ -65,6 +65,17 @@ cudaError_t launch(const SceneView& S, const BvhView& Bv, const float4* rays, ui
 
 }  // namespace
 
+// Kernel launches of one trace_rays call (the memset of the work counter is
+// not a kernel): the traversal, plus the key kernel and the radix sort of
+// the ray order for large batches.
+uint32_t trace_launches(const wpbr_ctx* ctx, uint64_t n, bool stats) {
+  if (n == 0) return 0;
+  if (stats) return 1;
+  const BvhView Bv = traversal_view(ctx);
+  if (ctx->ray_sort && n >= kRaySortMin && !Bv.empty) return 2 + radix_sort_launches((uint32_t)n, 3 * (int)ctx->ray_sort);
+  return 1;
+}
+
 wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* d_hits, uint32_t mode,
                        uint32_t* d_stats) {
   if (!ctx->bvh.built) return set_err(ctx, WPBR_ERR_NOT_BUILT, "collide: BVH not built");
