@@ -532,6 +532,15 @@ def main():
     hits = d_hits.cpu().numpy()
     hit_frac = float(np.mean(hits[:, 1].view(np.uint32) != 0xFFFFFFFF))
 
+    # the dominant kernel alone: CUDA events around each traversal launch,
+    # on the context's stream (the step also runs the ray-order sort)
+    ctx.set_kernel_timing(True)
+    for _ in range(args.steps):
+        ctx.collide_device(d_rays.data_ptr(), n, d_hits.data_ptr(), W.TRACE_CLOSEST)
+    trav_total_ms, trav_launches = ctx.kernel_timing()
+    ctx.set_kernel_timing(False)
+    trav_ms = trav_total_ms / max(trav_launches, 1)
+
     # any-hit
     ea = torch.cuda.Event(enable_timing=True)
     eb = torch.cuda.Event(enable_timing=True)
@@ -549,7 +558,7 @@ def main():
     V = float(st[:, 0].mean())
     P = float(st[:, 1].mean())
     bytes_per_ray = 48.0 + 32.0 * V + 36.0 * P
-    achieved = bytes_per_ray * n / (ms_step / 1e3) / 1e9
+    achieved = bytes_per_ray * n / (trav_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
     tpr = ncu_traffic_per_ray()
 
@@ -596,7 +605,9 @@ def main():
         "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 16 * n},
         "gpu_launches": args.steps * ctx.collide_launches(n),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind,
+                     "peak_source": peak_kind, "kernel": "k_trace_persistent (closest hit)",
+                     "kernel_ms_per_launch": trav_ms, "timed_launches": trav_launches,
+                     "step_frac": bytes_per_ray * n / (ms_step / 1e3) / 1e9 / peak,
                      "traffic": (tpr * n) if tpr else None,
                      "bytes_model": "48 + 32*V + 36*P per ray, V=%.2f box tests, P=%.2f triangle tests" % (V, P)},
         "clocks": ck,

@@ -140,6 +140,13 @@ WPBR_API wpbr_status wpbr_collide_stats(wpbr_ctx* ctx, const float* rays, uint64
  * context's current settings (the traversal, plus the ray-order key and
  * radix-sort kernels for large batches). */
 WPBR_API wpbr_status wpbr_collide_launches(const wpbr_ctx* ctx, uint64_t n, uint32_t* launches);
+/* Instrumentation: with timing enabled, each collide call's traversal
+ * launch is bracketed by CUDA events on the context's stream (the first 64
+ * launches after enabling or after the last read); wpbr_kernel_timing
+ * waits for them and returns their summed duration and count, then starts
+ * a new series. */
+WPBR_API wpbr_status wpbr_set_kernel_timing(wpbr_ctx* ctx, uint32_t enable);
+WPBR_API wpbr_status wpbr_kernel_timing(wpbr_ctx* ctx, float* total_ms, uint32_t* launches);
 
 /* ---- rendering -------------------------------------------------------------- */
 /* Film + sample streams for spp passes (JobGenerateFilmTiles,

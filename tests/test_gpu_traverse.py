@@ -119,6 +119,16 @@ def test_ray_reordering_keeps_hits(W, ctx):
     assert ctx.collide_launches(rays.shape[0]) > 4
     assert ctx.collide_launches(1000) == 1
     ctx.set_ray_sort(8)
+    # traversal launches timed with CUDA events when asked, and only then
+    ctx.set_kernel_timing(True)
+    ctx.collide(rays)
+    ctx.collide(rays, mode=W.TRACE_ANY)
+    ms, launches = ctx.kernel_timing()
+    assert launches == 2 and ms > 0.0
+    assert ctx.kernel_timing() == (0.0, 0)
+    ctx.set_kernel_timing(False)
+    ctx.collide(rays)
+    assert ctx.kernel_timing()[1] == 0
     assert np.array_equal(hs.view(np.uint32), h5.view(np.uint32))
     assert np.array_equal(hs.view(np.uint32), hu.view(np.uint32))
     assert np.array_equal(as_[:, 1].view(np.uint32) == 0xFFFFFFFF, au[:, 1].view(np.uint32) == 0xFFFFFFFF)

@@ -61,6 +61,8 @@ _SIGS = {
     "wpbr_collide_device": (C.c_int, [_VP, _VP, C.c_uint64, _VP, C.c_uint32]),
     "wpbr_collide_stats": (C.c_int, [_VP, _FP, C.c_uint64, _FP, _UP, C.c_uint32]),
     "wpbr_collide_launches": (C.c_int, [_VP, C.c_uint64, _UP]),
+    "wpbr_set_kernel_timing": (C.c_int, [_VP, C.c_uint32]),
+    "wpbr_kernel_timing": (C.c_int, [_VP, C.POINTER(C.c_float), _UP]),
     "wpbr_render_setup": (C.c_int, [_VP, C.c_uint32, C.c_uint32, C.c_uint32]),
     "wpbr_render_pass": (C.c_int, [_VP, C.c_uint32]),
     "wpbr_render": (C.c_int, [_VP]),
@@ -278,6 +280,15 @@ class Context:
         c = C.c_uint32()
         self._check(lib().wpbr_collide_launches(self._h, n, C.byref(c)), "collide_launches")
         return c.value
+
+    def set_kernel_timing(self, enable):
+        self._check(lib().wpbr_set_kernel_timing(self._h, 1 if enable else 0), "set_kernel_timing")
+
+    def kernel_timing(self):
+        """(summed ms, launches) of the traversal launches timed since the last read."""
+        ms, c = C.c_float(), C.c_uint32()
+        self._check(lib().wpbr_kernel_timing(self._h, C.byref(ms), C.byref(c)), "kernel_timing")
+        return ms.value, c.value
 
     def collide_device(self, d_rays, n, d_hits, mode=TRACE_CLOSEST):
         self._check(lib().wpbr_collide_device(self._h, d_rays, n, d_hits, mode), "collide_device")

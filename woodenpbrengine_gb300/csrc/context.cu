@@ -208,6 +208,8 @@ WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
   ctx->io_rays.release(); ctx->io_hits.release(); ctx->io_stats.release(); ctx->trace_counter.release();
   for (cudaEvent_t& ev : ctx->io_ev)
     if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t& ev : ctx->tev)
+    if (ev) cudaEventDestroy(ev);
   if (ctx->io_h2d) cudaStreamDestroy(ctx->io_h2d);
   if (ctx->io_d2h) cudaStreamDestroy(ctx->io_d2h);
   ctx->rs_k0.release(); ctx->rs_v0.release(); ctx->rs_k1.release(); ctx->rs_v1.release();
@@ -600,6 +602,28 @@ static wpbr_status collide_host(wpbr_ctx* ctx, const float* rays, uint64_t n, fl
   WPBR_CUDA(cudaMemcpyAsync(hits, ctx->io_hits.p, 16 * n, cudaMemcpyDeviceToHost, st));
   if (stats) WPBR_CUDA(cudaMemcpyAsync(stats, ctx->io_stats.p, 8 * n, cudaMemcpyDeviceToHost, st));
   WPBR_CUDA(cudaStreamSynchronize(st));
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_set_kernel_timing(wpbr_ctx* ctx, uint32_t enable) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  ctx->kernel_timing = enable != 0;
+  ctx->timed = 0;
+  return WPBR_OK;
+}
+
+WPBR_API wpbr_status wpbr_kernel_timing(wpbr_ctx* ctx, float* total_ms, uint32_t* launches) {
+  if (!ctx || !total_ms || !launches) return WPBR_ERR_INVALID_ARG;
+  float sum = 0.0f;
+  for (int i = 0; i < ctx->timed; ++i) {
+    float ms = 0.0f;
+    WPBR_CUDA(cudaEventSynchronize(ctx->tev[2 * i + 1]));
+    WPBR_CUDA(cudaEventElapsedTime(&ms, ctx->tev[2 * i], ctx->tev[2 * i + 1]));
+    sum += ms;
+  }
+  *total_ms = sum;
+  *launches = (uint32_t)ctx->timed;
+  ctx->timed = 0;
   return WPBR_OK;
 }
 

@@ -173,6 +173,11 @@ struct wpbr_ctx {
   // chunk i is traced on the context's stream
   cudaStream_t io_h2d = nullptr, io_d2h = nullptr;
   cudaEvent_t io_ev[3] = {nullptr, nullptr, nullptr};
+  // wpbr_set_kernel_timing: CUDA events around each collide traversal launch
+  static constexpr int kTimedMax = 64;
+  bool kernel_timing = false;
+  int timed = 0;  // event pairs recorded since the last wpbr_kernel_timing
+  cudaEvent_t tev[2 * kTimedMax] = {};
   wpbr::DevBuf<uint32_t> trace_counter;  // ray-fetch counters of the persistent traversal
   // ray reordering of large collide batches (keys, permutation, radix scratch)
   uint32_t ray_sort = 8;  // bits per axis of the origin grid (0: input order)

@@ -115,6 +115,14 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
           perm = vr;
         }
       }
+      // optional CUDA events around the traversal launch (wpbr_set_kernel_timing)
+      int slot = -1;
+      if (e == cudaSuccess && ctx->kernel_timing && ctx->timed < wpbr_ctx::kTimedMax) {
+        slot = ctx->timed;
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+          if (!ctx->tev[2 * slot + k]) e = cudaEventCreate(&ctx->tev[2 * slot + k]);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->tev[2 * slot], ctx->stream);
+      }
       if (e == cudaSuccess) {
         if (perm) {
           PermSrc src{d_rays, perm};
@@ -132,6 +140,10 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
             launch_traversal<false>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, ctx->stream);
         }
         e = cudaGetLastError();
+      }
+      if (e == cudaSuccess && slot >= 0) {
+        e = cudaEventRecord(ctx->tev[2 * slot + 1], ctx->stream);
+        if (e == cudaSuccess) ctx->timed = slot + 1;
       }
     }
   }
