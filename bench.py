@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--profile-render", action="store_true",
                    help="small render cases for ncu: full frame 640x360 x 2 spp, adjoint 256x256 x 2 spp "
                         "forward + backward, 8 batched scenes x 2 spp")
+    p.add_argument("--profile-spectral", type=int, nargs=2, metavar=("W", "H"),
+                   help="Sampled64 case for ncu: config 2 (level 8) at W x H, one 2-spp frame")
     return p.parse_args()
 
 
@@ -446,8 +448,36 @@ def run_render_profile_case():
     print(json.dumps(out))
 
 
+def run_spectral_profile_case(res):
+    """One 2-spp frame of the full-frame scene in Sampled64 mode (render
+    setup, two graph-captured passes, the frame's toRGB)."""
+    import torch
+
+    from __graft_entry__ import build
+
+    build()
+    import woodenpbrengine_gb300 as W
+
+    g = W.SceneGen(2, 0, tuple(res), level=LEVEL)
+    ctx = W.Context(0)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_spectrum(W.SPECTRUM_SAMPLED64)
+    ctx.upload(g.desc)
+    ctx.build()
+    ctx.render_setup(2, seed=0)
+    ctx.render()
+    torch.cuda.synchronize()
+    ctx.check_device_errors()
+    ctx.close()
+    print(json.dumps({"profile_case": "Sampled64 config 2, %dx%d, 2 spp" % tuple(res)}))
+
+
 def main():
     args = parse()
+    if args.profile_spectral:
+        run_spectral_profile_case(args.profile_spectral)
+        return
     if args.profile_render:
         run_render_profile_case()
         return

@@ -36,6 +36,30 @@ WPBR_HD bool slab_test(V3 lo, V3 hi, V3 o, V3 inv, const int neg[3], float tmax_
   return (tMin < tmax_ray) && (tMax > 0.0f);
 }
 
+// slab_test without branches: all six plane distances, the same comparisons
+// in the same order folded into selects and one boolean, so the result (and
+// the entry distance when it is true) equals slab_test's for every input,
+// NaN included; a warp never diverges inside it.
+WPBR_HD bool slab_test_flat(V3 lo, V3 hi, V3 o, V3 inv, const int neg[3], float tmax_ray, float* tentry) {
+  float tMin = ((neg[0] ? hi.x : lo.x) - o.x) * inv.x;
+  float tMax = ((neg[0] ? lo.x : hi.x) - o.x) * inv.x;
+  float tyMin = ((neg[1] ? hi.y : lo.y) - o.y) * inv.y;
+  float tyMax = ((neg[1] ? lo.y : hi.y) - o.y) * inv.y;
+  float tzMin = ((neg[2] ? hi.z : lo.z) - o.z) * inv.z;
+  float tzMax = ((neg[2] ? lo.z : hi.z) - o.z) * inv.z;
+  tMax = tMax * kSlabScale;
+  tyMax = tyMax * kSlabScale;
+  tzMax = tzMax * kSlabScale;
+  bool ok = !(tMin > tyMax || tyMin > tMax);
+  tMin = (tyMin > tMin) ? tyMin : tMin;
+  tMax = (tyMax < tMax) ? tyMax : tMax;
+  ok = ok && !(tMin > tzMax || tzMin > tMax);
+  tMin = (tzMin > tMin) ? tzMin : tMin;
+  tMax = (tzMax < tMax) ? tzMax : tMax;
+  *tentry = tMin;
+  return ok && (tMin < tmax_ray) && (tMax > 0.0f);
+}
+
 // JobProcessTriangleInteractionRequests (WoodenPBREngine/CSTriangle.cpp:9-108):
 // watertight test in the reference's SIMD lane order. The edge functions come
 // out as (e2, e0, e1), the determinant is (e2 + e0) + e1 and 1/det is

@@ -122,10 +122,9 @@ __global__ void __launch_bounds__(kPersistBlock, WPBR_TRACE_MIN_BLOCKS) k_trace_
         float4 b0 = __ldg(&np_->b0), b1 = __ldg(&np_->b1), bz = __ldg(&np_->bz);
         int4 m = __ldg(&np_->meta);
         float t0, t1;
-        bool h0 = slab_test(V3{b0.x, b0.z, bz.x}, V3{b0.y, b0.w, bz.y}, o, inv, neg, tmax, &t0) &&
-                  !(t0 > tb * kPruneScale);
-        bool h1 = slab_test(V3{b1.x, b1.z, bz.z}, V3{b1.y, b1.w, bz.w}, o, inv, neg, tmax, &t1) &&
-                  !(t1 > tb * kPruneScale);
+        float tbs = tb * kPruneScale;
+        bool h0 = slab_test_flat(V3{b0.x, b0.z, bz.x}, V3{b0.y, b0.w, bz.y}, o, inv, neg, tmax, &t0) && !(t0 > tbs);
+        bool h1 = slab_test_flat(V3{b1.x, b1.z, bz.z}, V3{b1.y, b1.w, bz.w}, o, inv, neg, tmax, &t1) && !(t1 > tbs);
         uint32_t axis = ((uint32_t)m.w) >> 30;
         uint32_t c0n = (uint32_t)m.z, c1n = ((uint32_t)m.w) & 0x3FFFFFFFu;
         if (h0 && h1) {
