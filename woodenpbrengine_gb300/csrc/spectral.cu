@@ -7,8 +7,9 @@
 // persistent traversals (render.cu); k_sspawn (one thread per pixel) does
 // the scalar part of shading and sampling and records, per pixel, the
 // scalar factors every spectral term needs; k_sfinish gives each pixel a
-// half-warp, 16 lanes x 4 bins, for the per-bin Fresnel terms and products,
-// k_sfilm 8 lanes x 8 bins for the Mitchell film gather; k_sresolve
+// half-warp, 16 lanes x 4 bins, for the per-bin Fresnel terms and products;
+// k_sfilm stages 8x8-pixel tiles of sample spectra in shared memory for the
+// Mitchell film gather (4 threads x 16 bins per pixel); k_sresolve
 // converts the film to RGB once per frame (or before a film read). Every per-bin value is
 // computed with the same operations in the same order as the one-thread
 // restatement, so the film is bit-identical to it; sums over bins (toXYZ)
@@ -408,74 +409,115 @@ __global__ void __launch_bounds__(128) k_sfinish(PassCtx P, SpecCtx C, const flo
   st_bins(C.L + (size_t)pix * kSpecN + b0, L);
 }
 
-// Tile-clipped Mitchell gather of film_gather, 64 bins per sample, with 8
-// lanes per pixel and 8 bins per lane (the per-neighbour bookkeeping is
-// shared by 8 bins). The lanes of a pixel first evaluate the footprint test
-// and filter weight of the up to 25 neighbouring samples in parallel (lane
-// l: neighbours l, l + 8, l + 16, l + 24 in row-major order); the
-// accumulation then walks the neighbours in the reference's order,
-// broadcasting each weight.
-constexpr int kFilmLanes = 8;
-__global__ void __launch_bounds__(128) k_sfilm(uint32_t W, uint32_t H, const float2* pf, const float* L, float* acc,
-                                               float4* accw) {
-  uint32_t pix = (blockIdx.x * blockDim.x + threadIdx.x) / kFilmLanes;
-  if (pix >= W * H) return;  // the pixel's lanes leave together
-  uint32_t lane = threadIdx.x & 31u;
-  uint32_t gbase = lane & ~(uint32_t)(kFilmLanes - 1);
-  uint32_t gmask = 0xFFu << gbase;
-  uint32_t l8 = lane - gbase;
-  int b0 = 8 * (int)l8;
-  uint32_t x = pix % W, y = pix / W;
-  uint32_t tx0 = (x / 32) * 32, ty0 = (y / 32) * 32;
-  uint32_t tx1 = min(tx0 + 31, W - 1), ty1 = min(ty0 + 31, H - 1);
-  int sy0 = max((int)ty0, (int)y - 2), sy1 = min((int)ty1, (int)y + 2);
-  int sx0 = max((int)tx0, (int)x - 2), sx1 = min((int)tx1, (int)x + 2);
-  int nsx = sx1 - sx0 + 1, cnt = nsx * (sy1 - sy0 + 1);
-  float wk[4];
-  uint32_t vbits = 0;  // bit r: neighbour l8 + 8 r lies in the sample's clipped footprint
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    int k = (int)l8 + kFilmLanes * r;
-    wk[r] = 0.0f;
-    if (k < cnt) {
-      int sy = sy0 + k / nsx, sx = sx0 + k % nsx;
+// Tile-clipped Mitchell gather of film_gather, 64 bins per sample. A block
+// handles an 8x8 pixel tile (inside one 32x32 film tile): it stages the
+// 12x12 halo of sample spectra (those inside the film tile's clipped window)
+// in shared memory with asynchronous copies, computes the 64 x 25 neighbour
+// weights and footprint tests meanwhile, flags black samples, then each
+// pixel's 4 threads (16
+// bins each) walk the 25 neighbours in row-major order — the reference's
+// sample order within the clipped window — with invalid or black samples
+// predicated off, so the threads of a warp never diverge.
+constexpr int kFT = 8;                    // block tile side (pixels)
+constexpr int kHalo = kFT + 4;            // staged samples per side
+constexpr int kSStride = kSpecN + 4;      // floats per staged sample (float4-aligned, bank-skewed)
+constexpr int kFilmThreads = kFT * kFT * 4;
+constexpr int kFilmBins = kSpecN / 4;
+__global__ void __launch_bounds__(kFilmThreads, 4) k_sfilm(uint32_t W, uint32_t H, const float2* pf, const float* L,
+                                                        float* acc, float4* accw) {
+  __shared__ __align__(16) float S[kHalo * kHalo * kSStride];
+  __shared__ float wt[kFT * kFT * 25];
+  __shared__ uint32_t vmask[kFT * kFT];
+  __shared__ uint8_t black[kHalo * kHalo];
+  const int tid = (int)threadIdx.x;
+  const int bx0 = (int)blockIdx.x * kFT, by0 = (int)blockIdx.y * kFT;
+  const int tx0 = (bx0 / 32) * 32, ty0 = (by0 / 32) * 32;
+  const int tx1 = min(tx0 + 31, (int)W - 1), ty1 = min(ty0 + 31, (int)H - 1);
+  // halo spectra: asynchronous 16-byte global-to-shared copies (cp.async),
+  // zero-filled outside the film tile's clipped window; they land while the
+  // weights are computed
+  for (int i = tid; i < kHalo * kHalo * 16; i += kFilmThreads) {
+    int h = i / 16, c = i % 16;
+    int sy = by0 - 2 + h / kHalo, sx = bx0 - 2 + h % kHalo;
+    bool in = sy >= ty0 && sy <= ty1 && sx >= tx0 && sx <= tx1;
+    const float* src = in ? L + ((size_t)sy * W + sx) * kSpecN + 4 * c : L;
+    uint32_t dst = (uint32_t)__cvta_generic_to_shared(S + h * kSStride + 4 * c);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(in ? 16 : 0) : "memory");
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  if (tid < kFT * kFT) vmask[tid] = 0u;
+  __syncthreads();
+  // neighbour weights: entry p * 25 + k is neighbour k (row-major in the 5x5 window) of pixel p
+  for (int e = tid; e < kFT * kFT * 25; e += kFilmThreads) {
+    int p = e / 25, k = e % 25;
+    int x = bx0 + p % kFT, y = by0 + p / kFT;
+    int sx = x - 2 + k % 5, sy = y - 2 + k / 5;
+    float w = 0.0f;
+    if (x < (int)W && y < (int)H && sx >= tx0 && sx <= tx1 && sy >= ty0 && sy <= ty1) {
       float2 f = pf[(size_t)sy * W + sx];
       float dx0 = f.x - 0.5f, dy0 = f.y - 0.5f;
       int pminx = (int)ceilf(dx0 - 2.0f), pmaxx = (int)floorf(dx0 + 2.0f);
       int pminy = (int)ceilf(dy0 - 2.0f), pmaxy = (int)floorf(dy0 + 2.0f);
-      pminx = max(pminx, (int)tx0);
-      pminy = max(pminy, (int)ty0);
-      pmaxx = min(pmaxx, (int)tx1);
-      pmaxy = min(pmaxy, (int)ty1);
-      if (!((int)x < pminx || (int)x > pmaxx || (int)y < pminy || (int)y > pmaxy)) {
-        vbits |= 1u << r;
-        wk[r] = mitchell1(((float)x - f.x) / 2.0f) * mitchell1(((float)y - f.y) / 2.0f);
+      pminx = max(pminx, tx0);
+      pminy = max(pminy, ty0);
+      pmaxx = min(pmaxx, tx1);
+      pmaxy = min(pmaxy, ty1);
+      if (!(x < pminx || x > pmaxx || y < pminy || y > pmaxy)) {
+        w = mitchell1(((float)x - f.x) / 2.0f) * mitchell1(((float)y - f.y) / 2.0f);
+        atomicOr(&vmask[p], 1u << k);
       }
     }
+    wt[e] = w;
   }
-  float* ap = acc + (size_t)pix * kSpecN + b0;
-  Bins4 a0 = ld_bins(ap), a1 = ld_bins(ap + 4);
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncthreads();
+  // each sample's black flag, 16 threads (a half-warp) per sample
+  for (int i = tid; i < kHalo * kHalo * 16; i += kFilmThreads) {
+    int h = i / 16, c = i % 16;
+    float4 v = *reinterpret_cast<const float4*>(S + h * kSStride + 4 * c);
+    bool nz = v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f;
+    uint32_t bal = __ballot_sync(0xFFFFFFFFu, nz);
+    if (c == 0) black[h] = ((bal >> (threadIdx.x & 16u)) & 0xFFFFu) == 0u;
+  }
+  __syncthreads();
+  const int p = tid / 4, q = tid % 4;
+  const int lx = p % kFT, ly = p / kFT;
+  const int x = bx0 + lx, y = by0 + ly;
+  if (x >= (int)W || y >= (int)H) return;
+  const size_t pix = (size_t)y * W + x;
+  float* ap = acc + pix * kSpecN + kFilmBins * q;
+  float a[kFilmBins];
+#pragma unroll
+  for (int j = 0; j < kFilmBins / 4; ++j) {
+    float4 t = *reinterpret_cast<const float4*>(ap + 4 * j);
+    a[4 * j] = t.x; a[4 * j + 1] = t.y; a[4 * j + 2] = t.z; a[4 * j + 3] = t.w;
+  }
   float ws = accw[pix].w;
-  int k = 0;
-  for (int sy = sy0; sy <= sy1; ++sy)
-    for (int sx = sx0; sx <= sx1; ++sx, ++k) {
-      uint32_t src = gbase | (uint32_t)(k & (kFilmLanes - 1));
-      int r = k / kFilmLanes;
-      float mine = r == 0 ? wk[0] : r == 1 ? wk[1] : r == 2 ? wk[2] : wk[3];
-      float w = __shfl_sync(gmask, mine, src);
-      uint32_t vb = __shfl_sync(gmask, vbits, src);
-      if (!((vb >> r) & 1u)) continue;
-      const float* sp = L + ((size_t)sy * W + sx) * kSpecN + b0;
-      Bins4 s0 = ld_bins(sp), s1 = ld_bins(sp + 4);
-      if (__ballot_sync(gmask, bins_nonzero(s0) || bins_nonzero(s1)) & gmask) {
-        for (int j = 0; j < 4; ++j) a0.v[j] = a0.v[j] + s0.v[j] * w;
-        for (int j = 0; j < 4; ++j) a1.v[j] = a1.v[j] + s1.v[j] * w;
-      }
-      ws = ws + w;
+  const uint32_t vm = vmask[p];
+  const float* base = S + (ly * kHalo + lx) * kSStride + kFilmBins * q;
+  const uint8_t* bl = black + ly * kHalo + lx;
+  const float* wp = wt + p * 25;
+#pragma unroll
+  for (int k = 0; k < 25; ++k) {
+    const int off = (k / 5) * kHalo + k % 5;
+    const bool v = (vm >> k) & 1u;
+    const float w = wp[k];
+    const bool take = v && !bl[off];
+    const float* sp = base + off * kSStride;
+#pragma unroll
+    for (int j = 0; j < kFilmBins / 4; ++j) {
+      float4 t = *reinterpret_cast<const float4*>(sp + 4 * j);
+      a[4 * j] = take ? a[4 * j] + t.x * w : a[4 * j];
+      a[4 * j + 1] = take ? a[4 * j + 1] + t.y * w : a[4 * j + 1];
+      a[4 * j + 2] = take ? a[4 * j + 2] + t.z * w : a[4 * j + 2];
+      a[4 * j + 3] = take ? a[4 * j + 3] + t.w * w : a[4 * j + 3];
     }
-  st_bins(ap, a0);
-  st_bins(ap + 4, a1);
-  if (l8 == 0) accw[pix].w = ws;
+    ws = v ? ws + w : ws;
+  }
+#pragma unroll
+  for (int j = 0; j < kFilmBins / 4; ++j)
+    *reinterpret_cast<float4*>(ap + 4 * j) = make_float4(a[4 * j], a[4 * j + 1], a[4 * j + 2], a[4 * j + 3]);
+  if (q == 0) accw[pix].w = ws;
 }
 
 // toRGB of the accumulated spectra (s64_to_rgb: per bin products, the three
@@ -584,7 +626,8 @@ cudaError_t spectral_finish_launch(wpbr_ctx* ctx) {
   SpecCtx C{(const SpecMat*)R.spec_mats.p, (const S64*)R.spec_le.p, R.spec_L.p};
   k_sfinish<<<div_up((uint64_t)n * kBinLanes, 128), 128, 0, ctx->stream>>>(spec_pass_ctx(ctx), C, R.pstate.p,
                                                                             R.shadow_hit.p);
-  k_sfilm<<<div_up((uint64_t)n * kFilmLanes, 128), 128, 0, ctx->stream>>>(R.W, R.H, R.pfilm.p, R.spec_L.p, R.spec_acc.p, (float4*)R.acc.p);
+  dim3 fg(div_up(R.W, kFT), div_up(R.H, kFT));
+  k_sfilm<<<fg, kFilmThreads, 0, ctx->stream>>>(R.W, R.H, R.pfilm.p, R.spec_L.p, R.spec_acc.p, (float4*)R.acc.p);
   return cudaGetLastError();
 }
 
