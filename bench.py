@@ -623,6 +623,13 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu, _ = cpu_trace_rate(g.desc, rays, args.cpu_seconds)
+        # the same restatement on one core (a smaller contiguous sample)
+        cores = cpu["cores"]
+        one, _ = cpu_trace_rate(g.desc, rays, args.cpu_seconds / 4, threads=1)
+        from oracle import binding as _O
+
+        _O.lib().orc_set_threads(cores)
+        cpu["single_core"] = {"value": one["value"], "unit": "Mrays/s", "sample": one["sample"]}
 
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,

@@ -205,15 +205,15 @@ WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
   R.acc.release(); R.hit_prim.release(); R.shadow_rays.release(); R.shadow_hit.release(); R.pstate.release();
   R.Lbuf.release(); R.pfilm.release(); R.pass_dev.release(); R.counters.release();
   R.spec_mats.release(); R.spec_le.release(); R.spec_L.release(); R.spec_acc.release();
-  ctx->io_rays.release(); ctx->io_hits.release(); ctx->io_stats.release(); ctx->trace_counter.release();
+  ctx->io_rays.release(); ctx->io_hits.release(); ctx->io_stats.release();
+  ctx->tscr[0].release(); ctx->tscr[1].release();
   for (cudaEvent_t& ev : ctx->io_ev)
     if (ev) cudaEventDestroy(ev);
   for (cudaEvent_t& ev : ctx->tev)
     if (ev) cudaEventDestroy(ev);
   if (ctx->io_h2d) cudaStreamDestroy(ctx->io_h2d);
+  if (ctx->io_comp) cudaStreamDestroy(ctx->io_comp);
   if (ctx->io_d2h) cudaStreamDestroy(ctx->io_d2h);
-  ctx->rs_k0.release(); ctx->rs_v0.release(); ctx->rs_k1.release(); ctx->rs_v1.release();
-  ctx->rs_hist.release(); ctx->rs_scan.release();
   for (auto& f : R.f) f.release();
   for (auto& u : R.u) u.release();
   ctx->adj.release();
@@ -545,44 +545,52 @@ WPBR_API wpbr_status wpbr_collide_device(wpbr_ctx* ctx, const void* d_rays, uint
 }
 
 // Batches of at least kPipeMin rays are collided in up to kPipeChunks
-// chunks (of at least kPipeMinChunk rays) whose copies overlap the
-// traversal of their neighbours. Each chunk adds its own ray-order sort and
-// traversal tail (about 0.25 ms at 2M rays), so a few large chunks beat many
-// small ones: measured on 8.4M rays with 210 / 190 GB/s host copies, 7.35 ms
-// serial, 6.7 ms in 2 or 4 chunks, 7.7 ms in 8.
+// chunks (of at least kPipeMinChunk rays): rays go up on one copy stream,
+// hits come down on another, and the chunks are traced alternately on the
+// context's stream and a second traversal stream (each with its own
+// scratch), so one chunk's copies overlap its neighbours' traversal and the
+// tail of one traversal overlaps the start of the next. Measured on 8.4M
+// rays with 210 / 190 GB/s host copies: 7.35 ms serial, 6.72 ms in four
+// chunks on one traversal stream.
 constexpr uint64_t kPipeMin = 1ull << 22, kPipeMinChunk = 1ull << 21;
 constexpr uint64_t kPipeChunks = 4;
 
 static wpbr_status collide_pipelined(wpbr_ctx* ctx, const float* rays, uint64_t n, float* hits, uint32_t mode) {
   if (!ctx->io_h2d) WPBR_CUDA(cudaStreamCreateWithFlags(&ctx->io_h2d, cudaStreamNonBlocking));
   if (!ctx->io_d2h) WPBR_CUDA(cudaStreamCreateWithFlags(&ctx->io_d2h, cudaStreamNonBlocking));
+  if (!ctx->io_comp) WPBR_CUDA(cudaStreamCreateWithFlags(&ctx->io_comp, cudaStreamNonBlocking));
   for (cudaEvent_t& ev : ctx->io_ev)
     if (!ev) WPBR_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   cudaStream_t st = ctx->stream;
+  cudaStream_t comp[2] = {st, ctx->io_comp};
   uint64_t k = (n + kPipeMinChunk - 1) / kPipeMinChunk;
   if (k > kPipeChunks) k = kPipeChunks;
   uint64_t chunk = (n + k - 1) / k;
-  // the staging buffers are reused only after the work already queued on
-  // the context's stream
+  // everything starts after the work already queued on the context's stream
   WPBR_CUDA(cudaEventRecord(ctx->io_ev[2], st));
   WPBR_CUDA(cudaStreamWaitEvent(ctx->io_h2d, ctx->io_ev[2], 0));
-  for (uint64_t off = 0; off < n; off += chunk) {
+  WPBR_CUDA(cudaStreamWaitEvent(ctx->io_comp, ctx->io_ev[2], 0));
+  int i = 0;
+  wpbr_status s = WPBR_OK;
+  for (uint64_t off = 0; off < n && s == WPBR_OK; off += chunk, ++i) {
     uint64_t c = n - off < chunk ? n - off : chunk;
+    cudaStream_t cs = comp[i & 1];
     WPBR_CUDA(cudaMemcpyAsync(ctx->io_rays.p + 2 * off, rays + 8 * off, 32 * c, cudaMemcpyHostToDevice, ctx->io_h2d));
     WPBR_CUDA(cudaEventRecord(ctx->io_ev[0], ctx->io_h2d));
-    WPBR_CUDA(cudaStreamWaitEvent(st, ctx->io_ev[0], 0));
-    wpbr_status s = trace_rays(ctx, ctx->io_rays.p + 2 * off, c, ctx->io_hits.p + off, mode, nullptr);
-    if (s != WPBR_OK) {
-      cudaStreamSynchronize(ctx->io_h2d);
-      cudaStreamSynchronize(ctx->io_d2h);
-      return s;
-    }
-    WPBR_CUDA(cudaEventRecord(ctx->io_ev[1], st));
+    WPBR_CUDA(cudaStreamWaitEvent(cs, ctx->io_ev[0], 0));
+    s = trace_rays(ctx, ctx->io_rays.p + 2 * off, c, ctx->io_hits.p + off, mode, nullptr, i & 1, cs);
+    if (s != WPBR_OK) break;
+    WPBR_CUDA(cudaEventRecord(ctx->io_ev[1], cs));
     WPBR_CUDA(cudaStreamWaitEvent(ctx->io_d2h, ctx->io_ev[1], 0));
     WPBR_CUDA(cudaMemcpyAsync(hits + 4 * off, ctx->io_hits.p + off, 16 * c, cudaMemcpyDeviceToHost, ctx->io_d2h));
   }
-  WPBR_CUDA(cudaStreamSynchronize(ctx->io_d2h));
-  WPBR_CUDA(cudaStreamSynchronize(st));
+  cudaError_t e1 = cudaStreamSynchronize(ctx->io_h2d);
+  cudaError_t e2 = cudaStreamSynchronize(ctx->io_comp);
+  cudaError_t e3 = cudaStreamSynchronize(ctx->io_d2h);
+  cudaError_t e4 = cudaStreamSynchronize(st);
+  if (s != WPBR_OK) return s;
+  for (cudaError_t e : {e1, e2, e3, e4})
+    if (e != cudaSuccess) return cuda_err(ctx, e, "collide");
   return WPBR_OK;
 }
 

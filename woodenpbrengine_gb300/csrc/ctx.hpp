@@ -178,10 +178,19 @@ struct wpbr_ctx {
   bool kernel_timing = false;
   int timed = 0;  // event pairs recorded since the last wpbr_kernel_timing
   cudaEvent_t tev[2 * kTimedMax] = {};
-  wpbr::DevBuf<uint32_t> trace_counter;  // ray-fetch counters of the persistent traversal
-  // ray reordering of large collide batches (keys, permutation, radix scratch)
+  // per-collide scratch: the persistent traversal's ray-fetch counter and the
+  // ray reordering of large batches (keys, permutation, radix scratch). Set 1
+  // belongs to io_comp, the second traversal stream of the chunked host
+  // collide, so two chunks can be traced at once.
+  struct TraceScratch {
+    wpbr::DevBuf<uint32_t> counter, k0, v0, k1, v1, hist, scan;
+    void release() {
+      counter.release(); k0.release(); v0.release(); k1.release(); v1.release(); hist.release(); scan.release();
+    }
+  };
+  TraceScratch tscr[2];
+  cudaStream_t io_comp = nullptr;
   uint32_t ray_sort = 8;  // bits per axis of the origin grid (0: input order)
-  wpbr::DevBuf<uint32_t> rs_k0, rs_v0, rs_k1, rs_v1, rs_hist, rs_scan;
 };
 
 namespace wpbr {
@@ -199,8 +208,9 @@ wpbr_status bvh_build(wpbr_ctx* ctx);
 cudaError_t radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t n, int bits,
                              DevBuf<uint32_t>& hist, DevBuf<uint32_t>& scan_tmp, cudaStream_t st, uint32_t** kres,
                              uint32_t** vres);
+// Traces on `stream` (the context's when null) with scratch set `scratch`.
 wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* d_hits, uint32_t mode,
-                       uint32_t* d_stats);
+                       uint32_t* d_stats, int scratch = 0, cudaStream_t stream = nullptr);
 wpbr_status env_preprocess(wpbr_ctx* ctx);
 // Distribution2D of an environment image (JobLightInfiniteAreaPreprocessSampling)
 // into caller-owned arrays: cond_func/cond_cdf/cond_int of H rows of W, marg_* of H.

@@ -77,7 +77,9 @@ uint32_t trace_launches(const wpbr_ctx* ctx, uint64_t n, bool stats) {
 }
 
 wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* d_hits, uint32_t mode,
-                       uint32_t* d_stats) {
+                       uint32_t* d_stats, int scratch, cudaStream_t stream) {
+  cudaStream_t st = stream ? stream : ctx->stream;
+  wpbr_ctx::TraceScratch& X = ctx->tscr[scratch];
   if (!ctx->bvh.built) return set_err(ctx, WPBR_ERR_NOT_BUILT, "collide: BVH not built");
   if (ctx->bvh.view.max_depth >= 250) return set_err(ctx, WPBR_ERR_TRAVERSAL_LIMIT, "collide: BVH deeper than 250");
   if (n == 0) return WPBR_OK;
@@ -85,20 +87,20 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
   const BvhView Bv = traversal_view(ctx);
   cudaError_t e;
   if (d_stats) {
-    e = (mode == WPBR_TRACE_ANY) ? launch<true, true>(S, Bv, d_rays, n, d_hits, d_stats, ctx->d_err.p, ctx->stream)
-                                 : launch<false, true>(S, Bv, d_rays, n, d_hits, d_stats, ctx->d_err.p, ctx->stream);
+    e = (mode == WPBR_TRACE_ANY) ? launch<true, true>(S, Bv, d_rays, n, d_hits, d_stats, ctx->d_err.p, st)
+                                 : launch<false, true>(S, Bv, d_rays, n, d_hits, d_stats, ctx->d_err.p, st);
   } else {
     if (n >= 0xFFFFFFFFull) return set_err(ctx, WPBR_ERR_INVALID_ARG, "collide: more than 2^32-1 rays per call");
-    e = ctx->trace_counter.ensure(4);
+    e = X.counter.ensure(4);
     if (e == cudaSuccess) {
-      uint32_t* c = ctx->trace_counter.p;
-      e = cudaMemsetAsync(c, 0, sizeof(uint32_t), ctx->stream);
+      uint32_t* c = X.counter.p;
+      e = cudaMemsetAsync(c, 0, sizeof(uint32_t), st);
       // large batches are traced in the order of their origins' Morton cells:
       // neighbouring rays of a warp then share nodes (hits are per ray, so the
       // order does not change them)
       const uint32_t* perm = nullptr;
       if (e == cudaSuccess && ctx->ray_sort && n >= kRaySortMin && !Bv.empty) {
-        for (DevBuf<uint32_t>* b : {&ctx->rs_k0, &ctx->rs_v0, &ctx->rs_k1, &ctx->rs_v1})
+        for (DevBuf<uint32_t>* b : {&X.k0, &X.v0, &X.k1, &X.v1})
           if (e == cudaSuccess) e = b->ensure(n);
         if (e == cudaSuccess) {
           float3 lo = make_float3(Bv.root_lo[0], Bv.root_lo[1], Bv.root_lo[2]);
@@ -107,11 +109,11 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
           float cells = (float)(1u << b);
           float3 sc = make_float3(ex[0] > 0.0f ? cells / ex[0] : 0.0f, ex[1] > 0.0f ? cells / ex[1] : 0.0f,
                                   ex[2] > 0.0f ? cells / ex[2] : 0.0f);
-          k_ray_keys<<<div_up(n, 256), 256, 0, ctx->stream>>>(d_rays, (uint32_t)n, lo, sc, 1u << b, ctx->rs_k0.p,
-                                                              ctx->rs_v0.p);
+          k_ray_keys<<<div_up(n, 256), 256, 0, st>>>(d_rays, (uint32_t)n, lo, sc, 1u << b, X.k0.p,
+                                                              X.v0.p);
           uint32_t *kr = nullptr, *vr = nullptr;
-          e = radix_sort_pairs(ctx->rs_k0.p, ctx->rs_v0.p, ctx->rs_k1.p, ctx->rs_v1.p, (uint32_t)n, 3 * (int)b,
-                               ctx->rs_hist, ctx->rs_scan, ctx->stream, &kr, &vr);
+          e = radix_sort_pairs(X.k0.p, X.v0.p, X.k1.p, X.v1.p, (uint32_t)n, 3 * (int)b,
+                               X.hist, X.scan, st, &kr, &vr);
           perm = vr;
         }
       }
@@ -121,28 +123,28 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
         slot = ctx->timed;
         for (int k = 0; k < 2 && e == cudaSuccess; ++k)
           if (!ctx->tev[2 * slot + k]) e = cudaEventCreate(&ctx->tev[2 * slot + k]);
-        if (e == cudaSuccess) e = cudaEventRecord(ctx->tev[2 * slot], ctx->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->tev[2 * slot], st);
       }
       if (e == cudaSuccess) {
         if (perm) {
           PermSrc src{d_rays, perm};
           PermHitSink4 sink{d_hits, perm};
           if (mode == WPBR_TRACE_ANY)
-            launch_traversal<true>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, ctx->stream);
+            launch_traversal<true>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, st);
           else
-            launch_traversal<false>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, ctx->stream);
+            launch_traversal<false>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, st);
         } else {
           BufferSrc src{d_rays};
           HitSink4 sink{d_hits};
           if (mode == WPBR_TRACE_ANY)
-            launch_traversal<true>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, ctx->stream);
+            launch_traversal<true>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, st);
           else
-            launch_traversal<false>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, ctx->stream);
+            launch_traversal<false>(S, Bv, src, sink, (uint32_t)n, c, ctx->d_err.p, st);
         }
         e = cudaGetLastError();
       }
       if (e == cudaSuccess && slot >= 0) {
-        e = cudaEventRecord(ctx->tev[2 * slot + 1], ctx->stream);
+        e = cudaEventRecord(ctx->tev[2 * slot + 1], st);
         if (e == cudaSuccess) ctx->timed = slot + 1;
       }
     }
