@@ -19,9 +19,12 @@ namespace wpbr {
 
 constexpr int kEnd = (int)0x80000000;  // no node (empty stack)
 constexpr int kPersistBlock = 128;
-#ifndef WPBR_TRACE_MIN_BLOCKS
-#define WPBR_TRACE_MIN_BLOCKS 8
-#endif
+// Resident blocks per SM each traversal instantiation is compiled for
+// (Sink::kMinBlocks): the collide kernels (full hit records) run best at 10
+// (48 registers, some spilled; 1.4% faster than 8 on the 8.4M-ray
+// microbenchmark, 11-12 the same, 14 19% slower); the render passes' kernels
+// (camera rays generated in the source, prim-id sinks) at 8 (64 registers),
+// where 10 cost them 5%.
 
 // Ray data the warp's lanes read when they test primitives for another lane.
 struct SharedRay {
@@ -31,7 +34,7 @@ struct SharedRay {
 };
 
 template <bool ANY, int STACK, class Src, class Sink>
-__global__ void __launch_bounds__(kPersistBlock, WPBR_TRACE_MIN_BLOCKS) k_trace_persistent(SceneView S, BvhView Bv,
+__global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persistent(SceneView S, BvhView Bv,
                                                                                            Src src, Sink sink,
                                                                     uint32_t n, uint32_t* counter, uint32_t* err) {
   __shared__ SharedRay s_ray[kPersistBlock / 32][32];
@@ -529,6 +532,7 @@ struct BufferSrc {
   }
 };
 struct HitSink4 {
+  static constexpr int kMinBlocks = 10;
   float4* hits;
   __device__ __forceinline__ void store(uint32_t i, const HitRec& h) const {
     hits[i] = make_float4(h.t, __uint_as_float(h.prim), h.b1, h.b2);
@@ -546,6 +550,7 @@ struct PermSrc {
   }
 };
 struct PermHitSink4 {
+  static constexpr int kMinBlocks = 10;
   float4* hits;
   const uint32_t* perm;
   __device__ __forceinline__ void store(uint32_t i, const HitRec& h) const {
@@ -553,6 +558,7 @@ struct PermHitSink4 {
   }
 };
 struct PrimSink {
+  static constexpr int kMinBlocks = 8;
   uint32_t* prims;
   __device__ __forceinline__ void store(uint32_t i, const HitRec& h) const { prims[i] = h.prim; }
 };
