@@ -62,7 +62,7 @@ struct MatGrad {
 __device__ __forceinline__ bool finite3(RGB3 c) { return isfinite(c.r) && isfinite(c.g) && isfinite(c.b); }
 
 // ---- sample generation with the sampling parameters --------------------------
-__global__ void __launch_bounds__(kTB) k_adj_spawn(PassCtx P, AdjView A, const uint32_t* pass_dev,
+__global__ void __launch_bounds__(kTB, WPBR_ADJ_SPAWN_MIN_BLOCKS) k_adj_spawn(PassCtx P, AdjView A, const uint32_t* pass_dev,
                                                    const uint32_t* hit_prim, float4* state, float4* rays, float2* pf) {
   uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= P.W * P.H) return;
@@ -406,7 +406,7 @@ __device__ RGB3 film_adjoint(uint32_t W, uint32_t H, uint32_t pix, float2 f, con
 }
 
 // Backward: replayed sample, film adjoint, reverse sweep.
-__global__ void __launch_bounds__(kTB) k_adj_back(PassCtx P, AdjView A, const float4* state, const uint32_t* shadow,
+__global__ void __launch_bounds__(kTB, WPBR_ADJ_BACK_MIN_BLOCKS) k_adj_back(PassCtx P, AdjView A, const float4* state, const uint32_t* shadow,
                                                   const float2* pf, AdjGrad G) {
   extern __shared__ float smem[];
   __shared__ double zsum[kTB / 32];

@@ -347,9 +347,14 @@ WPBR_API wpbr_status wpbr_scene_upload(wpbr_ctx* ctx, const wpbr_scene_desc* d) 
   if (d->n_spheres + (uint64_t)d->n_triangles >= (1ull << 29))
     return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: more than 2^29 primitives");
   if (d->n_textures && !d->textures) return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: textures pointer is null");
-  for (uint32_t i = 0; i < d->n_textures; ++i)
+  uint64_t texels = 0;
+  for (uint32_t i = 0; i < d->n_textures; ++i) {
     if (d->textures[i].width < 4 || d->textures[i].height < 4 || !d->textures[i].rgb)
       return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: textures must be at least 4x4");
+    texels += 2 * (uint64_t)d->textures[i].width * d->textures[i].height;  // bound on the pyramid
+  }
+  if (texels >= (1ull << 31))
+    return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: more than 2^30 texels of textures");
   bool has_metal = false;
   for (uint32_t m = 0; m < d->n_materials; ++m) {
     const wpbr_material& mt = d->materials[m];

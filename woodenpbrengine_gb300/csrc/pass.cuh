@@ -15,6 +15,24 @@ namespace wpbr {
 namespace {
 
 constexpr int kTB = 128;
+// Resident blocks per SM of the spawn kernels (surface interaction and
+// sampling, 127 registers unbounded): the light and environment sampling is
+// a chain of dependent loads (CDF searches), so occupancy pays even with
+// spills. 1080p full frame, RGB / Sampled64 Msamples/s: unbounded 1093 /
+// 621, 8 blocks 1188 / 649, 12 blocks (40 registers) 1229 / 667, 14 blocks
+// 1246 / 677 but the 256x256 frame 4% slower.
+#ifndef WPBR_SPAWN_MIN_BLOCKS
+#define WPBR_SPAWN_MIN_BLOCKS 12
+#endif
+// The differentiable estimator's spawn: forward 4.06 -> 3.84 ms at 12 blocks
+// (512x512 x 16 spp).
+#ifndef WPBR_ADJ_SPAWN_MIN_BLOCKS
+#define WPBR_ADJ_SPAWN_MIN_BLOCKS 12
+#endif
+// ... and its reverse sweep: backward 5.63 -> 5.19 ms at 12 blocks (8: 5.43).
+#ifndef WPBR_ADJ_BACK_MIN_BLOCKS
+#define WPBR_ADJ_BACK_MIN_BLOCKS 12
+#endif
 
 struct PassCtx {
   SceneView S;

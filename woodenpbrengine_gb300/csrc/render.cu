@@ -252,7 +252,7 @@ __global__ void k_film(uint32_t W, uint32_t H, const float2* pf, const float4* L
 constexpr int kStateF4 = kPassStateF4;
 enum : uint32_t { SF_VALID = 1u, SF_TRACE_L = 2u, SF_TRACE_B = 4u, SF_HIT = 8u, SF_METAL = 16u };
 
-__global__ void __launch_bounds__(kTB) k_spawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
+__global__ void __launch_bounds__(kTB, WPBR_SPAWN_MIN_BLOCKS) k_spawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
                                                float4* state, float4* rays, float4* Lb, float2* pf) {
   uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= P.W * P.H) return;

@@ -134,7 +134,7 @@ __device__ __forceinline__ FScalars f_scalars(const wpbr_material& m, float d_wh
   return F;
 }
 
-__global__ void __launch_bounds__(kTB) k_sspawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
+__global__ void __launch_bounds__(kTB, WPBR_SPAWN_MIN_BLOCKS) k_sspawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
                                                 float4* state, float4* rays, float2* pf) {
   uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= P.W * P.H) return;
