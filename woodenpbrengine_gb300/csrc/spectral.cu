@@ -347,7 +347,10 @@ __device__ __forceinline__ Bins4 bins_f(bool cond, bool zero, float c, float kf,
   return f;
 }
 
-__global__ void __launch_bounds__(128) k_sfinish(PassCtx P, SpecCtx C, const float4* state, const uint32_t* shadow) {
+// 12 resident blocks per SM (40 registers): 1080p Sampled64 669 -> 682
+// Msamples/s against the unbounded 64 registers (16 blocks: 675).
+__global__ void __launch_bounds__(128, 12) k_sfinish(PassCtx P, SpecCtx C, const float4* state,
+                                                     const uint32_t* shadow) {
   uint32_t pix = (blockIdx.x * blockDim.x + threadIdx.x) / kBinLanes;
   if (pix >= P.W * P.H) return;  // the whole half-warp leaves together
   uint32_t lane = threadIdx.x & 31u;
