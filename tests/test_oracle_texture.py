@@ -141,3 +141,11 @@ def test_isotropic_sampler_blurs_with_width(O):
     # width 2w: below one texel of level 0 -> level 0; 6/128 -> between levels 0 and 1
     assert abs(vals[0] - 0.5) > abs(vals[1] - 0.5) > abs(vals[2] - 0.5)
     assert abs(vals[2] - 0.5) < 0.05
+
+
+def test_nan_footprint_gives_nan_without_touching_texels(O):
+    t = np.random.default_rng(3).random((32, 32, 3), dtype=np.float32)
+    nan = float("nan")
+    for fp in [(0.5, 0.5, nan, 0.01, 0.02, 0.0), (nan, 0.5, 0.01, 0.0, 0.0, 0.01), (0.5, 0.5, nan, nan, nan, nan)]:
+        v = O.texture_eval(t, fp)
+        assert np.all(np.isnan(v)), (fp, v)

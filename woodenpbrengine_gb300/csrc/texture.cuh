@@ -87,6 +87,11 @@ WPBR_HD RGB3 tex_ewa(const TexView& T, const TexInfo& ti, const TexFootprint& fp
   float s1f = clampf(sx + us, 0.0f, rx - 1.0f), t1f = clampf(sy + vs, 0.0f, ry - 1.0f);
   int is0 = (int)ceilf(s0f), it0 = (int)ceilf(t0f);
   int is1 = (int)floorf(s1f), it1 = (int)floorf(t1f);
+  // a NaN footprint (from a NaN hit frame): no texel is visited, 0 / 0
+  if (!(s0f == s0f && t0f == t0f && s1f == s1f && t1f == t1f)) {
+    is0 = it0 = 1;
+    is1 = it1 = 0;
+  }
   RGB3 sum = rgb1(0.0f);
   float sw = 0.0f;
   for (int it = it0; it <= it1; ++it) {
