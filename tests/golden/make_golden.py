@@ -30,6 +30,19 @@ def compute(W, O):
     out["c1_sorted_prims"] = e1["sorted_prims"]
     out["c1_nodes"] = e1["nodes"]
     out["c1_hits"] = o1.trace(g1.rays(), mode=0)
+    # textured metal (scene config 5) and the Sampled64 film
+    g5 = W.SceneGen(5, 0, (24, 16))
+    o5 = O.OracleScene(g5.desc)
+    out["c5_film_L"], out["c5_film_w"] = o5.render(24, 16, 2)
+    out["c0_spectral_L"], _ = o0.render_spectral(32, 32, 1, 0, 0)
+    # MIP pyramid and both texture samplers on a small odd-sized texture
+    rng = np.random.default_rng(9)
+    tex = rng.random((12, 20, 3), dtype=np.float32)
+    for i, lv in enumerate(O.texture_levels(tex)):
+        out["tex_level%d" % i] = lv
+    fps = np.concatenate([rng.uniform(0.0, 1.0, (16, 2)), rng.normal(0.0, 0.05, (16, 4))], axis=1)
+    out["tex_aniso"] = np.stack([O.texture_eval(tex, fp) for fp in fps])
+    out["tex_iso"] = np.stack([O.texture_eval(tex, fp, isotropic=True) for fp in fps])
     return out
 
 
