@@ -114,3 +114,70 @@ def test_host_runner_renders_obj_with_environment(W, host, tmp_path):
     assert out.returncode == 0, out.stderr
     I = _read_pfm(str(tmp_path / "o.pfm"))
     assert np.isfinite(I).all() and I.max() > 0.0
+
+
+def test_obj_textured_metal_ingestion(W, host, tmp_path):
+    pos, idx = _mesh(W)
+    uv = np.stack([pos[:, 0] * 0.5 + 0.5, pos[:, 1] * 0.5 + 0.5], 1)
+    rng = np.random.default_rng(1)
+    k, r = str(tmp_path / "k.pfm"), str(tmp_path / "r.pfm")
+    _write_pfm(k, rng.uniform(0.2, 3.0, (16, 16, 3)).astype(np.float32))
+    _write_pfm(r, rng.uniform(0.0, 0.01, (8, 8, 3)).astype(np.float32))
+    obj = str(tmp_path / "m.obj")
+    _write_obj(obj, pos, idx, uv=uv)
+    out = subprocess.run([host, "--obj", obj, "--metal", k, r, "--dump-scene"], capture_output=True, text=True,
+                         timeout=60)
+    assert out.returncode == 0, out.stderr
+    assert json.loads(out.stdout)["textures"] == 2
+    plain = str(tmp_path / "p.obj")
+    _write_obj(plain, pos, idx)  # no texture coordinates
+    bad = subprocess.run([host, "--obj", plain, "--metal", k, r, "--dump-scene"], capture_output=True, text=True,
+                         timeout=60)
+    assert bad.returncode == 2 and "texture coordinates" in bad.stderr
+    both = subprocess.run([host, "--config", "0", "--staged", "--spectral"], capture_output=True, text=True,
+                          timeout=60)
+    assert both.returncode == 2
+
+
+@pytest.mark.gpu
+def test_host_runner_sampled64_textured_matches_binding(W, ctx, host, tmp_path):
+    Wd, Hd, spp = 48, 32, 2
+    out = subprocess.run([host, "--config", "5", "--res", "%dx%d" % (Wd, Hd), "--spp", str(spp), "--spectral",
+                          "--out", str(tmp_path / "s")], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    assert json.loads(out.stdout)["mode"] == "fused-sampled64"
+    I = _read_pfm(str(tmp_path / "s.pfm"))
+    g = W.SceneGen(5, 0, (Wd, Hd))
+    ctx.set_quirks(0)
+    ctx.set_spectrum(W.SPECTRUM_SAMPLED64)
+    try:
+        ctx.upload(g.desc)
+        ctx.build()
+        ctx.render_setup(spp, seed=0, stream=0)
+        ctx.render()
+        L, w = ctx.film(Wd, Hd)
+    finally:
+        ctx.set_spectrum(W.SPECTRUM_RGB)
+    ref = (L / w[..., None]).astype(np.float32)
+    same = (I.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(I) & np.isnan(ref))
+    assert same.all()
+
+
+@pytest.mark.gpu
+def test_host_runner_renders_textured_obj(W, host, tmp_path):
+    pos, idx = _mesh(W)
+    uv = np.stack([pos[:, 0] * 0.5 + 0.5, pos[:, 1] * 0.5 + 0.5], 1)
+    obj = str(tmp_path / "m.obj")
+    _write_obj(obj, pos, idx, uv=uv)
+    rng = np.random.default_rng(2)
+    k, r = str(tmp_path / "k.pfm"), str(tmp_path / "r.pfm")
+    _write_pfm(k, rng.uniform(0.2, 3.0, (16, 16, 3)).astype(np.float32))
+    _write_pfm(r, rng.uniform(0.0, 0.01, (8, 8, 3)).astype(np.float32))
+    base = [host, "--obj", obj, "--res", "48x32", "--spp", "2"]
+    a = subprocess.run(base + ["--metal", k, r, "--out", str(tmp_path / "a")], capture_output=True, text=True,
+                       timeout=300)
+    b = subprocess.run(base + ["--out", str(tmp_path / "b")], capture_output=True, text=True, timeout=300)
+    assert a.returncode == 0 and b.returncode == 0, (a.stderr, b.stderr)
+    Ia, Ib = _read_pfm(str(tmp_path / "a.pfm")), _read_pfm(str(tmp_path / "b.pfm"))
+    assert np.isfinite(Ia).mean() > 0.99 and np.nanmax(Ia) > 0.0
+    assert not np.array_equal(np.nan_to_num(Ia), np.nan_to_num(Ib))

@@ -11,6 +11,8 @@
 //   wpbr_host --config 0 --res 256x256 --spp 4 --out film
 //   wpbr_host --obj mesh.obj [--env sky.pfm] --res 512x512 --spp 16 --staged
 //   wpbr_host --obj mesh.obj --dump-scene          (parse only, no GPU)
+//   wpbr_host --obj mesh.obj --metal k.pfm rough.pfm --spectral   (textured
+//       metal from two PFM textures, CMaterialMetal; Sampled64 spectra)
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -26,17 +28,18 @@ namespace {
 struct Args {
   int config = -1;
   uint32_t level = 0, seed = 0, render_seed = 0, spp = 4, quirks = 0, W = 256, H = 256;
-  std::string obj, env, out;
-  bool staged = false, dump = false;
+  std::string obj, env, out, metal_k, metal_rough;
+  bool staged = false, dump = false, spectral = false;
   float fov = 45.0f;
 };
 
 [[noreturn]] void usage(const char* msg) {
   fprintf(stderr, "wpbr_host: %s\n", msg);
   fprintf(stderr,
-          "usage: wpbr_host (--config N [--level L] [--seed S] | --obj FILE [--env FILE.pfm] [--fov DEG])\n"
-          "                 [--res WxH] [--spp N] [--render-seed S] [--quirks Q] [--staged] [--out PREFIX]\n"
-          "                 [--dump-scene]\n");
+          "usage: wpbr_host (--config N [--level L] [--seed S] | --obj FILE [--env FILE.pfm] [--fov DEG]\n"
+          "                  [--metal K.pfm ROUGHNESS.pfm])\n"
+          "                 [--res WxH] [--spp N] [--render-seed S] [--quirks Q] [--staged | --spectral]\n"
+          "                 [--out PREFIX] [--dump-scene]\n");
   exit(2);
 }
 
@@ -59,6 +62,11 @@ Args parse(int argc, char** argv) {
     else if (k == "--env") a.env = next();
     else if (k == "--out") a.out = next();
     else if (k == "--staged") a.staged = true;
+    else if (k == "--spectral") a.spectral = true;
+    else if (k == "--metal") {
+      a.metal_k = next();
+      a.metal_rough = next();
+    }
     else if (k == "--dump-scene") a.dump = true;
     else if (k == "--res") {
       std::string v = next();
@@ -66,6 +74,8 @@ Args parse(int argc, char** argv) {
     } else usage(("unknown option " + k).c_str());
   }
   if ((a.config < 0) == a.obj.empty()) usage("give exactly one of --config and --obj");
+  if (a.staged && a.spectral) usage("the staged jobs run in RGB only");
+  if (!a.metal_k.empty() && a.obj.empty()) usage("--metal applies to an --obj mesh");
   return a;
 }
 
@@ -112,6 +122,8 @@ struct ObjScene {
   wpbr_host::ObjMesh mesh;
   std::vector<float> env_rgb;
   uint32_t envW = 0, envH = 0;
+  std::vector<float> tex_rgb[2];  // metallic, roughness
+  wpbr_texture texs[2];
   wpbr_material mats[2];
   wpbr_mesh meshes[1];
   wpbr_sphere sphere;
@@ -150,6 +162,24 @@ void build_obj_scene(const Args& a, ObjScene& s) {
   // both: the mesh is shaded with its geometric normals.
   s.meshes[0] = wpbr_mesh{0, (uint32_t)(s.mesh.idx.size() / 3), 0, 0};
   if (s.mesh.has_uv) s.meshes[0].flags |= WPBR_MESH_UVS;
+  memset(&s.desc, 0, sizeof(s.desc));
+  if (!a.metal_k.empty()) {
+    // CMaterialMetal with its two texture bindings (metallic k, roughness in
+    // the red channel), looked up at the mesh's uvs
+    if (!s.mesh.has_uv) throw std::runtime_error("--metal needs an OBJ with texture coordinates (vt)");
+    const std::string* files[2] = {&a.metal_k, &a.metal_rough};
+    for (int t = 0; t < 2; ++t) {
+      uint32_t tw = 0, th = 0;
+      s.tex_rgb[t] = wpbr_host::read_pfm(*files[t], &tw, &th);
+      if (tw < 4 || th < 4) throw std::runtime_error("texture smaller than 4x4: " + *files[t]);
+      s.texs[t] = wpbr_texture{tw, th, s.tex_rgb[t].data()};
+    }
+    s.mats[0].type = WPBR_MAT_METAL;
+    s.mats[0].tex[0] = 0;
+    s.mats[0].tex[1] = 1;
+    s.desc.textures = s.texs;
+    s.desc.n_textures = 2;
+  }
   double lr = 0.1 * ext;
   double lp[3] = {ctr[0], hi[1] + 1.5 * ext, ctr[2]};
   M4 o2w{}, w2o{};
@@ -165,7 +195,6 @@ void build_obj_scene(const Args& a, ObjScene& s) {
   s.sphere.material = 1;
   uint32_t nl = 0;
   s.lights[nl++] = wpbr_light{WPBR_LIGHT_SPHERE, 0, {50.0f, 50.0f, 50.0f}};
-  memset(&s.desc, 0, sizeof(s.desc));
   if (!a.env.empty()) {
     s.env_rgb = wpbr_host::read_pfm(a.env, &s.envW, &s.envH);
     memset(&s.envmap, 0, sizeof(s.envmap));
@@ -264,9 +293,10 @@ int main(int argc, char** argv) {
     for (uint32_t i = 0; i < desc->n_vertices * 3; ++i) psum += desc->positions[i];
     for (uint32_t i = 0; i < desc->n_triangles * 3; ++i) isum += desc->indices[i];
     printf("{\"vertices\": %u, \"triangles\": %u, \"spheres\": %u, \"lights\": %u, \"uvs\": %d, "
-           "\"position_sum\": %.9g, \"index_sum\": %llu, \"env\": [%u, %u]}\n",
+           "\"position_sum\": %.9g, \"index_sum\": %llu, \"env\": [%u, %u], \"textures\": %u}\n",
            desc->n_vertices, desc->n_triangles, desc->n_spheres, desc->n_lights, desc->uvs != nullptr, psum,
-           (unsigned long long)isum, desc->envmap ? desc->envmap->width : 0, desc->envmap ? desc->envmap->height : 0);
+           (unsigned long long)isum, desc->envmap ? desc->envmap->width : 0, desc->envmap ? desc->envmap->height : 0,
+           desc->n_textures);
     if (gen) wpbr_scenegen_destroy(gen);
     return 0;
   }
@@ -278,6 +308,7 @@ int main(int argc, char** argv) {
   }
   const uint32_t W = desc->camera.res_x, H = desc->camera.res_y;
   CHECK(wpbr_set_quirks(gpu, a.quirks));
+  if (a.spectral) CHECK(wpbr_set_spectrum(gpu, WPBR_SPECTRUM_SAMPLED64));
   CHECK(wpbr_scene_upload(gpu, desc));
   double t0 = now_ms();
   CHECK(wpbr_bvh_build(gpu));
@@ -312,7 +343,8 @@ int main(int argc, char** argv) {
   }
   printf("{\"film\": [%u, %u], \"spp\": %u, \"mode\": \"%s\", \"triangles\": %u, \"spheres\": %u, "
          "\"build_ms\": %.3f, \"render_ms\": %.3f, \"msamples_per_s\": %.3f}\n",
-         W, H, a.spp, a.staged ? "staged" : "fused", desc->n_triangles, desc->n_spheres, t1 - t0, t2 - t1,
+         W, H, a.spp, a.staged ? "staged" : (a.spectral ? "fused-sampled64" : "fused"), desc->n_triangles,
+         desc->n_spheres, t1 - t0, t2 - t1,
          (double)W * H * a.spp / ((t2 - t1) * 1e3));
   wpbr_destroy(gpu);
   if (gen) wpbr_scenegen_destroy(gen);
