@@ -24,6 +24,12 @@ constexpr int kTB = 128;
 #ifndef WPBR_SPAWN_MIN_BLOCKS
 #define WPBR_SPAWN_MIN_BLOCKS 12
 #endif
+// The same kernels compiled with the texture path (scenes with textured
+// metal): the EWA loops need registers, and bounding them lost (textured
+// scene at 1080p: 1535 Msamples/s unbounded, 1487 at 8 blocks, 1439 at 12).
+#ifndef WPBR_SPAWN_TEX_MIN_BLOCKS
+#define WPBR_SPAWN_TEX_MIN_BLOCKS 1
+#endif
 // The differentiable estimator's spawn: forward 4.06 -> 3.84 ms at 12 blocks
 // (512x512 x 16 spp).
 #ifndef WPBR_ADJ_SPAWN_MIN_BLOCKS
@@ -88,10 +94,13 @@ __device__ SurfInt make_si(const SceneView& S, uint32_t prim, V3 o, V3 d) {
 // The material of a hit: the scene's, or for textured metal the conductor
 // built from its textures at the hit's footprint (camera-ray differentials,
 // sphere or uv mapping).
+// TEX = false compiles the texture path out, for scenes without textured
+// materials (the context knows: has_metal).
+template <bool TEX = true>
 __device__ wpbr_material hit_material(const SceneView& S, uint32_t prim, uint32_t mid, const SurfInt& s,
                                       const RayD& r) {
   wpbr_material m = S.mats[mid];
-  if (!WPBR_MAT_TEXTURED(m.type)) return m;
+  if (!TEX || !WPBR_MAT_TEXTURED(m.type)) return m;
   SurfDiff D = surf_differentials(s, r);
   TexFootprint fp = prim < S.ns ? sphere_footprint(S.sph_w2o[prim], s, D) : uv_footprint(s, D);
   return metal_material(S.tex, m, fp);

@@ -252,7 +252,8 @@ __global__ void k_film(uint32_t W, uint32_t H, const float2* pf, const float4* L
 constexpr int kStateF4 = kPassStateF4;
 enum : uint32_t { SF_VALID = 1u, SF_TRACE_L = 2u, SF_TRACE_B = 4u, SF_HIT = 8u, SF_METAL = 16u };
 
-__global__ void __launch_bounds__(kTB, WPBR_SPAWN_MIN_BLOCKS) k_spawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
+template <bool TEX>
+__global__ void __launch_bounds__(kTB, TEX ? WPBR_SPAWN_TEX_MIN_BLOCKS : WPBR_SPAWN_MIN_BLOCKS) k_spawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
                                                float4* state, float4* rays, float4* Lb, float2* pf) {
   uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= P.W * P.H) return;
@@ -278,8 +279,8 @@ __global__ void __launch_bounds__(kTB, WPBR_SPAWN_MIN_BLOCKS) k_spawn(PassCtx P,
   SurfInt s = make_si(P.S, prim, r.o, r.d);
   Frame fr = bsdf_frame(s);
   uint32_t mid = prim_material(P.S, prim);
-  const wpbr_material m = hit_material(P.S, prim, mid, s, r);
-  if (WPBR_MAT_TEXTURED(P.S.mats[mid].type)) {
+  const wpbr_material m = hit_material<TEX>(P.S, prim, mid, s, r);
+  if (TEX && WPBR_MAT_TEXTURED(P.S.mats[mid].type)) {
     flags |= SF_METAL;
     st[6] = metal_pack(m);
   }
@@ -531,8 +532,8 @@ wpbr_status render_pass_launch(wpbr_ctx* ctx) {
   if (spectral)
     WPBR_CUDA(spectral_spawn_launch(ctx, pass_ptr));
   else
-    k_spawn<<<div_up(n, kTB), kTB, 0, st>>>(P, pass_ptr, R.hit_prim.p, R.pstate.p, R.shadow_rays.p, R.Lbuf.p,
-                                            R.pfilm.p);
+    (ctx->has_metal ? k_spawn<true> : k_spawn<false>)<<<div_up(n, kTB), kTB, 0, st>>>(
+        P, pass_ptr, R.hit_prim.p, R.pstate.p, R.shadow_rays.p, R.Lbuf.p, R.pfilm.p);
   launch_traversal<false>(P.S, P.Bv, BufferSrc{R.shadow_rays.p}, PrimSink{R.shadow_hit.p}, 2 * n, R.counters.p + 1,
                           P.err, st, R.trace_grid);
   if (spectral) {

@@ -134,7 +134,8 @@ __device__ __forceinline__ FScalars f_scalars(const wpbr_material& m, float d_wh
   return F;
 }
 
-__global__ void __launch_bounds__(kTB, WPBR_SPAWN_MIN_BLOCKS) k_sspawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
+template <bool TEX>
+__global__ void __launch_bounds__(kTB, TEX ? WPBR_SPAWN_TEX_MIN_BLOCKS : WPBR_SPAWN_MIN_BLOCKS) k_sspawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
                                                 float4* state, float4* rays, float2* pf) {
   uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= P.W * P.H) return;
@@ -167,8 +168,8 @@ __global__ void __launch_bounds__(kTB, WPBR_SPAWN_MIN_BLOCKS) k_sspawn(PassCtx P
   SurfInt si = make_si(P.S, prim, r.o, r.d);
   Frame fr = bsdf_frame(si);
   uint32_t mid = prim_material(P.S, prim);
-  const wpbr_material m = hit_material(P.S, prim, mid, si, r);
-  if (WPBR_MAT_TEXTURED(P.S.mats[mid].type)) {
+  const wpbr_material m = hit_material<TEX>(P.S, prim, mid, si, r);
+  if (TEX && WPBR_MAT_TEXTURED(P.S.mats[mid].type)) {
     flags |= SS_TEX;
     st[4] = make_float4(m.k[0], m.k[1], m.k[2], 0.0f);
   }
@@ -617,7 +618,7 @@ static PassCtx spec_pass_ctx(wpbr_ctx* ctx) {
 cudaError_t spectral_spawn_launch(wpbr_ctx* ctx, const uint32_t* pass_ptr) {
   RenderState& R = ctx->rs;
   uint32_t n = R.W * R.H;
-  k_sspawn<<<div_up(n, kTB), kTB, 0, ctx->stream>>>(spec_pass_ctx(ctx), pass_ptr, R.hit_prim.p, R.pstate.p,
+  (ctx->has_metal ? k_sspawn<true> : k_sspawn<false>)<<<div_up(n, kTB), kTB, 0, ctx->stream>>>(spec_pass_ctx(ctx), pass_ptr, R.hit_prim.p, R.pstate.p,
                                                      R.shadow_rays.p, R.pfilm.p);
   return cudaGetLastError();
 }
