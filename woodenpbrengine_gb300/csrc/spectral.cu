@@ -508,13 +508,15 @@ __global__ void __launch_bounds__(kFilmThreads, 4) k_sfilm(uint32_t W, uint32_t 
     const float w = wp[k];
     const bool take = v && !bl[off];
     const float* sp = base + off * kSStride;
+    if (take) {
 #pragma unroll
-    for (int j = 0; j < kFilmBins / 4; ++j) {
-      float4 t = *reinterpret_cast<const float4*>(sp + 4 * j);
-      a[4 * j] = take ? a[4 * j] + t.x * w : a[4 * j];
-      a[4 * j + 1] = take ? a[4 * j + 1] + t.y * w : a[4 * j + 1];
-      a[4 * j + 2] = take ? a[4 * j + 2] + t.z * w : a[4 * j + 2];
-      a[4 * j + 3] = take ? a[4 * j + 3] + t.w * w : a[4 * j + 3];
+      for (int j = 0; j < kFilmBins / 4; ++j) {
+        float4 t = *reinterpret_cast<const float4*>(sp + 4 * j);
+        a[4 * j] = a[4 * j] + t.x * w;
+        a[4 * j + 1] = a[4 * j + 1] + t.y * w;
+        a[4 * j + 2] = a[4 * j + 2] + t.z * w;
+        a[4 * j + 3] = a[4 * j + 3] + t.w * w;
+      }
     }
     ws = v ? ws + w : ws;
   }
