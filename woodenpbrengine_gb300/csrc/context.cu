@@ -404,6 +404,9 @@ WPBR_API wpbr_status wpbr_scene_upload(wpbr_ctx* ctx, const wpbr_scene_desc* d) 
   ctx->h_lights.assign(d->lights, d->lights + d->n_lights);
   WPBR_CUDA(upload(ctx->lights, d->lights, d->n_lights, st));
   ctx->has_env = d->envmap != nullptr;
+  ctx->env_lights_only = d->n_lights > 0;
+  for (uint32_t i = 0; i < d->n_lights; ++i)
+    if (d->lights[i].type != WPBR_LIGHT_ENV) ctx->env_lights_only = false;
   if (ctx->has_env) {
     const wpbr_envmap& e = *d->envmap;
     ctx->envW = (int)e.width;

@@ -155,6 +155,9 @@ struct wpbr_ctx {
   wpbr::DevBuf<wpbr_light> lights;
   std::vector<wpbr_light> h_lights;
   bool has_env = false;
+  // every light is an environment light: a shadow ray is unoccluded iff it
+  // hits nothing, so the fused pass traces shadow rays any-hit
+  bool env_lights_only = false;
   int envW = 0, envH = 0;
   wpbr::DevBuf<float4> env_rgb;
   wpbr::DevBuf<float> cond_func, cond_cdf, cond_int, marg_func, marg_cdf, marg_int, env_lum;

@@ -534,8 +534,16 @@ wpbr_status render_pass_launch(wpbr_ctx* ctx) {
   else
     (ctx->has_metal ? k_spawn<true> : k_spawn<false>)<<<div_up(n, kTB), kTB, 0, st>>>(
         P, pass_ptr, R.hit_prim.p, R.pstate.p, R.shadow_rays.p, R.Lbuf.p, R.pfilm.p);
-  launch_traversal<false>(P.S, P.Bv, BufferSrc{R.shadow_rays.p}, PrimSink{R.shadow_hit.p}, 2 * n, R.counters.p + 1,
-                          P.err, st, R.trace_grid);
+  // shadow rays: unoccluded iff no hit or the closest hit is the sampled
+  // light's primitive; with environment lights only that is "no hit", which
+  // the any-hit traversal decides with the same primitive tests, stopping at
+  // the first hit (the stored id is then some hit, never a light's)
+  if (ctx->env_lights_only)
+    launch_traversal<true>(P.S, P.Bv, BufferSrc{R.shadow_rays.p}, PrimSink{R.shadow_hit.p}, 2 * n,
+                           R.counters.p + 1, P.err, st, R.trace_grid);
+  else
+    launch_traversal<false>(P.S, P.Bv, BufferSrc{R.shadow_rays.p}, PrimSink{R.shadow_hit.p}, 2 * n,
+                            R.counters.p + 1, P.err, st, R.trace_grid);
   if (spectral) {
     WPBR_CUDA(spectral_finish_launch(ctx));
   } else {
