@@ -123,8 +123,8 @@ WPBR_API wpbr_status wpbr_bvh_export(wpbr_ctx* ctx, float* prim_bounds, float* c
 enum wpbr_trace_mode { WPBR_TRACE_CLOSEST = 0, WPBR_TRACE_ANY = 1 };
 /* Host buffers (rays: n x 8 floats o.xyz, 0, d.xyz, tmax; hits: n x 4 floats
  * t, prim id bits, b1, b2). Batches of 2^22 rays and more are copied and
- * traced in up to 4 chunks, the copies of one chunk overlapping the
- * traversal of its neighbours (page-locked host buffers let them overlap). */
+ * traced in four chunks, the copies of one chunk overlapping the traversal
+ * of its neighbours (page-locked host buffers let them overlap). */
 WPBR_API wpbr_status wpbr_collide(wpbr_ctx* ctx, const float* rays, uint64_t n, float* hits, uint32_t mode);
 WPBR_API wpbr_status wpbr_collide_device(wpbr_ctx* ctx, const void* d_rays, uint64_t n, void* d_hits,
                                          uint32_t mode);

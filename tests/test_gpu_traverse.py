@@ -147,7 +147,7 @@ def test_chunked_host_collide_matches_device_collide(W, ctx):
     ctx.build()
     rays = g.rays()
     rays = np.concatenate([rays, rays, rays])
-    n = (1 << 22) + (1 << 21) + 777  # 4 chunks, the last one short
+    n = (1 << 22) + (1 << 21) + 777  # 4 uneven chunks, none a multiple of the others
     rays = np.concatenate([rays, rays[: n - rays.shape[0]]])
     assert rays.shape[0] == n
     d_rays = torch.from_numpy(rays).cuda()
