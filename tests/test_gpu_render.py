@@ -141,3 +141,19 @@ def test_pass_graph_reuse_and_invalidation(W, O, ctx):
     Lo, wo = O.OracleScene(g1.desc).render(40, 24, 2, 9, 0)
     assert np.array_equal(d[0].view(np.uint32), Lo.view(np.uint32)) and np.array_equal(d[1], wo)
     ctx.check_device_errors()
+
+
+@pytest.mark.parametrize("res", [(45, 27), (33, 65)])
+def test_fused_film_odd_sizes(W, O, ctx, res):
+    # films whose sides are not multiples of the 32x32 tiles or of any block
+    g = W.SceneGen(0, 0, res)
+    ctx.set_quirks(0)
+    ctx.upload(g.desc)
+    ctx.build()
+    ctx.render_setup(3, seed=2, stream=1)
+    ctx.render()
+    Lg, wg = ctx.film(*res)
+    Lo, wo = O.OracleScene(g.desc).render(res[0], res[1], 3, 2, 1)
+    assert np.array_equal(wg, wo)
+    assert np.array_equal(Lg.view(np.uint32), Lo.view(np.uint32))
+    ctx.check_device_errors()

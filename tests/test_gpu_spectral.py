@@ -12,7 +12,8 @@ def _same_nan_aware(a, b):
     return bool(np.all((a.view(np.uint32) == b.view(np.uint32)) | (np.isnan(a) & np.isnan(b))))
 
 
-@pytest.mark.parametrize("config,res,level,quirks", [(0, (64, 48), 0, 0), (2, (48, 32), 4, 2), (2, (48, 32), 4, 32)])
+@pytest.mark.parametrize("config,res,level,quirks", [(0, (64, 48), 0, 0), (2, (48, 32), 4, 2), (2, (48, 32), 4, 32),
+                                                     (0, (37, 23), 0, 0), (2, (70, 41), 4, 0)])
 def test_spectral_film_matches_oracle(W, O, ctx, config, res, level, quirks):
     g = W.SceneGen(config, 0, res, level=level)
     ctx.set_quirks(quirks)
