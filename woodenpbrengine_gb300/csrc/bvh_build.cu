@@ -1017,9 +1017,35 @@ __global__ void k_flatten(uint32_t N, uint32_t nsah, uint32_t root, uint32_t M, 
   }
 }
 
+// Traversal-layout order of the interior nodes: the root first, then, for
+// each interior node in preorder, its interior children side by side. The
+// two children a traversal step chooses between share a cache line, and a
+// left subtree's records follow its parent's closely. kids[r] counts the
+// interior children of the interior node of preorder rank r.
+__global__ void k_int_kids(uint32_t M, const uint32_t* lin_node, const uint32_t* is_int, const uint32_t* int_index,
+                           uint32_t* kids) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M || !is_int[i]) return;
+  uint32_t c1 = lin_node[(size_t)i * 3];
+  uint32_t k = (i + 1 < M ? is_int[i + 1] : 0u) + (c1 < M ? is_int[c1] : 0u);
+  kids[int_index[i]] = k;
+}
+// slot[rank] = the node's index in the traversal layout; off = exclusive scan of kids
+__global__ void k_int_slots(uint32_t M, const uint32_t* lin_node, const uint32_t* is_int, const uint32_t* int_index,
+                            const uint32_t* off, uint32_t* slot) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M || !is_int[i]) return;
+  uint32_t r = int_index[i];
+  if (r == 0) slot[0] = 0;
+  uint32_t s = 1 + off[r];
+  uint32_t c0 = i + 1, c1 = lin_node[(size_t)i * 3];
+  if (c0 < M && is_int[c0]) slot[int_index[c0]] = s++;
+  if (c1 < M && is_int[c1]) slot[int_index[c1]] = s;
+}
+
 // Child-pair traversal layout.
 __global__ void k_node2(uint32_t M, const uint32_t* lin_node, const float* lin_bounds, const uint32_t* is_int,
-                        const uint32_t* int_index, Node2* out) {
+                        const uint32_t* int_index, const uint32_t* slot, Node2* out) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= M || !is_int[i]) return;
   uint32_t c[2] = {i + 1, lin_node[(size_t)i * 3]};
@@ -1031,7 +1057,7 @@ __global__ void k_node2(uint32_t M, const uint32_t* lin_node, const float* lin_b
     uint32_t ci = c[k];
     for (int q = 0; q < 6; ++q) b[k][q] = lin_bounds[(size_t)ci * 6 + q];
     if (is_int[ci]) {
-      ref[k] = (int)int_index[ci];
+      ref[k] = (int)slot[int_index[ci]];
       cnt[k] = 0;
     } else {
       ref[k] = ~(int)lin_node[(size_t)ci * 3];
@@ -1043,7 +1069,7 @@ __global__ void k_node2(uint32_t M, const uint32_t* lin_node, const float* lin_b
   nd.b1 = make_float4(b[1][0], b[1][3], b[1][1], b[1][4]);
   nd.bz = make_float4(b[0][2], b[0][5], b[1][2], b[1][5]);
   nd.meta = make_int4(ref[0], ref[1], (int)cnt[0], (int)((lin_node[(size_t)i * 3 + 2] << 30) | (cnt[1] & 0x3FFFFFFFu)));
-  out[int_index[i]] = nd;
+  out[slot[int_index[i]]] = nd;
 }
 
 // Primitive records in leaf order: triangles carry their vertices, spheres
@@ -1518,8 +1544,16 @@ wpbr_status bvh_build(wpbr_ctx* ctx) {
   B.max_depth = depth;
   WPBR_CUDA(B.nodes2.ensure(B.n_int ? B.n_int : 1));
   WPBR_CUDA(B.prims.ensure((size_t)3 * N));
-  if (B.n_int)
-    k_node2<<<div_up(M, kB), kB, 0, st>>>(M, B.lin_node.p, B.lin_bounds.p, B.is_int.p, B.int_index.p, B.nodes2.p);
+  if (B.n_int) {
+    WPBR_CUDA(B.int_kids.ensure(B.n_int));
+    WPBR_CUDA(B.int_slot.ensure(B.n_int));
+    k_int_kids<<<div_up(M, kB), kB, 0, st>>>(M, B.lin_node.p, B.is_int.p, B.int_index.p, B.int_kids.p);
+    WPBR_CUDA(scan_exclusive(B.int_kids.p, B.int_kids.p, B.n_int, B.scan_tmp, st));
+    k_int_slots<<<div_up(M, kB), kB, 0, st>>>(M, B.lin_node.p, B.is_int.p, B.int_index.p, B.int_kids.p,
+                                              B.int_slot.p);
+    k_node2<<<div_up(M, kB), kB, 0, st>>>(M, B.lin_node.p, B.lin_bounds.p, B.is_int.p, B.int_index.p,
+                                          B.int_slot.p, B.nodes2.p);
+  }
   k_prims<<<g, kB, 0, st>>>(S, B.sprim, B.prims.p);
   WPBR_CUDA(cudaGetLastError());
   // four-wide traversal layout, level by level from the root

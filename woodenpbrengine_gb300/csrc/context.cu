@@ -144,6 +144,7 @@ void bvh_release(wpbr_ctx* ctx, bool keep_traversal) {
   B.seg_bucket_cnt.release(); B.seg_bucket_enc.release(); B.small_start.release(); B.small_end.release();
   B.small_node.release(); B.counters.release(); B.sah_axis.release(); B.lin_node.release();
   B.lin_bounds.release(); B.is_int.release(); B.int_index.release(); B.depth_max.release();
+  B.int_kids.release(); B.int_slot.release();
   B.wq_bin0.release(); B.wq_bin1.release(); B.wq_wide0.release(); B.wq_wide1.release();
   B.wcnt.release(); B.woff.release();
   if (!keep_traversal) {

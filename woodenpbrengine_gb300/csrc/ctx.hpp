@@ -61,6 +61,7 @@ struct BvhState {
   DevBuf<uint32_t> lin_node;  // M*3: offset, n_shapes, axis
   DevBuf<float> lin_bounds;   // M*6
   DevBuf<uint32_t> is_int, int_index, depth_max;
+  DevBuf<uint32_t> int_kids, int_slot;  // traversal-layout order of the interior nodes
   DevBuf<Node2> nodes2;
   DevBuf<Node4> nodes4;
   DevBuf<uint32_t> wq_bin0, wq_bin1, wq_wide0, wq_wide1, wcnt, woff;  // wide collapse queues
