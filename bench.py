@@ -172,6 +172,23 @@ def render_rate(W, torch, config, res, spp, level=0, frames=1, spectrum=None):
             "kernel_launches_per_pass": 5}
 
 
+def cpu_render_rate(W, config, res, spp, spectral=False):
+    """The oracle's render (the per-sample job list restated on the CPU, all
+    host cores) of the same frame: Msamples/s beside the GPU's."""
+    from oracle import binding as O
+
+    g = W.SceneGen(config, 0, res)
+    o = O.OracleScene(g.desc)  # builds the oracle's BVH
+    t = time.perf_counter()
+    if spectral:
+        o.render_spectral(res[0], res[1], spp)
+    else:
+        o.render(res[0], res[1], spp)
+    dt = time.perf_counter() - t
+    return {"msamples_per_s": res[0] * res[1] * spp / dt / 1e6, "cores": O.lib().orc_num_threads(), "kind": "port",
+            "sample": "%dx%d x %d spp, one frame, %.2f s" % (res[0], res[1], spp, dt)}
+
+
 def batch_rate(W, torch, n_scenes=32, spp=16, film_scale=1024, max_count=2000000):
     """Aggregate Msamples/s of the batched-scenes set (32 scenes, triangle
     counts log-uniform on [10k, 2M], films from {256..1024}^2, 16 spp): all
@@ -612,7 +629,11 @@ def main():
 
     render = None
     if rank == 0 and not args.no_render:
-        render = {"c0_plain_256x256_4spp": render_rate(W, torch, 0, (256, 256), 4, frames=3),
+        c0 = render_rate(W, torch, 0, (256, 256), 4, frames=3)
+        if not args.no_cpu:
+            c0["cpu_baseline"] = cpu_render_rate(W, 0, (256, 256), 4)
+            c0["cpu_baseline_sampled64"] = cpu_render_rate(W, 0, (256, 256), 4, spectral=True)
+        render = {"c0_plain_256x256_4spp": c0,
                   "c2_fullframe_1080p_64spp": render_rate(W, torch, 2, (1920, 1080), 64, level=LEVEL),
                   "c2_fullframe_1080p_16spp_sampled64": render_rate(W, torch, 2, (1920, 1080), 16, level=LEVEL,
                                                                     spectrum=W.SPECTRUM_SAMPLED64),
