@@ -179,14 +179,19 @@ def cpu_render_rate(W, config, res, spp, spectral=False):
 
     g = W.SceneGen(config, 0, res)
     o = O.OracleScene(g.desc)  # builds the oracle's BVH
+    frames = 0
     t = time.perf_counter()
-    if spectral:
-        o.render_spectral(res[0], res[1], spp)
-    else:
-        o.render(res[0], res[1], spp)
-    dt = time.perf_counter() - t
-    return {"msamples_per_s": res[0] * res[1] * spp / dt / 1e6, "cores": O.lib().orc_num_threads(), "kind": "port",
-            "sample": "%dx%d x %d spp, one frame, %.2f s" % (res[0], res[1], spp, dt)}
+    while True:  # whole frames until about a second has passed
+        if spectral:
+            o.render_spectral(res[0], res[1], spp)
+        else:
+            o.render(res[0], res[1], spp)
+        frames += 1
+        dt = time.perf_counter() - t
+        if dt > 1.0:
+            break
+    return {"msamples_per_s": res[0] * res[1] * spp * frames / dt / 1e6, "cores": O.lib().orc_num_threads(),
+            "kind": "port", "sample": "%dx%d x %d spp, %d frames, %.2f s" % (res[0], res[1], spp, frames, dt)}
 
 
 def batch_rate(W, torch, n_scenes=32, spp=16, film_scale=1024, max_count=2000000):
