@@ -48,3 +48,32 @@ def test_back_to_rgb_after_spectral(W, O, ctx):
     L, w = ctx.film(32, 32)
     Lo, wo = O.OracleScene(g.desc).render(32, 32, 2)
     assert np.array_equal(L.view(np.uint32), Lo.view(np.uint32)) and np.array_equal(w, wo)
+
+
+def test_spectral_passes_one_at_a_time(W, O, ctx):
+    # wpbr_render_pass leaves the film's toRGB to the next film read
+    g = W.SceneGen(0, 0, (40, 24))
+    ctx.set_quirks(0)
+    ctx.set_spectrum(W.SPECTRUM_SAMPLED64)
+    try:
+        ctx.upload(g.desc)
+        ctx.build()
+        ctx.render_setup(3, seed=4, stream=2)
+        o = O.OracleScene(g.desc)
+        for p in range(3):
+            ctx.render_pass(p)
+        L, w = ctx.film(40, 24)
+        Lo, wo = o.render_spectral(40, 24, 3, 4, 2)
+        assert np.array_equal(w, wo)
+        assert _same_nan_aware(L, Lo)
+        # a film read after each pass sees the film so far
+        ctx.render_setup(3, seed=4, stream=2)
+        ctx.render_pass(0)
+        L1, w1 = ctx.film(40, 24)
+        ctx.render_pass(1)
+        ctx.render_pass(2)
+        L3, w3 = ctx.film(40, 24)
+        assert _same_nan_aware(L3, Lo) and not np.array_equal(w1, w3)
+    finally:
+        ctx.set_spectrum(W.SPECTRUM_RGB)
+    ctx.check_device_errors()
