@@ -49,6 +49,16 @@ def test_host_entry_points_validate_arguments(W):
     assert W.lib().wpbr_create(0, None) == W.ERR_INVALID_ARG
 
 
+def test_instrumentation_entry_points_validate_arguments(W):
+    L = W.lib()
+    c = C.c_uint32()
+    f = C.c_float()
+    assert L.wpbr_collide_launches(None, 1000, C.byref(c)) == W.ERR_INVALID_ARG
+    assert L.wpbr_set_kernel_timing(None, 1) == W.ERR_INVALID_ARG
+    assert L.wpbr_kernel_timing(None, C.byref(f), C.byref(c)) == W.ERR_INVALID_ARG
+    assert L.wpbr_collide(None, None, 0, None, 0) == W.ERR_INVALID_ARG
+
+
 def test_no_device_is_reported_not_faked(W):
     if W.device_available():
         pytest.skip("a GPU is present")
