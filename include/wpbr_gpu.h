@@ -210,9 +210,8 @@ WPBR_API void wpbr_scenegen_destroy(wpbr_scenegen* g);
  * No counterpart in the reference (its sort runs inside JobSortsShapesByMortonCode
  * on the engine's temp allocator). For callers that cannot allocate device
  * memory: hosts that hand out all device memory from their own arena and
- * forbid allocation inside a job, loops that must not take cudaMalloc's
- * device-wide synchronisation, and work recorded into a CUDA graph while a
- * stream is being captured. Stable LSD radix sort of n Morton codes by their
+ * forbid allocation inside a job, and loops that must not take cudaMalloc's
+ * device-wide synchronisation. Stable LSD radix sort of n Morton codes by their
  * low key_bits bits (24: the order the reference builds over; 30: full), the
  * same permutation as wpbr_bvh_build. Device buffers in and out (no aliasing),
  * asynchronous on `stream`, no allocation: temporaries live in one file-scope

@@ -3,7 +3,7 @@ sort inside wpbr_bvh_build.
 
 It exists for callers that cannot allocate device memory — hosts that own all
 device memory through their own arena, loops that must not take cudaMalloc's
-synchronisation, work recorded into a CUDA graph — and keeps its temporaries in
+synchronisation — and keeps its temporaries in
 a fixed file-scope device array. Two calls in a row must both reproduce the
 build's sorted codes and permutation exactly (integer data: bit-exact), and a
 size above the fixed capacity must be rejected. Collected last on purpose."""

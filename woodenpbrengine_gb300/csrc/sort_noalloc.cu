@@ -4,10 +4,8 @@
 //
 // Who needs it: hosts that own every byte of device memory through their own
 // arena and forbid allocation inside a job (the reference engine hands each
-// ECS job a linear temp allocator and resets it after the job), real-time loops
-// that must not take cudaMalloc's device-wide synchronisation, and code that
-// records work into a CUDA graph, where allocation calls are not allowed while
-// the stream is being captured. They pass their own input and output buffers
+// ECS job a linear temp allocator and resets it after the job), and real-time
+// loops that must not take cudaMalloc's device-wide synchronisation. They pass their own input and output buffers
 // and the sort keeps its temporaries in one file-scope device array.
 //
 // The array (g_scratch, about 8.5 MB) is part of the library image: every
