@@ -66,9 +66,12 @@ WPBR_API wpbr_status wpbr_set_quirks(wpbr_ctx* ctx, uint32_t quirks);
 WPBR_API wpbr_status wpbr_synchronize(wpbr_ctx* ctx);
 /* Traversal layout (an implementation choice of this library; the results
  * are the same): BINARY (default) traverses the child-pair layout of the
- * reference's tree; WIDE a four-wide collapse of it, built by the next
- * wpbr_bvh_build after the mode is set. */
-enum wpbr_traversal { WPBR_TRAVERSAL_BINARY = 0, WPBR_TRAVERSAL_WIDE = 1 };
+ * reference's tree with every leaf of more than 8 (and at most 4096)
+ * primitives subdivided into a small tree over ranges of its sorted
+ * positions, visited in position order; BINARY_FULL_LEAVES the same layout with the reference's leaves as
+ * they are; WIDE a four-wide collapse of the reference's tree, built by the
+ * next wpbr_bvh_build after the mode is set. */
+enum wpbr_traversal { WPBR_TRAVERSAL_BINARY = 0, WPBR_TRAVERSAL_WIDE = 1, WPBR_TRAVERSAL_BINARY_FULL_LEAVES = 2 };
 WPBR_API wpbr_status wpbr_set_traversal(wpbr_ctx* ctx, uint32_t mode);
 /* Spectral representation of the render passes. RGB (default) carries three
  * channels; SAMPLED64 is the reference's Spectrum (SampledSpectrum, 64 bins
@@ -133,7 +136,8 @@ WPBR_API wpbr_status wpbr_collide_device(wpbr_ctx* ctx, const void* d_rays, uint
  * (b = bits_per_axis, default 8, at most 10) and written back at their input
  * positions; the hits do not depend on the order. 0 traces in input order. */
 WPBR_API wpbr_status wpbr_set_ray_sort(wpbr_ctx* ctx, uint32_t bits_per_axis);
-/* Per-ray node visits and primitive tests (u32 pairs), for the byte model. */
+/* Per-ray node visits and primitive tests (u32 pairs) of the near-first
+ * traversal over the reference's leaves as they are, for the byte model. */
 WPBR_API wpbr_status wpbr_collide_stats(wpbr_ctx* ctx, const float* rays, uint64_t n, float* hits,
                                         uint32_t* stats, uint32_t mode);
 /* Number of kernels one wpbr_collide_device call of n rays launches with the

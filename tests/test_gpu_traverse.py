@@ -163,3 +163,122 @@ def test_chunked_host_collide_matches_device_collide(W, ctx):
         else:
             assert np.array_equal(hh[:, 1].view(np.uint32) == 0xFFFFFFFF, hd[:, 1].view(np.uint32) == 0xFFFFFFFF)
     ctx.check_device_errors()
+
+
+def _grid_desc(W, n=48):
+    """A flat n x n grid of unit quads (2 triangles each) on the plane y = 0
+    at integer x, z, and one triangle below it (so the centroid bounds are not
+    flat in y). A ray straight down onto a quad's diagonal hits both of its
+    triangles at exactly the same t."""
+    import ctypes as C
+
+    from woodenpbrengine_gb300 import _abi as A
+
+    xs, zs = np.meshgrid(np.arange(n + 1, dtype=np.float32), np.arange(n + 1, dtype=np.float32), indexing="ij")
+    grid = np.stack([xs.ravel() - n / 2, np.zeros((n + 1) ** 2, np.float32), zs.ravel() - n / 2], 1)
+    below = np.array([[-1.0, -10.0, -1.0], [1.0, -10.0, -1.0], [0.0, -10.0, 1.0]], np.float32)
+    pos = np.ascontiguousarray(np.concatenate([grid, below]), np.float32).ravel()
+    v = lambda i, j: i * (n + 1) + j  # noqa: E731
+    tris = []
+    for i in range(n):
+        for j in range(n):
+            tris += [v(i, j), v(i + 1, j), v(i + 1, j + 1), v(i, j), v(i + 1, j + 1), v(i, j + 1)]
+    m = (n + 1) ** 2
+    tris += [m, m + 1, m + 2]
+    idx = np.asarray(tris, np.uint32)
+    nt = idx.size // 3
+    mesh = A.Mesh(0, nt, 0, 0)
+    mat = A.Material()
+    mat.type = 0
+    mat.alpha_x = mat.alpha_y = 0.2
+    d = A.SceneDesc()
+    d.n_vertices = m + 3
+    d.positions = pos.ctypes.data_as(C.POINTER(C.c_float))
+    d.n_triangles = nt
+    d.indices = idx.ctypes.data_as(C.POINTER(C.c_uint32))
+    d.meshes = C.pointer(mesh)
+    d.n_meshes = 1
+    d.materials = C.pointer(mat)
+    d.n_materials = 1
+    for k in range(4):
+        d.camera.camera_to_world.m[5 * k] = 1.0
+        d.camera.world_to_camera.m[5 * k] = 1.0
+    d.camera.fov_deg = 60.0
+    d.camera.near_z, d.camera.far_z = 0.1, 1000.0
+    d.camera.screen[:] = [-1.0, -1.0, 1.0, 1.0]
+    d.camera.res_x = d.camera.res_y = 8
+    keep = (pos, idx, mesh, mat)
+    return C.pointer(d), keep
+
+
+@pytest.mark.parametrize("full_sort", [False, True])
+def test_leaf_split_keeps_ties_and_first_hits(W, O, ctx, full_sort):
+    # Leaves of more than eight primitives are subdivided for traversal into
+    # small trees over position ranges, visited lowest range first. Rays
+    # straight down onto the diagonals of a flat grid's quads hit two
+    # triangles at exactly t = 5 (with the full 30-bit sort the grid's leaves
+    # hold 18 triangles, so some tied pairs straddle two ranges): the winner
+    # must still be the first in the reference's order, and any-hit the first
+    # hit of its scan.
+    desc, keep = _grid_desc(W)
+    q = W.Q_FULL_MORTON_SORT if full_sort else 0
+    ctx.set_quirks(q)
+    ctx.upload(desc)
+    ctx.build()
+    rng = np.random.default_rng(11)
+    n = 40000
+    o = np.zeros((n, 3), np.float32)
+    s = rng.choice([0.25, 0.5, 0.75], n).astype(np.float32)
+    o[:, 0] = rng.integers(-24, 24, n) + s
+    o[:, 2] = rng.integers(-24, 24, n) + s
+    o[:, 1] = 5.0
+    o[-10000:, [0, 2]] = rng.uniform(-24, 24, (10000, 2))  # off the diagonals
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, :3] = o
+    rays[:, 5] = -1.0
+    rays[:, 7] = np.inf
+    sl = rng.normal(size=(5000, 3))  # and slanted rays
+    sl[:, 1] = -np.abs(sl[:, 1]) - 0.1
+    rays[-5000:, 4:7] = sl / np.linalg.norm(sl, axis=1, keepdims=True)
+    oracle = O.OracleScene(desc, q)
+    ho, ha_o = oracle.trace(rays, mode=0), oracle.trace(rays, mode=2)
+    assert np.mean(ho[: n - 10000, 0] == 5.0) > 0.99
+    for mode in (W.TRAVERSAL_BINARY, W.TRAVERSAL_BINARY_FULL_LEAVES):
+        ctx.set_traversal(mode)
+        _check(ctx.collide(rays), ho)
+        _check(ctx.collide(rays, mode=W.TRACE_ANY), ha_o)
+    ctx.set_traversal(W.TRAVERSAL_BINARY)
+    ctx.set_quirks(0)
+    ctx.check_device_errors()
+    del keep
+
+
+@pytest.mark.parametrize("config,level,res", [(1, 6, (128, 128)), (0, 0, (64, 64)), (2, 4, (64, 36))])
+def test_leaf_split_layout_matches_reference_leaves(W, O, ctx, config, level, res):
+    # closest- and any-hit records of the default (leaf-split) layout equal
+    # those over the reference's leaves as they are and the oracle's
+    g = W.SceneGen(config, 0, res, level=level, rays=(config == 1))
+    ctx.set_quirks(0)
+    ctx.upload(g.desc)
+    ctx.build()
+    if config == 1:
+        rays = g.rays()
+    else:
+        rng = np.random.default_rng(4)
+        n = 30000
+        rays = np.zeros((n, 8), np.float32)
+        rays[:, :3] = rng.uniform(-12, 12, (n, 3))
+        d = rng.normal(size=(n, 3))
+        rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+        rays[:, 7] = np.inf
+    oracle = O.OracleScene(g.desc)
+    ctx.set_traversal(W.TRAVERSAL_BINARY)
+    hs, as_ = ctx.collide(rays), ctx.collide(rays, mode=W.TRACE_ANY)
+    ctx.set_traversal(W.TRAVERSAL_BINARY_FULL_LEAVES)
+    hf, af = ctx.collide(rays), ctx.collide(rays, mode=W.TRACE_ANY)
+    ctx.set_traversal(W.TRAVERSAL_BINARY)
+    assert np.array_equal(hs.view(np.uint32), hf.view(np.uint32))
+    assert np.array_equal(as_.view(np.uint32), af.view(np.uint32))
+    _check(hs, oracle.trace(rays, mode=0))
+    _check(as_, oracle.trace(rays, mode=2))
+    ctx.check_device_errors()

@@ -558,7 +558,7 @@ AdjView adj_view(const wpbr_ctx* ctx) {
 PassCtx adj_pass_ctx(wpbr_ctx* ctx) {
   PassCtx P;
   P.S = scene_view(ctx);
-  P.Bv = traversal_view(ctx);
+  P.Bv = render_traversal_view(ctx);
   P.rs = wpbr_rng::Stream{ctx->adj.seed, ctx->adj.stream, ctx->adj.spp};
   P.W = ctx->adj.W;
   P.H = ctx->adj.H;

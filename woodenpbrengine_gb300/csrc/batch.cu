@@ -322,9 +322,12 @@ WPBR_API wpbr_status wpbr_batch_build(wpbr_batch* b) {
     }
     BATCH_CUDA(cudaStreamSynchronize(c->stream));
     c->bvh.nodes2.release();
+    c->bvh.nodes_split.release();
     c->bvh.nodes4.release();
     c->bvh.prims.release();
     v.nodes = nd;
+    v.nodes_ref = nullptr;  // the arena keeps the layout traversed only
+    v.n_ref_int = 0;
     if (v.nodes4) v.nodes4 = wd;
     v.prims = pd;
   }

@@ -146,9 +146,10 @@ void bvh_release(wpbr_ctx* ctx, bool keep_traversal) {
   B.lin_bounds.release(); B.is_int.release(); B.int_index.release(); B.depth_max.release();
   B.int_kids.release(); B.int_slot.release();
   B.wq_bin0.release(); B.wq_bin1.release(); B.wq_wide0.release(); B.wq_wide1.release();
-  B.wcnt.release(); B.woff.release();
+  B.wcnt.release(); B.woff.release(); B.split_cnt.release(); B.split_off.release();
   if (!keep_traversal) {
     B.nodes2.release();
+    B.nodes_split.release();
     B.nodes4.release();
     B.prims.release();
   }
@@ -263,7 +264,7 @@ WPBR_API wpbr_status wpbr_set_quirks(wpbr_ctx* ctx, uint32_t quirks) {
 
 WPBR_API wpbr_status wpbr_set_traversal(wpbr_ctx* ctx, uint32_t mode) {
   if (!ctx) return WPBR_ERR_INVALID_ARG;
-  if (mode > WPBR_TRAVERSAL_WIDE) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_traversal: unknown mode");
+  if (mode > WPBR_TRAVERSAL_BINARY_FULL_LEAVES) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_traversal: unknown mode");
   ctx->traversal = mode;
   ++ctx->epoch;
   return WPBR_OK;

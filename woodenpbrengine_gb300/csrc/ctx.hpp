@@ -63,6 +63,8 @@ struct BvhState {
   DevBuf<uint32_t> is_int, int_index, depth_max;
   DevBuf<uint32_t> int_kids, int_slot;  // traversal-layout order of the interior nodes
   DevBuf<Node2> nodes2;
+  DevBuf<Node2> nodes_split;             // leaf-split layout: nodes2 + the records splitting large leaves
+  DevBuf<uint32_t> split_cnt, split_off;  // records per child slot, and their offsets
   DevBuf<Node4> nodes4;
   DevBuf<uint32_t> wq_bin0, wq_bin1, wq_wide0, wq_wide1, wcnt, woff;  // wide collapse queues
   DevBuf<float4> prims;
@@ -134,7 +136,7 @@ struct wpbr_ctx {
   std::string err;
   uint32_t quirks = 0;
   uint64_t epoch = 0;  // bumped by every scene upload, BVH build, quirk or traversal change
-  uint32_t traversal = 0;  // wpbr_traversal: 0 binary, 1 wide (collapsed at build time)
+  uint32_t traversal = 0;  // wpbr_traversal: 0 binary (leaf-split), 1 wide, 2 binary over the reference's leaves
   uint32_t spectrum = 0;   // wpbr_spectrum: 0 RGB, 1 Sampled64
   wpbr::DevBuf<uint32_t> d_err;
   // scene
@@ -198,13 +200,25 @@ struct wpbr_ctx {
 };
 
 namespace wpbr {
-// The BVH view the traversal kernels receive (the wide layout only when the
-// context asks for the wide traversal).
+// The BVH view the traversal kernels receive: the wide layout only when the
+// context asks for the wide traversal, the child-pair records of the
+// reference's leaves as they are for WPBR_TRAVERSAL_BINARY_FULL_LEAVES, else
+// the leaf-split child-pair layout.
 inline BvhView traversal_view(const wpbr_ctx* ctx) {
   BvhView v = ctx->bvh.view;
-  if (ctx->traversal != 1) v.nodes4 = nullptr;
+  if (ctx->traversal != WPBR_TRAVERSAL_WIDE) v.nodes4 = nullptr;
+  if (ctx->traversal == WPBR_TRAVERSAL_BINARY_FULL_LEAVES) v = reference_leaves_view(v);
   return v;
 }
+// The view of the render passes' traversals (camera and shadow rays of the
+// fused, staged, Sampled64 and differentiable passes): the reference's leaves
+// as they are. The leaf split speeds up collide batches (8.4M-ray closest hit
+// 4.27 -> 4.19 ms) but slows the passes' traversals, whose warps mostly share
+// leaves (1080p x 64 spp full frame: 1,261 Msamples/s over the reference's
+// leaves, 1,250 with split camera rays, 1,228 with split shadow rays, 1,214
+// with both). A batch's arena keeps only the split layout, which its passes
+// then traverse (32 scenes: 941 against 930 Msamples/s unsplit).
+inline BvhView render_traversal_view(const wpbr_ctx* ctx) { return reference_leaves_view(traversal_view(ctx)); }
 wpbr_status set_err(wpbr_ctx* ctx, wpbr_status st, const std::string& msg);
 wpbr_status cuda_err(wpbr_ctx* ctx, cudaError_t e, const char* what);
 SceneView scene_view(const wpbr_ctx* ctx);

@@ -437,7 +437,7 @@ __global__ void k_tonemap(uint32_t n, const float4* acc, uint8_t* out) {
 PassCtx make_pass_ctx(wpbr_ctx* ctx) {
   PassCtx P;
   P.S = scene_view(ctx);
-  P.Bv = traversal_view(ctx);
+  P.Bv = render_traversal_view(ctx);
   P.rs = wpbr_rng::Stream{ctx->rs.seed, ctx->rs.stream, ctx->rs.spp};
   P.W = ctx->rs.W;
   P.H = ctx->rs.H;

@@ -607,7 +607,7 @@ wpbr_status spectral_setup(wpbr_ctx* ctx) {
 static PassCtx spec_pass_ctx(wpbr_ctx* ctx) {
   PassCtx P;
   P.S = scene_view(ctx);
-  P.Bv = traversal_view(ctx);
+  P.Bv = render_traversal_view(ctx);
   P.rs = wpbr_rng::Stream{ctx->rs.seed, ctx->rs.stream, ctx->rs.spp};
   P.W = ctx->rs.W;
   P.H = ctx->rs.H;

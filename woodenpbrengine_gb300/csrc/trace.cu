@@ -87,8 +87,10 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
   const BvhView Bv = traversal_view(ctx);
   cudaError_t e;
   if (d_stats) {
-    e = (mode == WPBR_TRACE_ANY) ? launch<true, true>(S, Bv, d_rays, n, d_hits, d_stats, ctx->d_err.p, st)
-                                 : launch<false, true>(S, Bv, d_rays, n, d_hits, d_stats, ctx->d_err.p, st);
+    // statistics count the box and primitive tests over the reference's leaves
+    const BvhView Br = reference_leaves_view(Bv);
+    e = (mode == WPBR_TRACE_ANY) ? launch<true, true>(S, Br, d_rays, n, d_hits, d_stats, ctx->d_err.p, st)
+                                 : launch<false, true>(S, Br, d_rays, n, d_hits, d_stats, ctx->d_err.p, st);
   } else {
     if (n >= 0xFFFFFFFFull) return set_err(ctx, WPBR_ERR_INVALID_ARG, "collide: more than 2^32-1 rays per call");
     e = X.counter.ensure(4);

@@ -10,7 +10,10 @@
 // the traversal prunes boxes whose entry distance exceeds the current best t
 // by more than 2^-10 relative: no primitive inside such a box can undercut the
 // best hit, and a later candidate with an equal t never replaces an earlier
-// one, so the hit is unchanged.
+// one, so the hit is unchanged. In the leaf-split layout a large leaf is a
+// small tree over ranges of its sorted positions, visited lowest range first:
+// its primitives are still tested in sorted order, the boxes of the ranges
+// only let a ray skip primitives whose box it misses.
 #pragma once
 
 #include "common.cuh"
@@ -26,6 +29,14 @@ struct HitRec {
   uint32_t prim;
   float b1, b2;
 };
+
+// Order of a child-pair record's two children: axis 0-2 visits the child on
+// the ray's negative side of that split axis first (dirIsNeg[axis],
+// SLBVH.cpp:133-145); axis code 3 (the records splitting one large leaf)
+// visits child 0, the lower sorted positions, first.
+__device__ __forceinline__ bool second_child_first(const int neg[3], uint32_t axis) {
+  return axis == 0 ? neg[0] != 0 : (axis == 1 ? neg[1] != 0 : (axis == 2 ? neg[2] != 0 : false));
+}
 
 __device__ __forceinline__ float prim_test(const SceneView& S, const float4* prims, uint32_t pos, V3 o, V3 d,
                                            const RayTri& R, uint32_t* prim_out, float* b1, float* b2) {
@@ -94,7 +105,7 @@ __device__ HitRec trace_ray(const SceneView& S, const BvhView& Bv, V3 o, V3 d, f
       uint32_t axis = ((uint32_t)m.w) >> 30;
       uint32_t c0n = (uint32_t)m.z, c1n = ((uint32_t)m.w) & 0x3FFFFFFFu;
       if (h0 && h1) {
-        bool first1 = neg[axis] != 0;
+        bool first1 = second_child_first(neg, axis);
         if (sp >= STACK) {
           atomicOr(err, kErrStackOverflow);
           break;

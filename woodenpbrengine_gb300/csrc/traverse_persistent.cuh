@@ -33,12 +33,59 @@ constexpr int kPersistBlock = 128;
 // (camera rays generated in the source, prim-id sinks) at 8 (64 registers),
 // where 10 cost them 5%.
 
-// Ray data the warp's lanes read when they test primitives for another lane.
-struct SharedRay {
-  float ox, oy, oz, dx, dy, dz, tmax;
-  float sx, sy, sz, rox, roy, roz;
-  uint32_t kpack;  // kx | ky << 2 | kz << 4 | miss_all << 6
+// Ray data the warp's lanes read when they test primitives for another lane:
+// a triangle test reads the first two float4s (two 16-byte shared loads), a
+// sphere test also the direction, and takes the world origin back from the
+// permuted one (the permutation only moves components, so it is exact).
+struct __align__(16) SharedRay {
+  float4 s;   // sx, sy, sz of the triangle test's shear; w: the ray's tmax
+  float4 po;  // origin permuted to (kx, ky, kz); w: kx | ky << 2 | kz << 4 | miss_all << 6
+  float4 d;   // world direction (sphere tests)
 };
+
+__device__ __forceinline__ RayTri unpack_ray_tri(float4 s, float4 po) {
+  uint32_t kp = __float_as_uint(po.w);
+  RayTri R;
+  R.kx = (int)(kp & 3u);
+  R.ky = (int)((kp >> 2) & 3u);
+  R.kz = (int)((kp >> 4) & 3u);
+  R.miss_all = (kp >> 6) & 1u;
+  R.sx = s.x;
+  R.sy = s.y;
+  R.sz = s.z;
+  R.ox = po.x;
+  R.oy = po.y;
+  R.oz = po.z;
+  return R;
+}
+
+// prim_test for another lane's ray: the world origin and direction are read
+// on the sphere branch only.
+__device__ __forceinline__ float prim_test_shared(const SceneView& S, const float4* prims, uint32_t pos,
+                                                  const SharedRay& sr, const RayTri& R, uint32_t* prim_out,
+                                                  float* b1, float* b2) {
+  const float4* r = prims + (size_t)pos * 3;
+  float4 r0 = __ldg(r), r1 = __ldg(r + 1);
+  *prim_out = __float_as_uint(r0.w);
+  if (__float_as_uint(r1.w) == 1u) {
+    uint32_t s = __float_as_uint(r1.x);
+    float4 dd = sr.d;
+    // (kx, ky, kz) is a permutation of (0, 1, 2): o[kx] = R.ox, o[ky] = R.oy, o[kz] = R.oz
+    V3 o{R.kx == 0 ? R.ox : (R.ky == 0 ? R.oy : R.oz), R.kx == 1 ? R.ox : (R.ky == 1 ? R.oy : R.oz),
+         R.kx == 2 ? R.ox : (R.ky == 2 ? R.oy : R.oz)};
+    V3 rlo, rld, ph;
+    float t = sphere_intersect(S.sph_w2o[s], S.sph_r[s], o, V3{dd.x, dd.y, dd.z}, &rlo, &rld, &ph);
+    *b1 = 0.0f;
+    *b2 = 0.0f;
+    return t;
+  }
+  float4 r2 = __ldg(r + 2);
+  float c0, c1, c2;
+  float t = tri_intersect_pre(V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, V3{r2.x, r2.y, r2.z}, R, &c0, &c1, &c2);
+  *b1 = c1;
+  *b2 = c2;
+  return t;
+}
 
 template <bool ANY, int STACK, class Src, class Sink>
 __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persistent(SceneView S, BvhView Bv,
@@ -92,12 +139,11 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
           neg[2] = inv.z < 0.0f;
           RayTri R = ray_tri_setup(o, d, S.quirks);
           SharedRay& sr = s_ray[wid][lane];
-          sr.ox = o.x; sr.oy = o.y; sr.oz = o.z;
-          sr.dx = d.x; sr.dy = d.y; sr.dz = d.z;
-          sr.tmax = tmax;
-          sr.sx = R.sx; sr.sy = R.sy; sr.sz = R.sz;
-          sr.rox = R.ox; sr.roy = R.oy; sr.roz = R.oz;
-          sr.kpack = (uint32_t)R.kx | ((uint32_t)R.ky << 2) | ((uint32_t)R.kz << 4) | ((R.miss_all ? 1u : 0u) << 6);
+          uint32_t kpack =
+              (uint32_t)R.kx | ((uint32_t)R.ky << 2) | ((uint32_t)R.kz << 4) | ((R.miss_all ? 1u : 0u) << 6);
+          sr.s = make_float4(R.sx, R.sy, R.sz, tmax);
+          sr.po = make_float4(R.ox, R.oy, R.oz, __uint_as_float(kpack));
+          sr.d = make_float4(d.x, d.y, d.z, 0.0f);
           tb = inf_();
           h = HitRec{inf_(), kNoHit, 0.0f, 0.0f};
           sp = 0;
@@ -138,7 +184,7 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
         uint32_t axis = ((uint32_t)m.w) >> 30;
         uint32_t c0n = (uint32_t)m.z, c1n = ((uint32_t)m.w) & 0x3FFFFFFFu;
         if (h0 && h1) {
-          bool first1 = neg[axis] != 0;
+          bool first1 = second_child_first(neg, axis);
           if (sp >= STACK) {
             atomicOr(err, kErrStackOverflow);
             ref = kEnd;
@@ -241,18 +287,13 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
         uint32_t oexcl = __shfl_sync(0xFFFFFFFFu, excl, owner);
         if (g < total) {
           const SharedRay& sr = s_ray[wid][owner];
-          RayTri R;
-          R.kx = (int)(sr.kpack & 3u);
-          R.ky = (int)((sr.kpack >> 2) & 3u);
-          R.kz = (int)((sr.kpack >> 4) & 3u);
-          R.miss_all = (sr.kpack >> 6) & 1u;
-          R.sx = sr.sx; R.sy = sr.sy; R.sz = sr.sz;
-          R.ox = sr.rox; R.oy = sr.roy; R.oz = sr.roz;
+          float4 s4 = sr.s;
+          RayTri R = unpack_ray_tri(s4, sr.po);
           uint32_t pos = ofirst + (g - oexcl);
           uint32_t prim;
           float b1, b2;
-          float t = prim_test(S, Bv.prims, pos, V3{sr.ox, sr.oy, sr.oz}, V3{sr.dx, sr.dy, sr.dz}, R, &prim, &b1, &b2);
-          if (t != 0.0f && t < sr.tmax) {
+          float t = prim_test_shared(S, Bv.prims, pos, sr, R, &prim, &b1, &b2);
+          if (t != 0.0f && t < s4.w) {
             unsigned long long key = ANY ? (((unsigned long long)pos << 32) | __float_as_uint(t))
                                          : (((unsigned long long)__float_as_uint(t) << 32) | pos);
             atomicMin(&s_key[wid][owner], key);

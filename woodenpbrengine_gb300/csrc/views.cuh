@@ -39,7 +39,9 @@ struct SceneView {
 // the flattened CSceneTreeLBVH, so one 64-byte fetch tests two boxes.
 // ref >= 0: interior node index; ref < 0: leaf whose primitives start at
 // sorted position ~ref, count in cnt0 / (cnt1 & 0x3FFFFFFF). axis in the
-// top two bits of cnt1 (the parent's split axis, for near-first order).
+// top two bits of cnt1 (the parent's split axis, for near-first order);
+// axis code 3 marks the records of the leaf-split layout that subdivide one
+// large leaf of the reference's tree: child 0 (the lower positions) first.
 struct __align__(16) Node2 {
   float4 b0;   // c0 lo.x hi.x lo.y hi.y
   float4 b1;   // c1 lo.x hi.x lo.y hi.y
@@ -63,7 +65,8 @@ struct __align__(16) Node4 {
 };
 
 struct BvhView {
-  const Node2* nodes;
+  const Node2* nodes;    // the layout traversed (leaf-split by default)
+  const Node2* nodes_ref;  // the reference's leaves as they are (null once moved into a batch arena)
   const Node4* nodes4;   // null: binary traversal
   const float4* prims;   // 3 float4 per sorted primitive
   int empty;
@@ -72,8 +75,21 @@ struct BvhView {
   float root_lo[3], root_hi[3];
   uint32_t max_depth;
   uint32_t n_prims, n_int;  // bounds for the index guards in traversal
+  uint32_t n_ref_int;       // records of nodes_ref
+  uint32_t ref_depth;       // depth of the reference's tree (max_depth adds the split levels)
   uint32_t n_wide;          // wide node count (index guard)
   uint32_t wide_depth;      // levels of the wide tree
 };
+
+// The same tree traversed over the reference's leaves as they are (the
+// statistics kernel counts box and primitive tests of this layout).
+inline BvhView reference_leaves_view(BvhView v) {
+  if (v.nodes_ref) {
+    v.nodes = v.nodes_ref;
+    v.n_int = v.n_ref_int;
+    v.max_depth = v.ref_depth;
+  }
+  return v;
+}
 
 }  // namespace wpbr
