@@ -165,34 +165,22 @@ def test_chunked_host_collide_matches_device_collide(W, ctx):
     ctx.check_device_errors()
 
 
-def _grid_desc(W, n=48):
-    """A flat n x n grid of unit quads (2 triangles each) on the plane y = 0
-    at integer x, z, and one triangle below it (so the centroid bounds are not
-    flat in y). A ray straight down onto a quad's diagonal hits both of its
-    triangles at exactly the same t."""
+def _mesh_desc(pos, idx):
+    """A scene descriptor of one triangle mesh (world-space positions, one
+    material, no lights); returns it and the arrays it points into."""
     import ctypes as C
 
     from woodenpbrengine_gb300 import _abi as A
 
-    xs, zs = np.meshgrid(np.arange(n + 1, dtype=np.float32), np.arange(n + 1, dtype=np.float32), indexing="ij")
-    grid = np.stack([xs.ravel() - n / 2, np.zeros((n + 1) ** 2, np.float32), zs.ravel() - n / 2], 1)
-    below = np.array([[-1.0, -10.0, -1.0], [1.0, -10.0, -1.0], [0.0, -10.0, 1.0]], np.float32)
-    pos = np.ascontiguousarray(np.concatenate([grid, below]), np.float32).ravel()
-    v = lambda i, j: i * (n + 1) + j  # noqa: E731
-    tris = []
-    for i in range(n):
-        for j in range(n):
-            tris += [v(i, j), v(i + 1, j), v(i + 1, j + 1), v(i, j), v(i + 1, j + 1), v(i, j + 1)]
-    m = (n + 1) ** 2
-    tris += [m, m + 1, m + 2]
-    idx = np.asarray(tris, np.uint32)
+    pos = np.ascontiguousarray(pos, np.float32).ravel()
+    idx = np.ascontiguousarray(idx, np.uint32).ravel()
     nt = idx.size // 3
     mesh = A.Mesh(0, nt, 0, 0)
     mat = A.Material()
     mat.type = 0
     mat.alpha_x = mat.alpha_y = 0.2
     d = A.SceneDesc()
-    d.n_vertices = m + 3
+    d.n_vertices = pos.size // 3
     d.positions = pos.ctypes.data_as(C.POINTER(C.c_float))
     d.n_triangles = nt
     d.indices = idx.ctypes.data_as(C.POINTER(C.c_uint32))
@@ -207,8 +195,25 @@ def _grid_desc(W, n=48):
     d.camera.near_z, d.camera.far_z = 0.1, 1000.0
     d.camera.screen[:] = [-1.0, -1.0, 1.0, 1.0]
     d.camera.res_x = d.camera.res_y = 8
-    keep = (pos, idx, mesh, mat)
-    return C.pointer(d), keep
+    return C.pointer(d), (pos, idx, mesh, mat)
+
+
+def _grid_desc(W, n=48):
+    """A flat n x n grid of unit quads (2 triangles each) on the plane y = 0
+    at integer x, z, and one triangle below it (so the centroid bounds are not
+    flat in y). A ray straight down onto a quad's diagonal hits both of its
+    triangles at exactly the same t."""
+    xs, zs = np.meshgrid(np.arange(n + 1, dtype=np.float32), np.arange(n + 1, dtype=np.float32), indexing="ij")
+    grid = np.stack([xs.ravel() - n / 2, np.zeros((n + 1) ** 2, np.float32), zs.ravel() - n / 2], 1)
+    below = np.array([[-1.0, -10.0, -1.0], [1.0, -10.0, -1.0], [0.0, -10.0, 1.0]], np.float32)
+    v = lambda i, j: i * (n + 1) + j  # noqa: E731
+    tris = []
+    for i in range(n):
+        for j in range(n):
+            tris += [v(i, j), v(i + 1, j), v(i + 1, j + 1), v(i, j), v(i + 1, j + 1), v(i, j + 1)]
+    m = (n + 1) ** 2
+    tris += [m, m + 1, m + 2]
+    return _mesh_desc(np.concatenate([grid, below]), np.asarray(tris, np.uint32))
 
 
 @pytest.mark.parametrize("full_sort", [False, True])
@@ -282,3 +287,41 @@ def test_leaf_split_layout_matches_reference_leaves(W, O, ctx, config, level, re
     _check(hs, oracle.trace(rays, mode=0))
     _check(as_, oracle.trace(rays, mode=2))
     ctx.check_device_errors()
+
+
+@pytest.mark.parametrize("k", [100, 5000])
+def test_leaf_split_of_one_large_leaf(W, O, ctx, k):
+    # k triangles far smaller than one Morton cell share a code, so the
+    # reference's tree holds them in one leaf: 100 become a range tree of
+    # depth 4, 5000 exceed the split's bound (4096) and stay one leaf. Rays
+    # aimed at the cluster hit many of them; closest and any-hit records must
+    # equal the oracle's either way.
+    rng = np.random.default_rng(k)
+    tris = rng.normal(size=(k, 3, 3)).astype(np.float32)
+    tris -= tris.mean(1, keepdims=True)
+    tris *= (0.004 / np.abs(tris).max(axis=(1, 2)))[:, None, None]
+    tris += np.float32(0.5)
+    far = np.array([[[1000, 1000, 1000], [1001, 1000, 1000], [1000, 1001, 1000]]], np.float32)
+    desc, keep = _mesh_desc(np.concatenate([tris, far]).reshape(-1, 3), np.arange(3 * (k + 1), dtype=np.uint32))
+    ctx.set_quirks(0)
+    ctx.upload(desc)
+    ctx.build()
+    oracle = O.OracleScene(desc)
+    nodes = oracle.bvh_export()["nodes"].reshape(-1, 3)
+    assert nodes[nodes[:, 1] > 0, 1].max() == k
+    n = 4000
+    dirs = rng.normal(size=(n, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, :3] = 0.5 - 2.0 * dirs + rng.uniform(-0.002, 0.002, (n, 3))
+    rays[:, 4:7] = dirs
+    rays[:, 7] = np.inf
+    ho, ha_o = oracle.trace(rays, mode=0), oracle.trace(rays, mode=2)
+    assert np.mean(ho[:, 1].view(np.uint32) != 0xFFFFFFFF) > 0.9
+    for mode in (W.TRAVERSAL_BINARY, W.TRAVERSAL_BINARY_FULL_LEAVES):
+        ctx.set_traversal(mode)
+        _check(ctx.collide(rays), ho)
+        _check(ctx.collide(rays, mode=W.TRACE_ANY), ha_o)
+    ctx.set_traversal(W.TRAVERSAL_BINARY)
+    ctx.check_device_errors()
+    del keep
