@@ -485,10 +485,25 @@ __global__ void k_seg_init(uint32_t nseg, uint32_t* benc, uint32_t* cenc, uint32
 }
 
 // Bounds and centroid bounds per segment: warp-segmented reduce over the
-// contiguous runs, one atomic per run and warp.
+// contiguous runs, then per block: the runs of the block's first kSegSlots
+// segments meet in shared memory and leave one global atomic per block and
+// segment (near the root a level has a handful of segments, and one atomic per
+// warp on the same words serialised in L2); runs of later segments go to
+// global memory directly. Min and max are order-independent, so the bounds
+// are exact whatever the grouping.
+constexpr int kSegSlots = 16;
 __global__ void k_seg_reduce(SahArgs A, const uint32_t* cur, const uint32_t* pos_seg, uint32_t* benc, uint32_t* cenc) {
+  __shared__ uint32_t s_min;
+  __shared__ uint32_t s_red[kSegSlots * 12];  // slot * 12 + (lo xyz, hi xyz, centroid lo xyz, centroid hi xyz)
+  if (threadIdx.x == 0) s_min = kNone;
+  for (int k = threadIdx.x; k < kSegSlots * 12; k += blockDim.x) s_red[k] = ((k % 12) / 3) % 2 == 0 ? 0xFFFFFFFFu : 0u;
+  __syncthreads();
   uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t s = (p < A.T) ? pos_seg[p] : kNone;
+  uint32_t wmin = __reduce_min_sync(0xFFFFFFFFu, s);
+  if (lane_id() == 0 && wmin != kNone) atomicMin(&s_min, wmin);
+  __syncthreads();
+  const uint32_t smin = s_min;
   uint32_t e[12];
   if (s != kNone) {
     V3 lo, hi;
@@ -516,10 +531,33 @@ __global__ void k_seg_reduce(SahArgs A, const uint32_t* cur, const uint32_t* pos
   uint32_t sp = __shfl_up_sync(0xFFFFFFFFu, s, 1);
   bool head = (s != kNone) && (lane == 0 || sp != s);
   if (head) {
-    for (int k = 0; k < 3; ++k) atomicMin(&benc[s * 6 + k], e[k]);
-    for (int k = 3; k < 6; ++k) atomicMax(&benc[s * 6 + k], e[k]);
-    for (int k = 0; k < 3; ++k) atomicMin(&cenc[s * 6 + k], e[6 + k]);
-    for (int k = 0; k < 3; ++k) atomicMax(&cenc[s * 6 + 3 + k], e[9 + k]);
+    uint32_t slot = s - smin;  // s >= smin for every s != kNone of the block
+    if (slot < (uint32_t)kSegSlots) {
+      uint32_t* r = s_red + slot * 12;
+      for (int k = 0; k < 3; ++k) atomicMin(&r[k], e[k]);
+      for (int k = 3; k < 6; ++k) atomicMax(&r[k], e[k]);
+      for (int k = 6; k < 9; ++k) atomicMin(&r[k], e[k]);
+      for (int k = 9; k < 12; ++k) atomicMax(&r[k], e[k]);
+    } else {
+      for (int k = 0; k < 3; ++k) atomicMin(&benc[s * 6 + k], e[k]);
+      for (int k = 3; k < 6; ++k) atomicMax(&benc[s * 6 + k], e[k]);
+      for (int k = 0; k < 3; ++k) atomicMin(&cenc[s * 6 + k], e[6 + k]);
+      for (int k = 0; k < 3; ++k) atomicMax(&cenc[s * 6 + 3 + k], e[9 + k]);
+    }
+  }
+  __syncthreads();
+  if (smin == kNone) return;
+  for (int k = threadIdx.x; k < kSegSlots * 12; k += blockDim.x) {
+    uint32_t v = s_red[k];
+    int j = k % 12;
+    bool is_min = (j / 3) % 2 == 0;
+    if (v == (is_min ? 0xFFFFFFFFu : 0u)) continue;  // no run of this slot's segment in the block
+    uint32_t seg = smin + (uint32_t)(k / 12);
+    uint32_t* dst = (j < 6 ? benc : cenc) + seg * 6 + (j < 6 ? j : j - 6);
+    if (is_min)
+      atomicMin(dst, v);
+    else
+      atomicMax(dst, v);
   }
 }
 
@@ -529,7 +567,6 @@ __device__ __forceinline__ Bounds dec_bounds(const uint32_t* e) {
 
 // Bucket of every root (JobBuildUpperSAH, SLBVH.cpp:484-502) and per-bucket
 // counts / bounds, pre-aggregated in shared memory per block.
-constexpr int kSegSlots = 16;
 __global__ void k_seg_bucket(SahArgs A, const uint32_t* cur, const uint32_t* pos_seg, const uint32_t* cenc,
                              uint32_t* bucket, uint32_t* bcnt, uint32_t* bkenc) {
   __shared__ uint32_t s_min;
@@ -649,23 +686,40 @@ __global__ void k_seg_split(uint32_t nseg, SegLevel L, const uint32_t* benc, con
   uint32_t ln = mid - a, rn = b - mid + 1;
   uint32_t cl = kNone, cr = kNone;
   uint32_t nl = 0;
-  if (ln >= 2) {
-    cl = atomicAdd(&counters[0], 1u);
+  // node ids and small-segment slots: one atomic per warp (the ids only
+  // label nodes; the flattened tree follows the child links). Deep levels
+  // have ~10^4 segments, whose per-child atomics on one counter serialised.
+  const uint32_t act = __activemask(), lt = act & ((1u << lane_id()) - 1u);
+  const uint32_t leader = __ffs(act) - 1;
+  const bool l_node = ln >= 2, r_node = rn >= 2;
+  const bool l_small = l_node && ln <= kSmallSeg, r_small = r_node && rn <= kSmallSeg;
+  uint32_t bl = __ballot_sync(act, l_node), br = __ballot_sync(act, r_node);
+  uint32_t sl = __ballot_sync(act, l_small), sr = __ballot_sync(act, r_small);
+  uint32_t node_base = 0, small_base = 0;
+  if (lane_id() == leader) {
+    uint32_t nn = __popc(bl) + __popc(br), ns = __popc(sl) + __popc(sr);
+    if (nn) node_base = atomicAdd(&counters[0], nn);
+    if (ns) small_base = atomicAdd(&counters[2], ns);
+  }
+  node_base = __shfl_sync(act, node_base, leader) + __popc(bl & lt) + __popc(br & lt);
+  small_base = __shfl_sync(act, small_base, leader) + __popc(sl & lt) + __popc(sr & lt);
+  if (l_node) {
+    cl = node_base++;
     child0[me] = N2 + cl;
     parent[N2 + cl] = (me << 1) | 0u;
-    if (ln > kSmallSeg) ++nl;
+    if (!l_small) ++nl;
     else {
-      uint32_t q = atomicAdd(&counters[2], 1u);
+      uint32_t q = small_base++;
       small_start[q] = a; small_end[q] = mid - 1; small_node[q] = cl;
     }
   }
-  if (rn >= 2) {
-    cr = atomicAdd(&counters[0], 1u);
+  if (r_node) {
+    cr = node_base;
     child1[me] = N2 + cr;
     parent[N2 + cr] = (me << 1) | 1u;
-    if (rn > kSmallSeg) ++nl;
+    if (!r_small) ++nl;
     else {
-      uint32_t q = atomicAdd(&counters[2], 1u);
+      uint32_t q = small_base;
       small_start[q] = mid; small_end[q] = b; small_node[q] = cr;
     }
   }
