@@ -27,9 +27,11 @@ constexpr int kPersistBlock = 128;
 #define WPBR_REFILL_MIN 20
 #endif
 // Resident blocks per SM each traversal instantiation is compiled for
-// (Sink::kMinBlocks): the collide kernels (full hit records) run best at 10
-// (48 registers, some spilled; 1.4% faster than 8 on the 8.4M-ray
-// microbenchmark, 11-12 the same, 14 19% slower); the render passes' kernels
+// (Sink::kMinBlocks): the collide kernels (full hit records) run best at 12
+// (40 registers, some spilled; on the 8.4M-ray microbenchmark 10 blocks at 48
+// registers were 1.4% faster than 8, and with the packed stack entries 12
+// blocks 0.8% faster than 10 for closest hit, 0.4% slower for any-hit; 9
+// blocks 1.2% slower; 14 were 19% slower before); the render passes' kernels
 // (camera rays generated in the source, prim-id sinks) at 8 (64 registers),
 // where 10 cost them 5%.
 
@@ -625,7 +627,7 @@ struct BufferSrc {
   }
 };
 #ifndef WPBR_COLLIDE_BLOCKS
-#define WPBR_COLLIDE_BLOCKS 10
+#define WPBR_COLLIDE_BLOCKS 12
 #endif
 struct HitSink4 {
   static constexpr int kMinBlocks = WPBR_COLLIDE_BLOCKS;
