@@ -620,24 +620,48 @@ __global__ void k_seg_bucket(SahArgs A, const uint32_t* cur, const uint32_t* pos
 }
 
 // Cost of the 11 candidate splits, SLBVH.cpp:504-538, and the child layout.
+// The two sides of split i are the unions of the non-empty buckets 0..i and
+// i+1..11 (JobBuildUpperSAH's two inner loops): the right sides are built
+// once as suffix unions and the left sides accumulated in bucket order, 24
+// bucket decodes instead of 132 (one thread decides a segment; near the root
+// that chain of dependent loads was the level's longest kernel). Min and max
+// of finite coordinates do not depend on the grouping; only a zero's sign
+// could, which no area or cost sees.
 __device__ void sah_decide(const uint32_t* bcnt, const uint32_t* bkenc, const Bounds& bounds, uint32_t n, int* best_out,
                            uint32_t* k_out) {
   float barea_ = barea(bounds);
   float cost_min = 0.0f;
   int best = 0;
+  uint32_t c[12];
+#pragma unroll
+  for (int j = 0; j < 12; ++j) c[j] = bcnt[j];
+  Bounds suf[11];
+  uint32_t nsuf[11];
+  suf[10] = bempty();
+  nsuf[10] = 0;
+  if (c[11]) {
+    suf[10] = bunion(suf[10], dec_bounds(bkenc + 11 * 6));
+    nsuf[10] = c[11];
+  }
+#pragma unroll
+  for (int i = 9; i >= 0; --i) {
+    suf[i] = suf[i + 1];
+    nsuf[i] = nsuf[i + 1];
+    if (c[i + 1]) {
+      suf[i] = bunion(suf[i], dec_bounds(bkenc + (i + 1) * 6));
+      nsuf[i] += c[i + 1];
+    }
+  }
+  Bounds b0 = bempty();
+  uint32_t n0 = 0;
+#pragma unroll
   for (int i = 0; i < 11; ++i) {
-    Bounds b0 = bempty(), b1 = bempty();
-    uint32_t n0 = 0, n1 = 0;
-    for (int j = 0; j <= i; ++j)
-      if (bcnt[j]) {
-        b0 = bunion(b0, dec_bounds(bkenc + j * 6));
-        n0 += bcnt[j];
-      }
-    for (int j = i + 1; j < 12; ++j)
-      if (bcnt[j]) {
-        b1 = bunion(b1, dec_bounds(bkenc + j * 6));
-        n1 += bcnt[j];
-      }
+    if (c[i]) {
+      b0 = bunion(b0, dec_bounds(bkenc + i * 6));
+      n0 += c[i];
+    }
+    const Bounds& b1 = suf[i];
+    uint32_t n1 = nsuf[i];
     float l = (n0 == 0) ? 0.0f : (float)n0 * barea(b0);
     float r = (n1 == 0) ? 0.0f : (float)n1 * barea(b1);
     float cost = (float)(0.125 + (double)((l + r) / barea_));
@@ -647,7 +671,7 @@ __device__ void sah_decide(const uint32_t* bcnt, const uint32_t* bkenc, const Bo
     }
   }
   uint32_t k = 0;
-  for (int j = 0; j <= best; ++j) k += bcnt[j];
+  for (int j = 0; j <= best; ++j) k += c[j];
   (void)n;
   *best_out = best;
   *k_out = k;
