@@ -830,6 +830,17 @@ __global__ void k_seg_children(uint32_t nseg, SegLevel L, const uint32_t* seg_mi
 // one per lane (the same float operations as sah_decide) and the sequential
 // first-minimum rule by a lexicographic (cost, split) reduction. The
 // segment's n - 2 new SAH node ids are reserved with one atomic.
+__device__ __forceinline__ Bounds shfl_bounds_up(const Bounds& b, uint32_t o) {
+  const uint32_t F = 0xFFFFFFFFu;
+  return Bounds{V3{__shfl_up_sync(F, b.lo.x, o), __shfl_up_sync(F, b.lo.y, o), __shfl_up_sync(F, b.lo.z, o)},
+                V3{__shfl_up_sync(F, b.hi.x, o), __shfl_up_sync(F, b.hi.y, o), __shfl_up_sync(F, b.hi.z, o)}};
+}
+__device__ __forceinline__ Bounds shfl_bounds_down(const Bounds& b, uint32_t o) {
+  const uint32_t F = 0xFFFFFFFFu;
+  return Bounds{V3{__shfl_down_sync(F, b.lo.x, o), __shfl_down_sync(F, b.lo.y, o), __shfl_down_sync(F, b.lo.z, o)},
+                V3{__shfl_down_sync(F, b.hi.x, o), __shfl_down_sync(F, b.hi.y, o), __shfl_down_sync(F, b.hi.z, o)}};
+}
+
 __global__ void k_small_sah(SahArgs A, uint32_t nsmall, const uint32_t* sm_start, const uint32_t* sm_end,
                             const uint32_t* sm_node, uint32_t* cur, uint32_t* counters, uint32_t* sah_axis,
                             float4* nb_lo, float4* nb_hi, uint32_t* child0, uint32_t* child1, uint32_t* parent,
@@ -909,22 +920,36 @@ __global__ void k_small_sah(SahArgs A, uint32_t nsmall, const uint32_t* sm_start
       atomicMax(be + 5, fenc(hi.z));
     }
     __syncwarp();
-    // SAH cost of split `lane` (sah_decide's loop body)
+    // SAH cost of split `lane` (sah_decide's loop body). Lane j < 12 holds
+    // bucket j; shuffle scans give each lane the union and count of buckets
+    // 0..j (prefix) and j..11 (suffix), so split i takes lane i's prefix and
+    // lane i+1's suffix. Min and max of finite coordinates do not depend on
+    // the grouping (only a zero's sign could, which no area or cost sees).
+    uint32_t cj = lane < 12 ? bcnt[lane] : 0u;
+    Bounds pre = (lane < 12 && cj) ? dec_bounds(benc + lane * 6) : bempty();
+    Bounds suf = pre;
+    uint32_t npre = cj, nsuf = cj;
+#pragma unroll
+    for (uint32_t o = 1; o < 16; o <<= 1) {
+      Bounds u = shfl_bounds_up(pre, o);
+      uint32_t nu = __shfl_up_sync(FULL, npre, o);
+      Bounds v = shfl_bounds_down(suf, o);
+      uint32_t nv = __shfl_down_sync(FULL, nsuf, o);
+      if (lane >= o) {
+        pre = bunion(u, pre);
+        npre += nu;
+      }
+      if (lane + o < 12) {
+        suf = bunion(suf, v);
+        nsuf += nv;
+      }
+    }
+    Bounds b1 = shfl_bounds_down(suf, 1);
+    uint32_t n1 = __shfl_down_sync(FULL, nsuf, 1);
     float cost = 0.0f;
     if (lane < 11) {
-      Bounds b0 = bempty(), b1 = bempty();
-      uint32_t n0 = 0, n1 = 0;
-      for (int j = 0; j < 12; ++j) {
-        uint32_t cj = bcnt[j];
-        if (!cj) continue;
-        if (j <= (int)lane) {
-          b0 = bunion(b0, dec_bounds(benc + j * 6));
-          n0 += cj;
-        } else {
-          b1 = bunion(b1, dec_bounds(benc + j * 6));
-          n1 += cj;
-        }
-      }
+      const Bounds& b0 = pre;
+      uint32_t n0 = npre;
       float l = (n0 == 0) ? 0.0f : (float)n0 * barea(b0);
       float r = (n1 == 0) ? 0.0f : (float)n1 * barea(b1);
       cost = (float)(0.125 + (double)((l + r) / barea(bb)));
