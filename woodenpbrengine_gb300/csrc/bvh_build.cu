@@ -43,43 +43,46 @@ constexpr int kB = 256;
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
 
 // ---------------------------------------------------------------------------
-// exclusive scan (tile scan + recursive block sums)
+// exclusive scan (tile scan + recursive block sums) of 32-bit counts, or of
+// 64-bit words that pack two 32-bit counts whose sums stay below 2^32 (no
+// carry crosses the halves, so one scan gives both prefix sums)
 // ---------------------------------------------------------------------------
-__global__ void k_scan_tile(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* bsum) {
-  __shared__ uint32_t sh[kScanTile];
-  __shared__ uint32_t wsum[kScanBlock / 32];
+template <class V>
+__global__ void k_scan_tile(const V* in, V* out, uint32_t n, V* bsum) {
+  __shared__ V sh[kScanTile];
+  __shared__ V wsum[kScanBlock / 32];
   const uint32_t base = blockIdx.x * kScanTile;
   for (int k = 0; k < kScanItems; ++k) {
     uint32_t i = base + threadIdx.x + k * kScanBlock;
-    sh[threadIdx.x + k * kScanBlock] = i < n ? in[i] : 0u;
+    sh[threadIdx.x + k * kScanBlock] = i < n ? in[i] : V(0);
   }
   __syncthreads();
-  uint32_t v[kScanItems];
-  uint32_t sum = 0;
+  V v[kScanItems];
+  V sum = 0;
   for (int k = 0; k < kScanItems; ++k) {
     v[k] = sh[threadIdx.x * kScanItems + k];
     sum += v[k];
   }
   uint32_t lane = lane_id(), w = threadIdx.x >> 5;
-  uint32_t x = sum;
+  V x = sum;
   for (int o = 1; o < 32; o <<= 1) {
-    uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    V y = __shfl_up_sync(0xFFFFFFFFu, x, o);
     if (lane >= (uint32_t)o) x += y;
   }
   if (lane == 31) wsum[w] = x;
   __syncthreads();
   if (w == 0) {
-    uint32_t ws = lane < kScanBlock / 32 ? wsum[lane] : 0u;
-    uint32_t inc = ws;
+    V ws = lane < kScanBlock / 32 ? wsum[lane] : V(0);
+    V inc = ws;
     for (int o = 1; o < 32; o <<= 1) {
-      uint32_t y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+      V y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
       if (lane >= (uint32_t)o) inc += y;
     }
     if (lane < kScanBlock / 32) wsum[lane] = inc - ws;
   }
   __syncthreads();
-  uint32_t run = (x - sum) + wsum[w];
-  uint32_t total_before = run;
+  V run = (x - sum) + wsum[w];
+  V total_before = run;
   for (int k = 0; k < kScanItems; ++k) {
     sh[threadIdx.x * kScanItems + k] = run;
     run += v[k];
@@ -92,9 +95,64 @@ __global__ void k_scan_tile(const uint32_t* in, uint32_t* out, uint32_t n, uint3
   if (threadIdx.x == kScanBlock - 1 && bsum) bsum[blockIdx.x] = total_before + sum;
 }
 
-__global__ void k_scan_add(uint32_t* out, uint32_t n, const uint32_t* boff) {
+template <class V>
+__global__ void k_scan_add(V* out, uint32_t n, const V* boff) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] += boff[i / kScanTile];
+}
+
+template <class V>
+cudaError_t scan_exclusive_t(const V* in, V* out, uint32_t n, V* tmp, size_t tmp_n, cudaStream_t s) {
+  struct Lvl {
+    const V* in;
+    V* out;
+    uint32_t n;
+    V* sums;
+  };
+  Lvl lv[8];
+  int L = 0;
+  size_t off = 0;
+  const V* cin = in;
+  V* cout = out;
+  uint32_t m = n;
+  while (true) {
+    uint32_t nb = div_up(m, kScanTile);
+    V* sums = nb > 1 ? tmp + off : nullptr;
+    lv[L++] = Lvl{cin, cout, m, sums};
+    if (nb <= 1) break;
+    off += nb + 1;
+    if (off > tmp_n) return cudaErrorInvalidValue;
+    cin = sums;
+    cout = sums;
+    m = nb;
+    if (L >= 8) return cudaErrorInvalidValue;
+  }
+  for (int i = 0; i < L; ++i) {
+    uint32_t nb = div_up(lv[i].n, kScanTile);
+    k_scan_tile<V><<<nb, kScanBlock, 0, s>>>(lv[i].in, lv[i].out, lv[i].n, lv[i].sums);
+  }
+  for (int i = L - 2; i >= 0; --i) {
+    k_scan_add<V><<<div_up(lv[i].n, 256), 256, 0, s>>>(lv[i].out, lv[i].n, lv[i].sums);
+  }
+  return cudaGetLastError();
+}
+
+size_t scan_tmp_need(uint32_t n) {
+  size_t need = 0;
+  for (uint32_t m = n; m > (uint32_t)kScanTile; m = div_up(m, kScanTile)) need += div_up(m, kScanTile) + 1;
+  return need;
+}
+
+// Both partition counts of the SAH levels in one pass (two 32-bit prefix sums
+// packed in 64-bit words); tmp holds the block sums as 32-bit words, two each.
+cudaError_t scan_exclusive_pair(const unsigned long long* in, unsigned long long* out, uint32_t n,
+                                DevBuf<uint32_t>& tmp, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  size_t need = scan_tmp_need(n);
+  cudaError_t e = tmp.ensure(2 * need + 16);
+  if (e != cudaSuccess) return e;
+  unsigned long long* t64 = reinterpret_cast<unsigned long long*>(tmp.p);
+  return scan_exclusive_t(in, out, n, t64, need + 8, s);
 }
 
 }  // namespace
@@ -111,41 +169,10 @@ uint32_t scan_launches(uint32_t n) {
 cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, DevBuf<uint32_t>& tmp, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   // tmp layout: level-1 sums, level-2 sums, ...
-  size_t need = 0;
-  for (uint32_t m = n; m > (uint32_t)kScanTile; m = div_up(m, kScanTile)) need += div_up(m, kScanTile) + 1;
+  size_t need = scan_tmp_need(n);
   cudaError_t e = tmp.ensure(need + 8);
   if (e != cudaSuccess) return e;
-  struct Lvl {
-    const uint32_t* in;
-    uint32_t* out;
-    uint32_t n;
-    uint32_t* sums;
-  };
-  Lvl lv[8];
-  int L = 0;
-  size_t off = 0;
-  const uint32_t* cin = in;
-  uint32_t* cout = out;
-  uint32_t m = n;
-  while (true) {
-    uint32_t nb = div_up(m, kScanTile);
-    uint32_t* sums = nb > 1 ? tmp.p + off : nullptr;
-    lv[L++] = Lvl{cin, cout, m, sums};
-    if (nb <= 1) break;
-    off += nb + 1;
-    cin = sums;
-    cout = sums;
-    m = nb;
-    if (L >= 8) return cudaErrorInvalidValue;
-  }
-  for (int i = 0; i < L; ++i) {
-    uint32_t nb = div_up(lv[i].n, kScanTile);
-    k_scan_tile<<<nb, kScanBlock, 0, s>>>(lv[i].in, lv[i].out, lv[i].n, lv[i].sums);
-  }
-  for (int i = L - 2; i >= 0; --i) {
-    k_scan_add<<<div_up(lv[i].n, 256), 256, 0, s>>>(lv[i].out, lv[i].n, lv[i].sums);
-  }
-  return cudaGetLastError();
+  return scan_exclusive_t(in, out, n, tmp.p, need + 8, s);
 }
 
 namespace {
@@ -755,8 +782,12 @@ __global__ void k_seg_split(uint32_t nseg, SegLevel L, const uint32_t* benc, con
 // std::partition(first, last, bucket <= best) — the two-pointer swap scheme:
 // the r-th "false" element left of the partition point (from the left) trades
 // places with the r-th "true" element right of it (from the right).
+// The two flags of a position packed as (true << 32) | false, and their
+// prefix sums packed the same way (one scan for both).
+__device__ __forceinline__ uint32_t lo32(unsigned long long v) { return (uint32_t)(v & 0xFFFFFFFFull); }
+__device__ __forceinline__ uint32_t hi32(unsigned long long v) { return (uint32_t)(v >> 32); }
 __global__ void k_part_flags(uint32_t T, const uint32_t* pos_seg, const uint32_t* bucket, const uint32_t* seg_k,
-                             const uint32_t* seg_best, uint32_t* fl, uint32_t* tr) {
+                             const uint32_t* seg_best, unsigned long long* ft) {
   uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= T) return;
   uint32_t s = pos_seg[p];
@@ -767,30 +798,31 @@ __global__ void k_part_flags(uint32_t T, const uint32_t* pos_seg, const uint32_t
     f = (p < sp && !pred) ? 1u : 0u;
     t = (p >= sp && pred) ? 1u : 0u;
   }
-  fl[p] = f;
-  tr[p] = t;
+  ft[p] = ((unsigned long long)t << 32) | f;
 }
-__global__ void k_part_ranks(uint32_t T, SegLevel L, const uint32_t* pos_seg, const uint32_t* fl, const uint32_t* tr,
-                             const uint32_t* fscan, const uint32_t* tscan, uint32_t* posF, uint32_t* posT) {
+__global__ void k_part_ranks(uint32_t T, SegLevel L, const uint32_t* pos_seg, const unsigned long long* ft,
+                             const unsigned long long* ftscan, uint32_t* posF, uint32_t* posT) {
   uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= T) return;
   uint32_t s = pos_seg[p];
   if (s == kNone) return;
   uint32_t a = L.start[s], b = L.end[s];
-  if (fl[p]) posF[a + (fscan[p] - fscan[a])] = p;
-  if (tr[p]) posT[a + ((tscan[b] + tr[b]) - (tscan[p] + 1u))] = p;
+  unsigned long long fp = ft[p], sp = ftscan[p];
+  if (lo32(fp)) posF[a + (lo32(sp) - lo32(ftscan[a]))] = p;
+  if (hi32(fp)) posT[a + ((hi32(ftscan[b]) + hi32(ft[b])) - (hi32(sp) + 1u))] = p;
 }
-__global__ void k_part_scatter(uint32_t T, SegLevel L, const uint32_t* pos_seg, const uint32_t* fl, const uint32_t* tr,
-                               const uint32_t* fscan, const uint32_t* tscan, const uint32_t* posF,
-                               const uint32_t* posT, const uint32_t* cur, uint32_t* nxt) {
+__global__ void k_part_scatter(uint32_t T, SegLevel L, const uint32_t* pos_seg, const unsigned long long* ft,
+                               const unsigned long long* ftscan, const uint32_t* posF, const uint32_t* posT,
+                               const uint32_t* cur, uint32_t* nxt) {
   uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= T) return;
   uint32_t s = pos_seg[p];
   uint32_t dst = p;
   if (s != kNone) {
     uint32_t a = L.start[s], b = L.end[s];
-    if (fl[p]) dst = posT[a + (fscan[p] - fscan[a])];
-    else if (tr[p]) dst = posF[a + ((tscan[b] + tr[b]) - (tscan[p] + 1u))];
+    unsigned long long fp = ft[p], sp = ftscan[p];
+    if (lo32(fp)) dst = posT[a + (lo32(sp) - lo32(ftscan[a]))];
+    else if (hi32(fp)) dst = posF[a + ((hi32(ftscan[b]) + hi32(ft[b])) - (hi32(sp) + 1u))];
   }
   nxt[dst] = cur[p];
 }
@@ -1632,9 +1664,8 @@ wpbr_status bvh_build(wpbr_ctx* ctx) {
     WPBR_CUDA(B.pos_seg.ensure(T));
     WPBR_CUDA(B.bucket.ensure(T));
     WPBR_CUDA(B.fl.ensure(T));
-    WPBR_CUDA(B.tr.ensure(T));
-    WPBR_CUDA(B.fscan.ensure(T));
-    WPBR_CUDA(B.tscan.ensure(T));
+    WPBR_CUDA(B.ft.ensure(T));
+    WPBR_CUDA(B.ftscan.ensure(T));
     WPBR_CUDA(B.posF.ensure(T));
     WPBR_CUDA(B.posT.ensure(T));
     WPBR_CUDA(B.sah_axis.ensure(T));
@@ -1704,12 +1735,11 @@ wpbr_status bvh_build(wpbr_ctx* ctx) {
           nlarge, L, B.seg_benc.p, B.seg_cenc.p, B.seg_bucket_cnt.p, B.seg_bucket_enc.p, B.seg_k.p, B.seg_dim.p,
           B.seg_mid.p, B.seg_a.p, B.seg_b.p, B.counters.p, B.sah_axis.p, B.nb_lo.p, B.nb_hi.p, B.child0.p,
           B.child1.p, B.parent.p, B.flags.p, B.small_start.p, B.small_end.p, B.small_node.p, N2);
-      k_part_flags<<<gT, kB, 0, st>>>(T, B.pos_seg.p, B.bucket.p, B.seg_k.p, B.seg_dim.p, B.fl.p, B.tr.p);
-      WPBR_CUDA(scan_exclusive(B.fl.p, B.fscan.p, T, B.scan_tmp, st));
-      WPBR_CUDA(scan_exclusive(B.tr.p, B.tscan.p, T, B.scan_tmp, st));
-      k_part_ranks<<<gT, kB, 0, st>>>(T, L, B.pos_seg.p, B.fl.p, B.tr.p, B.fscan.p, B.tscan.p, B.posF.p, B.posT.p);
-      k_part_scatter<<<gT, kB, 0, st>>>(T, L, B.pos_seg.p, B.fl.p, B.tr.p, B.fscan.p, B.tscan.p, B.posF.p,
-                                        B.posT.p, B.cur.p, B.nxt.p);
+      k_part_flags<<<gT, kB, 0, st>>>(T, B.pos_seg.p, B.bucket.p, B.seg_k.p, B.seg_dim.p, B.ft.p);
+      WPBR_CUDA(scan_exclusive_pair(B.ft.p, B.ftscan.p, T, B.scan_tmp, st));
+      k_part_ranks<<<gT, kB, 0, st>>>(T, L, B.pos_seg.p, B.ft.p, B.ftscan.p, B.posF.p, B.posT.p);
+      k_part_scatter<<<gT, kB, 0, st>>>(T, L, B.pos_seg.p, B.ft.p, B.ftscan.p, B.posF.p, B.posT.p, B.cur.p,
+                                        B.nxt.p);
       std::swap(B.cur, B.nxt);
       // next level list (ordered by start)
       uint32_t last_cnt = 0, last_sc = 0;

@@ -137,8 +137,8 @@ void bvh_release(wpbr_ctx* ctx, bool keep_traversal) {
   B.flags.release(); B.tid.release(); B.tstart.release(); B.tsize.release(); B.troot.release();
   B.rng_lo.release(); B.rng_hi.release(); B.child0.release(); B.child1.release(); B.parent.release();
   B.visits.release(); B.size.release(); B.nb_lo.release(); B.nb_hi.release();
-  B.cur.release(); B.nxt.release(); B.pos_seg.release(); B.bucket.release(); B.fl.release(); B.tr.release();
-  B.fscan.release(); B.tscan.release(); B.posF.release(); B.posT.release();
+  B.cur.release(); B.nxt.release(); B.pos_seg.release(); B.bucket.release(); B.fl.release();
+  B.ft.release(); B.ftscan.release(); B.posF.release(); B.posT.release();
   B.seg_a.release(); B.seg_b.release(); B.seg_start.release(); B.seg_end.release(); B.seg_node.release();
   B.seg_k.release(); B.seg_mid.release(); B.seg_dim.release(); B.seg_benc.release(); B.seg_cenc.release();
   B.seg_bucket_cnt.release(); B.seg_bucket_enc.release(); B.small_start.release(); B.small_end.release();

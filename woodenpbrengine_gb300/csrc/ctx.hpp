@@ -52,7 +52,8 @@ struct BvhState {
   DevBuf<uint32_t> parent, visits, size;            // size 2N+T
   DevBuf<float4> nb_lo, nb_hi;                      // node bounds, unified ids
   // SAH
-  DevBuf<uint32_t> cur, nxt, pos_seg, bucket, fl, tr, fscan, tscan, posF, posT;
+  DevBuf<uint32_t> cur, nxt, pos_seg, bucket, fl, posF, posT;
+  DevBuf<unsigned long long> ft, ftscan;  // partition flags (true << 32 | false) and their prefix sums
   DevBuf<uint32_t> seg_a, seg_b, seg_start, seg_end, seg_node, seg_k, seg_mid, seg_dim;
   DevBuf<uint32_t> seg_benc, seg_cenc, seg_bucket_cnt, seg_bucket_enc;
   DevBuf<uint32_t> small_start, small_end, small_node, counters;
