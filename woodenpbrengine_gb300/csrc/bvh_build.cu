@@ -857,11 +857,7 @@ __global__ void k_seg_children(uint32_t nseg, SegLevel L, const uint32_t* seg_mi
   }
 }
 
-// Segments of 2..32 roots: the whole SAH recursion inside one warp. Bounds
-// by warp reductions, buckets by shared-memory atomics, the 11 split costs
-// one per lane (the same float operations as sah_decide) and the sequential
-// first-minimum rule by a lexicographic (cost, split) reduction. The
-// segment's n - 2 new SAH node ids are reserved with one atomic.
+// Bounds of another lane (shuffled component by component).
 __device__ __forceinline__ Bounds shfl_bounds_up(const Bounds& b, uint32_t o) {
   const uint32_t F = 0xFFFFFFFFu;
   return Bounds{V3{__shfl_up_sync(F, b.lo.x, o), __shfl_up_sync(F, b.lo.y, o), __shfl_up_sync(F, b.lo.z, o)},
@@ -873,6 +869,11 @@ __device__ __forceinline__ Bounds shfl_bounds_down(const Bounds& b, uint32_t o) 
                 V3{__shfl_down_sync(F, b.hi.x, o), __shfl_down_sync(F, b.hi.y, o), __shfl_down_sync(F, b.hi.z, o)}};
 }
 
+// Segments of 2..32 roots: the whole SAH recursion inside one warp. Bounds
+// by warp reductions, buckets by shared-memory atomics, the 11 split costs
+// one per lane (sah_decide's float operations on the same boxes) and the sequential
+// first-minimum rule by a lexicographic (cost, split) reduction. The
+// segment's n - 2 new SAH node ids are reserved with one atomic.
 __global__ void k_small_sah(SahArgs A, uint32_t nsmall, const uint32_t* sm_start, const uint32_t* sm_end,
                             const uint32_t* sm_node, uint32_t* cur, uint32_t* counters, uint32_t* sah_axis,
                             float4* nb_lo, float4* nb_hi, uint32_t* child0, uint32_t* child1, uint32_t* parent,
