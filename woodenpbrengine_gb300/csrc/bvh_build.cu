@@ -483,10 +483,14 @@ __global__ void k_fill(uint32_t* p, uint32_t n, uint32_t v) {
 
 // Segment of every position (kNone outside the level's large segments): a
 // binary search over the segment starts, which are in ascending order.
-__global__ void k_pos_seg(uint32_t T, uint32_t nseg, const uint32_t* seg_start, const uint32_t* seg_end,
+// The SAH levels' kernels read the level's count of large segments from
+// device memory (nseg_p), so the host can queue a level before the previous
+// one has finished.
+__global__ void k_pos_seg(uint32_t T, const uint32_t* nseg_p, const uint32_t* seg_start, const uint32_t* seg_end,
                           uint32_t* pos_seg) {
   uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= T) return;
+  const uint32_t nseg = *nseg_p;
   uint32_t lo = 0, hi = nseg;
   while (lo < hi) {
     uint32_t mid = (lo + hi) >> 1;
@@ -498,9 +502,9 @@ __global__ void k_pos_seg(uint32_t T, uint32_t nseg, const uint32_t* seg_start, 
   pos_seg[p] = (lo > 0 && p <= __ldg(seg_end + lo - 1)) ? lo - 1 : kNone;
 }
 
-__global__ void k_seg_init(uint32_t nseg, uint32_t* benc, uint32_t* cenc, uint32_t* bcnt, uint32_t* bkenc) {
+__global__ void k_seg_init(const uint32_t* nseg_p, uint32_t* benc, uint32_t* cenc, uint32_t* bcnt, uint32_t* bkenc) {
   uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nseg) return;
+  if (s >= *nseg_p) return;
   for (int k = 0; k < 6; ++k) {
     benc[s * 6 + k] = k < 3 ? 0xFFFFFFFFu : 0u;
     cenc[s * 6 + k] = k < 3 ? 0xFFFFFFFFu : 0u;
@@ -710,14 +714,17 @@ struct SegLevel {
   const uint32_t* node;
 };
 
-__global__ void k_seg_split(uint32_t nseg, SegLevel L, const uint32_t* benc, const uint32_t* cenc,
+__global__ void k_seg_split(const uint32_t* nseg_p, uint32_t nscan, SegLevel L, const uint32_t* benc, const uint32_t* cenc,
                             const uint32_t* bcnt, const uint32_t* bkenc, uint32_t* seg_k, uint32_t* seg_best,
                             uint32_t* seg_mid, uint32_t* seg_cl, uint32_t* seg_cr, uint32_t* counters,
                             uint32_t* sah_axis, float4* nb_lo, float4* nb_hi, uint32_t* child0, uint32_t* child1,
                             uint32_t* parent, uint32_t* nlarge_cnt, uint32_t* small_start, uint32_t* small_end,
                             uint32_t* small_node, uint32_t N2) {
   uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nseg) return;
+  if (s >= *nseg_p) {
+    if (s < nscan) nlarge_cnt[s] = 0u;  // the scan of the counts runs over nscan entries
+    return;
+  }
   uint32_t a = L.start[s], b = L.end[s], nd = L.node[s];
   uint32_t n = b - a + 1;
   Bounds bb = dec_bounds(benc + s * 6);
@@ -828,12 +835,16 @@ __global__ void k_part_scatter(uint32_t T, SegLevel L, const uint32_t* pos_seg, 
 }
 
 // Size-1 children (a single treelet root) and the next level's large segments.
-__global__ void k_seg_children(uint32_t nseg, SegLevel L, const uint32_t* seg_mid, const uint32_t* seg_cl,
-                               const uint32_t* seg_cr, const uint32_t* nlarge_scan, const uint32_t* cur,
-                               const uint32_t* troot, uint32_t* child0, uint32_t* child1, uint32_t* parent,
-                               uint32_t* ns_start, uint32_t* ns_end, uint32_t* ns_node, uint32_t N2) {
+// nseg_next receives the next level's count: the exclusive scan's last entry
+// (nscan exceeds every level's count, so that entry's own count is 0).
+__global__ void k_seg_children(const uint32_t* nseg_p, uint32_t nscan, uint32_t* nseg_next, SegLevel L,
+                               const uint32_t* seg_mid, const uint32_t* seg_cl, const uint32_t* seg_cr,
+                               const uint32_t* nlarge_scan, const uint32_t* cur, const uint32_t* troot,
+                               uint32_t* child0, uint32_t* child1, uint32_t* parent, uint32_t* ns_start,
+                               uint32_t* ns_end, uint32_t* ns_node, uint32_t N2) {
   uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nseg) return;
+  if (s == 0) *nseg_next = nlarge_scan[nscan - 1];
+  if (s >= *nseg_p) return;
   uint32_t a = L.start[s], b = L.end[s], mid = seg_mid[s];
   uint32_t me = N2 + L.node[s];
   uint32_t ln = mid - a, rn = b - mid + 1;
@@ -1722,18 +1733,36 @@ wpbr_status bvh_build(wpbr_ctx* ctx) {
     }
     WPBR_CUDA(cudaMemcpyAsync(B.counters.p, h_counters, sizeof(h_counters), cudaMemcpyHostToDevice, st));
     const unsigned gT = div_up(T, kB);
+    const unsigned gS = div_up(maxseg, kB);
+    // Level counts live in two device words (this level's and the next's);
+    // each level's next count is also copied into a small pinned ring. Level
+    // L is queued as soon as level L - 2's copy shows that level L - 1 has
+    // large segments, so the GPU always has the next level queued instead of
+    // idling through a host round trip per level; the level after the last
+    // one is queued too and finds no segment.
+    WPBR_CUDA(B.nseg.ensure(2));
+    WPBR_CUDA(cudaMemcpyAsync(B.nseg.p, &nlarge, 4, cudaMemcpyHostToDevice, st));
+    if (!B.h_nseg) WPBR_CUDA(cudaMallocHost((void**)&B.h_nseg, sizeof(uint32_t) * BvhState::kLevelRing));
+    for (cudaEvent_t& ev : B.lev_ev)
+      if (!ev) WPBR_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     int level = 0;
-    while (nlarge > 0) {
-      if (++level > 100000) return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: SAH level limit");
+    while (nlarge > 0) {  // level 0 has a large segment; later levels end on the ring's counts
+      if (level >= 2) {
+        const int r = (level - 2) % BvhState::kLevelRing;
+        WPBR_CUDA(cudaEventSynchronize(B.lev_ev[r]));
+        if (B.h_nseg[r] == 0) break;  // level - 1 had no large segment
+      }
+      if (level >= 100000) return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: SAH level limit");
+      const uint32_t* nseg = B.nseg.p + (level & 1);
+      uint32_t* nseg_next = B.nseg.p + ((level + 1) & 1);
       SegLevel L{L_start, L_end, L_node};
-      k_pos_seg<<<gT, kB, 0, st>>>(T, nlarge, L_start, L_end, B.pos_seg.p);
-      k_seg_init<<<div_up(nlarge, kB), kB, 0, st>>>(nlarge, B.seg_benc.p, B.seg_cenc.p, B.seg_bucket_cnt.p,
-                                                    B.seg_bucket_enc.p);
+      k_pos_seg<<<gT, kB, 0, st>>>(T, nseg, L_start, L_end, B.pos_seg.p);
+      k_seg_init<<<gS, kB, 0, st>>>(nseg, B.seg_benc.p, B.seg_cenc.p, B.seg_bucket_cnt.p, B.seg_bucket_enc.p);
       k_seg_reduce<<<gT, kB, 0, st>>>(A, B.cur.p, B.pos_seg.p, B.seg_benc.p, B.seg_cenc.p);
       k_seg_bucket<<<gT, kB, 0, st>>>(A, B.cur.p, B.pos_seg.p, B.seg_cenc.p, B.bucket.p, B.seg_bucket_cnt.p,
                                       B.seg_bucket_enc.p);
-      k_seg_split<<<div_up(nlarge, kB), kB, 0, st>>>(
-          nlarge, L, B.seg_benc.p, B.seg_cenc.p, B.seg_bucket_cnt.p, B.seg_bucket_enc.p, B.seg_k.p, B.seg_dim.p,
+      k_seg_split<<<gS, kB, 0, st>>>(
+          nseg, maxseg, L, B.seg_benc.p, B.seg_cenc.p, B.seg_bucket_cnt.p, B.seg_bucket_enc.p, B.seg_k.p, B.seg_dim.p,
           B.seg_mid.p, B.seg_a.p, B.seg_b.p, B.counters.p, B.sah_axis.p, B.nb_lo.p, B.nb_hi.p, B.child0.p,
           B.child1.p, B.parent.p, B.flags.p, B.small_start.p, B.small_end.p, B.small_node.p, N2);
       k_part_flags<<<gT, kB, 0, st>>>(T, B.pos_seg.p, B.bucket.p, B.seg_k.p, B.seg_dim.p, B.ft.p);
@@ -1743,15 +1772,14 @@ wpbr_status bvh_build(wpbr_ctx* ctx) {
                                         B.nxt.p);
       std::swap(B.cur, B.nxt);
       // next level list (ordered by start)
-      uint32_t last_cnt = 0, last_sc = 0;
-      WPBR_CUDA(cudaMemcpyAsync(&last_cnt, B.flags.p + nlarge - 1, 4, cudaMemcpyDeviceToHost, st));
-      WPBR_CUDA(scan_exclusive(B.flags.p, B.flags.p, nlarge, B.scan_tmp, st));
-      WPBR_CUDA(cudaMemcpyAsync(&last_sc, B.flags.p + nlarge - 1, 4, cudaMemcpyDeviceToHost, st));
-      k_seg_children<<<div_up(nlarge, kB), kB, 0, st>>>(nlarge, L, B.seg_mid.p, B.seg_a.p, B.seg_b.p, B.flags.p,
-                                                        B.cur.p, B.troot.p, B.child0.p, B.child1.p, B.parent.p,
-                                                        Nx_start, Nx_end, Nx_node, N2);
-      WPBR_CUDA(cudaStreamSynchronize(st));
-      nlarge = last_cnt + last_sc;
+      WPBR_CUDA(scan_exclusive(B.flags.p, B.flags.p, maxseg, B.scan_tmp, st));
+      k_seg_children<<<gS, kB, 0, st>>>(nseg, maxseg, nseg_next, L, B.seg_mid.p, B.seg_a.p, B.seg_b.p, B.flags.p,
+                                        B.cur.p, B.troot.p, B.child0.p, B.child1.p, B.parent.p, Nx_start, Nx_end,
+                                        Nx_node, N2);
+      const int r = level % BvhState::kLevelRing;
+      WPBR_CUDA(cudaMemcpyAsync(B.h_nseg + r, nseg_next, 4, cudaMemcpyDeviceToHost, st));
+      WPBR_CUDA(cudaEventRecord(B.lev_ev[r], st));
+      ++level;
       std::swap(L_start, Nx_start);
       std::swap(L_end, Nx_end);
       std::swap(L_node, Nx_node);

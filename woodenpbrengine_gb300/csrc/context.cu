@@ -142,7 +142,7 @@ void bvh_release(wpbr_ctx* ctx, bool keep_traversal) {
   B.seg_a.release(); B.seg_b.release(); B.seg_start.release(); B.seg_end.release(); B.seg_node.release();
   B.seg_k.release(); B.seg_mid.release(); B.seg_dim.release(); B.seg_benc.release(); B.seg_cenc.release();
   B.seg_bucket_cnt.release(); B.seg_bucket_enc.release(); B.small_start.release(); B.small_end.release();
-  B.small_node.release(); B.counters.release(); B.sah_axis.release(); B.lin_node.release();
+  B.small_node.release(); B.counters.release(); B.nseg.release(); B.sah_axis.release(); B.lin_node.release();
   B.lin_bounds.release(); B.is_int.release(); B.int_index.release(); B.depth_max.release();
   B.int_kids.release(); B.int_slot.release();
   B.wq_bin0.release(); B.wq_bin1.release(); B.wq_wide0.release(); B.wq_wide1.release();
@@ -203,6 +203,9 @@ WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
   ctx->marg_func.release(); ctx->marg_cdf.release(); ctx->marg_int.release(); ctx->env_lum.release();
   ctx->tex_texels.release(); ctx->tex_levels.release(); ctx->tex_info.release(); ctx->tex_gauss.release();
   bvh_release(ctx, false);
+  if (ctx->bvh.h_nseg) cudaFreeHost(ctx->bvh.h_nseg);
+  for (cudaEvent_t& ev : ctx->bvh.lev_ev)
+    if (ev) cudaEventDestroy(ev);
   RenderState& R = ctx->rs;
   R.acc.release(); R.hit_prim.release(); R.shadow_rays.release(); R.shadow_hit.release(); R.pstate.release();
   R.Lbuf.release(); R.pfilm.release(); R.pass_dev.release(); R.counters.release();

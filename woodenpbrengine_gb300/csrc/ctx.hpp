@@ -57,6 +57,10 @@ struct BvhState {
   DevBuf<uint32_t> seg_a, seg_b, seg_start, seg_end, seg_node, seg_k, seg_mid, seg_dim;
   DevBuf<uint32_t> seg_benc, seg_cenc, seg_bucket_cnt, seg_bucket_enc;
   DevBuf<uint32_t> small_start, small_end, small_node, counters;
+  DevBuf<uint32_t> nseg;  // large-segment counts of the current and the next SAH level
+  static constexpr int kLevelRing = 4;
+  uint32_t* h_nseg = nullptr;  // pinned copies of each level's next count (a ring)
+  cudaEvent_t lev_ev[kLevelRing] = {};
   DevBuf<uint32_t> sah_axis;
   // flattened tree (CSceneTreeLBVH) + traversal layout
   DevBuf<uint32_t> lin_node;  // M*3: offset, n_shapes, axis
