@@ -52,6 +52,8 @@ def parse():
                         "forward + backward, 8 batched scenes x 2 spp")
     p.add_argument("--profile-spectral", type=int, nargs=2, metavar=("W", "H"),
                    help="Sampled64 case for ncu: config 2 (level 8) at W x H, one 2-spp frame")
+    p.add_argument("--profile-build", action="store_true",
+                   help="LBVH build case for ncu: 8 builds of the 1,310,720-triangle mesh (3 warm-up, 5 timed)")
     return p.parse_args()
 
 
@@ -495,8 +497,37 @@ def run_spectral_profile_case(res):
     print(json.dumps({"profile_case": "Sampled64 config 2, %dx%d, 2 spp" % tuple(res)}))
 
 
+def run_build_profile_case():
+    """Eight LBVH builds of the 1,310,720-triangle microbenchmark mesh (three
+    warm-up builds, then five timed back to back on the context's stream)."""
+    from __graft_entry__ import build
+
+    build()
+    import woodenpbrengine_gb300 as W
+
+    g = W.SceneGen(1, 0, (64, 64), level=LEVEL)
+    ctx = W.Context(0)
+    ctx.upload(g.desc)
+    for _ in range(3):
+        ctx.build()
+    ctx.synchronize()
+    t = time.perf_counter()
+    for _ in range(5):
+        ctx.build()
+    ctx.synchronize()
+    ms = (time.perf_counter() - t) / 5 * 1e3
+    ctx.check_device_errors()
+    info = ctx.bvh_info()
+    ctx.close()
+    print(json.dumps({"profile_case": "LBVH build, %d triangles" % info["n_prims"], "ms_per_build": ms,
+                      "mprims_per_s": info["n_prims"] / ms / 1e3}))
+
+
 def main():
     args = parse()
+    if args.profile_build:
+        run_build_profile_case()
+        return
     if args.profile_spectral:
         run_spectral_profile_case(args.profile_spectral)
         return
