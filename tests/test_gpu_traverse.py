@@ -325,3 +325,12 @@ def test_leaf_split_of_one_large_leaf(W, O, ctx, k):
     ctx.set_traversal(W.TRAVERSAL_BINARY)
     ctx.check_device_errors()
     del keep
+
+
+def test_traversal_modes(W, ctx):
+    # three layouts; anything else is an invalid argument
+    for mode in (W.TRAVERSAL_BINARY, W.TRAVERSAL_WIDE, W.TRAVERSAL_BINARY_FULL_LEAVES):
+        ctx.set_traversal(mode)
+    with pytest.raises(W.WpbrError):
+        ctx.set_traversal(3)
+    ctx.set_traversal(W.TRAVERSAL_BINARY)
