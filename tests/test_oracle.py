@@ -48,6 +48,61 @@ def test_pruned_traversal_equals_faithful(W, O):
         assert np.array_equal(ha[:, 1].view(np.uint32) == 0xFFFFFFFF, hf[:, 1].view(np.uint32) == 0xFFFFFFFF)
 
 
+@pytest.mark.parametrize("full_sort", [False, True])
+def test_pruned_traversal_equals_faithful_on_exact_ties(W, O, full_sort):
+    # Rays straight down onto the diagonals of a flat grid's quads hit both
+    # triangles of the quad at exactly t = 5: the pruned traversal must pick
+    # the same one as the prune-free candidate list, and any-hit must find a
+    # hit exactly where the closest-hit does.
+    from scenes import grid_desc
+
+    desc, keep = grid_desc()
+    q = W.Q_FULL_MORTON_SORT if full_sort else 0
+    o = O.OracleScene(desc, q)
+    nodes = o.bvh_export()["nodes"].reshape(-1, 3)
+    assert nodes[nodes[:, 1] > 0, 1].max() == (18 if full_sort else 2)
+    rng = np.random.default_rng(3)
+    n = 20000
+    s = rng.choice([0.25, 0.5, 0.75], n).astype(np.float32)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0] = rng.integers(-24, 24, n) + s
+    rays[:, 2] = rng.integers(-24, 24, n) + s
+    rays[:, 1] = 5.0
+    rays[:, 5] = -1.0
+    rays[:, 7] = np.inf
+    hf = o.trace(rays, mode=0)
+    hp = o.trace(rays, mode=1)
+    assert np.all(hf[:, 0] == 5.0)
+    assert np.array_equal(hf.view(np.uint32), hp.view(np.uint32))
+    ha = o.trace(rays, mode=2)
+    assert np.array_equal(ha[:, 1].view(np.uint32) == 0xFFFFFFFF, hf[:, 1].view(np.uint32) == 0xFFFFFFFF)
+    del keep
+
+
+def test_pruned_traversal_equals_faithful_in_one_large_leaf(W, O):
+    # 100 triangles sharing one Morton code form one leaf; rays through the
+    # cluster hit many of them
+    from scenes import cluster_desc
+
+    desc, keep = cluster_desc(100)
+    o = O.OracleScene(desc)
+    nodes = o.bvh_export()["nodes"].reshape(-1, 3)
+    assert nodes[nodes[:, 1] > 0, 1].max() == 100
+    rng = np.random.default_rng(5)
+    n = 5000
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, :3] = 0.5 - 2.0 * d + rng.uniform(-0.002, 0.002, (n, 3))
+    rays[:, 4:7] = d
+    rays[:, 7] = np.inf
+    hf = o.trace(rays, mode=0)
+    hp = o.trace(rays, mode=1)
+    assert np.mean(hf[:, 1].view(np.uint32) != 0xFFFFFFFF) > 0.9
+    assert np.array_equal(hf.view(np.uint32), hp.view(np.uint32))
+    del keep
+
+
 def check_tree(e):
     nodes = e["nodes"].reshape(-1, 3)
     nb = e["node_bounds"].reshape(-1, 6)
