@@ -6,7 +6,7 @@ the same published tables pbrt uses. Literals are copied digit for digit
 (double literals in float arrays, as the reference initialises them), so the
 float values are identical.
 
-    python -m woodenpbrengine_gb300.spectrum_data <path to SpectrumData.h>
+    python include/make_spectrum_data.py <path to SpectrumData.h>
 """
 import os
 import re
@@ -43,7 +43,7 @@ def parse(text):
 
 def render(tables):
     lines = [
-        "/* wpbr_spectrum_data.h — generated by woodenpbrengine_gb300/spectrum_data.py; do not edit.",
+        "/* wpbr_spectrum_data.h — generated by include/make_spectrum_data.py; do not edit.",
         " * Tabulated data of the 64-sample spectral representation: CIE 1931",
         " * colour matching functions (360-830 nm, 1 nm) and the RGB-to-spectrum",
         " * bases (Smits) for reflectances and illuminants, the data the reference's",
@@ -72,7 +72,7 @@ def render(tables):
 
 def main(argv):
     src = argv[1] if len(argv) > 1 else os.path.join("/root/reference", "WoodenPBREngine", "SpectrumData.h")
-    out = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "wpbr_spectrum_data.h")
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "wpbr_spectrum_data.h")
     with open(src) as f:
         text = f.read()
     with open(out, "w") as f:

@@ -68,19 +68,20 @@ WPBR_API wpbr_status wpbr_synchronize(wpbr_ctx* ctx);
  * are the same): BINARY (default) traverses the child-pair layout of the
  * reference's tree with every leaf of more than 8 (and at most 4096)
  * primitives subdivided into a small tree over ranges of its sorted
- * positions, visited in position order; BINARY_FULL_LEAVES the same layout with the reference's leaves as
- * they are; WIDE a four-wide collapse of the reference's tree, built by the
- * next wpbr_bvh_build after the mode is set. */
-enum wpbr_traversal { WPBR_TRAVERSAL_BINARY = 0, WPBR_TRAVERSAL_WIDE = 1, WPBR_TRAVERSAL_BINARY_FULL_LEAVES = 2 };
+ * positions, visited in position order; BINARY_FULL_LEAVES the same layout
+ * with the reference's leaves as they are. Value 1 (a four-wide collapse,
+ * slower on this GPU) is no longer accepted. */
+enum wpbr_traversal { WPBR_TRAVERSAL_BINARY = 0, WPBR_TRAVERSAL_BINARY_FULL_LEAVES = 2 };
 WPBR_API wpbr_status wpbr_set_traversal(wpbr_ctx* ctx, uint32_t mode);
 /* Spectral representation of the render passes. RGB (default) carries three
  * channels; SAMPLED64 is the reference's Spectrum (SampledSpectrum, 64 bins
  * over 400-700 nm, CSpectrum.h:8): scene RGB values become spectra (grey
  * values constant, others through the RGB-to-spectrum bases; environment
  * texels as illuminants), shading runs per bin, and the film accumulates
- * spectra that wpbr_film_read / wpbr_film_tonemap see through toRGB. A
- * parity mode: one thread per sample, no staged jobs, no adjoint. Takes
- * effect at the next wpbr_render_setup. */
+ * spectra that wpbr_film_read / wpbr_film_tonemap see through toRGB. Its
+ * wavefront shares the RGB pass's traversals and replaces spawn, finish and
+ * film with per-bin kernels; no staged jobs, no adjoint. Takes effect at the
+ * next wpbr_render_setup. */
 enum wpbr_spectrum { WPBR_SPECTRUM_RGB = 0, WPBR_SPECTRUM_SAMPLED64 = 1 };
 WPBR_API wpbr_status wpbr_set_spectrum(wpbr_ctx* ctx, uint32_t mode);
 /* Device error word (traversal limits etc.) since the last call; cleared. */
@@ -220,8 +221,11 @@ WPBR_API void wpbr_scenegen_destroy(wpbr_scenegen* g);
  * same permutation as wpbr_bvh_build. Device buffers in and out (no aliasing),
  * asynchronous on `stream`, no allocation: temporaries live in one file-scope
  * device array of WPBR_SORT_NOALLOC_MAX_KEYS keys (about 8.5 MB per GPU that
- * loads the library, held until exit). The first call on a device looks up the
- * array's address and should come before any stream capture. All calls share
+ * loads the library, held until exit). Every call made outside stream capture
+ * looks up the array's address in the current device context (so a device
+ * reset or a switch of context is picked up); a call on a capturing stream
+ * reuses the address last looked up on that device, so the first call on a
+ * device must come before any stream capture (it is refused otherwise). All calls share
  * the array; calls whose GPU work overlaps race. n above the maximum returns
  * WPBR_ERR_INVALID_ARG; wpbr_sort_morton_noalloc_error() says why. */
 #define WPBR_SORT_NOALLOC_MAX_KEYS (1u << 20)

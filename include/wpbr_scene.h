@@ -164,7 +164,15 @@ enum wpbr_quirk {
   /* Sampled64 mode only: xyzToRGB's stored matrix has 0.041556 where the
    * standard XYZ-to-sRGB matrix has 0.055648 (blue from X,
    * CoefficientSpectrum.h:17-19). Set to use the standard value. */
-  WPBR_Q_XYZ_MATRIX_FIX = 1u << 5
+  WPBR_Q_XYZ_MATRIX_FIX = 1u << 5,
+  /* Draw samples from the reference's per-pixel stratified arrays
+   * (CSSamplerStratified.cpp:8-90 over the sizes of CSFilm.cpp:22-23): 80
+   * shuffled 1D values stratified over [0, 1), and 272 shuffled 2D entries of
+   * which 256 are stratified with the 1/data.size() scale of :79 (all inside
+   * [0, 1/17)^2) and 16 are (0, 0). Pass p reads 1D position p and 2D
+   * positions 3p, 3p+1, 3p+2 (camera, light, BSDF) of the pixel's arrays.
+   * Default: stratification over the passes with the intended 1/n scale. */
+  WPBR_Q_REF_SAMPLER_ARRAYS = 1u << 6
 };
 
 #ifdef __cplusplus

@@ -23,6 +23,13 @@ _SIGS = {
     "orc_env_distribution": (None, [_VP, _FP, _FP, _FP, _FP]),
     "orc_render_pass": (None, [_VP] + [C.c_uint32] * 8 + [C.POINTER(A.PassRecord)]),
     "orc_render": (None, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, _FP, _FP]),
+    "orc_render_passes": (None, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _UP, _FP, _FP]),
+    # the oracle library's own copy of the synthetic scene generator
+    "wpbr_scenegen_create": (C.c_int, [C.c_uint32] * 6 + [C.POINTER(_VP)]),
+    "wpbr_scenegen_desc": (C.POINTER(A.SceneDesc), [_VP]),
+    "wpbr_scenegen_ray_count": (C.c_uint64, [_VP]),
+    "wpbr_scenegen_rays": (_FP, [_VP]),
+    "wpbr_scenegen_destroy": (None, [_VP]),
     "orc_fresnel_dielectric": (C.c_float, [C.c_float] * 3),
     "orc_fresnel_conductor": (C.c_float, [C.c_float] * 4),
     "orc_tr_d": (C.c_float, [C.c_float] * 5),
@@ -30,8 +37,8 @@ _SIGS = {
     "orc_mitchell": (C.c_float, [C.c_float]),
     "orc_left_shift3": (C.c_uint32, [C.c_uint32]),
     "orc_roughness_to_alpha": (C.c_float, [C.c_float]),
-    "orc_sample2d": (None, [C.c_uint32] * 6 + [_FP]),
-    "orc_sample1d": (C.c_float, [C.c_uint32] * 6),
+    "orc_sample2d": (None, [C.c_uint32] * 7 + [_FP]),
+    "orc_sample1d": (C.c_float, [C.c_uint32] * 7),
     "orc_philox": (None, [_UP, _UP, _UP]),
     "orc_fmath": (None, [C.c_int, _FP, _FP, _FP, C.c_uint64]),
     "orc_fmath_d": (None, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_uint64]),
@@ -65,6 +72,40 @@ def _fp(a):
 
 def _up(a):
     return a.ctypes.data_as(_UP) if a is not None else None
+
+
+class SceneGen:
+    """The seeded synthetic scenes and rays, generated by the oracle library's
+    copy of the scene generator (the same source and flags as the product's),
+    so a CPU-only process never loads the product library."""
+
+    def __init__(self, config, seed=0, res=(256, 256), level=0, rays=False):
+        self._h = _VP()
+        st = lib().wpbr_scenegen_create(config, seed, res[0], res[1], level, 1 if rays else 0, C.byref(self._h))
+        if st != 0:
+            raise RuntimeError("scenegen_create(config=%d) failed with status %d" % (config, st))
+
+    @property
+    def desc(self):
+        return lib().wpbr_scenegen_desc(self._h)
+
+    def rays(self):
+        n = lib().wpbr_scenegen_ray_count(self._h)
+        if n == 0:
+            return np.zeros((0, 8), np.float32)
+        p = lib().wpbr_scenegen_rays(self._h)
+        return np.ctypeslib.as_array(p, shape=(n * 8,)).reshape(n, 8).copy()
+
+    def close(self):
+        if self._h:
+            lib().wpbr_scenegen_destroy(self._h)
+            self._h = _VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class OracleScene:
@@ -159,6 +200,14 @@ class OracleScene:
         lib().orc_render(self._h, spp, seed, stream, _fp(L), _fp(w))
         return L.reshape(H, W, 3), w.reshape(H, W)
 
+    def render_passes(self, W, H, spp, passes, seed=0, stream=0):
+        """Film of the listed passes of an spp-pass render, accumulated in order."""
+        p = np.ascontiguousarray(passes, np.uint32)
+        L = np.zeros(W * H * 3, np.float32)
+        w = np.zeros(W * H, np.float32)
+        lib().orc_render_passes(self._h, spp, seed, stream, p.size, _up(p), _fp(L), _fp(w))
+        return L.reshape(H, W, 3), w.reshape(H, W)
+
 
 def spectral_tables():
     t = np.zeros(17 * 64, np.float32)
@@ -225,11 +274,11 @@ def fmath_d(name, x):
     return o
 
 
-def sample2d(seed, stream, spp, pixel, p, dim):
+def sample2d(seed, stream, spp, pixel, p, dim, arrays=0):
     u = np.zeros(2, np.float32)
-    lib().orc_sample2d(seed, stream, spp, pixel, p, dim, _fp(u))
+    lib().orc_sample2d(seed, stream, spp, pixel, p, dim, arrays, _fp(u))
     return u
 
 
-def sample1d(seed, stream, spp, pixel, p, dim):
-    return lib().orc_sample1d(seed, stream, spp, pixel, p, dim)
+def sample1d(seed, stream, spp, pixel, p, dim, arrays=0):
+    return lib().orc_sample1d(seed, stream, spp, pixel, p, dim, arrays)

@@ -1265,7 +1265,7 @@ void orc_env_distribution(void* h, float* cond_cdf, float* cond_int, float* marg
 void orc_render_pass(void* h, uint32_t pass, uint32_t spp, uint32_t seed, uint32_t stream, uint32_t x0, uint32_t y0,
                      uint32_t x1, uint32_t y1, wpbr_pass_record* rec) {
   Scene* s = (Scene*)h;
-  wpbr_rng::Stream rs{seed, stream, spp};
+  wpbr_rng::Stream rs{seed, stream, spp, (s->quirks & WPBR_Q_REF_SAMPLER_ARRAYS) ? 1u : 0u};
   uint32_t w = x1 - x0;
   long long n = (long long)w * (y1 - y0);
 #pragma omp parallel for schedule(dynamic, 64)
@@ -1279,10 +1279,27 @@ void orc_render_pass(void* h, uint32_t pass, uint32_t spp, uint32_t seed, uint32
  * (acc_L [W*H*3], acc_w [W*H], zero-initialised by the caller). */
 void orc_render(void* h, uint32_t spp, uint32_t seed, uint32_t stream, float* acc_L, float* acc_w) {
   Scene* s = (Scene*)h;
-  wpbr_rng::Stream rs{seed, stream, spp};
+  wpbr_rng::Stream rs{seed, stream, spp, (s->quirks & WPBR_Q_REF_SAMPLER_ARRAYS) ? 1u : 0u};
   uint32_t W = s->cam.W, H = s->cam.H;
   std::vector<SampleOut> smp((size_t)W * H);
   for (uint32_t pass = 0; pass < spp; ++pass) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long long i = 0; i < (long long)W * H; ++i)
+      smp[i] = shade_sample(*s, rs, (uint32_t)(i % W), (uint32_t)(i / W), pass, nullptr, 0);
+    film_splat(*s, smp, acc_L, acc_w);
+  }
+}
+
+/* The passes listed in `passes` (in that order) of an spp-pass render,
+ * accumulated into the film arrays as orc_render accumulates every pass. */
+void orc_render_passes(void* h, uint32_t spp, uint32_t seed, uint32_t stream, uint32_t n_passes,
+                       const uint32_t* passes, float* acc_L, float* acc_w) {
+  Scene* s = (Scene*)h;
+  wpbr_rng::Stream rs{seed, stream, spp, (s->quirks & WPBR_Q_REF_SAMPLER_ARRAYS) ? 1u : 0u};
+  uint32_t W = s->cam.W, H = s->cam.H;
+  std::vector<SampleOut> smp((size_t)W * H);
+  for (uint32_t k = 0; k < n_passes; ++k) {
+    uint32_t pass = passes[k];
 #pragma omp parallel for schedule(dynamic, 64)
     for (long long i = 0; i < (long long)W * H; ++i)
       smp[i] = shade_sample(*s, rs, (uint32_t)(i % W), (uint32_t)(i / W), pass, nullptr, 0);
@@ -1298,8 +1315,9 @@ float orc_power_heuristic(float f, float g) { return power_heuristic(f, g); }
 float orc_mitchell(float x) { return mitchell1(x); }
 uint32_t orc_left_shift3(uint32_t x) { return left_shift3(x); }
 float orc_roughness_to_alpha(float r) { return roughness_to_alpha(r); }
-void orc_sample2d(uint32_t seed, uint32_t stream, uint32_t spp, uint32_t pixel, uint32_t pass, uint32_t dim, float* u) {
-  wpbr_rng::Stream rs{seed, stream, spp};
+void orc_sample2d(uint32_t seed, uint32_t stream, uint32_t spp, uint32_t pixel, uint32_t pass, uint32_t dim,
+                  uint32_t arrays, float* u) {
+  wpbr_rng::Stream rs{seed, stream, spp, arrays};
   wpbr_rng::sample2d(rs, pixel, pass, dim, &u[0], &u[1]);
 }
 void orc_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) { wpbr_rng::philox4x32_10(ctr, key, out); }
@@ -1321,8 +1339,9 @@ void orc_fmath(int fn, const float* x, const float* y, float* out, uint64_t n) {
 void orc_fmath_d(int fn, const double* x, double* out, uint64_t n) {
   for (uint64_t i = 0; i < n; ++i) out[i] = fn == 0 ? sin_d(x[i]) : cos_d(x[i]);
 }
-float orc_sample1d(uint32_t seed, uint32_t stream, uint32_t spp, uint32_t pixel, uint32_t pass, uint32_t dim) {
-  wpbr_rng::Stream rs{seed, stream, spp};
+float orc_sample1d(uint32_t seed, uint32_t stream, uint32_t spp, uint32_t pixel, uint32_t pass, uint32_t dim,
+                   uint32_t arrays) {
+  wpbr_rng::Stream rs{seed, stream, spp, arrays};
   return wpbr_rng::sample1d(rs, pixel, pass, dim);
 }
 /* The FP64 frozen-direction estimator: sampling parameters are the scene's

@@ -161,3 +161,46 @@ def test_textured_scene_generation(W):
         assert not np.array_equal(a, texels(d3, i))
     rough = texels(d, 1).reshape(64, 64, 3)[..., 0]
     assert 1e-6 < rough.min() and rough.max() <= 1e-2
+
+
+def _desc_bytes(desc):
+    """Every array and struct a scene description points to, as raw bytes."""
+    d = desc.contents
+    out = [bytes(d.camera)]
+
+    def arr(ptr, n, ctype):
+        if n == 0 or not ptr:
+            return b""
+        return bytes((ctype * n).from_address(C.addressof(ptr.contents)))
+
+    out.append(arr(d.spheres, d.n_spheres, type(d.spheres.contents) if d.n_spheres else C.c_uint8))
+    for name in ("positions", "normals", "tangents", "uvs"):
+        p = getattr(d, name)
+        k = 2 if name == "uvs" else 3
+        out.append(arr(p, d.n_vertices * k, C.c_float) if p else b"")
+    out.append(arr(d.indices, 3 * d.n_triangles, C.c_uint32))
+    for name, n in (("meshes", d.n_meshes), ("materials", d.n_materials), ("lights", d.n_lights)):
+        p = getattr(d, name)
+        out.append(arr(p, n, type(p.contents)) if n else b"")
+    if d.envmap:
+        e = d.envmap.contents
+        out.append(bytes(e.light_to_world) + bytes(e.world_to_light))
+        out.append(arr(e.rgb, 3 * e.width * e.height, C.c_float))
+    for i in range(d.n_textures):
+        t = d.textures[i]
+        out.append(arr(t.rgb, 3 * t.width * t.height, C.c_float))
+    return out
+
+
+@pytest.mark.parametrize("config,level,res,rays", [
+    (0, 0, (256, 256), False), (1, 4, (256, 256), True), (2, 3, (64, 36), False), (3, 13, (1024, 2000000), False),
+    (3, 2, (128, 20000), False), (4, 1, (64, 64), False), (5, 0, (48, 32), False)])
+def test_oracle_copy_of_scene_generator_is_identical(W, O, config, level, res, rays):
+    # the CPU baseline and the reference arm of the benchmark take their inputs
+    # from the oracle library's copy of the generator: same source, same flags,
+    # byte-identical scenes and rays
+    a = W.SceneGen(config, 0, res, level=level, rays=rays)
+    b = O.SceneGen(config, 0, res, level=level, rays=rays)
+    assert _desc_bytes(a.desc) == _desc_bytes(b.desc)
+    if rays:
+        assert np.array_equal(a.rays().view(np.uint32), b.rays().view(np.uint32))

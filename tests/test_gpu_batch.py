@@ -73,7 +73,7 @@ def test_batch_matches_single_scenes_and_oracle(W, O, singles):
         assert info["n_scenes"] == N_SCENES and info["spp"] == SPP
         assert info["total_prims"] == sum(g.desc.contents.n_triangles + g.desc.contents.n_spheres for g in gens)
         assert info["total_pixels"] == sum(g.desc.contents.camera.res_x * g.desc.contents.camera.res_y for g in gens)
-        # Node2 (64 B) and Node4 (128 B) per interior node + 48 B per primitive, 256-byte aligned blocks
+        # Node2 (64 B) per record (interior nodes + leaf-split records) + 48 B per primitive, 256-byte aligned blocks
         assert 48 * info["total_prims"] <= info["arena_bytes"] <= 240 * info["total_prims"] + 768 * N_SCENES
         b.render()
         b.check_device_errors()
@@ -85,6 +85,35 @@ def test_batch_matches_single_scenes_and_oracle(W, O, singles):
         L, w = films[k]
         assert np.array_equal(_bits(w), _bits(wo))
         assert _same_nan_aware(L, Lo)
+
+
+def test_batch_at_full_scene_sizes_matches_oracle(W, O):
+    # scenes of the batched set at their specified sizes: scene 3 (1,310,720
+    # triangles, 1024x1024 film), scene 29 (26,800 spheres, 1024x1024),
+    # scene 21 (47,620 spheres, 512x512) and scene 6 (20,480 triangles,
+    # 256x256), 2 passes each, every film against the oracle
+    picks = (3, 29, 21, 6)
+    gens = [W.SceneGen(3, seed=3, res=(1024, 2000000), level=k) for k in picks]
+    d3 = gens[0].desc.contents
+    assert d3.n_triangles == 1310720 and (d3.camera.res_x, d3.camera.res_y) == (1024, 1024)
+    with W.Batch(0) as b:
+        for k, g in enumerate(gens):
+            assert b.add(g.desc) == k
+        b.build()
+        b.render_setup(SPP, seed=SEED, first_stream=FIRST_STREAM)
+        b.render()
+        b.check_device_errors()
+        for k, (g, pick) in enumerate(zip(gens, picks)):
+            cam = g.desc.contents.camera
+            Lb, wb = b.film(k)
+            Lo, wo = O.OracleScene(g.desc).render(cam.res_x, cam.res_y, SPP, SEED, FIRST_STREAM + k)
+            assert np.array_equal(_bits(wb), _bits(wo)), pick
+            assert _same_nan_aware(Lb, Lo), pick
+            # per-pixel radiance within 1e-4 mean / 1e-3 max relative (finite pixels)
+            rg, ro = Lb / wb[..., None], Lo / wo[..., None]
+            fin = np.isfinite(ro) & np.isfinite(rg)
+            rel = np.abs(rg[fin] - ro[fin]) / np.maximum(np.abs(ro[fin]), 1e-12)
+            assert rel.mean() <= 1e-4 and rel.max() <= 1e-3, pick
 
 
 @pytest.mark.parametrize("rpb", [0, 4096, 256, 7])

@@ -70,12 +70,12 @@ def test_degenerate_rays_and_quirk(W, O, ctx):
 
 
 @pytest.mark.parametrize("config,level,res", [(1, 6, (128, 128)), (0, 0, (64, 64)), (2, 4, (64, 36))])
-def test_wide_and_binary_traversals_agree(W, O, ctx, config, level, res):
-    # the four-wide layout is collapsed from the same binary tree and visits
-    # leaves in the binary near-first order: identical hits, ties included
+def test_split_and_full_leaf_traversals_agree(W, O, ctx, config, level, res):
+    # the leaf-split layout visits a split leaf's primitives in their sorted
+    # order: identical hits to the reference's leaves as they are, ties included
     g = W.SceneGen(config, 0, res, level=level, rays=(config == 1))
     ctx.set_quirks(0)
-    ctx.set_traversal(W.TRAVERSAL_WIDE)
+    ctx.set_traversal(W.TRAVERSAL_BINARY_FULL_LEAVES)
     ctx.upload(g.desc)
     ctx.build()
     if config == 1:
@@ -273,9 +273,11 @@ def test_leaf_split_of_one_large_leaf(W, O, ctx, k):
 
 
 def test_traversal_modes(W, ctx):
-    # three layouts; anything else is an invalid argument
-    for mode in (W.TRAVERSAL_BINARY, W.TRAVERSAL_WIDE, W.TRAVERSAL_BINARY_FULL_LEAVES):
+    # two layouts; anything else (the retired four-wide value 1 included) is
+    # an invalid argument
+    for mode in (W.TRAVERSAL_BINARY, W.TRAVERSAL_BINARY_FULL_LEAVES):
         ctx.set_traversal(mode)
-    with pytest.raises(W.WpbrError):
-        ctx.set_traversal(3)
+    for bad in (1, 3):
+        with pytest.raises(W.WpbrError):
+            ctx.set_traversal(bad)
     ctx.set_traversal(W.TRAVERSAL_BINARY)

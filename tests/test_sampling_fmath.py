@@ -26,6 +26,37 @@ def test_streams_are_stratified(O):
         assert strata == set(range(spp))
 
 
+def test_reference_sample_arrays(O):
+    # WPBR_Q_REF_SAMPLER_ARRAYS: reading every position of a pixel's arrays
+    # returns each element of the reference's fill exactly once
+    # (CSSamplerStratified.cpp:28-39, 68-87 with the sizes of CSFilm.cpp:22-23)
+    inv1, inv2 = np.float32(1.0 / 80), np.float32(1.0 / 272)
+    for pixel in (0, 5, 99999):
+        v1 = np.array([O.sample1d(7, 0, 64, pixel, p, 1, arrays=1) for p in range(80)], np.float32)
+        strata = np.floor(v1 * 80).astype(int)
+        assert sorted(strata) == list(range(80))           # one value per stratum
+        assert not np.array_equal(strata, np.arange(80))   # shuffled
+        # element s = (s + u) * float(1/80): u recovered in [0, 1)
+        u = v1 / inv1 - strata
+        assert (u >= -1e-4).all() and (u < 1 + 1e-4).all()
+        # 2D: pass p reads positions 3p (camera, dim 0), 3p+1 (light, 2), 3p+2 (BSDF, 3)
+        pairs = []
+        for p in range(91):
+            for dim in (0, 2, 3):
+                if len(pairs) < 272:
+                    pairs.append(O.sample2d(7, 0, 64, pixel, p, dim, arrays=1))
+        pairs = np.array(pairs, np.float32)
+        assert (pairs < 1.0 / 17 + 1e-7).all()             # the 1/data.size() scale
+        zeros = np.all(pairs == 0, axis=1)
+        assert zeros.sum() == 16                           # 272 - 16*16 never-written pairs
+        cells = {(int(np.floor(a / inv2)), int(np.floor(b / inv2))) for a, b in pairs[~zeros]}
+        assert cells == {(i, j) for i in range(16) for j in range(16)}
+        # positions wrap after the array (pass 91 reads position 273 = 1)
+        assert np.array_equal(O.sample2d(7, 0, 64, pixel, 91, 0, arrays=1), pairs[1])
+    # off by default
+    assert O.sample1d(7, 0, 64, 3, 0, 1) != O.sample1d(7, 0, 64, 3, 0, 1, arrays=1)
+
+
 def _ulp(ref32):
     r = np.abs(ref32.astype(np.float32))
     return (np.nextafter(r, np.float32(np.inf)) - r).astype(np.float64)

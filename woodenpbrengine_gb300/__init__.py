@@ -18,9 +18,10 @@ LIB_PATH = os.path.join(_HERE, "libwpbr_gpu.so")
 
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TRAVERSAL_LIMIT, ERR_NOT_BUILT, ERR_NO_DEVICE = range(7)
 TRACE_CLOSEST, TRACE_ANY = 0, 1
-TRAVERSAL_BINARY, TRAVERSAL_WIDE, TRAVERSAL_BINARY_FULL_LEAVES = 0, 1, 2
+TRAVERSAL_BINARY, TRAVERSAL_BINARY_FULL_LEAVES = 0, 2
 SPECTRUM_RGB, SPECTRUM_SAMPLED64 = 0, 1
 Q_XYZ_MATRIX_FIX = 32
+Q_REF_SAMPLER_ARRAYS = 64
 Q_TRI_PERMUTATION_BUG, Q_ENV_LI_SAMPLE_FIX, Q_SPHERE_PDF_FIX, Q_ENV_DISTRIB_INDEX_BUG, Q_FULL_MORTON_SORT = (
     1, 2, 4, 8, 16)
 MAT_CONDUCTOR, MAT_DIELECTRIC, MAT_SPECULAR = 0, 1, 2

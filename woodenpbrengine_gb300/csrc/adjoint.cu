@@ -559,7 +559,7 @@ PassCtx adj_pass_ctx(wpbr_ctx* ctx) {
   PassCtx P;
   P.S = scene_view(ctx);
   P.Bv = render_traversal_view(ctx);
-  P.rs = wpbr_rng::Stream{ctx->adj.seed, ctx->adj.stream, ctx->adj.spp};
+  P.rs = wpbr_rng::Stream{ctx->adj.seed, ctx->adj.stream, ctx->adj.spp, (ctx->quirks & WPBR_Q_REF_SAMPLER_ARRAYS) ? 1u : 0u};
   P.W = ctx->adj.W;
   P.H = ctx->adj.H;
   P.err = ctx->d_err.p;

@@ -2,8 +2,7 @@
 //
 // A batch owns one wpbr_ctx per scene (scene buffers, per-pixel render state,
 // film) and one pooled device arena holding every scene's traversal layout
-// (Node2 array, Node4 array and primitive records, each block 256-byte
-// aligned). A sample pass of all scenes is one CUDA graph: a fork event on the
+// (Node2 array and primitive records, each block 256-byte aligned). A sample pass of all scenes is one CUDA graph: a fork event on the
 // batch stream, one branch per scene with the five kernels of the fused pass
 // (render_pass_launch) on that scene's stream, and a join back. All branches
 // read the pass index from one device word, so a pass costs one 4-byte copy and
@@ -88,7 +87,7 @@ void apply_depth(wpbr_batch* b, uint32_t rpb) {
 }
 
 // Captures one pass of every scene as a fork/join graph on the batch stream.
-wpbr_status capture(wpbr_batch* b) {
+wpbr_status capture_graph(wpbr_batch* b) {
   drop_graph(b);
   cudaGraph_t g = nullptr;
   BATCH_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -117,6 +116,15 @@ wpbr_status capture(wpbr_batch* b) {
   if (e2 != cudaSuccess) return bcuda(b, e2, "batch graph capture");
   if (!b->graph) return berr(b, WPBR_ERR_CUDA, "batch graph capture produced no graph");
   return WPBR_OK;
+}
+
+// A failed capture leaves no graph, so the batch stops being ready: later
+// render calls return WPBR_ERR_NOT_BUILT until wpbr_batch_render_setup
+// succeeds again, instead of launching a null graph.
+wpbr_status capture(wpbr_batch* b) {
+  wpbr_status st = capture_graph(b);
+  if (st != WPBR_OK) b->ready = false;
+  return st;
 }
 
 wpbr_status launch_pass(wpbr_batch* b, uint32_t pass) {
@@ -284,7 +292,7 @@ WPBR_API wpbr_status wpbr_batch_build(wpbr_batch* b) {
   if (b->scenes.empty()) return berr(b, WPBR_ERR_INVALID_ARG, "batch_build: no scenes");
   cudaSetDevice(b->device);
   // build one scene at a time; each frees its build scratch before the next
-  std::vector<uint64_t> off_nodes(b->scenes.size()), off_wide(b->scenes.size()), off_prims(b->scenes.size());
+  std::vector<uint64_t> off_nodes(b->scenes.size()), off_prims(b->scenes.size());
   uint64_t total = 0, prims = 0;
   auto block = [&total](uint64_t bytes) {
     uint64_t at = total;
@@ -298,7 +306,6 @@ WPBR_API wpbr_status wpbr_batch_build(wpbr_batch* b) {
     bvh_release(c, true);
     const BvhView& v = c->bvh.view;
     off_nodes[k] = block(v.empty ? 0 : (uint64_t)v.n_int * sizeof(Node2));
-    off_wide[k] = block(v.nodes4 ? (uint64_t)v.n_wide * sizeof(Node4) : 0);
     off_prims[k] = block(v.empty ? 0 : (uint64_t)3 * v.n_prims * sizeof(float4));
     prims += c->N;
   }
@@ -308,14 +315,10 @@ WPBR_API wpbr_status wpbr_batch_build(wpbr_batch* b) {
     wpbr_ctx* c = b->scenes[k];
     BvhView& v = c->bvh.view;
     Node2* nd = (Node2*)(b->arena.p + off_nodes[k]);
-    Node4* wd = (Node4*)(b->arena.p + off_wide[k]);
     float4* pd = (float4*)(b->arena.p + off_prims[k]);
     if (!v.empty) {
       if (v.n_int)
         BATCH_CUDA(cudaMemcpyAsync(nd, v.nodes, (size_t)v.n_int * sizeof(Node2), cudaMemcpyDeviceToDevice,
-                                   c->stream));
-      if (v.nodes4)
-        BATCH_CUDA(cudaMemcpyAsync(wd, v.nodes4, (size_t)v.n_wide * sizeof(Node4), cudaMemcpyDeviceToDevice,
                                    c->stream));
       BATCH_CUDA(cudaMemcpyAsync(pd, v.prims, (size_t)3 * v.n_prims * sizeof(float4), cudaMemcpyDeviceToDevice,
                                  c->stream));
@@ -323,12 +326,10 @@ WPBR_API wpbr_status wpbr_batch_build(wpbr_batch* b) {
     BATCH_CUDA(cudaStreamSynchronize(c->stream));
     c->bvh.nodes2.release();
     c->bvh.nodes_split.release();
-    c->bvh.nodes4.release();
     c->bvh.prims.release();
     v.nodes = nd;
     v.nodes_ref = nullptr;  // the arena keeps the layout traversed only
     v.n_ref_int = 0;
-    if (v.nodes4) v.nodes4 = wd;
     v.prims = pd;
   }
   b->arena_bytes = total;
@@ -372,7 +373,7 @@ WPBR_API wpbr_status wpbr_batch_set_rays_per_block(wpbr_batch* b, uint32_t rays_
 
 WPBR_API wpbr_status wpbr_batch_autotune(wpbr_batch* b, int use_cache) {
   if (!b) return WPBR_ERR_INVALID_ARG;
-  if (!b->ready) return berr(b, WPBR_ERR_NOT_BUILT, "batch_autotune: render_setup not called");
+  if (!b->ready) return berr(b, WPBR_ERR_NOT_BUILT, "batch_autotune: no pass graph (render_setup not called, or the last graph capture failed)");
   cudaSetDevice(b->device);
   std::string key = tune_key(b);
   uint32_t rpb = 0;
@@ -428,7 +429,7 @@ WPBR_API wpbr_status wpbr_batch_autotune(wpbr_batch* b, int use_cache) {
 
 WPBR_API wpbr_status wpbr_batch_render_pass(wpbr_batch* b, uint32_t pass) {
   if (!b) return WPBR_ERR_INVALID_ARG;
-  if (!b->ready) return berr(b, WPBR_ERR_NOT_BUILT, "batch_render_pass: render_setup not called");
+  if (!b->ready) return berr(b, WPBR_ERR_NOT_BUILT, "batch_render_pass: no pass graph (render_setup not called, or the last graph capture failed)");
   if (pass >= b->spp) return berr(b, WPBR_ERR_INVALID_ARG, "batch_render_pass: pass >= spp");
   cudaSetDevice(b->device);
   return launch_pass(b, pass);
@@ -436,7 +437,7 @@ WPBR_API wpbr_status wpbr_batch_render_pass(wpbr_batch* b, uint32_t pass) {
 
 WPBR_API wpbr_status wpbr_batch_render(wpbr_batch* b) {
   if (!b) return WPBR_ERR_INVALID_ARG;
-  if (!b->ready) return berr(b, WPBR_ERR_NOT_BUILT, "batch_render: render_setup not called");
+  if (!b->ready) return berr(b, WPBR_ERR_NOT_BUILT, "batch_render: no pass graph (render_setup not called, or the last graph capture failed)");
   cudaSetDevice(b->device);
   for (uint32_t p = 0; p < b->spp; ++p) {
     wpbr_status st = launch_pass(b, p);
@@ -474,7 +475,7 @@ WPBR_API wpbr_status wpbr_batch_film_size(const wpbr_batch* b, uint32_t scene, u
 
 WPBR_API wpbr_status wpbr_batch_film_read(wpbr_batch* b, uint32_t scene, float* acc_L, float* acc_w) {
   if (!b || scene >= b->scenes.size()) return WPBR_ERR_INVALID_ARG;
-  if (!b->ready) return berr(b, WPBR_ERR_NOT_BUILT, "batch_film_read: render_setup not called");
+  if (!b->ready) return berr(b, WPBR_ERR_NOT_BUILT, "batch_film_read: no pass graph (render_setup not called, or the last graph capture failed)");
   cudaSetDevice(b->device);
   BATCH_CUDA(cudaStreamSynchronize(b->stream));
   return from_scene(b, scene, wpbr_film_read(b->scenes[scene], acc_L, acc_w));

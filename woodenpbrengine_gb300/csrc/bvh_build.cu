@@ -1361,177 +1361,6 @@ __global__ void k_split_emit(uint32_t n_int, const Node2* nodes, const uint32_t*
   }
 }
 
-// ---------------------------------------------------------------------------
-// four-wide collapse of the child-pair tree (traversal layout, Node4)
-// ---------------------------------------------------------------------------
-struct Frontier {
-  int n;
-  int ref[4];
-  uint32_t cnt[4];
-  float lo[4][3], hi[4][3];
-  uint32_t bits[4], depth[4], axes[4];  // path from the wide node: bits MSB first, split axes 2 bits per level
-};
-
-__device__ __forceinline__ void node2_child(const Node2& nd, int k, int* ref, uint32_t* cnt, float lo[3], float hi[3]) {
-  if (k == 0) {
-    *ref = nd.meta.x;
-    *cnt = (uint32_t)nd.meta.z;
-    lo[0] = nd.b0.x; hi[0] = nd.b0.y; lo[1] = nd.b0.z; hi[1] = nd.b0.w; lo[2] = nd.bz.x; hi[2] = nd.bz.y;
-  } else {
-    *ref = nd.meta.y;
-    *cnt = ((uint32_t)nd.meta.w) & 0x3FFFFFFFu;
-    lo[0] = nd.b1.x; hi[0] = nd.b1.y; lo[1] = nd.b1.z; hi[1] = nd.b1.w; lo[2] = nd.bz.z; hi[2] = nd.bz.w;
-  }
-}
-
-// Frontier of binary interior node i: start from its two children and expand
-// the interior child of largest surface area until there are four.
-__device__ bool wide_frontier(const Node2* nodes, uint32_t n_int, uint32_t i, Frontier& F) {
-  if (i >= n_int) return false;
-  Node2 nd = nodes[i];
-  uint32_t axis = ((uint32_t)nd.meta.w) >> 30;
-  F.n = 2;
-  for (int k = 0; k < 2; ++k) {
-    node2_child(nd, k, &F.ref[k], &F.cnt[k], F.lo[k], F.hi[k]);
-    F.bits[k] = (uint32_t)k;
-    F.depth[k] = 1;
-    F.axes[k] = axis;
-  }
-  while (F.n < 4) {
-    int best = -1;
-    float best_a = -1.0f;
-    for (int j = 0; j < F.n; ++j) {
-      if (F.ref[j] < 0) continue;
-      float dx = F.hi[j][0] - F.lo[j][0], dy = F.hi[j][1] - F.lo[j][1], dz = F.hi[j][2] - F.lo[j][2];
-      float a = dx * dy + dy * dz + dz * dx;
-      if (a > best_a) {
-        best_a = a;
-        best = j;
-      }
-    }
-    if (best < 0) break;
-    if ((uint32_t)F.ref[best] >= n_int) return false;
-    Node2 c = nodes[F.ref[best]];
-    uint32_t cax = ((uint32_t)c.meta.w) >> 30;
-    uint32_t pb = F.bits[best], pd = F.depth[best], pa = F.axes[best];
-    for (int j = F.n; j > best + 1; --j) {
-      F.ref[j] = F.ref[j - 1];
-      F.cnt[j] = F.cnt[j - 1];
-      for (int q = 0; q < 3; ++q) {
-        F.lo[j][q] = F.lo[j - 1][q];
-        F.hi[j][q] = F.hi[j - 1][q];
-      }
-      F.bits[j] = F.bits[j - 1];
-      F.depth[j] = F.depth[j - 1];
-      F.axes[j] = F.axes[j - 1];
-    }
-    for (int k = 0; k < 2; ++k) {
-      int j = best + k;
-      node2_child(c, k, &F.ref[j], &F.cnt[j], F.lo[j], F.hi[j]);
-      F.bits[j] = (pb << 1) | (uint32_t)k;
-      F.depth[j] = pd + 1;
-      F.axes[j] = pa | (cax << (2 * pd));
-    }
-    ++F.n;
-  }
-  return true;
-}
-
-__global__ void k_wide_count(uint32_t nq, const uint32_t* q_bin, const Node2* nodes, uint32_t n_int, uint32_t* cnt,
-                             uint32_t* err) {
-  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nq) return;
-  Frontier F;
-  uint32_t c = 0;
-  if (!wide_frontier(nodes, n_int, q_bin[q], F)) {
-    atomicOr(err, kErrBuild);
-  } else {
-    for (int j = 0; j < F.n; ++j) c += F.ref[j] >= 0 ? 1u : 0u;
-  }
-  cnt[q] = c;
-}
-
-__global__ void k_wide_emit(uint32_t nq, uint32_t base, const uint32_t* q_bin, const uint32_t* q_wide,
-                            const uint32_t* off, const Node2* nodes, uint32_t n_int, Node4* out, uint32_t n_out,
-                            uint32_t* nq_bin, uint32_t* nq_wide, uint32_t* too_big, uint32_t* err) {
-  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nq) return;
-  Frontier F;
-  if (!wide_frontier(nodes, n_int, q_bin[q], F)) return;
-  uint32_t w = q_wide[q];
-  if (w >= n_out) {
-    atomicOr(err, kErrBuild);
-    return;
-  }
-  float lo[4][3], hi[4][3];
-  int ref[4];
-  uint32_t cnt[4] = {0, 0, 0, 0};
-  uint32_t k = 0;
-  for (int j = 0; j < 4; ++j) {
-    if (j < F.n) {
-      for (int a = 0; a < 3; ++a) {
-        lo[j][a] = F.lo[j][a];
-        hi[j][a] = F.hi[j][a];
-      }
-      if (F.ref[j] >= 0) {
-        uint32_t cw = base + off[q] + k;
-        nq_bin[off[q] + k] = (uint32_t)F.ref[j];
-        nq_wide[off[q] + k] = cw;
-        ref[j] = (int)cw;
-        ++k;
-      } else {
-        ref[j] = F.ref[j];
-        cnt[j] = F.cnt[j];
-        if (F.cnt[j] > 0xFFFFu) atomicOr(too_big, 1u);
-      }
-    } else {
-      for (int a = 0; a < 3; ++a) {
-        lo[j][a] = __int_as_float(0x7f800000);
-        hi[j][a] = __int_as_float(0xff800000);
-      }
-      ref[j] = (int)0x80000000;
-    }
-  }
-  // visit order per octant: the binary near-first rule at every level of
-  // the path (the child with bit == dirIsNeg[axis] first)
-  uint32_t order[2] = {0, 0};
-  for (uint32_t o = 0; o < 8; ++o) {
-    uint32_t key[4], idx[4];
-    for (int j = 0; j < 4; ++j) {
-      idx[j] = (uint32_t)j;
-      if (j >= F.n) {
-        key[j] = 8u + (uint32_t)j;
-        continue;
-      }
-      uint32_t kk = 0;
-      for (uint32_t l = 0; l < F.depth[j]; ++l) {
-        uint32_t bit = (F.bits[j] >> (F.depth[j] - 1 - l)) & 1u;
-        uint32_t ax = (F.axes[j] >> (2 * l)) & 3u;
-        kk |= (bit ^ ((o >> ax) & 1u)) << (2 - l);
-      }
-      key[j] = kk;
-    }
-    for (int a = 1; a < 4; ++a)
-      for (int b = a; b > 0 && key[idx[b]] < key[idx[b - 1]]; --b) {
-        uint32_t t = idx[b];
-        idx[b] = idx[b - 1];
-        idx[b - 1] = t;
-      }
-    uint32_t byte = idx[0] | (idx[1] << 2) | (idx[2] << 4) | (idx[3] << 6);
-    order[o >> 2] |= byte << (8 * (o & 3));
-  }
-  Node4 nd;
-  nd.lox = make_float4(lo[0][0], lo[1][0], lo[2][0], lo[3][0]);
-  nd.hix = make_float4(hi[0][0], hi[1][0], hi[2][0], hi[3][0]);
-  nd.loy = make_float4(lo[0][1], lo[1][1], lo[2][1], lo[3][1]);
-  nd.hiy = make_float4(hi[0][1], hi[1][1], hi[2][1], hi[3][1]);
-  nd.loz = make_float4(lo[0][2], lo[1][2], lo[2][2], lo[3][2]);
-  nd.hiz = make_float4(hi[0][2], hi[1][2], hi[2][2], hi[3][2]);
-  nd.ref = make_int4(ref[0], ref[1], ref[2], ref[3]);
-  nd.meta = make_uint4((cnt[0] & 0xFFFFu) | (cnt[1] << 16), (cnt[2] & 0xFFFFu) | (cnt[3] << 16), order[0], order[1]);
-  out[w] = nd;
-}
-
 }  // namespace
 
 // Kernel launches of radix_sort_pairs: per 8-bit pass a histogram, the
@@ -1838,40 +1667,6 @@ wpbr_status bvh_build(wpbr_ctx* ctx) {
   }
   k_prims<<<g, kB, 0, st>>>(S, B.sprim, B.prims.p);
   WPBR_CUDA(cudaGetLastError());
-  // four-wide traversal layout, level by level from the root
-  uint32_t n_wide = 0, wide_depth = 0, too_big = 0;
-  if (B.n_int && ctx->traversal == WPBR_TRAVERSAL_WIDE) {
-    WPBR_CUDA(B.nodes4.ensure(B.n_int));
-    for (DevBuf<uint32_t>* b : {&B.wq_bin0, &B.wq_bin1, &B.wq_wide0, &B.wq_wide1, &B.wcnt, &B.woff})
-      WPBR_CUDA(b->ensure(B.n_int));
-    WPBR_CUDA(B.counters.ensure(8));
-    WPBR_CUDA(cudaMemsetAsync(B.wq_bin0.p, 0, 4, st));
-    WPBR_CUDA(cudaMemsetAsync(B.wq_wide0.p, 0, 4, st));
-    WPBR_CUDA(cudaMemsetAsync(B.counters.p + 7, 0, 4, st));
-    uint32_t nq = 1, base = 1;
-    uint32_t *qb = B.wq_bin0.p, *qw = B.wq_wide0.p, *nb = B.wq_bin1.p, *nw = B.wq_wide1.p;
-    while (nq && wide_depth < 4096) {
-      k_wide_count<<<div_up(nq, kB), kB, 0, st>>>(nq, qb, B.nodes2.p, B.n_int, B.wcnt.p, ctx->d_err.p);
-      WPBR_CUDA(scan_exclusive(B.wcnt.p, B.woff.p, nq, B.scan_tmp, st));
-      uint32_t lastc = 0, lasto = 0;
-      WPBR_CUDA(cudaMemcpyAsync(&lastc, B.wcnt.p + nq - 1, 4, cudaMemcpyDeviceToHost, st));
-      WPBR_CUDA(cudaMemcpyAsync(&lasto, B.woff.p + nq - 1, 4, cudaMemcpyDeviceToHost, st));
-      WPBR_CUDA(cudaStreamSynchronize(st));
-      uint32_t next = lastc + lasto;
-      if (base + next > B.n_int) return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: wide tree larger than the binary tree");
-      k_wide_emit<<<div_up(nq, kB), kB, 0, st>>>(nq, base, qb, qw, B.woff.p, B.nodes2.p, B.n_int, B.nodes4.p,
-                                                 B.n_int, nb, nw, B.counters.p + 7, ctx->d_err.p);
-      WPBR_CUDA(cudaGetLastError());
-      base += next;
-      nq = next;
-      std::swap(qb, nb);
-      std::swap(qw, nw);
-      ++wide_depth;
-    }
-    n_wide = base;
-    WPBR_CUDA(cudaMemcpyAsync(&too_big, B.counters.p + 7, 4, cudaMemcpyDeviceToHost, st));
-    WPBR_CUDA(cudaStreamSynchronize(st));
-  }
   // leaf-split layout (the default binary traversal); a tree whose root is a
   // leaf keeps the reference layout
   uint32_t n_split = 0, split_d = 0;
@@ -1907,11 +1702,6 @@ wpbr_status bvh_build(wpbr_ctx* ctx) {
   v.nodes_ref = B.nodes2.p;
   v.n_ref_int = B.n_int;
   v.ref_depth = depth;
-  // leaves of more than 65535 primitives do not fit the wide layout's counts:
-  // such trees keep the binary traversal
-  v.nodes4 = (n_wide && !too_big) ? B.nodes4.p : nullptr;
-  v.n_wide = n_wide;
-  v.wide_depth = wide_depth;
   v.prims = B.prims.p;
   v.empty = 0;
   bool root_leaf = node0[1] > 0;

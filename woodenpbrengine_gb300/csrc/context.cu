@@ -145,12 +145,10 @@ void bvh_release(wpbr_ctx* ctx, bool keep_traversal) {
   B.small_node.release(); B.counters.release(); B.nseg.release(); B.sah_axis.release(); B.lin_node.release();
   B.lin_bounds.release(); B.is_int.release(); B.int_index.release(); B.depth_max.release();
   B.int_kids.release(); B.int_slot.release();
-  B.wq_bin0.release(); B.wq_bin1.release(); B.wq_wide0.release(); B.wq_wide1.release();
-  B.wcnt.release(); B.woff.release(); B.split_cnt.release(); B.split_off.release();
+  B.split_cnt.release(); B.split_off.release();
   if (!keep_traversal) {
     B.nodes2.release();
     B.nodes_split.release();
-    B.nodes4.release();
     B.prims.release();
   }
 }
@@ -267,7 +265,8 @@ WPBR_API wpbr_status wpbr_set_quirks(wpbr_ctx* ctx, uint32_t quirks) {
 
 WPBR_API wpbr_status wpbr_set_traversal(wpbr_ctx* ctx, uint32_t mode) {
   if (!ctx) return WPBR_ERR_INVALID_ARG;
-  if (mode > WPBR_TRAVERSAL_BINARY_FULL_LEAVES) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_traversal: unknown mode");
+  if (mode != WPBR_TRAVERSAL_BINARY && mode != WPBR_TRAVERSAL_BINARY_FULL_LEAVES)
+    return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_traversal: unknown mode");
   ctx->traversal = mode;
   ++ctx->epoch;
   return WPBR_OK;
@@ -585,26 +584,40 @@ static wpbr_status collide_pipelined(wpbr_ctx* ctx, const float* rays, uint64_t 
   WPBR_CUDA(cudaEventRecord(ctx->io_ev[2], st));
   WPBR_CUDA(cudaStreamWaitEvent(ctx->io_h2d, ctx->io_ev[2], 0));
   WPBR_CUDA(cudaStreamWaitEvent(ctx->io_comp, ctx->io_ev[2], 0));
-  int i = 0;
+  // A failure inside the loop leaves the loop (never returns from it): the
+  // copies already queued read `rays` and write `hits`, so all four streams
+  // are drained before the call returns, whatever happened.
   wpbr_status s = WPBR_OK;
-  for (; i < 4 && s == WPBR_OK; ++i) {
+  cudaError_t ce = cudaSuccess;
+  const char* what = "collide";
+  for (int i = 0; i < 4; ++i) {
     uint64_t off = bounds[i], c = bounds[i + 1] - bounds[i];
     if (c == 0) continue;
     cudaStream_t cs = comp[i & 1];
-    WPBR_CUDA(cudaMemcpyAsync(ctx->io_rays.p + 2 * off, rays + 8 * off, 32 * c, cudaMemcpyHostToDevice, ctx->io_h2d));
-    WPBR_CUDA(cudaEventRecord(ctx->io_ev[0], ctx->io_h2d));
-    WPBR_CUDA(cudaStreamWaitEvent(cs, ctx->io_ev[0], 0));
+    ce = cudaMemcpyAsync(ctx->io_rays.p + 2 * off, rays + 8 * off, 32 * c, cudaMemcpyHostToDevice, ctx->io_h2d);
+    if (ce == cudaSuccess) ce = cudaEventRecord(ctx->io_ev[0], ctx->io_h2d);
+    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(cs, ctx->io_ev[0], 0);
+    if (ce != cudaSuccess) {
+      what = "collide: rays to the device";
+      break;
+    }
     s = trace_rays(ctx, ctx->io_rays.p + 2 * off, c, ctx->io_hits.p + off, mode, nullptr, i & 1, cs);
     if (s != WPBR_OK) break;
-    WPBR_CUDA(cudaEventRecord(ctx->io_ev[1], cs));
-    WPBR_CUDA(cudaStreamWaitEvent(ctx->io_d2h, ctx->io_ev[1], 0));
-    WPBR_CUDA(cudaMemcpyAsync(hits + 4 * off, ctx->io_hits.p + off, 16 * c, cudaMemcpyDeviceToHost, ctx->io_d2h));
+    ce = cudaEventRecord(ctx->io_ev[1], cs);
+    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(ctx->io_d2h, ctx->io_ev[1], 0);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(hits + 4 * off, ctx->io_hits.p + off, 16 * c, cudaMemcpyDeviceToHost, ctx->io_d2h);
+    if (ce != cudaSuccess) {
+      what = "collide: hits to the host";
+      break;
+    }
   }
   cudaError_t e1 = cudaStreamSynchronize(ctx->io_h2d);
   cudaError_t e2 = cudaStreamSynchronize(ctx->io_comp);
   cudaError_t e3 = cudaStreamSynchronize(ctx->io_d2h);
   cudaError_t e4 = cudaStreamSynchronize(st);
   if (s != WPBR_OK) return s;
+  if (ce != cudaSuccess) return cuda_err(ctx, ce, what);
   for (cudaError_t e : {e1, e2, e3, e4})
     if (e != cudaSuccess) return cuda_err(ctx, e, "collide");
   return WPBR_OK;

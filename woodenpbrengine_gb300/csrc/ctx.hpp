@@ -70,8 +70,6 @@ struct BvhState {
   DevBuf<Node2> nodes2;
   DevBuf<Node2> nodes_split;             // leaf-split layout: nodes2 + the records splitting large leaves
   DevBuf<uint32_t> split_cnt, split_off;  // records per child slot, and their offsets
-  DevBuf<Node4> nodes4;
-  DevBuf<uint32_t> wq_bin0, wq_bin1, wq_wide0, wq_wide1, wcnt, woff;  // wide collapse queues
   DevBuf<float4> prims;
   BvhView view{};
 };
@@ -141,7 +139,7 @@ struct wpbr_ctx {
   std::string err;
   uint32_t quirks = 0;
   uint64_t epoch = 0;  // bumped by every scene upload, BVH build, quirk or traversal change
-  uint32_t traversal = 0;  // wpbr_traversal: 0 binary (leaf-split), 1 wide, 2 binary over the reference's leaves
+  uint32_t traversal = 0;  // wpbr_traversal: 0 binary (leaf-split), 2 binary over the reference's leaves
   uint32_t spectrum = 0;   // wpbr_spectrum: 0 RGB, 1 Sampled64
   wpbr::DevBuf<uint32_t> d_err;
   // scene
@@ -205,13 +203,11 @@ struct wpbr_ctx {
 };
 
 namespace wpbr {
-// The BVH view the traversal kernels receive: the wide layout only when the
-// context asks for the wide traversal, the child-pair records of the
+// The BVH view the traversal kernels receive: the child-pair records of the
 // reference's leaves as they are for WPBR_TRAVERSAL_BINARY_FULL_LEAVES, else
 // the leaf-split child-pair layout.
 inline BvhView traversal_view(const wpbr_ctx* ctx) {
   BvhView v = ctx->bvh.view;
-  if (ctx->traversal != WPBR_TRAVERSAL_WIDE) v.nodes4 = nullptr;
   if (ctx->traversal == WPBR_TRAVERSAL_BINARY_FULL_LEAVES) v = reference_leaves_view(v);
   return v;
 }

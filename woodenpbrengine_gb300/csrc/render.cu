@@ -438,7 +438,7 @@ PassCtx make_pass_ctx(wpbr_ctx* ctx) {
   PassCtx P;
   P.S = scene_view(ctx);
   P.Bv = render_traversal_view(ctx);
-  P.rs = wpbr_rng::Stream{ctx->rs.seed, ctx->rs.stream, ctx->rs.spp};
+  P.rs = wpbr_rng::Stream{ctx->rs.seed, ctx->rs.stream, ctx->rs.spp, (ctx->quirks & WPBR_Q_REF_SAMPLER_ARRAYS) ? 1u : 0u};
   P.W = ctx->rs.W;
   P.H = ctx->rs.H;
   P.err = ctx->d_err.p;
@@ -579,7 +579,7 @@ static uint64_t pass_graph_key(const wpbr_ctx* ctx) {
   mix((uint64_t)ctx->spectrum | ((uint64_t)ctx->quirks << 8));
   const void* ptrs[] = {R.acc.p,    R.hit_prim.p, R.shadow_rays.p,     R.shadow_hit.p,      R.pstate.p,
                         R.Lbuf.p,   R.pfilm.p,    R.pass_dev.p,        R.counters.p,        R.pass_ptr,
-                        ctx->d_err.p, ctx->bvh.view.nodes, ctx->bvh.view.nodes4,
+                        ctx->d_err.p, ctx->bvh.view.nodes,
                         ctx->bvh.view.prims, R.spec_mats.p, R.spec_le.p, R.spec_L.p, R.spec_acc.p};
   for (const void* q : ptrs) mix((uint64_t)(uintptr_t)q);
   return h;

@@ -9,13 +9,18 @@
 // and the sort keeps its temporaries in one file-scope device array.
 //
 // The array (g_scratch, about 8.5 MB) is part of the library image: every
-// GPU that loads the library holds it until the process exits. Its device
-// address is looked up once per device (cudaGetSymbolAddress, with that device
-// current) on the first call made while that device is current, so the first
-// call on a device should come before any stream capture. Every call shares
-// the one array and leaves its last contents behind; calls whose GPU work
-// overlaps (two streams, or two host threads) race on it and must be
-// serialised by the caller.
+// GPU that loads the library holds it until the process exits. Host code
+// cannot use the array's name as a device address, so each call made outside
+// stream capture looks the address up (cudaGetSymbolAddress, with the
+// caller's device and context current) and remembers it per device; a call
+// made while its stream is being captured uses the remembered address, which
+// is why the first call on a device must come before any stream capture (such
+// a call is refused otherwise). Looking the address up again on every
+// uncaptured call keeps it right after a cudaDeviceReset or when the caller
+// switches to another context of the same device. Every call shares the one
+// array and leaves its last contents behind; calls whose GPU work overlaps
+// (two streams, or two host threads) race on it and must be serialised by the
+// caller.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -43,7 +48,7 @@ struct Scratch {
 
 static __device__ __align__(256) Scratch g_scratch;
 
-// Per-device address of g_scratch (host-side; set up once per device).
+// Per-device address of g_scratch last looked up outside stream capture.
 constexpr int kMaxDevices = 64;
 Scratch* g_addr[kMaxDevices] = {};
 std::mutex g_mu;
@@ -181,10 +186,18 @@ WPBR_API wpbr_status wpbr_sort_morton_noalloc(const uint32_t* d_codes, uint32_t 
     cudaGetLastError();
     return fail(WPBR_ERR_NO_DEVICE, "sort_morton_noalloc: no current CUDA device");
   }
+  cudaStream_t st = (cudaStream_t)stream;
+  // A stream whose capture status cannot be read (the legacy stream while
+  // another stream captures in global mode) counts as capturing.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    cap = cudaStreamCaptureStatusActive;
+  }
   Scratch* S;
   {
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
       void* p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
       if (e != cudaSuccess || !p) {
@@ -192,10 +205,12 @@ WPBR_API wpbr_status wpbr_sort_morton_noalloc(const uint32_t* d_codes, uint32_t 
         return fail(WPBR_ERR_CUDA, "sort_morton_noalloc: cudaGetSymbolAddress(g_scratch) failed");
       }
       g_addr[dev] = (Scratch*)p;
+    } else if (!g_addr[dev]) {
+      return fail(WPBR_ERR_INVALID_ARG,
+                  "sort_morton_noalloc: the first call on a device must come before any stream capture");
     }
     S = g_addr[dev];
   }
-  cudaStream_t st = (cudaStream_t)stream;
   const uint32_t nblk = (n + kTileKeys - 1) / kTileKeys;
   const uint32_t nh = 256 * nblk;
   const uint32_t ntiles = (nh + kTileKeys - 1) / kTileKeys;

@@ -608,7 +608,7 @@ static PassCtx spec_pass_ctx(wpbr_ctx* ctx) {
   PassCtx P;
   P.S = scene_view(ctx);
   P.Bv = render_traversal_view(ctx);
-  P.rs = wpbr_rng::Stream{ctx->rs.seed, ctx->rs.stream, ctx->rs.spp};
+  P.rs = wpbr_rng::Stream{ctx->rs.seed, ctx->rs.stream, ctx->rs.spp, (ctx->quirks & WPBR_Q_REF_SAMPLER_ARRAYS) ? 1u : 0u};
   P.W = ctx->rs.W;
   P.H = ctx->rs.H;
   P.err = ctx->d_err.p;

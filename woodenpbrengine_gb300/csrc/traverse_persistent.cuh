@@ -393,231 +393,6 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
   }
 }
 
-// Four-wide variant over Node4: each node tests up to four boxes, then
-// continues with the first hit child in the binary tree's near-first order
-// for the ray's octant and pushes the other hit children (with their entry
-// distances) behind it, so leaves are reached in the same order as the
-// binary traversal and ties resolve the same way. Leaf postponing and ray
-// refill as in k_trace_persistent.
-template <bool ANY, int STACK, class Src, class Sink>
-__global__ void __launch_bounds__(kPersistBlock) k_trace_wide(SceneView S, BvhView Bv, Src src, Sink sink,
-                                                              uint32_t n, uint32_t* counter, uint32_t* err) {
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t lt_mask = (1u << lane) - 1u;
-  V3 o{0, 0, 0}, d{0, 0, 0}, inv{0, 0, 0};
-  int neg[3] = {0, 0, 0};
-  uint32_t oct = 0;
-  RayTri R{};
-  float tmax = 0.0f, tb = 0.0f;
-  HitRec h{0.0f, kNoHit, 0.0f, 0.0f};
-  int ref = kEnd;
-  uint32_t cnt = 0;
-  int lref = kEnd;
-  uint32_t lcnt = 0;
-  int sp = 0;
-  int st_ref[STACK];
-  uint32_t st_cnt[STACK];
-  float st_t[STACK];
-  uint32_t rid = 0;
-  bool active = false;
-  bool exhausted = false;
-  uint32_t guard = 0;
-
-  while (true) {
-    __syncwarp();
-    uint32_t idle = __ballot_sync(0xFFFFFFFFu, !active && !exhausted);
-    if (idle) {
-      uint32_t leader = __ffs(idle) - 1;
-      uint32_t base = 0;
-      if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(idle));
-      base = __shfl_sync(0xFFFFFFFFu, base, leader);
-      if (!active && !exhausted) {
-        uint32_t r = base + __popc(idle & lt_mask);
-        if (r >= n) {
-          exhausted = true;
-        } else {
-          rid = r;
-          float4 ro, rd;
-          src.load(r, &ro, &rd);
-          o = V3{ro.x, ro.y, ro.z};
-          d = V3{rd.x, rd.y, rd.z};
-          tmax = rd.w;
-          inv = V3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
-          neg[0] = inv.x < 0.0f;
-          neg[1] = inv.y < 0.0f;
-          neg[2] = inv.z < 0.0f;
-          oct = (uint32_t)neg[0] | ((uint32_t)neg[1] << 1) | ((uint32_t)neg[2] << 2);
-          R = ray_tri_setup(o, d, S.quirks);
-          tb = inf_();
-          h = HitRec{inf_(), kNoHit, 0.0f, 0.0f};
-          sp = 0;
-          lref = kEnd;
-          ref = kEnd;
-          float te;
-          if (!Bv.empty &&
-              slab_test(V3{Bv.root_lo[0], Bv.root_lo[1], Bv.root_lo[2]},
-                        V3{Bv.root_hi[0], Bv.root_hi[1], Bv.root_hi[2]}, o, inv, neg, tmax, &te)) {
-            ref = Bv.root_ref;
-            cnt = Bv.root_count;
-          }
-          active = true;
-        }
-      }
-    }
-    if (__all_sync(0xFFFFFFFFu, !active && exhausted)) break;
-    if (++guard > (1u << 26)) {
-      if (lane == 0) atomicOr(err, kErrLoopLimit);
-      break;
-    }
-
-    if (active) {
-      while (ref >= 0) {
-        if ((uint32_t)ref >= Bv.n_wide) {
-          atomicOr(err, kErrBuild);
-          ref = kEnd;
-          break;
-        }
-        const Node4* np_ = Bv.nodes4 + ref;
-        float4 lx = __ldg(&np_->lox), hx = __ldg(&np_->hix);
-        float4 ly = __ldg(&np_->loy), hy = __ldg(&np_->hiy);
-        float4 lz = __ldg(&np_->loz), hz = __ldg(&np_->hiz);
-        int4 rf = __ldg(&np_->ref);
-        uint4 mt = __ldg(&np_->meta);
-        float t0, t1, t2, t3;
-        bool h0 = slab_test(V3{lx.x, ly.x, lz.x}, V3{hx.x, hy.x, hz.x}, o, inv, neg, tmax, &t0) &&
-                  !(t0 > tb * kPruneScale);
-        bool h1 = slab_test(V3{lx.y, ly.y, lz.y}, V3{hx.y, hy.y, hz.y}, o, inv, neg, tmax, &t1) &&
-                  !(t1 > tb * kPruneScale);
-        bool h2 = slab_test(V3{lx.z, ly.z, lz.z}, V3{hx.z, hy.z, hz.z}, o, inv, neg, tmax, &t2) &&
-                  !(t2 > tb * kPruneScale);
-        bool h3 = slab_test(V3{lx.w, ly.w, lz.w}, V3{hx.w, hy.w, hz.w}, o, inv, neg, tmax, &t3) &&
-                  !(t3 > tb * kPruneScale);
-        uint32_t ord = ((oct < 4 ? mt.z : mt.w) >> (8 * (oct & 3))) & 0xFFu;
-        // walk the children from the last visited to the first: every hit
-        // child seen earlier in this walk (later in visit order) is pushed
-        // when an earlier-visited hit appears, so the stack top is always the
-        // next child in near-first order and the first visited is entered
-        int cref = kEnd;
-        uint32_t ccnt = 0;
-        float ct = 0.0f;
-        bool overflow = false;
-#pragma unroll
-        for (int k = 3; k >= 0; --k) {
-          uint32_t c = (ord >> (2 * k)) & 3u;
-          bool hc = c == 0 ? h0 : (c == 1 ? h1 : (c == 2 ? h2 : h3));
-          if (!hc) continue;
-          if (cref != kEnd) {
-            if (sp >= STACK) {
-              overflow = true;
-            } else {
-              st_ref[sp] = cref;
-              st_cnt[sp] = ccnt;
-              st_t[sp] = ct;
-              ++sp;
-            }
-          }
-          cref = c == 0 ? rf.x : (c == 1 ? rf.y : (c == 2 ? rf.z : rf.w));
-          ct = c == 0 ? t0 : (c == 1 ? t1 : (c == 2 ? t2 : t3));
-          ccnt = ((c < 2 ? mt.x : mt.y) >> (16 * (c & 1))) & 0xFFFFu;
-        }
-        if (overflow) {
-          atomicOr(err, kErrStackOverflow);
-          ref = kEnd;
-          break;
-        }
-        if (cref == kEnd) {
-          ref = kEnd;
-          while (sp > 0) {
-            --sp;
-            if (!(st_t[sp] > tb * kPruneScale)) {
-              ref = st_ref[sp];
-              cnt = st_cnt[sp];
-              break;
-            }
-          }
-        } else {
-          ref = cref;
-          cnt = ccnt;
-        }
-        if (ref < 0 && ref != kEnd && lref == kEnd) {
-          lref = ref;
-          lcnt = cnt;
-          ref = kEnd;
-          while (sp > 0) {
-            --sp;
-            if (!(st_t[sp] > tb * kPruneScale)) {
-              ref = st_ref[sp];
-              cnt = st_cnt[sp];
-              break;
-            }
-          }
-        }
-        if (!__any_sync(__activemask(), lref == kEnd)) break;
-      }
-      if (lref == kEnd && ref < 0 && ref != kEnd) {
-        lref = ref;
-        lcnt = cnt;
-        ref = kEnd;
-        while (sp > 0) {
-          --sp;
-          if (!(st_t[sp] > tb * kPruneScale)) {
-            ref = st_ref[sp];
-            cnt = st_cnt[sp];
-            break;
-          }
-        }
-      }
-      bool done_any = false;
-      while (lref != kEnd) {
-        uint32_t first = (uint32_t)(~lref);
-        if (first >= Bv.n_prims || lcnt > Bv.n_prims - first) {
-          atomicOr(err, kErrBuild);
-          lref = kEnd;
-          ref = kEnd;
-          break;
-        }
-        for (uint32_t k = 0; k < lcnt; ++k) {
-          uint32_t prim;
-          float b1, b2;
-          float t = prim_test(S, Bv.prims, first + k, o, d, R, &prim, &b1, &b2);
-          if (t == 0.0f || !(t < tmax)) continue;
-          if (tb > t) {
-            tb = t;
-            h = HitRec{t, prim, b1, b2};
-            if (ANY) {
-              done_any = true;
-              break;
-            }
-          }
-        }
-        if (done_any) {
-          lref = kEnd;
-          ref = kEnd;
-          break;
-        }
-        lref = kEnd;
-        if (ref < 0 && ref != kEnd) {
-          lref = ref;
-          lcnt = cnt;
-          ref = kEnd;
-          while (sp > 0) {
-            --sp;
-            if (!(st_t[sp] > tb * kPruneScale)) {
-              ref = st_ref[sp];
-              cnt = st_cnt[sp];
-              break;
-            }
-          }
-        }
-      }
-      if (ref == kEnd && lref == kEnd) {
-        sink.store(rid, h);
-        active = false;
-      }
-    }
-  }
-}
-
 // ---- ray sources and hit sinks -------------------------------------------------
 struct BufferSrc {
   const float4* rays;  // 2 float4 per ray: (o, unused), (d, tmax)
@@ -664,10 +439,12 @@ struct PrimSink {
   __device__ __forceinline__ void store(uint32_t i, const HitRec& h) const { prims[i] = h.prim; }
 };
 
-// Launches the traversal that fits the tree: the four-wide kernel when the
-// wide layout exists and its stack bound (three pushes per wide level) fits,
-// else the binary kernel; grid_cap limits the persistent grid (0: one full
-// wave of resident blocks).
+// Launches the traversal whose stack fits the tree: a lane's stack never
+// holds more entries than the tree is deep, so trees shallower than 60
+// levels take the 64-entry kernel and deeper ones (the callers refuse depths
+// of 250 and more) the 256-entry kernel of the reference's nodesToVisit[256]
+// (SLBVH.cpp:101); grid_cap limits the persistent grid (0: one full wave of
+// resident blocks).
 template <bool ANY, class Src, class Sink>
 inline void launch_traversal(const SceneView& S, const BvhView& Bv, const Src& src, const Sink& sink, uint32_t n,
                              uint32_t* counter, uint32_t* err, cudaStream_t st, uint32_t grid_cap = 0) {
@@ -676,11 +453,7 @@ inline void launch_traversal(const SceneView& S, const BvhView& Bv, const Src& s
     unsigned g = (grid_cap && grid_cap < full) ? grid_cap : full;
     kern<<<g, kPersistBlock, 0, st>>>(S, Bv, src, sink, n, counter, err);
   };
-  if (Bv.nodes4 && 3 * Bv.wide_depth <= 64)
-    go(k_trace_wide<ANY, 64, Src, Sink>);
-  else if (Bv.nodes4 && 3 * Bv.wide_depth <= 256)
-    go(k_trace_wide<ANY, 256, Src, Sink>);
-  else if (Bv.max_depth < 60)
+  if (Bv.max_depth < 60)
     go(k_trace_persistent<ANY, 64, Src, Sink>);
   else
     go(k_trace_persistent<ANY, 256, Src, Sink>);

@@ -49,25 +49,9 @@ struct __align__(16) Node2 {
   int4 meta;   // ref0, ref1, cnt0, (axis<<30)|cnt1
 };
 
-// Four-wide node collapsed from the binary tree: the frontier of up to four
-// descendants of one binary interior node (the largest-area interior child
-// expanded first), bounds in SoA form, so one 128-byte fetch tests four
-// boxes. ref >= 0: wide node index; ref < 0: leaf starting at sorted
-// position ~ref. meta.x / meta.y: leaf counts of children 0-1 / 2-3 (16 bits
-// each). meta.z / meta.w: for each ray octant (dirIsNeg x | y<<1 | z<<2,
-// octants 0-3 in z, 4-7 in w, 8 bits each) the children in the binary tree's
-// near-first depth-first order, 2 bits per child, first visited in the low
-// bits. Empty slots have lo = +inf, hi = -inf and never pass the slab test.
-struct __align__(16) Node4 {
-  float4 lox, hix, loy, hiy, loz, hiz;
-  int4 ref;
-  uint4 meta;
-};
-
 struct BvhView {
   const Node2* nodes;    // the layout traversed (leaf-split by default)
   const Node2* nodes_ref;  // the reference's leaves as they are (null once moved into a batch arena)
-  const Node4* nodes4;   // null: binary traversal
   const float4* prims;   // 3 float4 per sorted primitive
   int empty;
   int root_ref;          // >=0 interior index, <0 leaf (~first)
@@ -77,8 +61,6 @@ struct BvhView {
   uint32_t n_prims, n_int;  // bounds for the index guards in traversal
   uint32_t n_ref_int;       // records of nodes_ref
   uint32_t ref_depth;       // depth of the reference's tree (max_depth adds the split levels)
-  uint32_t n_wide;          // wide node count (index guard)
-  uint32_t wide_depth;      // levels of the wide tree
 };
 
 // The same tree traversed over the reference's leaves as they are (the

@@ -1,6 +1,8 @@
 """Host-side sharding for running the pipeline as independent replicas, one
-process per GPU (torch.distributed supplies the process group; no device
-collective is involved).
+process per GPU. The caller supplies the process group (any object with the
+torch.distributed-style get_rank / get_world_size / gather_object /
+all_gather_object calls, e.g. a gloo group); only host objects travel through
+it, and this module imports nothing but numpy.
 
 The path has no exchange step: pixels, film row slabs, sample passes and whole
 scenes are independent. A multi-GPU job therefore splits its units across
@@ -46,9 +48,12 @@ def gather_rows(local, total_rows, dist, dst=0):
 
 
 def allreduce_sum(arr, dist):
-    """Element-wise sum over ranks of a float array (float64 accumulation)."""
-    import torch
-
-    t = torch.from_numpy(np.ascontiguousarray(arr, np.float64))
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return t.numpy().astype(arr.dtype)
+    """Element-wise sum over ranks of a float array, on the host: every rank
+    receives every rank's array and adds them in rank order in float64, so
+    all ranks hold the same bits."""
+    parts = [None] * dist.get_world_size()
+    dist.all_gather_object(parts, np.ascontiguousarray(arr))
+    acc = np.zeros(np.shape(arr), np.float64)
+    for p in parts:
+        acc += np.asarray(p, np.float64)
+    return acc.astype(np.asarray(arr).dtype)
