@@ -15,8 +15,14 @@ LBVH build rate, the any-hit rate, the roofline of the traversal kernel and
 the oracle's CPU baseline (the reference's prune-free traversal restated in
 C++, all host threads, bounded sample).
 
+Every other reported rate carries a roofline of its own from the byte
+models below (`roofline` beside each render and build entry).
+
 `--impl reference` times that CPU implementation alone (the reference cannot
-be built here: its ECS, math and allocator libraries are not vendored).
+be built here: its ECS, math and allocator libraries are not vendored) on all
+8,388,608 rays of the same set in the same order, with inputs from the oracle
+library's own copy of the scene generator (the product library is not
+loaded).
 """
 import argparse
 import json
@@ -34,6 +40,26 @@ RES = 2048
 LEVEL = 8
 METRIC = "Mrays/s closest-hit"
 WORKLOAD = "LBVH microbench: icosphere L8 (1,310,720 tris, 3-octave noise), 4M coherent + 4M incoherent rays"
+
+# Algorithmic bytes of one sample of the direct-lighting pass (RGB): camera
+# sample 44, primary hit 40, surface interaction 140, light sample 52, shadow
+# ray 32, BSDF eval 104, MIS 56, BSDF sample 112, shadow ray 32, MIS 56, film
+# splat 16 px x 16 B = 256; an environment light adds its Li lookup (96) for
+# 1,020 B, a sphere light needs none (964 B). Traversal fetches come on top:
+# 32 B per box test and 36 B per primitive test of the camera ray and the
+# shadow rays. The 64-bin spectral pass moves the same per-sample data except
+# the film: its splat touches 16 pixels of 64 bins + weight (16 x 260 B =
+# 4,160 B instead of 256 B); its other spectra are made from RGB inputs in
+# registers and never stored.
+SAMPLE_BYTES_SPHERE = 964.0
+SAMPLE_BYTES_ENV = 1020.0
+SAMPLE_BYTES_SAMPLED64 = SAMPLE_BYTES_ENV - 256.0 + 16 * (64 * 4 + 4)
+# LBVH build per primitive: bounds and Morton codes 56 B (3 indices + 3
+# vertices in, 8 B out), radix sort 64 B (16 B per pass, 4 passes), emit and
+# refit 120 B (codes 12, node 12, leaf bounds 24, child bounds 48, write 24).
+BUILD_BYTES_PER_PRIM = 56.0 + 64.0 + 120.0
+STAGES = ["CAMERA_RAYS", "COLLIDE_PRIMARY", "EMITTED_LIGHT", "BSDF_SETUP", "SAMPLE_LIGHT", "SHADOW_LIGHT",
+          "BSDF_COMPUTE", "INTEGRATE_LIGHT", "SAMPLE_BSDF", "SHADOW_BSDF", "LIGHT_COMPUTE", "INTEGRATE_BSDF"]
 
 
 def parse():
@@ -115,6 +141,60 @@ def ncu_traffic_per_ray():
     return None
 
 
+def roofline(nbytes, seconds, model, what):
+    """Roofline entry of a rate: algorithmic bytes over the measured time,
+    against the measured HBM copy bandwidth."""
+    peak, kind = measured_peaks()
+    achieved = nbytes / seconds / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": kind, "bytes_model": model, "timed": what}
+
+
+def pass_traversal_terms(W, ctx, res, spp, shadow_any):
+    """Traversal bytes per sample of a direct-lighting pass: the staged jobs
+    of pass 0 run over the whole film, and the camera rays and the shadow rays
+    they trace (light branch o = p + 0.1 wi, BSDF branch o = p + 0.01 wi) are
+    counted by wpbr_collide_stats over the reference's leaves (a subsample of
+    at most 2^18 rays per kind): 32 B per box test + 36 B per primitive test,
+    times the rays of that kind per sample."""
+    import numpy as np
+
+    Wd, Hd = res
+    n = Wd * Hd
+    ctx.render_setup(spp, seed=0)
+    for s in STAGES:
+        ctx.job(s, 0)
+    rec = ctx.record(0, 0, Wd, Hd, fields=["ray_o", "ray_d", "si_p", "l_wi", "l_flags", "b_wi", "b_flags"])
+
+    def rays_of(o, d):
+        r = np.zeros((len(o), 8), np.float32)
+        r[:, :3] = o
+        r[:, 4:7] = d
+        r[:, 7] = np.inf
+        return r
+
+    untouched = np.uint32(0xFFFFFFFF)
+    lm = (rec["l_flags"] != untouched) & ((rec["l_flags"] & 1) != 0)
+    bm = (rec["b_flags"] != untouched) & ((rec["b_flags"] & 2) != 0)
+    kinds = [("camera", rays_of(rec["ray_o"], rec["ray_d"]), W.TRACE_CLOSEST),
+             ("light_shadow", rays_of(rec["si_p"][lm] + np.float32(0.1) * rec["l_wi"][lm], rec["l_wi"][lm]),
+              W.TRACE_ANY if shadow_any else W.TRACE_CLOSEST),
+             ("bsdf_shadow", rays_of(rec["si_p"][bm] + np.float32(0.01) * rec["b_wi"][bm], rec["b_wi"][bm]),
+              W.TRACE_ANY if shadow_any else W.TRACE_CLOSEST)]
+    total, out = 0.0, {}
+    for name, rays, mode in kinds:
+        if len(rays) == 0:
+            continue
+        sub = rays[:: max(1, len(rays) // 262144)]
+        _, st = ctx.collide(sub, mode=mode, stats=True)
+        V, P = float(st[:, 0].mean()), float(st[:, 1].mean())
+        per_sample = len(rays) / n
+        total += per_sample * (32.0 * V + 36.0 * P)
+        out[name] = {"rays_per_sample": per_sample, "box_tests": V, "prim_tests": P}
+    ctx.check_device_errors()
+    return total, out
+
+
 def cpu_trace_rate(desc, rays, seconds, threads=None):
     """Oracle (the reference's prune-free candidate traversal) on host cores."""
     import numpy as np
@@ -142,12 +222,18 @@ def cpu_trace_rate(desc, rays, seconds, threads=None):
                        % (2 * m, m, m, dt)), o
 
 
-def render_rate(W, torch, config, res, spp, level=0, frames=1, spectrum=None):
+def render_rate(W, torch, config, res, spp, level=0, frames=1, spectrum=None, profile=None):
     """Msamples/s of whole frames through the fused, graph-captured pass
     (config 0: 64 spheres + quad + sphere light; config 2: the 1.31 M-triangle
     mesh + 256 spheres + 1024x512 environment light; config 5: config 0 with
-    textured metal). spectrum=W.SPECTRUM_SAMPLED64 times the 64-bin pass."""
+    textured metal). spectrum=W.SPECTRUM_SAMPLED64 times the 64-bin pass.
+    The roofline divides the per-sample byte model (static part by light
+    kind and spectral representation, plus the traversal terms of the
+    frame's own rays) by the frame time."""
     g = W.SceneGen(config, 0, res, level=level)
+    d = g.desc.contents
+    env = bool(d.envmap)
+    env_only = env and all(d.lights[i].type == W.LIGHT_ENV for i in range(d.n_lights))
     ctx = W.Context(torch.cuda.current_device())
     stream = torch.cuda.Stream()  # a capturable (non-default) stream for the pass graph
     ctx.set_stream(stream.cuda_stream)
@@ -169,31 +255,70 @@ def render_rate(W, torch, config, res, spp, level=0, frames=1, spectrum=None):
     ctx.check_device_errors()
     ms = e0.elapsed_time(e1) / frames
     samples = res[0] * res[1] * spp
+    # byte model: static part + traversal terms of pass 0's rays (staged jobs, RGB)
+    ctx.set_spectrum(W.SPECTRUM_RGB)
+    trav, terms = pass_traversal_terms(W, ctx, res, spp, env_only)
     ctx.close()
-    return {"msamples_per_s": samples / ms / 1e3, "ms_per_frame": ms, "film": "%dx%d" % res, "spp": spp,
-            "kernel_launches_per_pass": 5}
+    static = SAMPLE_BYTES_SAMPLED64 if spectrum == W.SPECTRUM_SAMPLED64 else (
+        SAMPLE_BYTES_ENV if env else SAMPLE_BYTES_SPHERE)
+    per_sample = static + trav
+    out = {"msamples_per_s": samples / ms / 1e3, "ms_per_frame": ms, "film": "%dx%d" % res, "spp": spp,
+           "kernel_launches_per_pass": 5,
+           "roofline": roofline(per_sample * samples, ms / 1e3,
+                                "%.0f B/sample static + %.0f B/sample traversal (32 B per box test, 36 B per "
+                                "primitive test of the camera and shadow rays)%s"
+                                % (static, trav, "; texture fetches not counted" if d.n_textures else ""),
+                                "whole frame, CUDA events on the pass stream"),
+           "traversal_terms": terms}
+    if profile:
+        out["roofline"]["profile"] = profile
+    return out
 
 
-def cpu_render_rate(W, config, res, spp, spectral=False):
+def cpu_render_rate(W, config, res, spp, spectral=False, level=0, min_seconds=1.0):
     """The oracle's render (the per-sample job list restated on the CPU, all
-    host cores) of the same frame: Msamples/s beside the GPU's."""
+    host threads) of the same scene and film: whole passes (pass 0, 1, ...
+    of an spp-pass frame) until about min_seconds have passed, Msamples/s
+    beside the GPU's. Scene generation and the oracle's BVH build are not
+    timed."""
     from oracle import binding as O
 
-    g = W.SceneGen(config, 0, res)
+    g = O.SceneGen(config, 0, res, level=level)
     o = O.OracleScene(g.desc)  # builds the oracle's BVH
-    frames = 0
+    passes = 0
     t = time.perf_counter()
-    while True:  # whole frames until about a second has passed
+    while True:
         if spectral:
-            o.render_spectral(res[0], res[1], spp)
+            o.render_spectral(res[0], res[1], 1)
         else:
-            o.render(res[0], res[1], spp)
-        frames += 1
+            o.render_passes(res[0], res[1], spp, [passes % spp])
+        passes += 1
         dt = time.perf_counter() - t
-        if dt > 1.0:
+        if dt > min_seconds:
             break
-    return {"msamples_per_s": res[0] * res[1] * spp * frames / dt / 1e6, "cores": O.lib().orc_num_threads(),
-            "kind": "port", "sample": "%dx%d x %d spp, %d frames, %.2f s" % (res[0], res[1], spp, frames, dt)}
+    return {"value": res[0] * res[1] * passes / dt / 1e6, "unit": "Msamples/s", "cores": O.lib().orc_num_threads(),
+            "kind": "port",
+            "sample": "%dx%d film, %d whole pass%s%s, %.2f s" % (res[0], res[1], passes, "es" if passes > 1 else "",
+                                                                 " (Sampled64)" if spectral else "", dt)}
+
+
+def cpu_batch_rate(n_scenes=32, film_scale=1024, max_count=2000000):
+    """The oracle's render of pass 0 of every scene of the batched set, one
+    scene after another on all host threads (oracle BVH builds not timed)."""
+    from oracle import binding as O
+
+    samples, dt = 0, 0.0
+    for k in range(n_scenes):
+        g = O.SceneGen(3, seed=3, res=(film_scale, max_count), level=k)
+        cam = g.desc.contents.camera
+        o = O.OracleScene(g.desc)
+        t = time.perf_counter()
+        o.render_passes(cam.res_x, cam.res_y, 16, [0], 0, k)
+        dt += time.perf_counter() - t
+        samples += cam.res_x * cam.res_y
+        o.close()
+    return {"value": samples / dt / 1e6, "unit": "Msamples/s", "cores": O.lib().orc_num_threads(), "kind": "port",
+            "sample": "pass 0 of all %d scenes (%d samples), %.2f s" % (n_scenes, samples, dt)}
 
 
 def batch_rate(W, torch, n_scenes=32, spp=16, film_scale=1024, max_count=2000000):
@@ -254,7 +379,13 @@ def batch_rate(W, torch, n_scenes=32, spp=16, film_scale=1024, max_count=2000000
         c.close()
     same = bool((L0.view("u4") == L1.view("u4")).all() and (w0 == w1).all())
     samples = pixels * spp
-    return {"scenes": n_scenes, "spp": spp, "total_pixels": pixels, "total_prims": info["total_prims"],
+    model = ("%.0f B/sample (the static per-sample bytes with an environment light); traversal terms not "
+             "counted, so the fraction is a lower bound" % SAMPLE_BYTES_ENV)
+    return {"roofline": roofline(SAMPLE_BYTES_ENV * samples, ms_batch / 1e3, model,
+                                 "one batched frame (all scenes), CUDA events on the batch stream"),
+            "roofline_sequential": roofline(SAMPLE_BYTES_ENV * samples, ms_seq / 1e3, model,
+                                            "the same scenes one at a time"),
+            "scenes": n_scenes, "spp": spp, "total_pixels": pixels, "total_prims": info["total_prims"],
             "arena_bytes": info["arena_bytes"], "rays_per_block": info["rays_per_block"],
             "autotune_source": ["default", "measured", "cache", "caller"][info["autotune_source"]],
             "msamples_per_s_batched": samples / ms_batch / 1e3, "ms_per_frame_batched": ms_batch,
@@ -280,7 +411,10 @@ def adjoint_rate(W, torch, res=(512, 512), spp=16, n_fd=64, n_fp64=64, fp64=True
     materials x 10 parameters + a 256x128 RGB environment = 98,944
     parameters): forward + backward time, gradient parameters/s, the rate of
     central differences (h = 1e-3) through the same forward, their agreement,
-    and the FP64 oracle's dual-number gradient on a subset."""
+    and on the 64 parameters of those differences the FP64 oracle's
+    dual-number gradient and FP64 central differences (h = 1e-3) of the same
+    frozen estimator. Roofline: the forward pass's per-sample bytes (static
+    part + the traversal terms of its rays), the backward pass twice that."""
     import numpy as np
 
     g0 = W.SceneGen(4, 0, res, level=0)
@@ -350,8 +484,10 @@ def adjoint_rate(W, torch, res=(512, 512), spp=16, n_fd=64, n_fp64=64, fp64=True
     fd_s = time.perf_counter() - t
     ctx.adjoint_set_params(m0, e0)
     ctx.check_device_errors()
+    trav, terms = pass_traversal_terms(W, ctx, res, spp, False)
     ctx.close()
     g_sel = grad[sel]
+    fwd_bytes = (SAMPLE_BYTES_ENV + trav) * n * spp
     out = {"film": "%dx%d" % res, "spp": spp, "params": int(nm + ne), "loss": loss,
            "forward_ms": fwd_ms, "backward_ms": bwd_ms,
            "gradient_params_per_s": (nm + ne) / ((fwd_ms + bwd_ms) / 1e3),
@@ -359,7 +495,13 @@ def adjoint_rate(W, torch, res=(512, 512), spp=16, n_fd=64, n_fp64=64, fp64=True
            "speedup_vs_fd": ((nm + ne) / ((fwd_ms + bwd_ms) / 1e3)) / (n_fd / fd_s),
            "rel_err_vs_fd32_norm": float(np.linalg.norm(g_sel - fd) / np.linalg.norm(fd)),
            "e2e_forward_backward_s": e2e_s, "msamples_per_s_forward": n * spp / fwd_ms / 1e3,
-           "kernel_launches": {"forward_per_pass": 5, "backward_per_pass": 4}}
+           "kernel_launches": {"forward_per_pass": 5, "backward_per_pass": 4},
+           "roofline": roofline(3 * fwd_bytes, (fwd_ms + bwd_ms) / 1e3,
+                                "forward %.0f B/sample (%.0f static + %.0f traversal), backward twice the "
+                                "forward bytes" % (SAMPLE_BYTES_ENV + trav, SAMPLE_BYTES_ENV, trav),
+                                "forward + backward, CUDA events on the context stream"),
+           "roofline_forward": roofline(fwd_bytes, fwd_ms / 1e3, "forward bytes as above", "forward only"),
+           "traversal_terms": terms}
     if fp64:
         from oracle import binding as O
 
@@ -368,52 +510,75 @@ def adjoint_rate(W, torch, res=(512, 512), spp=16, n_fd=64, n_fp64=64, fp64=True
         t = time.perf_counter()
         _, _, g64 = o.adjoint_eval(res[0], res[1], spp, 0, 0, m0.astype(np.float64), e0.astype(np.float64),
                                    target, sub)
-        gs = grad[sub]
-        floor = 1e-2 * np.abs(g64).max()
-        out["fp64"] = {"params": int(len(sub)), "seconds": time.perf_counter() - t,
-                       "rel_err_max": float(np.max(np.abs(gs - g64) / np.maximum(np.abs(g64), floor))),
-                       "rel_err_norm": float(np.linalg.norm(gs - g64) / np.linalg.norm(g64)),
-                       "cores": O.lib().orc_num_threads()}
+        dual_s = time.perf_counter() - t
+        t = time.perf_counter()
+        fd64 = o.adjoint_fd(spp, 0, 0, m0.astype(np.float64), e0.astype(np.float64), target, sub, h=h)
+        fd64_s = time.perf_counter() - t
+        gs = grad[sub].astype(np.float64)
+
+        def errs(ref):
+            # per parameter |g - ref| / |ref|, unfloored; and with the
+            # denominator floored at 1 % of the largest |ref| of the set, which
+            # keeps parameters whose gradient is near zero (a texel few
+            # samples see) from dividing FP32 accumulation noise by ~0
+            a = np.abs(gs - ref)
+            nz = np.abs(ref) > 0
+            return {"rel_err_max": float(np.max(a / np.maximum(np.abs(ref), 1e-2 * np.abs(ref).max()))),
+                    "rel_err_max_unfloored": float(np.max(a[nz] / np.abs(ref[nz]))) if nz.any() else 0.0,
+                    "rel_err_median_unfloored": float(np.median(a[nz] / np.abs(ref[nz]))) if nz.any() else 0.0,
+                    "rel_err_norm": float(np.linalg.norm(gs - ref) / np.linalg.norm(ref))}
+
+        out["fp64"] = dict(params=int(len(sub)), seconds=dual_s, cores=O.lib().orc_num_threads(), **errs(g64))
+        out["fp64_central_differences"] = dict(params=int(len(sub)), h=h, seconds=fd64_s,
+                                               cores=O.lib().orc_num_threads(), **errs(fd64))
     return out
 
 
+def workload_config(n, sizes, hit_frac, world):
+    """The `config` object of both arms' lines (the same workload)."""
+    return {"workload": WORKLOAD, "rays_per_step": n, "triangles": sizes["n_prims"], "bvh_nodes": sizes["n_nodes"],
+            "treelets": sizes["n_treelets"], "bvh_depth": sizes["max_depth"], "hit_fraction": hit_frac,
+            "l2": "inputs larger than L2 (268 MB of rays), no flush",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def run_reference(args):
+    """The reference's CPU implementation of the path (the oracle's prune-free
+    candidate traversal + min-t reduce, JobProcessRayCasts/Results restated)
+    on every host thread: each step traces all 8,388,608 rays of the set, in
+    the GPU arm's order. Inputs come from the oracle library's copy of the
+    scene generator; the product library is never loaded."""
     import numpy as np
-    import woodenpbrengine_gb300 as W
 
-    g = W.SceneGen(1, 0, (RES, RES), level=LEVEL, rays=True)
-    rays = g.rays()
     from oracle import binding as O
+    from oracle.build import build_oracle
 
+    build_oracle()
+    g = O.SceneGen(1, 0, (RES, RES), level=LEVEL, rays=True)
+    rays = g.rays()
+    n = rays.shape[0]
     o = O.OracleScene(g.desc)
     cores = O.lib().orc_num_threads()
-    n = rays.shape[0]
-    step_rays = []
     times = []
-    rng = np.random.default_rng(3)
-    per_step = 4000
-    probe = rays[rng.choice(n, 2000, replace=False)]
-    t = time.perf_counter()
-    o.trace(probe, mode=0)
-    rate = probe.shape[0] / max(time.perf_counter() - t, 1e-6)
-    per_step = int(max(2000, rate * 2.0))
+    hits = None
     for s in range(args.warmup + args.steps):
-        sel = rng.choice(n, per_step, replace=False)
         t = time.perf_counter()
-        o.trace(rays[sel], mode=0)
+        hits = o.trace(rays, mode=0)
         dt = time.perf_counter() - t
         if s >= args.warmup:
             times.append(dt)
-            step_rays.append(per_step)
     tot = sum(times)
-    v = sum(step_rays) / tot / 1e6
+    v = n * args.steps / tot / 1e6
+    hit_frac = float(np.mean(hits[:, 1].view(np.uint32) != 0xFFFFFFFF))
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_rays_per_step": per_step},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded; the reference publishes no dataset)",
+        "config": workload_config(n, o.sizes(), hit_frac, 1),
         "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cores, "kind": "port",
-                         "sample": "%d random rays of the set per step, prune-free candidate traversal" % per_step},
+                         "sample": "all %d rays of the set per step, in the GPU arm's order; prune-free candidate "
+                                   "traversal + min-t reduce as in JobProcessRayCasts/Results" % n},
         "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -543,9 +708,6 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        from __graft_entry__ import build
-
-        build()
         run_reference(args)
         return
     import numpy as np
@@ -572,14 +734,23 @@ def main():
     ctx.upload(g.desc)
 
     # --- LBVH build rate (reported beside the headline) ---
+    # wpbr_bvh_build returns once the tree is built (it reads a few sizes back
+    # while it runs): wall time per build, and CUDA events on the context's
+    # stream from before its first kernel to after its last
     for _ in range(2):
         ctx.build()
     torch.cuda.synchronize()
-    t = time.perf_counter()
     nb = 5
+    eb0 = torch.cuda.Event(enable_timing=True)
+    eb1 = torch.cuda.Event(enable_timing=True)
+    build_dev_ms = 0.0
+    t = time.perf_counter()
     for _ in range(nb):
+        eb0.record(stream)
         ctx.build()
-    torch.cuda.synchronize()
+        eb1.record(stream)
+        eb1.synchronize()
+        build_dev_ms += eb0.elapsed_time(eb1) / nb
     build_s = (time.perf_counter() - t) / nb
     info = ctx.bvh_info()
 
@@ -644,6 +815,7 @@ def main():
     achieved = bytes_per_ray * n / (trav_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
     tpr = ncu_traffic_per_ray()
+    build_bytes = BUILD_BYTES_PER_PRIM * info["n_prims"]
 
     # --- e2e through the public host-buffer API (pinned) ---
     h_rays = torch.from_numpy(rays).pin_memory().numpy()
@@ -665,17 +837,30 @@ def main():
 
     render = None
     if rank == 0 and not args.no_render:
-        c0 = render_rate(W, torch, 0, (256, 256), 4, frames=3)
+        prof = "profiles/render_passes_profile_case.md"
+        render = {
+            "c0_plain_256x256_4spp": render_rate(W, torch, 0, (256, 256), 4, frames=3, profile=prof),
+            "c2_fullframe_1080p_64spp": render_rate(W, torch, 2, (1920, 1080), 64, level=LEVEL, profile=prof),
+            "c2_fullframe_1080p_16spp_sampled64": render_rate(W, torch, 2, (1920, 1080), 16, level=LEVEL,
+                                                              spectrum=W.SPECTRUM_SAMPLED64,
+                                                              profile="profiles/sampled64_pass_c2.md"),
+            "c5_textured_metal_1080p_16spp": render_rate(W, torch, 5, (1920, 1080), 16, profile=prof),
+            "c3_batched_32_scenes_16spp": batch_rate(W, torch),
+            "c4_adjoint_512x512_16spp": adjoint_rate(W, torch, fp64=not args.no_cpu)}
+        render["c3_batched_32_scenes_16spp"]["roofline"]["profile"] = prof
+        render["c4_adjoint_512x512_16spp"]["roofline"]["profile"] = prof
         if not args.no_cpu:
-            c0["cpu_baseline"] = cpu_render_rate(W, 0, (256, 256), 4)
-            c0["cpu_baseline_sampled64"] = cpu_render_rate(W, 0, (256, 256), 4, spectral=True)
-        render = {"c0_plain_256x256_4spp": c0,
-                  "c2_fullframe_1080p_64spp": render_rate(W, torch, 2, (1920, 1080), 64, level=LEVEL),
-                  "c2_fullframe_1080p_16spp_sampled64": render_rate(W, torch, 2, (1920, 1080), 16, level=LEVEL,
-                                                                    spectrum=W.SPECTRUM_SAMPLED64),
-                  "c5_textured_metal_1080p_16spp": render_rate(W, torch, 5, (1920, 1080), 16),
-                  "c3_batched_32_scenes_16spp": batch_rate(W, torch),
-                  "c4_adjoint_512x512_16spp": adjoint_rate(W, torch, fp64=not args.no_cpu)}
+            # the oracle's CPU render of the same frames on the host threads, beside each GPU rate
+            r = render
+            r["c0_plain_256x256_4spp"]["cpu_baseline"] = cpu_render_rate(W, 0, (256, 256), 4)
+            r["c0_plain_256x256_4spp"]["cpu_baseline_sampled64"] = cpu_render_rate(W, 0, (256, 256), 4,
+                                                                                   spectral=True)
+            r["c2_fullframe_1080p_64spp"]["cpu_baseline"] = cpu_render_rate(W, 2, (1920, 1080), 64, level=LEVEL)
+            r["c2_fullframe_1080p_16spp_sampled64"]["cpu_baseline"] = cpu_render_rate(
+                W, 2, (1920, 1080), 16, spectral=True, level=LEVEL)
+            r["c5_textured_metal_1080p_16spp"]["cpu_baseline"] = cpu_render_rate(W, 5, (1920, 1080), 16)
+            r["c3_batched_32_scenes_16spp"]["cpu_baseline"] = cpu_batch_rate()
+            r["c4_adjoint_512x512_16spp"]["cpu_baseline_forward"] = cpu_render_rate(W, 4, (512, 512), 16)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -692,10 +877,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; the reference publishes no dataset)",
-        "config": {"workload": WORKLOAD, "rays_per_step": n, "triangles": info["n_prims"],
-                   "bvh_nodes": info["n_nodes"], "treelets": info["n_treelets"], "bvh_depth": info["max_depth"],
-                   "hit_fraction": hit_frac, "l2": "inputs larger than L2 (268 MB of rays), no flush",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(n, info, hit_frac, world),
         "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 16 * n},
         "gpu_launches": args.steps * ctx.collide_launches(n),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -703,9 +885,18 @@ def main():
                      "kernel_ms_per_launch": trav_ms, "timed_launches": trav_launches,
                      "step_frac": bytes_per_ray * n / (ms_step / 1e3) / 1e9 / peak,
                      "traffic": (tpr * n) if tpr else None,
+                     # DRAM bytes actually moved (ncu, scaled by rays) over the launch time: most of the
+                     # byte model's node and primitive fetches are served from L2
+                     "traffic_frac": ((tpr * n) / (trav_ms / 1e3) / 1e9 / peak) if tpr else None,
                      "bytes_model": "48 + 32*V + 36*P per ray, V=%.2f box tests, P=%.2f triangle tests" % (V, P)},
         "clocks": ck,
-        "build": {"mprims_per_s": info["n_prims"] / build_s / 1e6, "ms": build_s * 1e3},
+        "build": {"mprims_per_s": info["n_prims"] / build_s / 1e6, "ms": build_s * 1e3,
+                  "mprims_per_s_device": info["n_prims"] / build_dev_ms / 1e3, "ms_device": build_dev_ms,
+                  "timing": "ms: wall time per build (host returns after the last kernel); ms_device: CUDA events "
+                            "around each build on the context's stream",
+                  "roofline": roofline(build_bytes, build_dev_ms / 1e3,
+                                       "240 B per primitive (bounds + Morton 56, radix sort 64, emit + refit 120)",
+                                       "CUDA events around one build")},
         "anyhit_mrays_per_s": any_rate,
         "render": render,
         "cpu_baseline": cpu,

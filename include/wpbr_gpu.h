@@ -317,6 +317,25 @@ WPBR_API wpbr_status wpbr_adjoint_forward_device(wpbr_ctx* ctx, const float* d_t
 WPBR_API wpbr_status wpbr_adjoint_backward(wpbr_ctx* ctx, float* grad_mat, float* grad_env);
 WPBR_API wpbr_status wpbr_adjoint_backward_device(wpbr_ctx* ctx, float* d_grad_mat, float* d_grad_env);
 
+/* ---- testing aids ------------------------------------------------------------
+ * No counterpart in the reference (its traversal stack, nodesToVisit[256] in
+ * SLBVH.cpp:101, is unchecked, and its allocators abort on failure). */
+/* Lowers the traversal's bounds so that their limit paths can be exercised:
+ * at most max_stack_entries entries on a lane's traversal stack (at most
+ * 256) and max_loop_steps iterations of a traversal loop (the persistent
+ * kernels count a warp's rounds); 0 restores a default (the stack the tree's
+ * depth needs, 2^26 steps). A traversal that reaches a bound gives up on the
+ * rays it holds (their hits are not valid), records the bound in the device
+ * error word and returns, so wpbr_check_device_errors returns
+ * WPBR_ERR_TRAVERSAL_LIMIT; nothing traps and the context stays usable.
+ * Applies to later launches (pass graphs are recaptured). */
+WPBR_API wpbr_status wpbr_set_traversal_limits(wpbr_ctx* ctx, uint32_t max_stack_entries, uint32_t max_loop_steps);
+/* Process-wide device-allocation fault injection: with n >= 0 the library's
+ * next n device allocations succeed and every later one fails (cudaMalloc is
+ * not called), so the call that needed it returns WPBR_ERR_OOM; n < 0 (the
+ * default) disables it. */
+WPBR_API void wpbr_debug_fail_allocations(int64_t n);
+
 /* Library build identification (host-only). */
 WPBR_API const char* wpbr_version(void);
 

@@ -174,6 +174,8 @@ enum wpbr_quirk {
    * Default: stratification over the passes with the intended 1/n scale. */
   WPBR_Q_REF_SAMPLER_ARRAYS = 1u << 6
 };
+/* Every defined quirk bit; other bits are rejected. */
+#define WPBR_QUIRK_MASK 0x7Fu
 
 #ifdef __cplusplus
 }

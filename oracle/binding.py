@@ -49,6 +49,8 @@ _SIGS = {
     "orc_adjoint_eval": (C.c_double, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_double),
                                       C.POINTER(C.c_double), _FP, C.POINTER(C.c_double), C.c_uint32, _UP,
                                       C.POINTER(C.c_double)]),
+    "orc_adjoint_fd": (None, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_double),
+                              C.POINTER(C.c_double), _FP, C.c_uint32, _UP, C.c_double, C.POINTER(C.c_double)]),
 }
 _lib = None
 
@@ -172,6 +174,19 @@ class OracleScene:
         rec, arrays = A.make_record((x1 - x0) * (y1 - y0), fields)
         lib().orc_render_pass(self._h, p, spp, seed, stream, x0, y0, x1, y1, C.byref(rec))
         return arrays
+
+    def adjoint_fd(self, spp, seed, stream, mat, env, target, sel, h=1e-3):
+        """FP64 central differences (step h) of the frozen estimator's loss
+        at the parameter indices `sel`."""
+        dp = C.POINTER(C.c_double)
+        mat = np.ascontiguousarray(mat, np.float64)
+        env = np.ascontiguousarray(env if env is not None else np.zeros(0), np.float64)
+        tgt = np.ascontiguousarray(target, np.float32)
+        sel_a = np.ascontiguousarray(sel, np.uint32)
+        fd = np.zeros(len(sel_a), np.float64)
+        lib().orc_adjoint_fd(self._h, spp, seed, stream, mat.ctypes.data_as(dp), env.ctypes.data_as(dp), _fp(tgt),
+                             len(sel_a), _up(sel_a), h, fd.ctypes.data_as(dp))
+        return fd
 
     def adjoint_eval(self, W, H, spp, seed, stream, mat, env, target=None, sel=None, image=False):
         """FP64 frozen-direction estimator at parameters (mat, env): returns

@@ -1375,6 +1375,31 @@ double orc_adjoint_eval(void* h, uint32_t spp, uint32_t seed, uint32_t stream, c
   }
   return loss;
 }
+/* FP64 central differences of the frozen-direction estimator's loss: for
+ * each parameter index in sel (materials first, then texels), the loss at
+ * the parameter + h and - h (the other parameters at mat / env, the frozen
+ * state computed once), fd[k] = (loss(+h) - loss(-h)) / (2h). */
+void orc_adjoint_fd(void* h, uint32_t spp, uint32_t seed, uint32_t stream, const double* mat, const double* env,
+                    const float* target, uint32_t n_sel, const uint32_t* sel, double step, double* fd) {
+  const Scene& sc = *(const Scene*)h;
+  std::vector<Frozen> fz = freeze_all(sc, spp, seed, stream);
+  const size_t nm = sc.mats.size() * 10;
+  EvalParams<double> P;
+  load_params(sc, mat, env, P);
+  for (uint32_t k = 0; k < n_sel; ++k) {
+    uint32_t idx = sel[k];
+    double* slot = idx < nm ? &P.mat[idx] : &P.env[idx - nm];
+    const double v0 = *slot;
+    double l[2];
+    for (int side = 0; side < 2; ++side) {
+      *slot = v0 + (side == 0 ? step : -step);
+      if (sc.has_env) eval_env_distribution(sc.env, sc.quirks, P);
+      l[side] = eval_loss(sc, fz, spp, P, target, nullptr);
+    }
+    *slot = v0;
+    fd[k] = (l[0] - l[1]) / (2.0 * step);
+  }
+}
 /* Sampled64 render: spp passes of the spectral per-sample job list; the
  * film's spectra resolved with toRGB (acc_L[W*H*3]) and the weights. */
 void orc_render_spectral(void* h, uint32_t spp, uint32_t seed, uint32_t stream, float* acc_L, float* acc_w) {

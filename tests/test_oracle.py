@@ -182,6 +182,9 @@ def test_fp64_estimator_dual_gradient_matches_central_differences(W, O):
             em[i - m0.size] -= h
         fd = (o.adjoint_eval(40, 32, 2, 0, 0, mp, ep, target)[0] - o.adjoint_eval(40, 32, 2, 0, 0, mm, em, target)[0]) / (2 * h)
         assert abs(grad[k] - fd) <= 1e-4 * max(abs(fd), 1e-3 * np.abs(grad).max()), (i, grad[k], fd)
+        # the same differences with the frozen state computed once
+        fd1 = o.adjoint_fd(2, 0, 0, m0, e0, target, [i], h=h)[0]
+        assert abs(fd1 - fd) <= 1e-9 * max(abs(fd), 1e-12), (i, fd, fd1)
 
 
 def test_spectral_tables_and_conversions(W, O):

@@ -104,6 +104,8 @@ _SIGS = {
     "wpbr_batch_film_read": (C.c_int, [_VP, C.c_uint32, _FP, _FP]),
     "wpbr_batch_set_stream": (C.c_int, [_VP, _VP]),
     "wpbr_batch_check_device_errors": (C.c_int, [_VP]),
+    "wpbr_set_traversal_limits": (C.c_int, [_VP, C.c_uint32, C.c_uint32]),
+    "wpbr_debug_fail_allocations": (None, [C.c_int64]),
 }
 SORT_NOALLOC_MAX_KEYS = 1 << 20
 EXPORTED = sorted(_SIGS)
@@ -138,6 +140,12 @@ def _fp(a):
 
 def _up(a):
     return a.ctypes.data_as(_UP) if a is not None else None
+
+
+def debug_fail_allocations(n):
+    """Testing aid: the library's next n device allocations succeed, later ones
+    fail as out-of-memory; n < 0 disables the injection."""
+    lib().wpbr_debug_fail_allocations(n)
 
 
 class SceneGen:
@@ -275,6 +283,11 @@ class Context:
             return hits, st
         self._check(lib().wpbr_collide(self._h, _fp(rays), n, _fp(hits), mode), "collide")
         return hits
+
+    def set_traversal_limits(self, max_stack_entries=0, max_loop_steps=0):
+        """Testing aid: lower the traversal's stack / loop bounds (0: default)."""
+        self._check(lib().wpbr_set_traversal_limits(self._h, max_stack_entries, max_loop_steps),
+                    "set_traversal_limits")
 
     def collide_launches(self, n):
         """Kernels one collide_device call of n rays launches."""

@@ -602,6 +602,7 @@ wpbr_status adjoint_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t s
     return set_err(ctx, WPBR_ERR_INVALID_ARG, "adjoint_setup: more than 1024 materials");
   AdjState& J = ctx->adj;
   cudaStream_t st = ctx->stream;
+  J.ready = false;  // until every buffer below exists
   J.spp = spp;
   J.seed = seed;
   J.stream = stream;

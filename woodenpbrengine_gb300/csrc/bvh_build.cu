@@ -1399,7 +1399,20 @@ cudaError_t radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t*
 // ---------------------------------------------------------------------------
 // host orchestration
 // ---------------------------------------------------------------------------
+static wpbr_status bvh_build_tree(wpbr_ctx* ctx);
+
+// A build that fails part way may have reallocated the traversal buffers
+// that a render or adjoint setup captured; those setups stop being ready.
 wpbr_status bvh_build(wpbr_ctx* ctx) {
+  wpbr_status st = bvh_build_tree(ctx);
+  if (st != WPBR_OK) {
+    ctx->rs.ready = false;
+    ctx->adj.ready = false;
+  }
+  return st;
+}
+
+static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   if (!ctx->has_scene) return set_err(ctx, WPBR_ERR_NOT_BUILT, "bvh_build: no scene uploaded");
   BvhState& B = ctx->bvh;
   cudaStream_t st = ctx->stream;
@@ -1412,6 +1425,8 @@ wpbr_status bvh_build(wpbr_ctx* ctx) {
     B.T = B.M = B.n_int = B.max_depth = 0;
     B.view = BvhView{};
     B.view.empty = 1;
+    B.view.stack_cap = kDefaultStackCap;
+    B.view.step_cap = kDefaultStepCap;
     B.built = true;
     return WPBR_OK;
   }
@@ -1712,6 +1727,8 @@ wpbr_status bvh_build(wpbr_ctx* ctx) {
     v.root_hi[k] = b0[3 + k];
   }
   v.max_depth = depth + split_d;
+  v.stack_cap = kDefaultStackCap;
+  v.step_cap = kDefaultStepCap;
   v.n_prims = N;
   v.n_int = B.n_int + n_split;
   B.view = v;

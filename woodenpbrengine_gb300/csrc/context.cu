@@ -153,11 +153,25 @@ void bvh_release(wpbr_ctx* ctx, bool keep_traversal) {
   }
 }
 
+std::atomic<long long> g_alloc_budget{-1};
+
 }  // namespace wpbr
 
 extern "C" {
 
 WPBR_API const char* wpbr_version(void) { return "wpbr-gb300 1.0 (sm_103a)"; }
+
+WPBR_API wpbr_status wpbr_set_traversal_limits(wpbr_ctx* ctx, uint32_t max_stack_entries, uint32_t max_loop_steps) {
+  if (!ctx) return WPBR_ERR_INVALID_ARG;
+  if (max_stack_entries > 256)
+    return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_traversal_limits: at most 256 stack entries");
+  ctx->lim_stack = max_stack_entries;
+  ctx->lim_steps = max_loop_steps;
+  ++ctx->epoch;  // the pass graphs bake the bounds into their kernel arguments
+  return WPBR_OK;
+}
+
+WPBR_API void wpbr_debug_fail_allocations(int64_t n) { g_alloc_budget.store(n < 0 ? -1 : (long long)n); }
 
 WPBR_API wpbr_status wpbr_create(int device, wpbr_ctx** out) {
   if (!out) return WPBR_ERR_INVALID_ARG;
@@ -178,6 +192,8 @@ WPBR_API wpbr_status wpbr_create(int device, wpbr_ctx** out) {
   if (e == cudaSuccess) e = cudaMemset(ctx->d_err.p, 0, 4);
   if (e != cudaSuccess) {
     cudaGetLastError();
+    ctx->d_err.release();
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return e == cudaErrorMemoryAllocation ? WPBR_ERR_OOM : WPBR_ERR_CUDA;
   }
@@ -245,7 +261,7 @@ WPBR_API void* wpbr_get_stream(const wpbr_ctx* ctx) { return ctx ? (void*)ctx->s
 
 WPBR_API wpbr_status wpbr_set_quirks(wpbr_ctx* ctx, uint32_t quirks) {
   if (!ctx) return WPBR_ERR_INVALID_ARG;
-  if (quirks & ~0x3Fu) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_quirks: unknown bits");
+  if (quirks & ~WPBR_QUIRK_MASK) return set_err(ctx, WPBR_ERR_INVALID_ARG, "set_quirks: unknown bits");
   uint32_t changed = ctx->quirks ^ quirks;
   ctx->quirks = quirks;
   ++ctx->epoch;
@@ -319,8 +335,18 @@ WPBR_API wpbr_status wpbr_scene_upload(wpbr_ctx* ctx, const wpbr_scene_desc* d) 
   for (uint64_t i = 0; i < 3ull * d->n_triangles; ++i)
     if (d->indices[i] >= d->n_vertices) return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: vertex index out of range");
   for (uint32_t i = 0; i < d->n_spheres; ++i)
-    if (d->spheres[i].material >= d->n_materials || !(d->spheres[i].radius > 0.0f))
+    if (d->spheres[i].material >= d->n_materials || !(d->spheres[i].radius > 0.0f) ||
+        !std::isfinite(d->spheres[i].radius))
       return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: sphere material or radius invalid");
+  // non-finite geometry would give NaN bounds and Morton codes (the
+  // reference's float-to-integer conversion of them is undefined)
+  for (uint32_t i = 0; i < d->n_spheres; ++i)
+    for (int k = 0; k < 16; ++k)
+      if (!std::isfinite(d->spheres[i].object_to_world.m[k]) || !std::isfinite(d->spheres[i].world_to_object.m[k]))
+        return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: non-finite sphere transform");
+  if (d->n_triangles)
+    for (uint64_t i = 0; i < 3ull * d->n_vertices; ++i)
+      if (!std::isfinite(d->positions[i])) return set_err(ctx, WPBR_ERR_INVALID_ARG, "scene: non-finite vertex position");
   std::vector<uint32_t> tmat(d->n_triangles, 0xFFFFFFFFu), tfl(d->n_triangles, 0);
   for (uint32_t m = 0; m < d->n_meshes; ++m) {
     const wpbr_mesh& ms = d->meshes[m];

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -12,6 +13,20 @@
 #include "wpbr_gpu.h"
 
 namespace wpbr {
+
+// Allocation fault injection (wpbr_debug_fail_allocations): while the
+// budget is >= 0, that many further device allocations succeed and every
+// later one fails as out-of-memory without reaching cudaMalloc. Process-wide;
+// -1 (the default) disables it.
+extern std::atomic<long long> g_alloc_budget;
+inline cudaError_t dev_malloc(void** p, size_t bytes) {
+  long long b = g_alloc_budget.load();
+  while (b >= 0) {
+    if (b == 0) return cudaErrorMemoryAllocation;
+    if (g_alloc_budget.compare_exchange_weak(b, b - 1)) break;
+  }
+  return cudaMalloc(p, bytes);
+}
 
 template <typename T>
 struct DevBuf {
@@ -23,7 +38,7 @@ struct DevBuf {
     p = nullptr;
     n = 0;
     size_t bytes = (count ? count : 1) * sizeof(T);
-    cudaError_t e = cudaMalloc((void**)&p, bytes);
+    cudaError_t e = dev_malloc((void**)&p, bytes);
     if (e == cudaSuccess) n = count;
     return e;
   }
@@ -140,6 +155,7 @@ struct wpbr_ctx {
   uint32_t quirks = 0;
   uint64_t epoch = 0;  // bumped by every scene upload, BVH build, quirk or traversal change
   uint32_t traversal = 0;  // wpbr_traversal: 0 binary (leaf-split), 2 binary over the reference's leaves
+  uint32_t lim_stack = 0, lim_steps = 0;  // wpbr_set_traversal_limits (0: the defaults)
   uint32_t spectrum = 0;   // wpbr_spectrum: 0 RGB, 1 Sampled64
   wpbr::DevBuf<uint32_t> d_err;
   // scene
@@ -209,6 +225,8 @@ namespace wpbr {
 inline BvhView traversal_view(const wpbr_ctx* ctx) {
   BvhView v = ctx->bvh.view;
   if (ctx->traversal == WPBR_TRAVERSAL_BINARY_FULL_LEAVES) v = reference_leaves_view(v);
+  if (ctx->lim_stack) v.stack_cap = ctx->lim_stack;
+  if (ctx->lim_steps) v.step_cap = ctx->lim_steps;
   return v;
 }
 // The view of the render passes' traversals (camera and shadow rays of the

@@ -489,6 +489,9 @@ wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t st
   if (!ctx->bvh.built) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render_setup: BVH not built");
   if (spp == 0) return set_err(ctx, WPBR_ERR_INVALID_ARG, "render_setup: spp must be > 0");
   RenderState& R = ctx->rs;
+  // not ready until every buffer below exists: a failed allocation here must
+  // not leave an earlier setup's graph (or its freed buffers) usable
+  R.ready = false;
   R.spp = spp;
   R.seed = seed;
   R.stream = stream;

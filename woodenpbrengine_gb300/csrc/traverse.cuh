@@ -86,7 +86,7 @@ __device__ HitRec trace_ray(const SceneView& S, const BvhView& Bv, V3 o, V3 d, f
   uint32_t iters = 0;
   while (true) {
     bool go = false;
-    if (++iters > (1u << 22)) {  // a well-formed tree never gets here
+    if (++iters > Bv.step_cap) {  // a well-formed tree never gets here
       atomicOr(err, kErrLoopLimit);
       break;
     }
@@ -106,7 +106,7 @@ __device__ HitRec trace_ray(const SceneView& S, const BvhView& Bv, V3 o, V3 d, f
       uint32_t c0n = (uint32_t)m.z, c1n = ((uint32_t)m.w) & 0x3FFFFFFFu;
       if (h0 && h1) {
         bool first1 = second_child_first(neg, axis);
-        if (sp >= STACK) {
+        if (sp >= STACK || (uint32_t)sp >= Bv.stack_cap) {
           atomicOr(err, kErrStackOverflow);
           break;
         }

@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
       }
     }
     if (__all_sync(0xFFFFFFFFu, !active && exhausted)) break;
-    if (++guard > (1u << 26)) {
+    if (++guard > Bv.step_cap) {
       if (lane == 0) atomicOr(err, kErrLoopLimit);
       break;
     }
@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
         uint32_t c0n = (uint32_t)m.z, c1n = ((uint32_t)m.w) & 0x3FFFFFFFu;
         if (h0 && h1) {
           bool first1 = second_child_first(neg, axis);
-          if (sp >= STACK) {
+          if ((uint32_t)sp >= Bv.stack_cap) {  // stack_cap <= STACK (launch_traversal clamps it)
             atomicOr(err, kErrStackOverflow);
             ref = kEnd;
             break;
@@ -448,15 +448,17 @@ struct PrimSink {
 template <bool ANY, class Src, class Sink>
 inline void launch_traversal(const SceneView& S, const BvhView& Bv, const Src& src, const Sink& sink, uint32_t n,
                              uint32_t* counter, uint32_t* err, cudaStream_t st, uint32_t grid_cap = 0) {
-  auto go = [&](auto kern) {
+  auto go = [&](auto kern, uint32_t stack) {
     unsigned full = persistent_grid((const void*)kern, kPersistBlock);
     unsigned g = (grid_cap && grid_cap < full) ? grid_cap : full;
-    kern<<<g, kPersistBlock, 0, st>>>(S, Bv, src, sink, n, counter, err);
+    BvhView B = Bv;
+    if (B.stack_cap > stack) B.stack_cap = stack;
+    kern<<<g, kPersistBlock, 0, st>>>(S, B, src, sink, n, counter, err);
   };
   if (Bv.max_depth < 60)
-    go(k_trace_persistent<ANY, 64, Src, Sink>);
+    go(k_trace_persistent<ANY, 64, Src, Sink>, 64u);
   else
-    go(k_trace_persistent<ANY, 256, Src, Sink>);
+    go(k_trace_persistent<ANY, 256, Src, Sink>, 256u);
 }
 
 }  // namespace wpbr

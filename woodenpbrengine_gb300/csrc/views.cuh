@@ -61,7 +61,16 @@ struct BvhView {
   uint32_t n_prims, n_int;  // bounds for the index guards in traversal
   uint32_t n_ref_int;       // records of nodes_ref
   uint32_t ref_depth;       // depth of the reference's tree (max_depth adds the split levels)
+  uint32_t stack_cap;       // stack entries a lane may use (launches clamp it to the kernel's array)
+  uint32_t step_cap;        // iterations of a traversal loop before the traversal gives up
 };
+
+// Bounds of a well-formed traversal: the stack never holds more entries than
+// the tree is deep (the kernels' arrays are sized for that), and no loop
+// comes near 2^26 iterations. wpbr_set_traversal_limits lowers them to
+// exercise the limit paths.
+constexpr uint32_t kDefaultStackCap = 0xFFFFFFFFu;
+constexpr uint32_t kDefaultStepCap = 1u << 26;
 
 // The same tree traversed over the reference's leaves as they are (the
 // statistics kernel counts box and primitive tests of this layout).
