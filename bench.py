@@ -58,6 +58,16 @@ SAMPLE_BYTES_SAMPLED64 = SAMPLE_BYTES_ENV - 256.0 + 16 * (64 * 4 + 4)
 # vertices in, 8 B out), radix sort 64 B (16 B per pass, 4 passes), emit and
 # refit 120 B (codes 12, node 12, leaf bounds 24, child bounds 48, write 24).
 BUILD_BYTES_PER_PRIM = 56.0 + 64.0 + 120.0
+# kernels of one fused sample pass: camera traversal, spawn, shadow traversal,
+# finish, film; films of 2^17 pixels and more add the two kernels that order
+# the pixels by material category
+SORT_MIN_PIXELS = 1 << 17
+
+
+def pass_launches(pixels):
+    return 5 + (2 if pixels >= SORT_MIN_PIXELS else 0)
+
+
 STAGES = ["CAMERA_RAYS", "COLLIDE_PRIMARY", "EMITTED_LIGHT", "BSDF_SETUP", "SAMPLE_LIGHT", "SHADOW_LIGHT",
           "BSDF_COMPUTE", "INTEGRATE_LIGHT", "SAMPLE_BSDF", "SHADOW_BSDF", "LIGHT_COMPUTE", "INTEGRATE_BSDF"]
 
@@ -263,7 +273,7 @@ def render_rate(W, torch, config, res, spp, level=0, frames=1, spectrum=None, pr
         SAMPLE_BYTES_ENV if env else SAMPLE_BYTES_SPHERE)
     per_sample = static + trav
     out = {"msamples_per_s": samples / ms / 1e3, "ms_per_frame": ms, "film": "%dx%d" % res, "spp": spp,
-           "kernel_launches_per_pass": 5,
+           "kernel_launches_per_pass": pass_launches(res[0] * res[1]),
            "roofline": roofline(per_sample * samples, ms / 1e3,
                                 "%.0f B/sample static + %.0f B/sample traversal (32 B per box test, 36 B per "
                                 "primitive test of the camera and shadow rays)%s"
@@ -392,7 +402,9 @@ def batch_rate(W, torch, n_scenes=32, spp=16, film_scale=1024, max_count=2000000
             "msamples_per_s_sequential": samples / ms_seq / 1e3, "ms_per_frame_sequential": ms_seq,
             "speedup": ms_seq / ms_batch, "build_ms_all_scenes": build_s * 1e3,
             "scene0_film_identical": same,
-            "graph_launches_per_frame": spp, "kernel_launches_per_frame": 5 * n_scenes * spp}
+            "graph_launches_per_frame": spp,
+            "kernel_launches_per_frame": spp * sum(pass_launches(g.desc.contents.camera.res_x *
+                                                                g.desc.contents.camera.res_y) for g in gens)}
 
 
 def _c4_params(desc):

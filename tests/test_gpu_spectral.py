@@ -13,7 +13,9 @@ def _same_nan_aware(a, b):
 
 
 @pytest.mark.parametrize("config,res,level,quirks", [(0, (64, 48), 0, 0), (2, (48, 32), 4, 2), (2, (48, 32), 4, 32),
-                                                     (0, (37, 23), 0, 0), (2, (70, 41), 4, 0)])
+                                                     (0, (37, 23), 0, 0), (2, (70, 41), 4, 0),
+                                                     # 2^17 pixels and more: spawn and finish in material order
+                                                     (2, (512, 256), 5, 0), (0, (400, 330), 0, 64)])
 def test_spectral_film_matches_oracle(W, O, ctx, config, res, level, quirks):
     g = W.SceneGen(config, 0, res, level=level)
     ctx.set_quirks(quirks)

@@ -131,6 +131,29 @@ def test_textures_change_the_image(W, O, ctx, scene):
     ctx.check_device_errors()
 
 
+@pytest.mark.parametrize("spectrum", [0, 1])
+def test_material_sorted_films_match_oracle(W, O, ctx, spectrum):
+    # a film of 2^17 pixels: the spawn and finish kernels run over the pixels
+    # ordered by primitive kind and material type (textured metal, conductor,
+    # dielectric, specular on spheres and the ground, misses), RGB and Sampled64
+    g = W.SceneGen(5, 0, (512, 256))
+    ctx.set_quirks(0)
+    ctx.set_spectrum(spectrum)
+    try:
+        ctx.upload(g.desc)
+        ctx.build()
+        ctx.render_setup(2, seed=1, stream=2)
+        ctx.render()
+        L, w = ctx.film(512, 256)
+        o = O.OracleScene(g.desc)
+        Lo, wo = o.render_spectral(512, 256, 2, 1, 2) if spectrum else o.render(512, 256, 2, 1, 2)
+        assert np.array_equal(w, wo)
+        assert _same_nan_aware(L, Lo)
+    finally:
+        ctx.set_spectrum(0)
+    ctx.check_device_errors()
+
+
 def test_spectral_film_matches_oracle(W, O, ctx, scene):
     Wd, Hd = RES
     ctx.set_quirks(0)

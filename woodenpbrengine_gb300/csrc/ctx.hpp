@@ -108,7 +108,9 @@ struct RenderState {
   cudaGraphExec_t graph = nullptr;
   uint64_t graph_key = 0;
   DevBuf<uint32_t> pass_dev;  // pass index read by the captured kernels
-  DevBuf<uint32_t> counters;  // ray-fetch counters of the pass's traversal launches
+  DevBuf<uint32_t> counters;  // ray-fetch counters of the pass's traversal launches, then the
+                              // per-category pixel counts and cursors of the material-sorted order
+  DevBuf<uint32_t> order;     // the pass's pixels grouped by material category (k_cat_scatter)
   // Sampled64 mode: material / light spectra, per-pixel sample spectra, film spectra
   DevBuf<float> spec_mats, spec_le, spec_L, spec_acc;
   bool spec_dirty = false;  // Sampled64 passes ran since the last toRGB of the film
@@ -261,8 +263,9 @@ wpbr_status render_pass_launch(wpbr_ctx* ctx);
 wpbr_status spectral_setup(wpbr_ctx* ctx);
 // Sampled64 pieces of render_pass_launch: the scalar spawn (replaces the
 // RGB spawn) and the per-bin finish + film (replace the RGB finish + film).
-cudaError_t spectral_spawn_launch(wpbr_ctx* ctx, const uint32_t* pass_ptr);
-cudaError_t spectral_finish_launch(wpbr_ctx* ctx);
+// `order`: the material-sorted pixel order (null: film order).
+cudaError_t spectral_spawn_launch(wpbr_ctx* ctx, const uint32_t* pass_ptr, const uint32_t* order);
+cudaError_t spectral_finish_launch(wpbr_ctx* ctx, const uint32_t* order);
 wpbr_status spectral_resolve(wpbr_ctx* ctx);
 // float4 per pixel of the fused pass's state buffer (RenderState::pstate);
 // the RGB and the Sampled64 spawn records both fit in it.

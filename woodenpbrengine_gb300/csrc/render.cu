@@ -254,8 +254,11 @@ enum : uint32_t { SF_VALID = 1u, SF_TRACE_L = 2u, SF_TRACE_B = 4u, SF_HIT = 8u, 
 
 template <bool TEX>
 __global__ void __launch_bounds__(kTB, TEX ? WPBR_SPAWN_TEX_MIN_BLOCKS : WPBR_SPAWN_MIN_BLOCKS) k_spawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
-                                               float4* state, float4* rays, float4* Lb, float2* pf) {
-  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+                                               float4* state, float4* rays, float4* Lb, float2* pf,
+                                               const uint32_t* order) {
+  uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= P.W * P.H) return;
+  uint32_t pix = order ? order[slot] : slot;  // material-sorted (large films)
   if (pix >= P.W * P.H) return;
   uint32_t pass = *pass_dev;
   float fx, fy;
@@ -323,8 +326,11 @@ __global__ void __launch_bounds__(kTB, TEX ? WPBR_SPAWN_TEX_MIN_BLOCKS : WPBR_SP
   Lb[pix] = make_float4(L.r, L.g, L.b, 0.0f);
 }
 
-__global__ void __launch_bounds__(kTB) k_finish(PassCtx P, const float4* state, const uint32_t* shadow, float4* Lb) {
-  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kTB) k_finish(PassCtx P, const float4* state, const uint32_t* shadow, float4* Lb,
+                                                const uint32_t* order) {
+  uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= P.W * P.H) return;
+  uint32_t pix = order ? order[slot] : slot;  // material-sorted (large films)
   if (pix >= P.W * P.H) return;
   const float4* st = state + (size_t)pix * kStateF4;
   float4 s4 = st[4];
@@ -506,7 +512,8 @@ wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t st
   WPBR_CUDA(R.Lbuf.ensure(n));
   WPBR_CUDA(R.pfilm.ensure(n));
   WPBR_CUDA(R.pass_dev.ensure(1));
-  WPBR_CUDA(R.counters.ensure(2));  // allocated before any graph capture
+  WPBR_CUDA(R.counters.ensure(2 + 2 * kPixCats));  // allocated before any graph capture
+  WPBR_CUDA(R.order.ensure(n));
   WPBR_CUDA(cudaMemsetAsync(R.acc.p, 0, n * 4 * sizeof(float), ctx->stream));
   if (ctx->spectrum == WPBR_SPECTRUM_SAMPLED64) {
     wpbr_status sst = spectral_setup(ctx);
@@ -527,16 +534,26 @@ wpbr_status render_pass_launch(wpbr_ctx* ctx) {
   uint32_t n = R.W * R.H;
   cudaStream_t st = ctx->stream;
   const uint32_t* pass_ptr = R.pass_ptr ? R.pass_ptr : R.pass_dev.p;
-  WPBR_CUDA(R.counters.ensure(2));
-  WPBR_CUDA(cudaMemsetAsync(R.counters.p, 0, 2 * sizeof(uint32_t), st));
+  WPBR_CUDA(R.counters.ensure(2 + 2 * kPixCats));
+  WPBR_CUDA(R.order.ensure(n));
+  WPBR_CUDA(cudaMemsetAsync(R.counters.p, 0, (2 + 2 * kPixCats) * sizeof(uint32_t), st));
   bool spectral = ctx->spectrum == WPBR_SPECTRUM_SAMPLED64;
   launch_traversal<false>(P.S, P.Bv, CameraSrc{P, pass_ptr}, PrimSink{R.hit_prim.p}, n, R.counters.p, P.err, st,
                           R.trace_grid);
+  // the pixels in material-sorted order for the spawn and finish kernels
+  const uint32_t* order = nullptr;
+  if (n >= kSortMinPixels) {
+    uint32_t* cat_counts = R.counters.p + 2;
+    k_cat_count<<<div_up(n, kCatBlock), kCatBlock, 0, st>>>(P.S, n, R.hit_prim.p, cat_counts);
+    k_cat_scatter<<<div_up(n, kCatBlock), kCatBlock, 0, st>>>(P.S, n, R.hit_prim.p, cat_counts,
+                                                              cat_counts + kPixCats, R.order.p, P.err);
+    order = R.order.p;
+  }
   if (spectral)
-    WPBR_CUDA(spectral_spawn_launch(ctx, pass_ptr));
+    WPBR_CUDA(spectral_spawn_launch(ctx, pass_ptr, order));
   else
     (ctx->has_metal ? k_spawn<true> : k_spawn<false>)<<<div_up(n, kTB), kTB, 0, st>>>(
-        P, pass_ptr, R.hit_prim.p, R.pstate.p, R.shadow_rays.p, R.Lbuf.p, R.pfilm.p);
+        P, pass_ptr, R.hit_prim.p, R.pstate.p, R.shadow_rays.p, R.Lbuf.p, R.pfilm.p, order);
   // shadow rays: unoccluded iff no hit or the closest hit is the sampled
   // light's primitive; with environment lights only that is "no hit", which
   // the any-hit traversal decides with the same primitive tests, stopping at
@@ -548,9 +565,9 @@ wpbr_status render_pass_launch(wpbr_ctx* ctx) {
     launch_traversal<false>(P.S, P.Bv, BufferSrc{R.shadow_rays.p}, PrimSink{R.shadow_hit.p}, 2 * n,
                             R.counters.p + 1, P.err, st, R.trace_grid);
   if (spectral) {
-    WPBR_CUDA(spectral_finish_launch(ctx));
+    WPBR_CUDA(spectral_finish_launch(ctx, order));
   } else {
-    k_finish<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pstate.p, R.shadow_hit.p, R.Lbuf.p);
+    k_finish<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pstate.p, R.shadow_hit.p, R.Lbuf.p, order);
     k_film<<<div_up(n, kTB), kTB, 0, st>>>(R.W, R.H, R.pfilm.p, R.Lbuf.p, (float4*)R.acc.p);
   }
   WPBR_CUDA(cudaGetLastError());
@@ -581,7 +598,7 @@ static uint64_t pass_graph_key(const wpbr_ctx* ctx) {
   mix((uint64_t)R.trace_grid);
   mix((uint64_t)ctx->spectrum | ((uint64_t)ctx->quirks << 8));
   const void* ptrs[] = {R.acc.p,    R.hit_prim.p, R.shadow_rays.p,     R.shadow_hit.p,      R.pstate.p,
-                        R.Lbuf.p,   R.pfilm.p,    R.pass_dev.p,        R.counters.p,        R.pass_ptr,
+                        R.Lbuf.p,   R.pfilm.p,    R.pass_dev.p,        R.counters.p,        R.pass_ptr, R.order.p,
                         ctx->d_err.p, ctx->bvh.view.nodes,
                         ctx->bvh.view.prims, R.spec_mats.p, R.spec_le.p, R.spec_L.p, R.spec_acc.p};
   for (const void* q : ptrs) mix((uint64_t)(uintptr_t)q);

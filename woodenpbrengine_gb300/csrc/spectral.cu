@@ -136,8 +136,10 @@ __device__ __forceinline__ FScalars f_scalars(const wpbr_material& m, float d_wh
 
 template <bool TEX>
 __global__ void __launch_bounds__(kTB, TEX ? WPBR_SPAWN_TEX_MIN_BLOCKS : WPBR_SPAWN_MIN_BLOCKS) k_sspawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
-                                                float4* state, float4* rays, float2* pf) {
-  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+                                                float4* state, float4* rays, float2* pf, const uint32_t* order) {
+  uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= P.W * P.H) return;
+  uint32_t pix = order ? order[slot] : slot;  // material-sorted (large films)
   if (pix >= P.W * P.H) return;
   uint32_t pass = *pass_dev;
   float fx, fy;
@@ -351,9 +353,11 @@ __device__ __forceinline__ Bins4 bins_f(bool cond, bool zero, float c, float kf,
 // 12 resident blocks per SM (40 registers): 1080p Sampled64 669 -> 682
 // Msamples/s against the unbounded 64 registers (16 blocks: 675).
 __global__ void __launch_bounds__(128, 12) k_sfinish(PassCtx P, SpecCtx C, const float4* state,
-                                                     const uint32_t* shadow) {
-  uint32_t pix = (blockIdx.x * blockDim.x + threadIdx.x) / kBinLanes;
-  if (pix >= P.W * P.H) return;  // the whole half-warp leaves together
+                                                     const uint32_t* shadow, const uint32_t* order) {
+  uint32_t slot = (blockIdx.x * blockDim.x + threadIdx.x) / kBinLanes;
+  if (slot >= P.W * P.H) return;  // the whole half-warp leaves together
+  uint32_t pix = order ? order[slot] : slot;  // material-sorted (large films)
+  if (pix >= P.W * P.H) return;
   uint32_t lane = threadIdx.x & 31u;
   uint32_t hmask = 0xFFFFu << (lane & 16u);
   int b0 = 4 * (int)(lane & 15u);
@@ -617,21 +621,21 @@ static PassCtx spec_pass_ctx(wpbr_ctx* ctx) {
 
 // The scalar spawn of the Sampled64 pass, between the camera traversal and
 // the shadow-ray traversal (render_pass_launch).
-cudaError_t spectral_spawn_launch(wpbr_ctx* ctx, const uint32_t* pass_ptr) {
+cudaError_t spectral_spawn_launch(wpbr_ctx* ctx, const uint32_t* pass_ptr, const uint32_t* order) {
   RenderState& R = ctx->rs;
   uint32_t n = R.W * R.H;
   (ctx->has_metal ? k_sspawn<true> : k_sspawn<false>)<<<div_up(n, kTB), kTB, 0, ctx->stream>>>(spec_pass_ctx(ctx), pass_ptr, R.hit_prim.p, R.pstate.p,
-                                                     R.shadow_rays.p, R.pfilm.p);
+                                                     R.shadow_rays.p, R.pfilm.p, order);
   return cudaGetLastError();
 }
 
 // The per-bin finish, film gather and toRGB after the shadow-ray traversal.
-cudaError_t spectral_finish_launch(wpbr_ctx* ctx) {
+cudaError_t spectral_finish_launch(wpbr_ctx* ctx, const uint32_t* order) {
   RenderState& R = ctx->rs;
   uint32_t n = R.W * R.H;
   SpecCtx C{(const SpecMat*)R.spec_mats.p, (const S64*)R.spec_le.p, R.spec_L.p};
   k_sfinish<<<div_up((uint64_t)n * kBinLanes, 128), 128, 0, ctx->stream>>>(spec_pass_ctx(ctx), C, R.pstate.p,
-                                                                            R.shadow_hit.p);
+                                                                            R.shadow_hit.p, order);
   dim3 fg(div_up(R.W, kFT), div_up(R.H, kFT));
   k_sfilm<<<fg, kFilmThreads, 0, ctx->stream>>>(R.W, R.H, R.pfilm.p, R.spec_L.p, R.spec_acc.p, (float4*)R.acc.p);
   return cudaGetLastError();

@@ -152,10 +152,16 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t wid = threadIdx.x >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  V3 o{0, 0, 0}, d{0, 0, 0}, inv{0, 0, 0};
+  V3 o{0, 0, 0}, inv{0, 0, 0};
   int neg[3] = {0, 0, 0};
   float tmax = 0.0f, tb = 0.0f;
+  // The render passes' kernels keep the hit record the cooperative leaf
+  // tests leave in shared memory; the collide kernels keep only the winning
+  // primitive's sorted position and test it once more when the ray is done
+  // (the direction then comes back from the ray's shared record), which
+  // keeps four registers and the direction out of the traversal loops.
   HitRec h{0.0f, kNoHit, 0.0f, 0.0f};
+  uint32_t hpos = kNoHit;
   int ref = kEnd;
   uint32_t cnt = 0;
   int lref = kEnd;
@@ -185,7 +191,7 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
           float4 ro, rd;
           src.load(r, &ro, &rd);
           o = V3{ro.x, ro.y, ro.z};
-          d = V3{rd.x, rd.y, rd.z};
+          const V3 d{rd.x, rd.y, rd.z};
           tmax = rd.w;
           inv = V3{1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
           neg[0] = inv.x < 0.0f;
@@ -200,6 +206,7 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
           sr.d = make_float4(d.x, d.y, d.z, 0.0f);
           tb = inf_();
           h = HitRec{inf_(), kNoHit, 0.0f, 0.0f};
+          hpos = kNoHit;
           sp = 0;
           lref = kEnd;
           ref = kEnd;
@@ -358,12 +365,7 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
           float t = __uint_as_float(ANY ? (uint32_t)(key & 0xFFFFFFFFull) : (uint32_t)(key >> 32));
           if (tb > t) {
             if (Sink::kCollide) {
-              uint32_t pos = ANY ? (uint32_t)(key >> 32) : (uint32_t)(key & 0xFFFFFFFFull);
-              RayTri R = ray_tri_setup(o, d, S.quirks);
-              uint32_t prim;
-              float b1, b2;
-              float tt = prim_test(S, Bv.prims, pos, o, d, R, &prim, &b1, &b2);
-              h = HitRec{tt, prim, b1, b2};
+              hpos = ANY ? (uint32_t)(key >> 32) : (uint32_t)(key & 0xFFFFFFFFull);
             } else {
               float2 bb = s_hbary[wid][lane];
               h = HitRec{t, s_hprim[wid][lane], bb.x, bb.y};
@@ -387,6 +389,15 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
       }
     }
     if (active && ref == kEnd && lref == kEnd) {
+      if (Sink::kCollide && hpos != kNoHit) {
+        const float4 dd = s_ray[wid][lane].d;
+        const V3 d{dd.x, dd.y, dd.z};
+        RayTri R = ray_tri_setup(o, d, S.quirks);
+        uint32_t prim;
+        float b1, b2;
+        float tt = prim_test(S, Bv.prims, hpos, o, d, R, &prim, &b1, &b2);
+        h = HitRec{tt, prim, b1, b2};
+      }
       sink.store(rid, h);
       active = false;
     }
