@@ -14,7 +14,8 @@
 //                                                reference's leaf rule (n < 30 or equal codes),
 //                                                bottom-up bounds (k_refit)
 //   JobBuildUpperSAH                             level-synchronous segmented 12-bucket SAH over
-//                                                treelet roots (k_seg_*), std::partition's
+//                                                treelet roots, every level in one cooperative
+//                                                launch (k_sah_levels), std::partition's
 //                                                two-pointer swap order reproduced with ranks;
 //                                                segments of <= 32 roots finish in one warp
 //                                                (k_small_sah)
@@ -25,6 +26,7 @@
 // primitives (sorted position + N), [2N, 2N + T) SAH nodes.
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 
 #include "common.cuh"
 #include "ctx.hpp"
@@ -40,7 +42,18 @@ constexpr uint32_t kSmallSeg = 32;
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr int kB = 256;
 
+// Sizes the build finds on the device (read by its later kernels, and by the
+// host once, at the end of the build): words of BvhState::dinfo.
+enum : uint32_t {
+  kInfoT = 0,      // treelets
+  kInfoRoot = 1,   // unified id of the root
+  kInfoM = 2,      // nodes of the flattened tree
+  kInfoSum = 16,   // summary block copied to the host (k_build_summary)
+  kInfoWords = 40
+};
+
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
+__device__ __forceinline__ uint32_t div_up_d(uint32_t a, uint32_t b) { return (uint32_t)(((uint64_t)a + b - 1) / b); }
 
 // ---------------------------------------------------------------------------
 // exclusive scan (tile scan + recursive block sums) of 32-bit counts, or of
@@ -141,18 +154,6 @@ size_t scan_tmp_need(uint32_t n) {
   size_t need = 0;
   for (uint32_t m = n; m > (uint32_t)kScanTile; m = div_up(m, kScanTile)) need += div_up(m, kScanTile) + 1;
   return need;
-}
-
-// Both partition counts of the SAH levels in one pass (two 32-bit prefix sums
-// packed in 64-bit words); tmp holds the block sums as 32-bit words, two each.
-cudaError_t scan_exclusive_pair(const unsigned long long* in, unsigned long long* out, uint32_t n,
-                                DevBuf<uint32_t>& tmp, cudaStream_t s) {
-  if (n == 0) return cudaSuccess;
-  size_t need = scan_tmp_need(n);
-  cudaError_t e = tmp.ensure(2 * need + 16);
-  if (e != cudaSuccess) return e;
-  unsigned long long* t64 = reinterpret_cast<unsigned long long*>(tmp.p);
-  return scan_exclusive_t(in, out, n, t64, need + 8, s);
 }
 
 }  // namespace
@@ -323,15 +324,17 @@ __global__ void k_treelet_flags(const uint32_t* skey, uint32_t N, uint32_t* flag
   if (i >= N) return;
   flags[i] = (i == 0 || ((skey[i] ^ skey[i - 1]) & kTreeletMask) != 0) ? 1u : 0u;
 }
-__global__ void k_treelet_ids(const uint32_t* flags, uint32_t* tid, uint32_t* tstart, uint32_t N) {
+__global__ void k_treelet_ids(const uint32_t* flags, uint32_t* tid, uint32_t* tstart, uint32_t N, uint32_t* info) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   uint32_t t = tid[i] + flags[i] - 1u;  // inclusive - 1
   tid[i] = t;
   if (flags[i]) tstart[t] = i;
+  if (i == N - 1) info[kInfoT] = t + 1u;
 }
-__global__ void k_treelet_sizes(const uint32_t* tstart, uint32_t* tsize, uint32_t T, uint32_t N) {
+__global__ void k_treelet_sizes(const uint32_t* tstart, uint32_t* tsize, const uint32_t* info, uint32_t N) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t T = info[kInfoT];
   if (t >= T) return;
   tsize[t] = (t + 1 < T ? tstart[t + 1] : N) - tstart[t];
 }
@@ -463,7 +466,7 @@ __global__ void k_refit(uint32_t N, const uint32_t* skey, const uint32_t* sprim,
 // A8: segmented SAH over treelet roots
 // ---------------------------------------------------------------------------
 struct SahArgs {
-  uint32_t N, T;
+  uint32_t N;
   const uint32_t* troot;
   const float4* nb_lo;
   const float4* nb_hi;
@@ -474,398 +477,6 @@ __device__ __forceinline__ void item_bounds(const SahArgs& A, uint32_t item, V3*
   float4 l = A.nb_lo[r], h = A.nb_hi[r];
   *lo = V3{l.x, l.y, l.z};
   *hi = V3{h.x, h.y, h.z};
-}
-
-__global__ void k_fill(uint32_t* p, uint32_t n, uint32_t v) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) p[i] = v;
-}
-
-// Segment of every position (kNone outside the level's large segments): a
-// binary search over the segment starts, which are in ascending order.
-// The SAH levels' kernels read the level's count of large segments from
-// device memory (nseg_p), so the host can queue a level before the previous
-// one has finished.
-__global__ void k_pos_seg(uint32_t T, const uint32_t* nseg_p, const uint32_t* seg_start, const uint32_t* seg_end,
-                          uint32_t* pos_seg) {
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= T) return;
-  const uint32_t nseg = *nseg_p;
-  uint32_t lo = 0, hi = nseg;
-  while (lo < hi) {
-    uint32_t mid = (lo + hi) >> 1;
-    if (__ldg(seg_start + mid) <= p)
-      lo = mid + 1;
-    else
-      hi = mid;
-  }
-  pos_seg[p] = (lo > 0 && p <= __ldg(seg_end + lo - 1)) ? lo - 1 : kNone;
-}
-
-__global__ void k_seg_init(const uint32_t* nseg_p, uint32_t* benc, uint32_t* cenc, uint32_t* bcnt, uint32_t* bkenc) {
-  uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= *nseg_p) return;
-  for (int k = 0; k < 6; ++k) {
-    benc[s * 6 + k] = k < 3 ? 0xFFFFFFFFu : 0u;
-    cenc[s * 6 + k] = k < 3 ? 0xFFFFFFFFu : 0u;
-  }
-  for (int b = 0; b < 12; ++b) {
-    bcnt[s * 12 + b] = 0;
-    for (int k = 0; k < 6; ++k) bkenc[(s * 12 + b) * 6 + k] = k < 3 ? 0xFFFFFFFFu : 0u;
-  }
-}
-
-// Bounds and centroid bounds per segment: warp-segmented reduce over the
-// contiguous runs, then per block: the runs of the block's first kSegSlots
-// segments meet in shared memory and leave one global atomic per block and
-// segment (near the root a level has a handful of segments, and one atomic per
-// warp on the same words serialised in L2); runs of later segments go to
-// global memory directly. Min and max are order-independent, so the bounds
-// are exact whatever the grouping.
-constexpr int kSegSlots = 16;
-__global__ void k_seg_reduce(SahArgs A, const uint32_t* cur, const uint32_t* pos_seg, uint32_t* benc, uint32_t* cenc) {
-  __shared__ uint32_t s_min;
-  __shared__ uint32_t s_red[kSegSlots * 12];  // slot * 12 + (lo xyz, hi xyz, centroid lo xyz, centroid hi xyz)
-  if (threadIdx.x == 0) s_min = kNone;
-  for (int k = threadIdx.x; k < kSegSlots * 12; k += blockDim.x) s_red[k] = ((k % 12) / 3) % 2 == 0 ? 0xFFFFFFFFu : 0u;
-  __syncthreads();
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t s = (p < A.T) ? pos_seg[p] : kNone;
-  uint32_t wmin = __reduce_min_sync(0xFFFFFFFFu, s);
-  if (lane_id() == 0 && wmin != kNone) atomicMin(&s_min, wmin);
-  __syncthreads();
-  const uint32_t smin = s_min;
-  uint32_t e[12];
-  if (s != kNone) {
-    V3 lo, hi;
-    item_bounds(A, cur[p], &lo, &hi);
-    V3 c = mul(add(lo, hi), 0.5f);
-    e[0] = fenc(lo.x); e[1] = fenc(lo.y); e[2] = fenc(lo.z);
-    e[3] = fenc(hi.x); e[4] = fenc(hi.y); e[5] = fenc(hi.z);
-    e[6] = fenc(c.x); e[7] = fenc(c.y); e[8] = fenc(c.z);
-    e[9] = e[6]; e[10] = e[7]; e[11] = e[8];
-  } else {
-    for (int k = 0; k < 12; ++k) e[k] = 0;
-  }
-  uint32_t lane = lane_id();
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t so = __shfl_down_sync(0xFFFFFFFFu, s, o);
-    bool take = (lane + o < 32) && (so == s) && (s != kNone);
-    for (int k = 0; k < 12; ++k) {
-      uint32_t y = __shfl_down_sync(0xFFFFFFFFu, e[k], o);
-      if (take) {
-        bool mn = (k < 3) || (k >= 6 && k < 9);
-        e[k] = mn ? min(e[k], y) : max(e[k], y);
-      }
-    }
-  }
-  uint32_t sp = __shfl_up_sync(0xFFFFFFFFu, s, 1);
-  bool head = (s != kNone) && (lane == 0 || sp != s);
-  if (head) {
-    uint32_t slot = s - smin;  // s >= smin for every s != kNone of the block
-    if (slot < (uint32_t)kSegSlots) {
-      uint32_t* r = s_red + slot * 12;
-      for (int k = 0; k < 3; ++k) atomicMin(&r[k], e[k]);
-      for (int k = 3; k < 6; ++k) atomicMax(&r[k], e[k]);
-      for (int k = 6; k < 9; ++k) atomicMin(&r[k], e[k]);
-      for (int k = 9; k < 12; ++k) atomicMax(&r[k], e[k]);
-    } else {
-      for (int k = 0; k < 3; ++k) atomicMin(&benc[s * 6 + k], e[k]);
-      for (int k = 3; k < 6; ++k) atomicMax(&benc[s * 6 + k], e[k]);
-      for (int k = 0; k < 3; ++k) atomicMin(&cenc[s * 6 + k], e[6 + k]);
-      for (int k = 0; k < 3; ++k) atomicMax(&cenc[s * 6 + 3 + k], e[9 + k]);
-    }
-  }
-  __syncthreads();
-  if (smin == kNone) return;
-  for (int k = threadIdx.x; k < kSegSlots * 12; k += blockDim.x) {
-    uint32_t v = s_red[k];
-    int j = k % 12;
-    bool is_min = (j / 3) % 2 == 0;
-    if (v == (is_min ? 0xFFFFFFFFu : 0u)) continue;  // no run of this slot's segment in the block
-    uint32_t seg = smin + (uint32_t)(k / 12);
-    uint32_t* dst = (j < 6 ? benc : cenc) + seg * 6 + (j < 6 ? j : j - 6);
-    if (is_min)
-      atomicMin(dst, v);
-    else
-      atomicMax(dst, v);
-  }
-}
-
-__device__ __forceinline__ Bounds dec_bounds(const uint32_t* e) {
-  return Bounds{V3{fdec(e[0]), fdec(e[1]), fdec(e[2])}, V3{fdec(e[3]), fdec(e[4]), fdec(e[5])}};
-}
-
-// Bucket of every root (JobBuildUpperSAH, SLBVH.cpp:484-502) and per-bucket
-// counts / bounds, pre-aggregated in shared memory per block.
-__global__ void k_seg_bucket(SahArgs A, const uint32_t* cur, const uint32_t* pos_seg, const uint32_t* cenc,
-                             uint32_t* bucket, uint32_t* bcnt, uint32_t* bkenc) {
-  __shared__ uint32_t s_min;
-  __shared__ uint32_t s_cnt[kSegSlots * 12];
-  __shared__ uint32_t s_enc[kSegSlots * 12 * 6];
-  if (threadIdx.x == 0) s_min = kNone;
-  for (int k = threadIdx.x; k < kSegSlots * 12; k += blockDim.x) s_cnt[k] = 0;
-  for (int k = threadIdx.x; k < kSegSlots * 12 * 6; k += blockDim.x) s_enc[k] = (k % 6) < 3 ? 0xFFFFFFFFu : 0u;
-  __syncthreads();
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t s = (p < A.T) ? pos_seg[p] : kNone;
-  if (s != kNone) atomicMin(&s_min, s);
-  __syncthreads();
-  if (s != kNone) {
-    V3 lo, hi;
-    item_bounds(A, cur[p], &lo, &hi);
-    Bounds cb = dec_bounds(cenc + s * 6);
-    int dim = bmax_extent(cb);
-    float dist = comp(cb.hi, dim) - comp(cb.lo, dim);
-    float c = (comp(lo, dim) + comp(hi, dim)) * 0.5f;
-    float t = (c - comp(cb.lo, dim)) / dist;
-    float bt = 12.0f * t;
-    uint32_t ib = (bt >= 0.0f) ? (uint32_t)bt : 0u;
-    if (ib >= 12u) ib = 11u;
-    bucket[p] = ib;
-    uint32_t e[6] = {fenc(lo.x), fenc(lo.y), fenc(lo.z), fenc(hi.x), fenc(hi.y), fenc(hi.z)};
-    uint32_t slot = s - s_min;
-    if (slot < (uint32_t)kSegSlots) {
-      atomicAdd(&s_cnt[slot * 12 + ib], 1u);
-      uint32_t* d = &s_enc[(slot * 12 + ib) * 6];
-      for (int k = 0; k < 3; ++k) atomicMin(&d[k], e[k]);
-      for (int k = 3; k < 6; ++k) atomicMax(&d[k], e[k]);
-    } else {
-      atomicAdd(&bcnt[s * 12 + ib], 1u);
-      uint32_t* d = &bkenc[(s * 12 + ib) * 6];
-      for (int k = 0; k < 3; ++k) atomicMin(&d[k], e[k]);
-      for (int k = 3; k < 6; ++k) atomicMax(&d[k], e[k]);
-    }
-  }
-  __syncthreads();
-  if (s_min == kNone) return;
-  for (int k = threadIdx.x; k < kSegSlots * 12; k += blockDim.x) {
-    uint32_t c = s_cnt[k];
-    if (c == 0) continue;
-    uint32_t gs = s_min + (uint32_t)(k / 12), b = (uint32_t)(k % 12);
-    atomicAdd(&bcnt[gs * 12 + b], c);
-    uint32_t* d = &bkenc[(gs * 12 + b) * 6];
-    for (int q = 0; q < 3; ++q) atomicMin(&d[q], s_enc[k * 6 + q]);
-    for (int q = 3; q < 6; ++q) atomicMax(&d[q], s_enc[k * 6 + q]);
-  }
-}
-
-// Cost of the 11 candidate splits, SLBVH.cpp:504-538, and the child layout.
-// The two sides of split i are the unions of the non-empty buckets 0..i and
-// i+1..11 (JobBuildUpperSAH's two inner loops): the right sides are built
-// once as suffix unions and the left sides accumulated in bucket order, 24
-// bucket decodes instead of 132 (one thread decides a segment; near the root
-// that chain of dependent loads was the level's longest kernel). Min and max
-// of finite coordinates do not depend on the grouping; only a zero's sign
-// could, which no area or cost sees.
-__device__ void sah_decide(const uint32_t* bcnt, const uint32_t* bkenc, const Bounds& bounds, uint32_t n, int* best_out,
-                           uint32_t* k_out) {
-  float barea_ = barea(bounds);
-  float cost_min = 0.0f;
-  int best = 0;
-  uint32_t c[12];
-#pragma unroll
-  for (int j = 0; j < 12; ++j) c[j] = bcnt[j];
-  Bounds suf[11];
-  uint32_t nsuf[11];
-  suf[10] = bempty();
-  nsuf[10] = 0;
-  if (c[11]) {
-    suf[10] = bunion(suf[10], dec_bounds(bkenc + 11 * 6));
-    nsuf[10] = c[11];
-  }
-#pragma unroll
-  for (int i = 9; i >= 0; --i) {
-    suf[i] = suf[i + 1];
-    nsuf[i] = nsuf[i + 1];
-    if (c[i + 1]) {
-      suf[i] = bunion(suf[i], dec_bounds(bkenc + (i + 1) * 6));
-      nsuf[i] += c[i + 1];
-    }
-  }
-  Bounds b0 = bempty();
-  uint32_t n0 = 0;
-#pragma unroll
-  for (int i = 0; i < 11; ++i) {
-    if (c[i]) {
-      b0 = bunion(b0, dec_bounds(bkenc + i * 6));
-      n0 += c[i];
-    }
-    const Bounds& b1 = suf[i];
-    uint32_t n1 = nsuf[i];
-    float l = (n0 == 0) ? 0.0f : (float)n0 * barea(b0);
-    float r = (n1 == 0) ? 0.0f : (float)n1 * barea(b1);
-    float cost = (float)(0.125 + (double)((l + r) / barea_));
-    if (i == 0 || cost < cost_min) {
-      cost_min = cost;
-      best = i;
-    }
-  }
-  uint32_t k = 0;
-  for (int j = 0; j <= best; ++j) k += c[j];
-  (void)n;
-  *best_out = best;
-  *k_out = k;
-}
-
-struct SegLevel {
-  const uint32_t* start;
-  const uint32_t* end;
-  const uint32_t* node;
-};
-
-__global__ void k_seg_split(const uint32_t* nseg_p, uint32_t nscan, SegLevel L, const uint32_t* benc, const uint32_t* cenc,
-                            const uint32_t* bcnt, const uint32_t* bkenc, uint32_t* seg_k, uint32_t* seg_best,
-                            uint32_t* seg_mid, uint32_t* seg_cl, uint32_t* seg_cr, uint32_t* counters,
-                            uint32_t* sah_axis, float4* nb_lo, float4* nb_hi, uint32_t* child0, uint32_t* child1,
-                            uint32_t* parent, uint32_t* nlarge_cnt, uint32_t* small_start, uint32_t* small_end,
-                            uint32_t* small_node, uint32_t N2) {
-  uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= *nseg_p) {
-    if (s < nscan) nlarge_cnt[s] = 0u;  // the scan of the counts runs over nscan entries
-    return;
-  }
-  uint32_t a = L.start[s], b = L.end[s], nd = L.node[s];
-  uint32_t n = b - a + 1;
-  Bounds bb = dec_bounds(benc + s * 6);
-  Bounds cb = dec_bounds(cenc + s * 6);
-  int dim = bmax_extent(cb);
-  int best;
-  uint32_t k;
-  sah_decide(bcnt + s * 12, bkenc + s * 12 * 6, bb, n, &best, &k);
-  uint32_t mid = (k == n) ? a + n / 2 : a + k;
-  seg_k[s] = a + k;
-  seg_best[s] = (uint32_t)best;
-  seg_mid[s] = mid;
-  uint32_t me = N2 + nd;
-  sah_axis[nd] = (uint32_t)dim;
-  nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
-  nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
-  uint32_t ln = mid - a, rn = b - mid + 1;
-  uint32_t cl = kNone, cr = kNone;
-  uint32_t nl = 0;
-  // node ids and small-segment slots: one atomic per warp (the ids only
-  // label nodes; the flattened tree follows the child links). Deep levels
-  // have ~10^4 segments, whose per-child atomics on one counter serialised.
-  const uint32_t act = __activemask(), lt = act & ((1u << lane_id()) - 1u);
-  const uint32_t leader = __ffs(act) - 1;
-  const bool l_node = ln >= 2, r_node = rn >= 2;
-  const bool l_small = l_node && ln <= kSmallSeg, r_small = r_node && rn <= kSmallSeg;
-  uint32_t bl = __ballot_sync(act, l_node), br = __ballot_sync(act, r_node);
-  uint32_t sl = __ballot_sync(act, l_small), sr = __ballot_sync(act, r_small);
-  uint32_t node_base = 0, small_base = 0;
-  if (lane_id() == leader) {
-    uint32_t nn = __popc(bl) + __popc(br), ns = __popc(sl) + __popc(sr);
-    if (nn) node_base = atomicAdd(&counters[0], nn);
-    if (ns) small_base = atomicAdd(&counters[2], ns);
-  }
-  node_base = __shfl_sync(act, node_base, leader) + __popc(bl & lt) + __popc(br & lt);
-  small_base = __shfl_sync(act, small_base, leader) + __popc(sl & lt) + __popc(sr & lt);
-  if (l_node) {
-    cl = node_base++;
-    child0[me] = N2 + cl;
-    parent[N2 + cl] = (me << 1) | 0u;
-    if (!l_small) ++nl;
-    else {
-      uint32_t q = small_base++;
-      small_start[q] = a; small_end[q] = mid - 1; small_node[q] = cl;
-    }
-  }
-  if (r_node) {
-    cr = node_base;
-    child1[me] = N2 + cr;
-    parent[N2 + cr] = (me << 1) | 1u;
-    if (!r_small) ++nl;
-    else {
-      uint32_t q = small_base;
-      small_start[q] = mid; small_end[q] = b; small_node[q] = cr;
-    }
-  }
-  seg_cl[s] = cl;
-  seg_cr[s] = cr;
-  nlarge_cnt[s] = nl;
-}
-
-// std::partition(first, last, bucket <= best) — the two-pointer swap scheme:
-// the r-th "false" element left of the partition point (from the left) trades
-// places with the r-th "true" element right of it (from the right).
-// The two flags of a position packed as (true << 32) | false, and their
-// prefix sums packed the same way (one scan for both).
-__device__ __forceinline__ uint32_t lo32(unsigned long long v) { return (uint32_t)(v & 0xFFFFFFFFull); }
-__device__ __forceinline__ uint32_t hi32(unsigned long long v) { return (uint32_t)(v >> 32); }
-__global__ void k_part_flags(uint32_t T, const uint32_t* pos_seg, const uint32_t* bucket, const uint32_t* seg_k,
-                             const uint32_t* seg_best, unsigned long long* ft) {
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= T) return;
-  uint32_t s = pos_seg[p];
-  uint32_t f = 0, t = 0;
-  if (s != kNone) {
-    bool pred = bucket[p] <= seg_best[s];
-    uint32_t sp = seg_k[s];
-    f = (p < sp && !pred) ? 1u : 0u;
-    t = (p >= sp && pred) ? 1u : 0u;
-  }
-  ft[p] = ((unsigned long long)t << 32) | f;
-}
-__global__ void k_part_ranks(uint32_t T, SegLevel L, const uint32_t* pos_seg, const unsigned long long* ft,
-                             const unsigned long long* ftscan, uint32_t* posF, uint32_t* posT) {
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= T) return;
-  uint32_t s = pos_seg[p];
-  if (s == kNone) return;
-  uint32_t a = L.start[s], b = L.end[s];
-  unsigned long long fp = ft[p], sp = ftscan[p];
-  if (lo32(fp)) posF[a + (lo32(sp) - lo32(ftscan[a]))] = p;
-  if (hi32(fp)) posT[a + ((hi32(ftscan[b]) + hi32(ft[b])) - (hi32(sp) + 1u))] = p;
-}
-__global__ void k_part_scatter(uint32_t T, SegLevel L, const uint32_t* pos_seg, const unsigned long long* ft,
-                               const unsigned long long* ftscan, const uint32_t* posF, const uint32_t* posT,
-                               const uint32_t* cur, uint32_t* nxt) {
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= T) return;
-  uint32_t s = pos_seg[p];
-  uint32_t dst = p;
-  if (s != kNone) {
-    uint32_t a = L.start[s], b = L.end[s];
-    unsigned long long fp = ft[p], sp = ftscan[p];
-    if (lo32(fp)) dst = posT[a + (lo32(sp) - lo32(ftscan[a]))];
-    else if (hi32(fp)) dst = posF[a + ((hi32(ftscan[b]) + hi32(ft[b])) - (hi32(sp) + 1u))];
-  }
-  nxt[dst] = cur[p];
-}
-
-// Size-1 children (a single treelet root) and the next level's large segments.
-// nseg_next receives the next level's count: the exclusive scan's last entry
-// (nscan exceeds every level's count, so that entry's own count is 0).
-__global__ void k_seg_children(const uint32_t* nseg_p, uint32_t nscan, uint32_t* nseg_next, SegLevel L,
-                               const uint32_t* seg_mid, const uint32_t* seg_cl, const uint32_t* seg_cr,
-                               const uint32_t* nlarge_scan, const uint32_t* cur, const uint32_t* troot,
-                               uint32_t* child0, uint32_t* child1, uint32_t* parent, uint32_t* ns_start,
-                               uint32_t* ns_end, uint32_t* ns_node, uint32_t N2) {
-  uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s == 0) *nseg_next = nlarge_scan[nscan - 1];
-  if (s >= *nseg_p) return;
-  uint32_t a = L.start[s], b = L.end[s], mid = seg_mid[s];
-  uint32_t me = N2 + L.node[s];
-  uint32_t ln = mid - a, rn = b - mid + 1;
-  if (ln == 1) {
-    uint32_t r = troot[cur[a]];
-    child0[me] = r;
-    parent[r] = (me << 1) | 0u;
-  }
-  if (rn == 1) {
-    uint32_t r = troot[cur[b]];
-    child1[me] = r;
-    parent[r] = (me << 1) | 1u;
-  }
-  uint32_t q = nlarge_scan[s];
-  if (ln > kSmallSeg) {
-    ns_start[q] = a; ns_end[q] = mid - 1; ns_node[q] = seg_cl[s];
-    ++q;
-  }
-  if (rn > kSmallSeg) {
-    ns_start[q] = mid; ns_end[q] = b; ns_node[q] = seg_cr[s];
-  }
 }
 
 // Bounds of another lane (shuffled component by component).
@@ -880,12 +491,833 @@ __device__ __forceinline__ Bounds shfl_bounds_down(const Bounds& b, uint32_t o) 
                 V3{__shfl_down_sync(F, b.hi.x, o), __shfl_down_sync(F, b.hi.y, o), __shfl_down_sync(F, b.hi.z, o)}};
 }
 
+__device__ __forceinline__ Bounds dec_bounds(const uint32_t* e) {
+  return Bounds{V3{fdec(e[0]), fdec(e[1]), fdec(e[2])}, V3{fdec(e[3]), fdec(e[4]), fdec(e[5])}};
+}
+__device__ __forceinline__ Bounds dec_bounds_cg(const uint32_t* e) {
+  uint32_t v[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) v[k] = __ldcg(e + k);
+  return dec_bounds(v);
+}
+
+// Split decision of JobBuildUpperSAH (SLBVH.cpp:504-538) by one warp: lane
+// j < 12 holds bucket j's count and bounds. Shuffle scans give every lane the
+// union and count of buckets 0..j (prefix) and j..11 (suffix), lane i < 11
+// costs split i from lane i's prefix and lane i+1's suffix (the unions of the
+// non-empty buckets on each side, as the reference's two inner loops form
+// them), and the sequential first-minimum rule is a lexicographic (cost,
+// split) reduction: a NaN never wins, and a NaN at split 0 keeps split 0.
+// Min and max of finite coordinates do not depend on the grouping; only a
+// zero's sign could, which no area or cost sees. Returns the split bucket
+// (warp-uniform); *k_out receives the count of buckets 0..best.
+__device__ int warp_sah_split(uint32_t cj, const Bounds& bj, float area_all, uint32_t* k_out) {
+  const uint32_t FULL = 0xFFFFFFFFu;
+  const uint32_t lane = lane_id();
+  Bounds pre = (lane < 12 && cj) ? bj : bempty();
+  Bounds suf = pre;
+  uint32_t npre = lane < 12 ? cj : 0u, nsuf = npre;
+#pragma unroll
+  for (uint32_t o = 1; o < 16; o <<= 1) {
+    Bounds u = shfl_bounds_up(pre, o);
+    uint32_t nu = __shfl_up_sync(FULL, npre, o);
+    Bounds v = shfl_bounds_down(suf, o);
+    uint32_t nv = __shfl_down_sync(FULL, nsuf, o);
+    if (lane >= o) {
+      pre = bunion(u, pre);
+      npre += nu;
+    }
+    if (lane + o < 12) {
+      suf = bunion(suf, v);
+      nsuf += nv;
+    }
+  }
+  Bounds b1 = shfl_bounds_down(suf, 1);
+  uint32_t n1 = __shfl_down_sync(FULL, nsuf, 1);
+  float cost = 0.0f;
+  if (lane < 11) {
+    float l = (npre == 0) ? 0.0f : (float)npre * barea(pre);
+    float r = (n1 == 0) ? 0.0f : (float)n1 * barea(b1);
+    cost = (float)(0.125 + (double)((l + r) / area_all));
+  }
+  float c0 = __shfl_sync(FULL, cost, 0);
+  float bc = (lane < 11 && !isnan(cost)) ? cost : __int_as_float(0x7f800000);
+  uint32_t bi = lane;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    float oc = __shfl_xor_sync(FULL, bc, o);
+    uint32_t oi = __shfl_xor_sync(FULL, bi, o);
+    if (oc < bc || (oc == bc && oi < bi)) {
+      bc = oc;
+      bi = oi;
+    }
+  }
+  int best = isnan(c0) ? 0 : (int)bi;
+  *k_out = __shfl_sync(FULL, npre, best);
+  return best;
+}
+
+// Bucket of a root (SLBVH.cpp:484-502): the centroid's position along the
+// centroid bounds' longest axis in 12 equal parts.
+__device__ __forceinline__ uint32_t sah_bucket(const V3& lo, const V3& hi, const Bounds& cb, int dim) {
+  float dist = comp(cb.hi, dim) - comp(cb.lo, dim);
+  float c = (comp(lo, dim) + comp(hi, dim)) * 0.5f;
+  float t = (c - comp(cb.lo, dim)) / dist;
+  float bt = 12.0f * t;
+  uint32_t ib = (bt >= 0.0f) ? (uint32_t)bt : 0u;
+  return ib >= 12u ? 11u : ib;
+}
+
+// ---------------------------------------------------------------------------
+// A8, segments of more than 32 treelet roots: every SAH level of the build in
+// one cooperative launch (all blocks resident), five phases per level
+// separated by grid barriers:
+//   A   bounds and centroid bounds of every segment (per-tile pre-reduction in
+//       shared memory, then global atomics on order-preserving encodings);
+//   B   the bucket of every root, bucket counts and bounds of every segment;
+//   C1  the split decision of every segment (one warp decides, the same float
+//       operations as the sequential loop) and the partition flags of
+//       std::partition's two-pointer scheme, scanned within each block's
+//       chunk of consecutive tiles, together with the children each segment
+//       creates (counted at its first position);
+//   C2  every block scans the chunk totals, which gives the global prefix of
+//       any position: the select tables (the r-th "false" root left of the
+//       partition point and the r-th "true" one right of it, from the right),
+//       and, at each segment's first position, its SAH node, its children's
+//       node ids, and the next level's segment slots (numbered in position
+//       order) or the small-segment queue;
+//   E   the swap: each pair trades places, the next level's position arrays
+//       are written, and single-root children are linked.
+// Segments of 2..32 roots go to the warp-local queue (k_small_sah). A tile is
+// kCoopBlock consecutive positions. Every grid barrier is bounded: past the
+// limit the kernel sets the error word and an abort flag, and every block
+// leaves at its next barrier. Indices derived from scanned values are checked
+// before use.
+// ---------------------------------------------------------------------------
+constexpr int kCoopBlock = 512;
+constexpr int kCoopWarps = kCoopBlock / 32;
+constexpr uint32_t kMaxCoopGrid = 2 * kCoopBlock;  // blocks of the cooperative grid (chunk prefixes in shared memory)
+constexpr uint32_t kSpinLimit = 1u << 24;   // barrier polls (100 ns apart) before giving up
+constexpr uint32_t kSegWords = 12;          // bounds lo/hi, centroid bounds lo/hi (encoded)
+constexpr uint32_t kBucketWords = 12 * 7;   // per bucket: count, lo xyz, hi xyz (encoded)
+
+struct CoopSah {
+  uint32_t N, N2;
+  uint32_t maxseg;  // capacity of each set of per-segment arrays
+  const uint32_t* T_p;  // treelet count
+  const uint32_t* troot;
+  float4* nb_lo;  // unified-id node bounds: treelet roots read, SAH nodes written
+  float4* nb_hi;
+  uint32_t* child0;
+  uint32_t* child1;
+  uint32_t* parent;
+  uint32_t* sah_axis;
+  // per position (two buffers each, swapped every level)
+  uint32_t* item[2];
+  uint32_t* seg_of[2];
+  float4* plo[2];
+  float4* phi[2];
+  uint8_t* bucket;
+  unsigned long long* ftl;  // exclusive prefix of the flags (true << 32) | false within the block's chunk
+  uint32_t* rnk;            // rank of a moving root among its segment's "false" (or "true") ones
+  uint32_t* posF;
+  uint32_t* posT;
+  // per segment (two buffers: the level's and the next level's)
+  uint32_t* sa[2];
+  uint32_t* sb[2];
+  uint32_t* snode[2];
+  uint32_t* sacc[2];  // kSegWords per segment
+  uint32_t* sbk[2];   // kBucketWords per segment
+  uint4* sdec;        // partition point, mid, left and right child segment (kNone: not large)
+  uint32_t* sbest;
+  unsigned long long* segpre;  // (large << 32 | new-node) children before the segment, within its chunk
+  unsigned long long* btot;    // per block: its chunk's flag totals and children totals
+  // level words, two sets: [0] large segments, [1] SAH nodes allocated before
+  // the level, [2] small segments queued before the level
+  uint32_t* lvl;
+  uint32_t* small_start;
+  uint32_t* small_end;
+  uint32_t* small_node;
+  uint32_t* counters;  // [0] SAH nodes allocated, [2] small segments queued
+  uint32_t* root_out;  // unified id of the tree's root
+  uint32_t* bar;       // grid barrier: [0] arrivals, [1] generation, [2] abort
+  uint32_t* err;
+};
+
+__device__ __forceinline__ uint32_t ld_vol(const uint32_t* p) { return *(const volatile uint32_t*)p; }
+
+// Grid-wide barrier of the cooperative launch. false: some block gave up
+// waiting (abort set), and the caller leaves the kernel.
+__device__ bool coop_sync(uint32_t* bar, uint32_t* err) {
+  __shared__ uint32_t s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t gen = ld_vol(bar + 1);
+    __threadfence();
+    bool ok = true;
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      uint32_t spins = 0;
+      while (ld_vol(bar + 1) == gen) {
+        if (ld_vol(bar + 2)) {
+          ok = false;
+          break;
+        }
+        if (++spins > kSpinLimit) {
+          atomicOr(bar + 2, 1u);
+          atomicOr(err, kErrLoopLimit);
+          ok = false;
+          break;
+        }
+        __nanosleep(100);
+      }
+    }
+    __threadfence();
+    if (ld_vol(bar + 2)) ok = false;
+    s_ok = ok ? 1u : 0u;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long warp_incl_scan64(unsigned long long v) {
+  const uint32_t lane = lane_id();
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, v, o);
+    if (lane >= (uint32_t)o) v += y;
+  }
+  return v;
+}
+
+// Exclusive scan of two 64-bit values over n <= 2 * blockDim.x entries of
+// src (pairs, entry i at src[2i], src[2i + 1]) into shared arrays; returns the
+// totals. Every thread of the block calls it.
+__device__ void block_scan_pairs(const unsigned long long* src, uint32_t n, unsigned long long* o1,
+                                 unsigned long long* o2, unsigned long long* w1, unsigned long long* w2,
+                                 unsigned long long* tot) {
+  const uint32_t lane = lane_id(), wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const uint32_t e0 = 2 * threadIdx.x, e1 = e0 + 1;
+  unsigned long long a1 = e0 < n ? __ldcg(src + 2 * e0) : 0ull, a2 = e0 < n ? __ldcg(src + 2 * e0 + 1) : 0ull;
+  unsigned long long b1 = e1 < n ? __ldcg(src + 2 * e1) : 0ull, b2 = e1 < n ? __ldcg(src + 2 * e1 + 1) : 0ull;
+  unsigned long long x1 = warp_incl_scan64(a1 + b1), x2 = warp_incl_scan64(a2 + b2);
+  if (lane == 31) {
+    w1[wid] = x1;
+    w2[wid] = x2;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    unsigned long long v1 = lane < nw ? w1[lane] : 0ull, v2 = lane < nw ? w2[lane] : 0ull;
+    unsigned long long y1 = warp_incl_scan64(v1), y2 = warp_incl_scan64(v2);
+    if (lane < nw) {
+      w1[lane] = y1 - v1;
+      w2[lane] = y2 - v2;
+    }
+    if (lane == 31) {
+      tot[0] = y1;
+      tot[1] = y2;
+    }
+  }
+  __syncthreads();
+  const unsigned long long base1 = w1[wid] + x1 - (a1 + b1), base2 = w2[wid] + x2 - (a2 + b2);
+  if (e0 < n) {
+    o1[e0] = base1;
+    o2[e0] = base2;
+  }
+  if (e1 < n) {
+    o1[e1] = base1 + a1;
+    o2[e1] = base2 + a2;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void init_segment(uint32_t* acc, uint32_t* bk) {
+  for (int k = 0; k < (int)kSegWords; ++k) acc[k] = ((k / 3) % 2 == 0) ? 0xFFFFFFFFu : 0u;
+  for (int b = 0; b < 12; ++b) {
+    bk[b * 7] = 0u;
+    for (int k = 0; k < 6; ++k) bk[b * 7 + 1 + k] = k < 3 ? 0xFFFFFFFFu : 0u;
+  }
+}
+
+// A large segment met by a block's batch of positions (shared memory). A
+// batch of kBatch consecutive positions meets at most 2 + (kBatch - 2) / 33
+// = 64 large segments (each holds more than 32 positions), and their ids are
+// consecutive (segments are numbered in position order), so s & 63 names
+// each one's slot without collisions.
+struct SlotSeg {
+  uint32_t s, a, b, node;
+  uint32_t spt, mid, best, kk;
+  uint32_t cl, cr;
+  unsigned long long ga, ge;  // global flag prefixes at a and at b + 1 (phase C2)
+  float cb[6];                // centroid bounds lo xyz, hi xyz (phase B)
+};
+constexpr int kBatchTiles = 4;
+constexpr uint32_t kBatch = kBatchTiles * kCoopBlock;
+constexpr uint32_t kSlots = 64;
+static_assert(2 + (kBatch - 2) / (kSmallSeg + 1) <= kSlots, "a batch meets at most kSlots large segments");
+
+// Positions of the block's batch starting at `base` (k-th tile of the batch:
+// base + k * kCoopBlock + thread) and their segments; marks the slots the
+// batch meets. Leaves one __syncthreads after the marks.
+__device__ __forceinline__ void batch_segments(const uint32_t* seg_of, uint32_t base, uint32_t end, uint32_t nseg,
+                                               uint32_t* p, uint32_t* s, SlotSeg* sl) {
+#pragma unroll
+  for (int k = 0; k < kBatchTiles; ++k) {
+    p[k] = base + k * kCoopBlock + threadIdx.x;
+    uint32_t v = p[k] < end ? __ldcg(seg_of + p[k]) : kNone;
+    s[k] = v < nseg ? v : kNone;
+  }
+  if (threadIdx.x < kSlots) sl[threadIdx.x].s = kNone;
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kBatchTiles; ++k)
+    if (s[k] != kNone) sl[s[k] & (kSlots - 1)].s = s[k];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
+  __shared__ SlotSeg sl[kSlots];
+  __shared__ uint32_t s_acc[kSlots * kSegWords];
+  __shared__ uint32_t s_bk[kSlots * kBucketWords];
+  __shared__ unsigned long long s_w1[kBatchTiles][kCoopWarps], s_w2[kBatchTiles][kCoopWarps];
+  __shared__ unsigned long long s_t1[kBatchTiles], s_t2[kBatchTiles];
+  __shared__ unsigned long long s_tot[2];
+  __shared__ unsigned long long s_bp1[kMaxCoopGrid], s_bp2[kMaxCoopGrid];  // chunk prefixes (phase C2)
+  const uint32_t FULL = 0xFFFFFFFFu;
+  const uint32_t T = *C.T_p;
+  const uint32_t lane = lane_id(), wid = threadIdx.x >> 5;
+
+  // ---- set-up: one treelet, a small segment, or level 0 over every root ----
+  if (T <= 1) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      *C.root_out = T == 1 ? C.troot[0] : kNone;
+      C.counters[0] = 0u;
+      C.counters[2] = 0u;
+    }
+    return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *C.root_out = C.N2;  // SAH node 0
+  if (T <= kSmallSeg) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < T; p += gridDim.x * blockDim.x) C.item[0][p] = p;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      C.small_start[0] = 0u;
+      C.small_end[0] = T - 1;
+      C.small_node[0] = 0u;
+      C.counters[0] = 1u;
+      C.counters[2] = 1u;
+    }
+    return;
+  }
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < T; p += gridDim.x * blockDim.x) {
+    uint32_t r = C.troot[p];
+    C.item[0][p] = p;
+    C.seg_of[0][p] = 0u;
+    C.plo[0][p] = C.nb_lo[r];
+    C.phi[0][p] = C.nb_hi[r];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    C.sa[0][0] = 0u;
+    C.sb[0][0] = T - 1;
+    C.snode[0][0] = 0u;
+    init_segment(C.sacc[0], C.sbk[0]);
+    C.lvl[0] = 1u;  // one large segment
+    C.lvl[1] = 1u;  // the root is SAH node 0
+    C.lvl[2] = 0u;
+  }
+  if (!coop_sync(C.bar, C.err)) return;
+
+  // every phase walks the block's chunk of consecutive positions in batches
+  const uint32_t ntiles = div_up_d(T, kCoopBlock);
+  const uint32_t chunk = div_up_d(ntiles, gridDim.x) * kCoopBlock;
+  const uint32_t c0 = min(blockIdx.x * chunk, T), c1 = min(c0 + chunk, T);
+  uint32_t par = 0;
+  for (uint32_t level = 0;; ++level) {
+    if (level > T) {  // every level splits each large segment: T levels at most
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(C.err, kErrLoopLimit);
+      return;
+    }
+    const uint32_t nx = par ^ 1u;
+    const uint32_t* Lc = C.lvl + 8 * par;
+    uint32_t* Ln = C.lvl + 8 * nx;
+    const uint32_t* seg_of = C.seg_of[par];
+    const float4* plo = C.plo[par];
+    const float4* phi = C.phi[par];
+    uint32_t* sacc = C.sacc[par];
+    uint32_t* sbk = C.sbk[par];
+    const uint32_t* sa = C.sa[par];
+    const uint32_t* sb = C.sb[par];
+    const uint32_t* snode = C.snode[par];
+    const uint32_t nseg = __ldcg(Lc);
+    if (nseg > C.maxseg) {  // every block reads the same word: all leave together
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(C.err, kErrBuild);
+      return;
+    }
+    uint32_t p[kBatchTiles], s[kBatchTiles];
+
+    // ---- A: segment bounds and centroid bounds ----
+    for (uint32_t base = c0; base < c1; base += kBatch) {
+      batch_segments(seg_of, base, c1, nseg, p, s, sl);
+      for (uint32_t k = threadIdx.x; k < kSlots * kSegWords; k += blockDim.x)
+        s_acc[k] = (((k % kSegWords) / 3) % 2 == 0) ? 0xFFFFFFFFu : 0u;
+      __syncthreads();
+      float4 l[kBatchTiles], h[kBatchTiles];
+#pragma unroll
+      for (int k = 0; k < kBatchTiles; ++k)
+        if (s[k] != kNone) {
+          l[k] = __ldcg(plo + p[k]);
+          h[k] = __ldcg(phi + p[k]);
+        }
+#pragma unroll 1
+      for (int k = 0; k < kBatchTiles; ++k) {
+        const uint32_t sk = s[k];
+        if (!__any_sync(FULL, sk != kNone)) continue;
+        uint32_t e[12];
+        if (sk != kNone) {
+          V3 lo{l[k].x, l[k].y, l[k].z}, hi{h[k].x, h[k].y, h[k].z};
+          V3 c = mul(add(lo, hi), 0.5f);
+          e[0] = fenc(lo.x); e[1] = fenc(lo.y); e[2] = fenc(lo.z);
+          e[3] = fenc(hi.x); e[4] = fenc(hi.y); e[5] = fenc(hi.z);
+          e[6] = fenc(c.x); e[7] = fenc(c.y); e[8] = fenc(c.z);
+          e[9] = e[6]; e[10] = e[7]; e[11] = e[8];
+        } else {
+#pragma unroll
+          for (int q = 0; q < 12; ++q) e[q] = ((q / 3) % 2 == 0) ? 0xFFFFFFFFu : 0u;
+        }
+        const uint32_t s0 = __shfl_sync(FULL, sk, 0);
+        if (__all_sync(FULL, sk == s0)) {  // one segment across the warp
+#pragma unroll
+          for (int q = 0; q < 12; ++q)
+            e[q] = ((q / 3) % 2 == 0) ? __reduce_min_sync(FULL, e[q]) : __reduce_max_sync(FULL, e[q]);
+          if (lane == 0) {
+            uint32_t* r = s_acc + (s0 & (kSlots - 1)) * kSegWords;
+            for (int q = 0; q < 12; ++q) {
+              if ((q / 3) % 2 == 0)
+                atomicMin(r + q, e[q]);
+              else
+                atomicMax(r + q, e[q]);
+            }
+          }
+        } else {  // runs of one segment meet at the run's first lane
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            uint32_t so = __shfl_down_sync(FULL, sk, o);
+            bool take = (lane + o < 32) && (so == sk) && (sk != kNone);
+#pragma unroll
+            for (int q = 0; q < 12; ++q) {
+              uint32_t y = __shfl_down_sync(FULL, e[q], o);
+              if (take) e[q] = ((q / 3) % 2 == 0) ? min(e[q], y) : max(e[q], y);
+            }
+          }
+          uint32_t sp = __shfl_up_sync(FULL, sk, 1);
+          if (sk != kNone && (lane == 0 || sp != sk)) {
+            uint32_t* r = s_acc + (sk & (kSlots - 1)) * kSegWords;
+            for (int q = 0; q < 12; ++q) {
+              if ((q / 3) % 2 == 0)
+                atomicMin(r + q, e[q]);
+              else
+                atomicMax(r + q, e[q]);
+            }
+          }
+        }
+      }
+      __syncthreads();
+      for (uint32_t k = threadIdx.x; k < kSlots * kSegWords; k += blockDim.x) {
+        const uint32_t seg = sl[k / kSegWords].s;
+        if (seg == kNone) continue;
+        const uint32_t v = s_acc[k];
+        const bool mn = ((k % kSegWords) / 3) % 2 == 0;
+        if (v == (mn ? 0xFFFFFFFFu : 0u)) continue;
+        uint32_t* dst = sacc + (size_t)seg * kSegWords + (k % kSegWords);
+        if (mn)
+          atomicMin(dst, v);
+        else
+          atomicMax(dst, v);
+      }
+      __syncthreads();
+    }
+    if (!coop_sync(C.bar, C.err)) return;
+
+    // ---- B: buckets ----
+    for (uint32_t base = c0; base < c1; base += kBatch) {
+      batch_segments(seg_of, base, c1, nseg, p, s, sl);
+      for (uint32_t k = threadIdx.x; k < kSlots * kBucketWords; k += blockDim.x)
+        s_bk[k] = (k % 7 == 0) ? 0u : ((k % 7) <= 3 ? 0xFFFFFFFFu : 0u);
+      if (threadIdx.x < kSlots * 6) {
+        const uint32_t j = threadIdx.x / 6, q = threadIdx.x % 6;
+        const uint32_t seg = sl[j].s;
+        if (seg != kNone) sl[j].cb[q] = fdec(__ldcg(sacc + (size_t)seg * kSegWords + 6 + q));
+      }
+      __syncthreads();
+      float4 l[kBatchTiles], h[kBatchTiles];
+#pragma unroll
+      for (int k = 0; k < kBatchTiles; ++k)
+        if (s[k] != kNone) {
+          l[k] = __ldcg(plo + p[k]);
+          h[k] = __ldcg(phi + p[k]);
+        }
+#pragma unroll 1
+      for (int k = 0; k < kBatchTiles; ++k) {
+        const uint32_t sk = s[k];
+        if (!__any_sync(FULL, sk != kNone)) continue;
+        V3 lo{0, 0, 0}, hi{0, 0, 0};
+        uint32_t ib = 0;
+        if (sk != kNone) {
+          lo = V3{l[k].x, l[k].y, l[k].z};
+          hi = V3{h[k].x, h[k].y, h[k].z};
+          const float* cbf = sl[sk & (kSlots - 1)].cb;
+          Bounds cb{V3{cbf[0], cbf[1], cbf[2]}, V3{cbf[3], cbf[4], cbf[5]}};
+          ib = sah_bucket(lo, hi, cb, bmax_extent(cb));
+          C.bucket[p[k]] = (uint8_t)ib;
+        }
+        const uint32_t s0 = __shfl_sync(FULL, sk, 0);
+        if (s0 != kNone && __all_sync(FULL, sk == s0)) {  // one segment: reduce per present bucket
+          uint32_t present = __reduce_or_sync(FULL, 1u << ib);
+          uint32_t* base_bk = s_bk + (s0 & (kSlots - 1)) * kBucketWords;
+          while (present) {
+            const uint32_t j = __ffs(present) - 1;
+            present &= present - 1;
+            const bool in = ib == j;
+            const uint32_t cnt = __popc(__ballot_sync(FULL, in));
+            uint32_t v0 = __reduce_min_sync(FULL, in ? fenc(lo.x) : 0xFFFFFFFFu);
+            uint32_t v1 = __reduce_min_sync(FULL, in ? fenc(lo.y) : 0xFFFFFFFFu);
+            uint32_t v2 = __reduce_min_sync(FULL, in ? fenc(lo.z) : 0xFFFFFFFFu);
+            uint32_t v3 = __reduce_max_sync(FULL, in ? fenc(hi.x) : 0u);
+            uint32_t v4 = __reduce_max_sync(FULL, in ? fenc(hi.y) : 0u);
+            uint32_t v5 = __reduce_max_sync(FULL, in ? fenc(hi.z) : 0u);
+            if (lane == 0) {
+              uint32_t* d = base_bk + j * 7;
+              atomicAdd(d, cnt);
+              atomicMin(d + 1, v0);
+              atomicMin(d + 2, v1);
+              atomicMin(d + 3, v2);
+              atomicMax(d + 4, v3);
+              atomicMax(d + 5, v4);
+              atomicMax(d + 6, v5);
+            }
+          }
+        } else if (sk != kNone) {
+          uint32_t* d = s_bk + (sk & (kSlots - 1)) * kBucketWords + ib * 7;
+          atomicAdd(d, 1u);
+          atomicMin(d + 1, fenc(lo.x));
+          atomicMin(d + 2, fenc(lo.y));
+          atomicMin(d + 3, fenc(lo.z));
+          atomicMax(d + 4, fenc(hi.x));
+          atomicMax(d + 5, fenc(hi.y));
+          atomicMax(d + 6, fenc(hi.z));
+        }
+      }
+      __syncthreads();
+      for (uint32_t k = threadIdx.x; k < kSlots * 12; k += blockDim.x) {
+        const uint32_t seg = sl[k / 12].s;
+        const uint32_t* src = s_bk + k * 7;
+        const uint32_t c = src[0];
+        if (seg == kNone || c == 0) continue;
+        uint32_t* d = sbk + (size_t)seg * kBucketWords + (k % 12) * 7;
+        atomicAdd(d, c);
+        for (int q = 1; q <= 3; ++q) atomicMin(d + q, src[q]);
+        for (int q = 4; q <= 6; ++q) atomicMax(d + q, src[q]);
+      }
+      __syncthreads();
+    }
+    if (!coop_sync(C.bar, C.err)) return;
+
+    // ---- C1: decisions, partition flags, scans within each block's chunk ----
+    {
+      unsigned long long carry1 = 0, carry2 = 0;
+      for (uint32_t base = c0; base < c1; base += kBatch) {
+        batch_segments(seg_of, base, c1, nseg, p, s, sl);
+        // one decision per segment the batch meets, one warp each
+        for (uint32_t j = wid; j < kSlots; j += kCoopWarps) {
+          const uint32_t sv = sl[j].s;
+          if (sv == kNone) continue;
+          const uint32_t* bk = sbk + (size_t)sv * kBucketWords;
+          uint32_t cj = 0;
+          Bounds bj = bempty();
+          if (lane < 12) {
+            cj = __ldcg(bk + lane * 7);
+            if (cj) bj = dec_bounds_cg(bk + lane * 7 + 1);
+          }
+          Bounds bb = dec_bounds_cg(sacc + (size_t)sv * kSegWords);
+          uint32_t kv;
+          int bv = warp_sah_split(cj, bj, barea(bb), &kv);
+          if (lane == 0) {
+            const uint32_t a = __ldcg(sa + sv), b = __ldcg(sb + sv);
+            const uint32_t n = b - a + 1;
+            sl[j].a = a;
+            sl[j].b = b;
+            sl[j].best = (uint32_t)bv;
+            sl[j].kk = kv;
+            sl[j].spt = a + kv;
+            sl[j].mid = (kv == n) ? a + n / 2 : a + kv;
+          }
+        }
+        __syncthreads();
+        unsigned long long v1[kBatchTiles], v2[kBatchTiles], i1[kBatchTiles], i2[kBatchTiles];
+        uint8_t bkt[kBatchTiles];
+#pragma unroll
+        for (int k = 0; k < kBatchTiles; ++k) bkt[k] = s[k] != kNone ? __ldcg(C.bucket + p[k]) : (uint8_t)0;
+#pragma unroll
+        for (int k = 0; k < kBatchTiles; ++k) {
+          bool fF = false, fT = false;
+          uint32_t nn = 0, nl = 0;
+          if (s[k] != kNone) {
+            const SlotSeg& g = sl[s[k] & (kSlots - 1)];
+            const bool pred = bkt[k] <= g.best;
+            fF = p[k] < g.spt && !pred;
+            fT = p[k] >= g.spt && pred;
+            if (p[k] == g.a) {
+              const uint32_t ln = g.mid - g.a, rn = g.b - g.mid + 1;
+              nn = (uint32_t)(ln >= 2) + (uint32_t)(rn >= 2);
+              nl = (uint32_t)(ln > kSmallSeg) + (uint32_t)(rn > kSmallSeg);
+            }
+          }
+          v1[k] = ((unsigned long long)fT << 32) | (unsigned long long)fF;
+          v2[k] = ((unsigned long long)nl << 32) | (unsigned long long)nn;
+          i1[k] = warp_incl_scan64(v1[k]);
+          i2[k] = warp_incl_scan64(v2[k]);
+          if (lane == 31) {
+            s_w1[k][wid] = i1[k];
+            s_w2[k][wid] = i2[k];
+          }
+        }
+        __syncthreads();
+        if (wid < (uint32_t)kBatchTiles) {  // warp k scans tile k's warp totals
+          const uint32_t k = wid;
+          unsigned long long w1 = lane < kCoopWarps ? s_w1[k][lane] : 0ull;
+          unsigned long long w2 = lane < kCoopWarps ? s_w2[k][lane] : 0ull;
+          unsigned long long x1 = warp_incl_scan64(w1), x2 = warp_incl_scan64(w2);
+          if (lane < kCoopWarps) {
+            s_w1[k][lane] = x1 - w1;
+            s_w2[k][lane] = x2 - w2;
+          }
+          if (lane == 31) {
+            s_t1[k] = x1;
+            s_t2[k] = x2;
+          }
+        }
+        __syncthreads();
+        unsigned long long o1 = carry1, o2 = carry2;
+#pragma unroll
+        for (int k = 0; k < kBatchTiles; ++k) {
+          if (p[k] < c1) C.ftl[p[k]] = o1 + s_w1[k][wid] + (i1[k] - v1[k]);
+          if (s[k] != kNone) {
+            const SlotSeg& g = sl[s[k] & (kSlots - 1)];
+            if (p[k] == g.a) {
+              C.segpre[s[k]] = o2 + s_w2[k][wid] + (i2[k] - v2[k]);
+              C.sdec[s[k]] = make_uint4(g.spt, g.mid, kNone, kNone);
+              C.sbest[s[k]] = g.best;
+            }
+          }
+          o1 += s_t1[k];
+          o2 += s_t2[k];
+        }
+        carry1 = o1;
+        carry2 = o2;
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) {
+        C.btot[2 * blockIdx.x] = carry1;
+        C.btot[2 * blockIdx.x + 1] = carry2;
+      }
+    }
+    if (!coop_sync(C.bar, C.err)) return;
+
+    // ---- C2: prefixes over the chunks, select tables, SAH nodes, children ----
+    block_scan_pairs(C.btot, gridDim.x, s_bp1, s_bp2, &s_w1[0][0], &s_w2[0][0], s_tot);
+    {
+      const unsigned long long gtot1 = s_tot[0], gtot2 = s_tot[1];
+      const uint32_t node_base = __ldcg(Lc + 1), small_base = __ldcg(Lc + 2);
+      if (blockIdx.x == 0 && threadIdx.x == 0) {  // the next level's words
+        const uint32_t tot_nn = (uint32_t)(gtot2 & 0xFFFFFFFFull), tot_nl = (uint32_t)(gtot2 >> 32);
+        Ln[0] = tot_nl;
+        Ln[1] = node_base + tot_nn;
+        Ln[2] = small_base + (tot_nn - tot_nl);
+      }
+      for (uint32_t base = c0; base < c1; base += kBatch) {
+        batch_segments(seg_of, base, c1, nseg, p, s, sl);
+        if (threadIdx.x < kSlots) {
+          SlotSeg& g = sl[threadIdx.x];
+          if (g.s != kNone) {
+            g.a = __ldcg(sa + g.s);
+            g.b = __ldcg(sb + g.s);
+            g.spt = __ldcg(&C.sdec[g.s].x);
+            g.mid = __ldcg(&C.sdec[g.s].y);
+            g.best = __ldcg(C.sbest + g.s);
+            const bool ok = g.a <= g.b && g.b < T;
+            if (!ok) {
+              atomicOr(C.err, kErrBuild);
+              g.s = kNone;
+            } else {
+              g.ga = s_bp1[g.a / chunk] + __ldcg(C.ftl + g.a);
+              g.ge = (g.b + 1 < T) ? s_bp1[(g.b + 1) / chunk] + __ldcg(C.ftl + g.b + 1) : gtot1;
+            }
+          }
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int k = 0; k < kBatchTiles; ++k) {
+          if (s[k] == kNone) continue;
+          const SlotSeg& g = sl[s[k] & (kSlots - 1)];
+          if (g.s == kNone) continue;
+          const uint32_t pk = p[k];
+          const bool pred = __ldcg(C.bucket + pk) <= g.best;
+          const bool fF = pk < g.spt && !pred, fT = pk >= g.spt && pred;
+          const uint32_t n = g.b - g.a + 1;
+          if (fF || fT) {
+            const unsigned long long gp = s_bp1[pk / chunk] + __ldcg(C.ftl + pk);
+            const uint32_t r = fF ? (uint32_t)(gp & 0xFFFFFFFFull) - (uint32_t)(g.ga & 0xFFFFFFFFull)
+                                  : (uint32_t)(g.ge >> 32) - (uint32_t)(gp >> 32) - 1u;
+            if (r < n) {
+              (fF ? C.posF : C.posT)[g.a + r] = pk;
+              C.rnk[pk] = r;
+            } else {
+              atomicOr(C.err, kErrBuild);
+              C.rnk[pk] = kNone;
+            }
+          }
+          if (pk != g.a) continue;
+          // the segment's SAH node and its children
+          const uint32_t sv = s[k];
+          const unsigned long long g2 = s_bp2[g.a / chunk] + __ldcg(C.segpre + sv);
+          const uint32_t nn_pre = (uint32_t)(g2 & 0xFFFFFFFFull), nl_pre = (uint32_t)(g2 >> 32);
+          const uint32_t a = g.a, b = g.b, mid = g.mid;
+          const uint32_t ln = mid - a, rn = b - mid + 1;
+          const uint32_t nd = __ldcg(snode + sv);
+          const uint32_t me = C.N2 + nd;
+          Bounds bb = dec_bounds_cg(sacc + (size_t)sv * kSegWords);
+          Bounds cb = dec_bounds_cg(sacc + (size_t)sv * kSegWords + 6);
+          C.sah_axis[nd] = (uint32_t)bmax_extent(cb);
+          C.nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
+          C.nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
+          uint32_t node = node_base + nn_pre, segn = nl_pre, small = small_base + (nn_pre - nl_pre);
+          uint32_t cseg[2] = {kNone, kNone};
+          const uint32_t ca[2] = {a, mid}, cb_[2] = {mid - 1, b}, cn[2] = {ln, rn};
+          for (int q = 0; q < 2; ++q) {
+            if (cn[q] < 2) continue;  // a single root: linked in phase E
+            const uint32_t id = node++;
+            if (id >= T || (cn[q] > kSmallSeg ? segn >= C.maxseg : small >= T)) {
+              atomicOr(C.err, kErrBuild);
+              continue;
+            }
+            (q ? C.child1 : C.child0)[me] = C.N2 + id;
+            C.parent[C.N2 + id] = (me << 1) | (uint32_t)q;
+            if (cn[q] > kSmallSeg) {
+              const uint32_t z = segn++;
+              cseg[q] = z;
+              C.sa[nx][z] = ca[q];
+              C.sb[nx][z] = cb_[q];
+              C.snode[nx][z] = id;
+              init_segment(C.sacc[nx] + (size_t)z * kSegWords, C.sbk[nx] + (size_t)z * kBucketWords);
+            } else {
+              const uint32_t z = small++;
+              C.small_start[z] = ca[q];
+              C.small_end[z] = cb_[q];
+              C.small_node[z] = id;
+            }
+          }
+          C.sdec[sv].z = cseg[0];
+          C.sdec[sv].w = cseg[1];
+        }
+        __syncthreads();
+      }
+    }
+    if (!coop_sync(C.bar, C.err)) return;
+
+    // ---- E: swap pairs, next level's position arrays, single-root children ----
+    {
+      const uint32_t* item = C.item[par];
+      uint32_t* item_n = C.item[nx];
+      uint32_t* seg_n = C.seg_of[nx];
+      for (uint32_t base = c0; base < c1; base += kBatch) {
+        batch_segments(seg_of, base, c1, nseg, p, s, sl);
+        if (threadIdx.x < kSlots) {
+          SlotSeg& g = sl[threadIdx.x];
+          if (g.s != kNone) {
+            g.a = __ldcg(sa + g.s);
+            g.b = __ldcg(sb + g.s);
+            const uint4 dec = __ldcg(&C.sdec[g.s]);  // spt, mid, left segment, right segment
+            g.spt = dec.x;
+            g.mid = dec.y;
+            g.cl = dec.z;
+            g.cr = dec.w;
+            g.best = __ldcg(C.sbest + g.s);
+            g.node = __ldcg(snode + g.s);
+            if (!(g.a <= g.b && g.b < T)) {
+              atomicOr(C.err, kErrBuild);
+              g.s = kNone;
+            }
+          }
+        }
+        __syncthreads();
+        uint32_t it[kBatchTiles];
+#pragma unroll
+        for (int k = 0; k < kBatchTiles; ++k) it[k] = p[k] < c1 ? __ldcg(item + p[k]) : 0u;
+#pragma unroll 1
+        for (int k = 0; k < kBatchTiles; ++k) {
+          const uint32_t pk = p[k];
+          if (pk >= c1) continue;
+          if (s[k] == kNone) {
+            item_n[pk] = it[k];
+            seg_n[pk] = kNone;
+            continue;
+          }
+          const SlotSeg& g = sl[s[k] & (kSlots - 1)];
+          if (g.s == kNone) continue;
+          const bool pred = __ldcg(C.bucket + pk) <= g.best;
+          const bool fF = pk < g.spt && !pred, fT = pk >= g.spt && pred;
+          uint32_t dst = pk;
+          const uint32_t n = g.b - g.a + 1;
+          if (fF || fT) {  // the r-th false (from the left) and the r-th true (from the right) trade places
+            const uint32_t r = __ldcg(C.rnk + pk);
+            dst = r < n ? __ldcg((fF ? C.posT : C.posF) + g.a + r) : kNone;
+          }
+          if (dst < g.a || dst > g.b) {
+            atomicOr(C.err, kErrBuild);
+            continue;
+          }
+          item_n[dst] = it[k];
+          C.plo[nx][dst] = __ldcg(plo + pk);
+          C.phi[nx][dst] = __ldcg(phi + pk);
+          seg_n[dst] = dst < g.mid ? g.cl : g.cr;
+          const uint32_t me = C.N2 + g.node;
+          if (dst == g.a && g.mid - g.a == 1) {
+            uint32_t r = C.troot[it[k]];
+            C.child0[me] = r;
+            C.parent[r] = (me << 1) | 0u;
+          }
+          if (dst == g.b && g.b - g.mid + 1 == 1) {
+            uint32_t r = C.troot[it[k]];
+            C.child1[me] = r;
+            C.parent[r] = (me << 1) | 1u;
+          }
+        }
+        __syncthreads();
+      }
+    }
+    if (!coop_sync(C.bar, C.err)) return;
+    par = nx;
+    if (__ldcg(C.lvl + 8 * par) == 0u) break;
+  }
+  // the positions end in buffer 0 (the warp-local SAH reads them there)
+  if (par == 1u)
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < T; p += gridDim.x * blockDim.x)
+      C.item[0][p] = __ldcg(C.item[1] + p);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    C.counters[0] = __ldcg(C.lvl + 8 * par + 1);
+    C.counters[2] = __ldcg(C.lvl + 8 * par + 2);
+  }
+}
+
 // Segments of 2..32 roots: the whole SAH recursion inside one warp. Bounds
-// by warp reductions, buckets by shared-memory atomics, the 11 split costs
-// one per lane (sah_decide's float operations on the same boxes) and the sequential
-// first-minimum rule by a lexicographic (cost, split) reduction. The
-// segment's n - 2 new SAH node ids are reserved with one atomic.
-__global__ void k_small_sah(SahArgs A, uint32_t nsmall, const uint32_t* sm_start, const uint32_t* sm_end,
+// by warp reductions, buckets by shared-memory atomics, the split decision by
+// warp_sah_split, the two-pointer partition by ballots. Each segment's n - 2
+// new SAH node ids are reserved with one atomic. A persistent grid of warps
+// walks the queue, whose length it reads from *nsmall_p (the cooperative
+// levels fill the queue on the device).
+__global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t* sm_start, const uint32_t* sm_end,
                             const uint32_t* sm_node, uint32_t* cur, uint32_t* counters, uint32_t* sah_axis,
                             float4* nb_lo, float4* nb_hi, uint32_t* child0, uint32_t* child1, uint32_t* parent,
                             uint32_t N2, uint32_t* err) {
@@ -894,191 +1326,148 @@ __global__ void k_small_sah(SahArgs A, uint32_t nsmall, const uint32_t* sm_start
   __shared__ uint32_t sh_stack[kB / 32][3 * 64];
   const uint32_t FULL = 0xFFFFFFFFu;
   const uint32_t w = threadIdx.x >> 5, lane = lane_id();
-  uint32_t seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (seg >= nsmall) return;
-  const uint32_t base = sm_start[seg];
-  const uint32_t n = sm_end[seg] - base + 1;
-  uint32_t item = lane < n ? cur[base + lane] : 0u;
-  V3 lo{0, 0, 0}, hi{0, 0, 0};
-  if (lane < n) item_bounds(A, item, &lo, &hi);
-  uint32_t id_base = 0, id_next = 0;
-  if (lane == 0 && n > 2) id_base = atomicAdd(&counters[0], n - 2);
-  id_base = __shfl_sync(FULL, id_base, 0);
-  uint32_t* stk = sh_stack[w];
-  int sp = 0;
-  if (lane == 0) {
-    stk[0] = 0;
-    stk[1] = n - 1;
-    stk[2] = sm_node[seg];
-  }
-  sp = 1;
-  __syncwarp();
-  uint32_t guard = 0;
-  while (sp > 0) {
-    if (++guard > 64) {
-      if (lane == 0) atomicOr(err, kErrLoopLimit);
-      break;
+  const uint32_t nsmall = *nsmall_p;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; seg < nsmall; seg += nwarps) {
+    const uint32_t base = sm_start[seg];
+    const uint32_t n = sm_end[seg] - base + 1;
+    if (n < 2 || n > kSmallSeg || sm_end[seg] >= A.N) {
+      if (lane == 0) atomicOr(err, kErrBuild);
+      continue;
     }
-    --sp;
-    uint32_t a = stk[3 * sp], b = stk[3 * sp + 1], nd = stk[3 * sp + 2];
+    uint32_t item = lane < n ? cur[base + lane] : 0u;
+    V3 lo{0, 0, 0}, hi{0, 0, 0};
+    if (lane < n) item_bounds(A, item, &lo, &hi);
+    uint32_t id_base = 0, id_next = 0;
+    if (lane == 0 && n > 2) id_base = atomicAdd(&counters[0], n - 2);
+    id_base = __shfl_sync(FULL, id_base, 0);
+    uint32_t* stk = sh_stack[w];
     __syncwarp();
-    bool act = lane >= a && lane <= b;
-    uint32_t cnt = b - a + 1;
-    V3 c = mul(add(lo, hi), 0.5f);
-    Bounds bb{V3{fdec(__reduce_min_sync(FULL, act ? fenc(lo.x) : 0xFFFFFFFFu)),
-                 fdec(__reduce_min_sync(FULL, act ? fenc(lo.y) : 0xFFFFFFFFu)),
-                 fdec(__reduce_min_sync(FULL, act ? fenc(lo.z) : 0xFFFFFFFFu))},
-              V3{fdec(__reduce_max_sync(FULL, act ? fenc(hi.x) : 0u)), fdec(__reduce_max_sync(FULL, act ? fenc(hi.y) : 0u)),
-                 fdec(__reduce_max_sync(FULL, act ? fenc(hi.z) : 0u))}};
-    Bounds cb{V3{fdec(__reduce_min_sync(FULL, act ? fenc(c.x) : 0xFFFFFFFFu)),
-                 fdec(__reduce_min_sync(FULL, act ? fenc(c.y) : 0xFFFFFFFFu)),
-                 fdec(__reduce_min_sync(FULL, act ? fenc(c.z) : 0xFFFFFFFFu))},
-              V3{fdec(__reduce_max_sync(FULL, act ? fenc(c.x) : 0u)), fdec(__reduce_max_sync(FULL, act ? fenc(c.y) : 0u)),
-                 fdec(__reduce_max_sync(FULL, act ? fenc(c.z) : 0u))}};
-    int dim = bmax_extent(cb);
-    float dist = comp(cb.hi, dim) - comp(cb.lo, dim);
-    uint32_t ib = 0;
-    if (act) {
-      float cc = (comp(lo, dim) + comp(hi, dim)) * 0.5f;
-      float t = (cc - comp(cb.lo, dim)) / dist;
-      float bt = 12.0f * t;
-      ib = (bt >= 0.0f) ? (uint32_t)bt : 0u;
-      if (ib >= 12u) ib = 11u;
-    }
-    // per-bucket counts and bounds
-    uint32_t* bcnt = sh_bcnt[w];
-    uint32_t* benc = sh_benc[w];
-    if (lane < 12) {
-      bcnt[lane] = 0;
-      for (int k = 0; k < 6; ++k) benc[lane * 6 + k] = k < 3 ? 0xFFFFFFFFu : 0u;
-    }
-    __syncwarp();
-    if (act) {
-      atomicAdd(&bcnt[ib], 1u);
-      uint32_t* be = benc + ib * 6;
-      atomicMin(be + 0, fenc(lo.x));
-      atomicMin(be + 1, fenc(lo.y));
-      atomicMin(be + 2, fenc(lo.z));
-      atomicMax(be + 3, fenc(hi.x));
-      atomicMax(be + 4, fenc(hi.y));
-      atomicMax(be + 5, fenc(hi.z));
-    }
-    __syncwarp();
-    // SAH cost of split `lane` (sah_decide's loop body). Lane j < 12 holds
-    // bucket j; shuffle scans give each lane the union and count of buckets
-    // 0..j (prefix) and j..11 (suffix), so split i takes lane i's prefix and
-    // lane i+1's suffix. Min and max of finite coordinates do not depend on
-    // the grouping (only a zero's sign could, which no area or cost sees).
-    uint32_t cj = lane < 12 ? bcnt[lane] : 0u;
-    Bounds pre = (lane < 12 && cj) ? dec_bounds(benc + lane * 6) : bempty();
-    Bounds suf = pre;
-    uint32_t npre = cj, nsuf = cj;
-#pragma unroll
-    for (uint32_t o = 1; o < 16; o <<= 1) {
-      Bounds u = shfl_bounds_up(pre, o);
-      uint32_t nu = __shfl_up_sync(FULL, npre, o);
-      Bounds v = shfl_bounds_down(suf, o);
-      uint32_t nv = __shfl_down_sync(FULL, nsuf, o);
-      if (lane >= o) {
-        pre = bunion(u, pre);
-        npre += nu;
-      }
-      if (lane + o < 12) {
-        suf = bunion(suf, v);
-        nsuf += nv;
-      }
-    }
-    Bounds b1 = shfl_bounds_down(suf, 1);
-    uint32_t n1 = __shfl_down_sync(FULL, nsuf, 1);
-    float cost = 0.0f;
-    if (lane < 11) {
-      const Bounds& b0 = pre;
-      uint32_t n0 = npre;
-      float l = (n0 == 0) ? 0.0f : (float)n0 * barea(b0);
-      float r = (n1 == 0) ? 0.0f : (float)n1 * barea(b1);
-      cost = (float)(0.125 + (double)((l + r) / barea(bb)));
-    }
-    // first index of the minimum; a NaN never wins, and a NaN at split 0 keeps split 0
-    float c0 = __shfl_sync(FULL, cost, 0);
-    float bc = (lane < 11 && !isnan(cost)) ? cost : __int_as_float(0x7f800000);
-    uint32_t bi = lane;
-    for (int o = 16; o > 0; o >>= 1) {
-      float oc = __shfl_xor_sync(FULL, bc, o);
-      uint32_t oi = __shfl_xor_sync(FULL, bi, o);
-      if (oc < bc || (oc == bc && oi < bi)) {
-        bc = oc;
-        bi = oi;
-      }
-    }
-    int best = isnan(c0) ? 0 : (int)bi;
-    uint32_t k = 0;
-    for (int j = 0; j <= best; ++j) k += bcnt[j];
-    // two-pointer partition of [a, b] by ib <= best
-    uint32_t spt = a + k;
-    bool pred = ib <= (uint32_t)best;
-    uint32_t fmask = __ballot_sync(FULL, act && lane < spt && !pred);
-    uint32_t tmask = __ballot_sync(FULL, act && lane >= spt && pred);
-    uint32_t src = lane;
-    if (act && lane < spt && !pred) {
-      uint32_t r = __popc(fmask & ((1u << lane) - 1u));
-      uint32_t m = __brev(tmask);  // r-th highest set bit of tmask
-      for (uint32_t q = 0; q < r; ++q) m &= m - 1u;
-      src = 31u - (uint32_t)(__ffs(m) - 1);
-    } else if (act && lane >= spt && pred) {
-      uint32_t r = __popc(tmask & ~((2u << lane) - 1u));  // trues above this lane
-      if (lane == 31) r = 0;
-      uint32_t m = fmask;
-      for (uint32_t q = 0; q < r; ++q) m &= m - 1u;
-      src = (uint32_t)(__ffs(m) - 1);
-    }
-    item = __shfl_sync(FULL, item, src);
-    lo.x = __shfl_sync(FULL, lo.x, src); lo.y = __shfl_sync(FULL, lo.y, src);
-    lo.z = __shfl_sync(FULL, lo.z, src); hi.x = __shfl_sync(FULL, hi.x, src);
-    hi.y = __shfl_sync(FULL, hi.y, src); hi.z = __shfl_sync(FULL, hi.z, src);
-    uint32_t mid = (k == cnt) ? a + cnt / 2 : a + k;
-    uint32_t me = N2 + nd;
     if (lane == 0) {
-      sah_axis[nd] = (uint32_t)dim;
-      nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
-      nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
+      stk[0] = 0;
+      stk[1] = n - 1;
+      stk[2] = sm_node[seg];
     }
-    uint32_t ln = mid - a, rn = b - mid + 1;
-    uint32_t litem = __shfl_sync(FULL, item, a);
-    uint32_t ritem = __shfl_sync(FULL, item, b);
-    if (lane == 0) {
-      if (ln == 1) {
-        uint32_t r = A.troot[litem];
-        child0[me] = r;
-        parent[r] = (me << 1) | 0u;
-      } else {
-        uint32_t cl = id_base + id_next++;
-        child0[me] = N2 + cl;
-        parent[N2 + cl] = (me << 1) | 0u;
-        stk[3 * sp] = a; stk[3 * sp + 1] = mid - 1; stk[3 * sp + 2] = cl;
-        ++sp;
+    int sp = 1;
+    __syncwarp();
+    uint32_t guard = 0;
+    while (sp > 0) {
+      if (++guard > 64) {
+        if (lane == 0) atomicOr(err, kErrLoopLimit);
+        break;
       }
-      if (rn == 1) {
-        uint32_t r = A.troot[ritem];
-        child1[me] = r;
-        parent[r] = (me << 1) | 1u;
-      } else {
-        uint32_t cr = id_base + id_next++;
-        child1[me] = N2 + cr;
-        parent[N2 + cr] = (me << 1) | 1u;
-        stk[3 * sp] = mid; stk[3 * sp + 1] = b; stk[3 * sp + 2] = cr;
-        ++sp;
+      --sp;
+      uint32_t a = stk[3 * sp], b = stk[3 * sp + 1], nd = stk[3 * sp + 2];
+      __syncwarp();
+      bool act = lane >= a && lane <= b;
+      uint32_t cnt = b - a + 1;
+      V3 c = mul(add(lo, hi), 0.5f);
+      Bounds bb{V3{fdec(__reduce_min_sync(FULL, act ? fenc(lo.x) : 0xFFFFFFFFu)),
+                   fdec(__reduce_min_sync(FULL, act ? fenc(lo.y) : 0xFFFFFFFFu)),
+                   fdec(__reduce_min_sync(FULL, act ? fenc(lo.z) : 0xFFFFFFFFu))},
+                V3{fdec(__reduce_max_sync(FULL, act ? fenc(hi.x) : 0u)),
+                   fdec(__reduce_max_sync(FULL, act ? fenc(hi.y) : 0u)),
+                   fdec(__reduce_max_sync(FULL, act ? fenc(hi.z) : 0u))}};
+      Bounds cb{V3{fdec(__reduce_min_sync(FULL, act ? fenc(c.x) : 0xFFFFFFFFu)),
+                   fdec(__reduce_min_sync(FULL, act ? fenc(c.y) : 0xFFFFFFFFu)),
+                   fdec(__reduce_min_sync(FULL, act ? fenc(c.z) : 0xFFFFFFFFu))},
+                V3{fdec(__reduce_max_sync(FULL, act ? fenc(c.x) : 0u)),
+                   fdec(__reduce_max_sync(FULL, act ? fenc(c.y) : 0u)),
+                   fdec(__reduce_max_sync(FULL, act ? fenc(c.z) : 0u))}};
+      int dim = bmax_extent(cb);
+      uint32_t ib = act ? sah_bucket(lo, hi, cb, dim) : 0u;
+      // per-bucket counts and bounds
+      uint32_t* bcnt = sh_bcnt[w];
+      uint32_t* benc = sh_benc[w];
+      if (lane < 12) {
+        bcnt[lane] = 0;
+        for (int k = 0; k < 6; ++k) benc[lane * 6 + k] = k < 3 ? 0xFFFFFFFFu : 0u;
       }
+      __syncwarp();
+      if (act) {
+        atomicAdd(&bcnt[ib], 1u);
+        uint32_t* be = benc + ib * 6;
+        atomicMin(be + 0, fenc(lo.x));
+        atomicMin(be + 1, fenc(lo.y));
+        atomicMin(be + 2, fenc(lo.z));
+        atomicMax(be + 3, fenc(hi.x));
+        atomicMax(be + 4, fenc(hi.y));
+        atomicMax(be + 5, fenc(hi.z));
+      }
+      __syncwarp();
+      uint32_t cj = lane < 12 ? bcnt[lane] : 0u;
+      Bounds bj = (lane < 12 && cj) ? dec_bounds(benc + lane * 6) : bempty();
+      uint32_t k;
+      int best = warp_sah_split(cj, bj, barea(bb), &k);
+      // two-pointer partition of [a, b] by ib <= best
+      uint32_t spt = a + k;
+      bool pred = ib <= (uint32_t)best;
+      uint32_t fmask = __ballot_sync(FULL, act && lane < spt && !pred);
+      uint32_t tmask = __ballot_sync(FULL, act && lane >= spt && pred);
+      uint32_t src = lane;
+      if (act && lane < spt && !pred) {
+        uint32_t r = __popc(fmask & ((1u << lane) - 1u));
+        uint32_t m = __brev(tmask);  // r-th highest set bit of tmask
+        for (uint32_t q = 0; q < r; ++q) m &= m - 1u;
+        src = 31u - (uint32_t)(__ffs(m) - 1);
+      } else if (act && lane >= spt && pred) {
+        uint32_t r = __popc(tmask & ~((2u << lane) - 1u));  // trues above this lane
+        if (lane == 31) r = 0;
+        uint32_t m = fmask;
+        for (uint32_t q = 0; q < r; ++q) m &= m - 1u;
+        src = (uint32_t)(__ffs(m) - 1);
+      }
+      item = __shfl_sync(FULL, item, src);
+      lo.x = __shfl_sync(FULL, lo.x, src); lo.y = __shfl_sync(FULL, lo.y, src);
+      lo.z = __shfl_sync(FULL, lo.z, src); hi.x = __shfl_sync(FULL, hi.x, src);
+      hi.y = __shfl_sync(FULL, hi.y, src); hi.z = __shfl_sync(FULL, hi.z, src);
+      uint32_t mid = (k == cnt) ? a + cnt / 2 : a + k;
+      uint32_t me = N2 + nd;
+      if (lane == 0) {
+        sah_axis[nd] = (uint32_t)dim;
+        nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
+        nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
+      }
+      uint32_t ln = mid - a, rn = b - mid + 1;
+      uint32_t litem = __shfl_sync(FULL, item, a);
+      uint32_t ritem = __shfl_sync(FULL, item, b);
+      if (lane == 0) {
+        if (ln == 1) {
+          uint32_t r = A.troot[litem];
+          child0[me] = r;
+          parent[r] = (me << 1) | 0u;
+        } else {
+          uint32_t cl = id_base + id_next++;
+          child0[me] = N2 + cl;
+          parent[N2 + cl] = (me << 1) | 0u;
+          stk[3 * sp] = a; stk[3 * sp + 1] = mid - 1; stk[3 * sp + 2] = cl;
+          ++sp;
+        }
+        if (rn == 1) {
+          uint32_t r = A.troot[ritem];
+          child1[me] = r;
+          parent[r] = (me << 1) | 1u;
+        } else {
+          uint32_t cr = id_base + id_next++;
+          child1[me] = N2 + cr;
+          parent[N2 + cr] = (me << 1) | 1u;
+          stk[3 * sp] = mid; stk[3 * sp + 1] = b; stk[3 * sp + 2] = cr;
+          ++sp;
+        }
+      }
+      sp = __shfl_sync(FULL, sp, 0);
+      __syncwarp();
     }
-    sp = __shfl_sync(FULL, sp, 0);
+    if (lane < n) cur[base + lane] = item;
     __syncwarp();
   }
-  if (lane < n) cur[base + lane] = item;
 }
 
 // Subtree node counts of SAH nodes, bottom-up from the treelet roots.
-__global__ void k_sah_sizes(uint32_t T, const uint32_t* troot, const uint32_t* parent, uint32_t* visits, uint32_t* size,
-                            const uint32_t* child0, const uint32_t* child1, uint32_t root, uint32_t* err) {
+__global__ void k_sah_sizes(const uint32_t* info, const uint32_t* troot, const uint32_t* parent, uint32_t* visits,
+                            uint32_t* size, const uint32_t* child0, const uint32_t* child1, uint32_t* err) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t T = info[kInfoT], root = info[kInfoRoot];
   if (t >= T) return;
   uint32_t cur = troot[t];
   uint32_t guard = 0;
@@ -1099,7 +1488,7 @@ __global__ void k_sah_sizes(uint32_t T, const uint32_t* troot, const uint32_t* p
 // ---------------------------------------------------------------------------
 // A9: flattenBVHTree — depth-first preorder index of every reference node
 // ---------------------------------------------------------------------------
-__global__ void k_flatten(uint32_t N, uint32_t nsah, uint32_t root, uint32_t M, const uint32_t* skey, const uint32_t* tid,
+__global__ void k_flatten(uint32_t N, uint32_t* info, const uint32_t* skey, const uint32_t* tid,
                           const uint32_t* tstart, const uint32_t* tsize, const uint32_t* rng_lo,
                           const uint32_t* rng_hi, const uint32_t* child0, const uint32_t* parent,
                           const uint32_t* size, const uint32_t* sah_axis, const float4* nb_lo, const float4* nb_hi,
@@ -1107,6 +1496,16 @@ __global__ void k_flatten(uint32_t N, uint32_t nsah, uint32_t root, uint32_t M, 
                           uint32_t* err) {
   uint32_t X = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t N2 = 2 * N;
+  const uint32_t nsah = info[kInfoT] - 1u, root = info[kInfoRoot];
+  const uint32_t M = root < N2 + N ? size[root] : kNone;
+  if (M > N2) {  // a flattened tree has at most 2N - 1 nodes
+    if (X == 0) {
+      info[kInfoM] = 0u;
+      atomicOr(err, kErrBuild);
+    }
+    return;
+  }
+  if (X == 0) info[kInfoM] = M;
   if (X >= N2 + nsah) return;
   uint32_t kind;  // 0 radix interior, 1 leaf, 2 SAH
   uint32_t lo = 0, hi = 0;
@@ -1169,18 +1568,26 @@ __global__ void k_flatten(uint32_t N, uint32_t nsah, uint32_t root, uint32_t M, 
 // two children a traversal step chooses between share a cache line, and a
 // left subtree's records follow its parent's closely. kids[r] counts the
 // interior children of the interior node of preorder rank r.
-__global__ void k_int_kids(uint32_t M, const uint32_t* lin_node, const uint32_t* is_int, const uint32_t* int_index,
-                           uint32_t* kids) {
+// Interior nodes of the flattened tree (the last prefix of the flags).
+__device__ __forceinline__ uint32_t n_int_of(const uint32_t* info, const uint32_t* is_int, const uint32_t* int_index) {
+  const uint32_t M = info[kInfoM];
+  return M ? int_index[M - 1] + is_int[M - 1] : 0u;
+}
+
+__global__ void k_int_kids(const uint32_t* info, const uint32_t* lin_node, const uint32_t* is_int,
+                           const uint32_t* int_index, uint32_t* kids) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t M = info[kInfoM];
   if (i >= M || !is_int[i]) return;
   uint32_t c1 = lin_node[(size_t)i * 3];
   uint32_t k = (i + 1 < M ? is_int[i + 1] : 0u) + (c1 < M ? is_int[c1] : 0u);
   kids[int_index[i]] = k;
 }
 // slot[rank] = the node's index in the traversal layout; off = exclusive scan of kids
-__global__ void k_int_slots(uint32_t M, const uint32_t* lin_node, const uint32_t* is_int, const uint32_t* int_index,
-                            const uint32_t* off, uint32_t* slot) {
+__global__ void k_int_slots(const uint32_t* info, const uint32_t* lin_node, const uint32_t* is_int,
+                            const uint32_t* int_index, const uint32_t* off, uint32_t* slot) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t M = info[kInfoM];
   if (i >= M || !is_int[i]) return;
   uint32_t r = int_index[i];
   if (r == 0) slot[0] = 0;
@@ -1191,9 +1598,12 @@ __global__ void k_int_slots(uint32_t M, const uint32_t* lin_node, const uint32_t
 }
 
 // Child-pair traversal layout.
-__global__ void k_node2(uint32_t M, const uint32_t* lin_node, const float* lin_bounds, const uint32_t* is_int,
-                        const uint32_t* int_index, const uint32_t* slot, Node2* out) {
+// The record is written twice: into the reference layout and into the
+// leaf-split layout's copy of it (k_split_emit then redirects split slots).
+__global__ void k_node2(const uint32_t* info, const uint32_t* lin_node, const float* lin_bounds, const uint32_t* is_int,
+                        const uint32_t* int_index, const uint32_t* slot, Node2* out, Node2* out_split) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t M = info[kInfoM];
   if (i >= M || !is_int[i]) return;
   uint32_t c[2] = {i + 1, lin_node[(size_t)i * 3]};
   if (c[0] >= M || c[1] >= M) return;  // malformed tree: traversal guards report it
@@ -1216,7 +1626,9 @@ __global__ void k_node2(uint32_t M, const uint32_t* lin_node, const float* lin_b
   nd.b1 = make_float4(b[1][0], b[1][3], b[1][1], b[1][4]);
   nd.bz = make_float4(b[0][2], b[0][5], b[1][2], b[1][5]);
   nd.meta = make_int4(ref[0], ref[1], (int)cnt[0], (int)((lin_node[(size_t)i * 3 + 2] << 30) | (cnt[1] & 0x3FFFFFFFu)));
-  out[slot[int_index[i]]] = nd;
+  const uint32_t at = slot[int_index[i]];
+  out[at] = nd;
+  out_split[at] = nd;
 }
 
 // Primitive records in leaf order: triangles carry their vertices, spheres
@@ -1276,9 +1688,16 @@ __host__ __device__ inline uint32_t split_depth(uint32_t c) {
 }
 
 // Records each child slot of the reference layout adds (slot s = 2 * record + child).
-__global__ void k_split_count(uint32_t n_int, const Node2* nodes, uint32_t* cnt, uint32_t* max_d) {
+// Slots past the tree's 2 * n_int (up to n_slots, the scanned length) count 0.
+__global__ void k_split_count(const uint32_t* info, const uint32_t* is_int, const uint32_t* int_index,
+                              const Node2* nodes, uint32_t* cnt, uint32_t n_slots, uint32_t* max_d) {
   uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= 2 * n_int) return;
+  if (s >= n_slots) return;
+  const uint32_t n_int = n_int_of(info, is_int, int_index);
+  if (s >= 2 * n_int) {
+    cnt[s] = 0u;
+    return;
+  }
   int4 m = nodes[s >> 1].meta;
   int ref = (s & 1) ? m.y : m.x;
   uint32_t c = (s & 1) ? ((uint32_t)m.w & 0x3FFFFFFFu) : (uint32_t)m.z;
@@ -1289,12 +1708,17 @@ __global__ void k_split_count(uint32_t n_int, const Node2* nodes, uint32_t* cnt,
 
 // One thread per child slot: redirects the slot to its range tree and writes
 // the tree's records (boxes = union of the primitive bounds of each range).
-// out holds a copy of the reference layout's n_int records on entry.
-__global__ void k_split_emit(uint32_t n_int, const Node2* nodes, const uint32_t* off, const uint32_t* sprim,
-                             const float4* pb_lo, const float4* pb_hi, uint32_t n_prims, Node2* out, uint32_t n_out,
+// out holds a copy of the reference layout's n_int records on entry and has
+// room for n_cap records.
+__global__ void k_split_emit(const uint32_t* info, const uint32_t* is_int, const uint32_t* int_index,
+                             const Node2* nodes, const uint32_t* cnt, const uint32_t* off, const uint32_t* sprim,
+                             const float4* pb_lo, const float4* pb_hi, uint32_t n_prims, Node2* out, uint32_t n_cap,
                              uint32_t* err) {
   uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t n_int = n_int_of(info, is_int, int_index);
   if (s >= 2 * n_int) return;
+  const uint32_t n_split = off[2 * n_int - 1] + cnt[2 * n_int - 1];
+  const uint32_t n_out = (uint64_t)n_int + n_split <= n_cap ? n_int + n_split : 0u;
   uint32_t i = s >> 1, k = s & 1;
   int4 m = nodes[i].meta;
   int ref = k ? m.y : m.x;
@@ -1360,6 +1784,30 @@ __global__ void k_split_emit(uint32_t n_int, const Node2* nodes, const uint32_t*
     out[base + h] = nd;
   }
 }
+
+// What the host needs once the tree is built, gathered for one copy:
+// treelets, flattened nodes, interior nodes, leaf-split records and depth,
+// tree depth, SAH nodes, the error word, the root's record and bounds.
+constexpr uint32_t kSumWords = 17;
+__global__ void k_build_summary(uint32_t* info, const uint32_t* is_int, const uint32_t* int_index,
+                                const uint32_t* split_cnt, const uint32_t* split_off, const uint32_t* counters,
+                                const uint32_t* depth_max, const uint32_t* lin_node, const float* lin_bounds,
+                                const uint32_t* err) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  uint32_t* o = info + kInfoSum;
+  const uint32_t n_int = n_int_of(info, is_int, int_index);
+  o[0] = info[kInfoT];
+  o[1] = info[kInfoM];
+  o[2] = n_int;
+  o[3] = n_int ? split_off[2 * n_int - 1] + split_cnt[2 * n_int - 1] : 0u;
+  o[4] = counters[6];
+  o[5] = *depth_max;
+  o[6] = counters[0];
+  o[7] = *err;
+  for (int k = 0; k < 3; ++k) o[8 + k] = lin_node[k];
+  for (int k = 0; k < 6; ++k) o[11 + k] = __float_as_uint(lin_bounds[k]);
+}
+static_assert(kInfoSum + kSumWords <= kInfoWords, "summary block fits the info words");
 
 }  // namespace
 
@@ -1431,7 +1879,15 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
     return WPBR_OK;
   }
   const bool full = (ctx->quirks & WPBR_Q_FULL_MORTON_SORT) != 0;
-  const uint32_t NU = 2 * N + N;  // unified id space upper bound (T <= N)
+  // Sizes found on the device are bounded by N, so every buffer is sized
+  // before the first kernel and the build reads back from the device only
+  // once, at the end: treelets T <= N, flattened nodes M <= 2N - 1, interior
+  // nodes < N, leaf-split records < N / 4 + 1 (a leaf of c primitives adds
+  // fewer than c / 4).
+  const uint32_t N2 = 2 * N;
+  const uint32_t NU = 3 * N;  // unified id space [0, 2N + T)
+  const uint32_t maxseg = N / (kSmallSeg + 1) + 2;
+  const size_t split_cap = (size_t)N + N / 4 + 2;
   WPBR_CUDA(B.pb_lo.ensure(N));
   WPBR_CUDA(B.pb_hi.ensure(N));
   WPBR_CUDA(B.centroid.ensure(N));
@@ -1441,7 +1897,7 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   WPBR_CUDA(B.k1.ensure(N));
   WPBR_CUDA(B.v0.ensure(N));
   WPBR_CUDA(B.v1.ensure(N));
-  uint32_t nblk = div_up(N, kRadixTile);
+  const uint32_t nblk = div_up(N, kRadixTile);
   WPBR_CUDA(B.hist.ensure((size_t)256 * nblk));
   WPBR_CUDA(B.flags.ensure(N));
   WPBR_CUDA(B.tid.ensure(N));
@@ -1457,13 +1913,51 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   WPBR_CUDA(B.size.ensure(NU));
   WPBR_CUDA(B.nb_lo.ensure(NU));
   WPBR_CUDA(B.nb_hi.ensure(NU));
+  WPBR_CUDA(B.cur.ensure(N));
+  WPBR_CUDA(B.nxt.ensure(N));
+  WPBR_CUDA(B.seg_of.ensure(N2));
+  WPBR_CUDA(B.pos_lo.ensure(N2));
+  WPBR_CUDA(B.pos_hi.ensure(N2));
+  WPBR_CUDA(B.posF.ensure(N));
+  WPBR_CUDA(B.posT.ensure(N));
+  WPBR_CUDA(B.bucket.ensure(N));
+  WPBR_CUDA(B.ftl.ensure(N));
+  WPBR_CUDA(B.rnk.ensure(N));
+  WPBR_CUDA(B.seg_start.ensure(2 * (size_t)maxseg));
+  WPBR_CUDA(B.seg_end.ensure(2 * (size_t)maxseg));
+  WPBR_CUDA(B.seg_node.ensure(2 * (size_t)maxseg));
+  WPBR_CUDA(B.seg_acc.ensure(2 * (size_t)maxseg * kSegWords));
+  WPBR_CUDA(B.seg_bk.ensure(2 * (size_t)maxseg * kBucketWords));
+  WPBR_CUDA(B.seg_best.ensure(maxseg));
+  WPBR_CUDA(B.seg_dec.ensure(maxseg));
+  WPBR_CUDA(B.seg_pre.ensure(maxseg));
+  WPBR_CUDA(B.chunk_tot.ensure(2 * (size_t)kMaxCoopGrid));
+  WPBR_CUDA(B.lvl.ensure(16));
+  WPBR_CUDA(B.bar.ensure(4));
+  WPBR_CUDA(B.small_start.ensure(N));
+  WPBR_CUDA(B.small_end.ensure(N));
+  WPBR_CUDA(B.small_node.ensure(N));
+  WPBR_CUDA(B.sah_axis.ensure(N));
   WPBR_CUDA(B.counters.ensure(8));
+  WPBR_CUDA(B.dinfo.ensure(kInfoWords));
+  WPBR_CUDA(B.lin_node.ensure((size_t)3 * N2));
+  WPBR_CUDA(B.lin_bounds.ensure((size_t)6 * N2));
+  WPBR_CUDA(B.is_int.ensure(N2));
+  WPBR_CUDA(B.int_index.ensure(N2));
   WPBR_CUDA(B.depth_max.ensure(1));
+  WPBR_CUDA(B.int_kids.ensure(N));
+  WPBR_CUDA(B.int_slot.ensure(N));
+  WPBR_CUDA(B.nodes2.ensure(N));
+  WPBR_CUDA(B.nodes_split.ensure(split_cap));
+  WPBR_CUDA(B.prims.ensure((size_t)3 * N));
+  WPBR_CUDA(B.split_cnt.ensure(N2));
+  WPBR_CUDA(B.split_off.ensure(N2));
+  if (!B.h_info) WPBR_CUDA(cudaMallocHost((void**)&B.h_info, sizeof(uint32_t) * kInfoWords));
 
   const unsigned g = div_up(N, kB);
-  // A3/A4
-  uint32_t cb_init[8] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u, 0u};
-  WPBR_CUDA(cudaMemcpyAsync(B.cb_enc.p, cb_init, sizeof(cb_init), cudaMemcpyHostToDevice, st));
+  // A3/A4: centroid bounds start empty (min words all ones, max words zero)
+  WPBR_CUDA(cudaMemsetAsync(B.cb_enc.p, 0xFF, 12, st));
+  WPBR_CUDA(cudaMemsetAsync(B.cb_enc.p + 3, 0, 12, st));
   k_prim_bounds<<<g, kB, 0, st>>>(S, B.pb_lo.p, B.pb_hi.p, B.centroid.p, B.cb_enc.p);
   // A5
   k_morton<<<g, kB, 0, st>>>(N, B.centroid.p, B.cb_enc.p, B.codes.p, B.k0.p, B.v0.p);
@@ -1489,14 +1983,8 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   // treelets
   k_treelet_flags<<<g, kB, 0, st>>>(B.skey, N, B.flags.p);
   WPBR_CUDA(scan_exclusive(B.flags.p, B.tid.p, N, B.scan_tmp, st));
-  uint32_t last_flag = 0, last_scan = 0;
-  WPBR_CUDA(cudaMemcpyAsync(&last_flag, B.flags.p + N - 1, 4, cudaMemcpyDeviceToHost, st));
-  WPBR_CUDA(cudaMemcpyAsync(&last_scan, B.tid.p + N - 1, 4, cudaMemcpyDeviceToHost, st));
-  WPBR_CUDA(cudaStreamSynchronize(st));
-  const uint32_t T = last_flag + last_scan;
-  B.T = T;
-  k_treelet_ids<<<g, kB, 0, st>>>(B.flags.p, B.tid.p, B.tstart.p, N);
-  k_treelet_sizes<<<div_up(T, kB), kB, 0, st>>>(B.tstart.p, B.tsize.p, T, N);
+  k_treelet_ids<<<g, kB, 0, st>>>(B.flags.p, B.tid.p, B.tstart.p, N, B.dinfo.p);
+  k_treelet_sizes<<<g, kB, 0, st>>>(B.tstart.p, B.tsize.p, B.dinfo.p, N);
   // A7
   WPBR_CUDA(cudaMemsetAsync(B.visits.p, 0, sizeof(uint32_t) * NU, st));
   WPBR_CUDA(cudaMemsetAsync(B.parent.p, 0xFF, sizeof(uint32_t) * NU, st));
@@ -1506,236 +1994,141 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   k_refit<<<div_up(2 * N, kB), kB, 0, st>>>(N, B.skey, B.sprim, B.tid.p, B.tstart.p, B.tsize.p, B.rng_lo.p,
                                             B.rng_hi.p, B.child0.p, B.child1.p, B.parent.p, B.visits.p, B.size.p,
                                             B.nb_lo.p, B.nb_hi.p, B.pb_lo.p, B.pb_hi.p, B.troot.p, ctx->d_err.p);
-  // A8
-  const uint32_t N2 = 2 * N;
-  uint32_t nsah = 0;
-  uint32_t root;
-  if (T == 1) {
-    WPBR_CUDA(cudaMemcpyAsync(&root, B.troot.p, 4, cudaMemcpyDeviceToHost, st));
-    WPBR_CUDA(cudaStreamSynchronize(st));
-  } else {
-    root = N2;
-    WPBR_CUDA(B.cur.ensure(T));
-    WPBR_CUDA(B.nxt.ensure(T));
-    WPBR_CUDA(B.pos_seg.ensure(T));
-    WPBR_CUDA(B.bucket.ensure(T));
-    WPBR_CUDA(B.fl.ensure(T));
-    WPBR_CUDA(B.ft.ensure(T));
-    WPBR_CUDA(B.ftscan.ensure(T));
-    WPBR_CUDA(B.posF.ensure(T));
-    WPBR_CUDA(B.posT.ensure(T));
-    WPBR_CUDA(B.sah_axis.ensure(T));
-    uint32_t maxseg = T / (kSmallSeg + 1) + 2;
-    WPBR_CUDA(B.seg_start.ensure(2 * maxseg));
-    WPBR_CUDA(B.seg_end.ensure(2 * maxseg));
-    WPBR_CUDA(B.seg_node.ensure(2 * maxseg));
-    WPBR_CUDA(B.seg_k.ensure(maxseg));
-    WPBR_CUDA(B.seg_mid.ensure(maxseg));
-    WPBR_CUDA(B.seg_dim.ensure(maxseg));  // best bucket
-    WPBR_CUDA(B.seg_a.ensure(maxseg));    // left child node
-    WPBR_CUDA(B.seg_b.ensure(maxseg));    // right child node
-    WPBR_CUDA(B.seg_benc.ensure((size_t)6 * maxseg));
-    WPBR_CUDA(B.seg_cenc.ensure((size_t)6 * maxseg));
-    WPBR_CUDA(B.seg_bucket_cnt.ensure((size_t)12 * maxseg));
-    WPBR_CUDA(B.seg_bucket_enc.ensure((size_t)72 * maxseg));
-    WPBR_CUDA(B.small_start.ensure(T));
-    WPBR_CUDA(B.small_end.ensure(T));
-    WPBR_CUDA(B.small_node.ensure(T));
-    WPBR_CUDA(B.flags.ensure(maxseg + 1));  // nlarge counts (reused)
-    SahArgs A{N, T, B.troot.p, B.nb_lo.p, B.nb_hi.p};
-    // iota
-    {
-      std::vector<uint32_t> dummy;
+  // A8: the large segments' levels in one cooperative launch, then the
+  // warp-local SAH of the small segments
+  {
+    int dev = 0, sms = 0, coop = 0, per_sm = 0;
+    WPBR_CUDA(cudaGetDevice(&dev));
+    WPBR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    WPBR_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    WPBR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sah_levels, kCoopBlock, 0));
+    if (!coop || per_sm < 1) return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: cooperative launch unavailable");
+    if (per_sm > 2) per_sm = 2;
+    if ((uint32_t)(per_sm * sms) > kMaxCoopGrid) per_sm = (int)(kMaxCoopGrid / (uint32_t)sms);
+    if (per_sm < 1) return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: too many SMs for the cooperative grid");
+    WPBR_CUDA(cudaMemsetAsync(B.bar.p, 0, sizeof(uint32_t) * 4, st));
+    CoopSah C{};
+    C.N = N;
+    C.N2 = N2;
+    C.maxseg = maxseg;
+    C.T_p = B.dinfo.p + kInfoT;
+    C.troot = B.troot.p;
+    C.nb_lo = B.nb_lo.p;
+    C.nb_hi = B.nb_hi.p;
+    C.child0 = B.child0.p;
+    C.child1 = B.child1.p;
+    C.parent = B.parent.p;
+    C.sah_axis = B.sah_axis.p;
+    C.item[0] = B.cur.p;
+    C.item[1] = B.nxt.p;
+    C.seg_of[0] = B.seg_of.p;
+    C.seg_of[1] = B.seg_of.p + N;
+    C.plo[0] = B.pos_lo.p;
+    C.plo[1] = B.pos_lo.p + N;
+    C.phi[0] = B.pos_hi.p;
+    C.phi[1] = B.pos_hi.p + N;
+    C.bucket = B.bucket.p;
+    C.ftl = B.ftl.p;
+    C.rnk = B.rnk.p;
+    C.posF = B.posF.p;
+    C.posT = B.posT.p;
+    for (int q = 0; q < 2; ++q) {
+      C.sa[q] = B.seg_start.p + (size_t)q * maxseg;
+      C.sb[q] = B.seg_end.p + (size_t)q * maxseg;
+      C.snode[q] = B.seg_node.p + (size_t)q * maxseg;
+      C.sacc[q] = B.seg_acc.p + (size_t)q * maxseg * kSegWords;
+      C.sbk[q] = B.seg_bk.p + (size_t)q * maxseg * kBucketWords;
     }
-    k_fill<<<div_up(T, kB), kB, 0, st>>>(B.pos_seg.p, T, 0);  // placeholder, replaced below
-    // cur = 0..T-1
-    {
-      // write iota via scan of ones
-      k_fill<<<div_up(T, kB), kB, 0, st>>>(B.fl.p, T, 1u);
-      WPBR_CUDA(scan_exclusive(B.fl.p, B.cur.p, T, B.scan_tmp, st));
-    }
-    uint32_t h_counters[8] = {1u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
-    uint32_t* L_start = B.seg_start.p;
-    uint32_t* L_end = B.seg_end.p;
-    uint32_t* L_node = B.seg_node.p;
-    uint32_t* Nx_start = B.seg_start.p + maxseg;
-    uint32_t* Nx_end = B.seg_end.p + maxseg;
-    uint32_t* Nx_node = B.seg_node.p + maxseg;
-    uint32_t nlarge = 0;
-    if (T > kSmallSeg) {
-      uint32_t init[3] = {0u, T - 1, 0u};
-      WPBR_CUDA(cudaMemcpyAsync(L_start, &init[0], 4, cudaMemcpyHostToDevice, st));
-      WPBR_CUDA(cudaMemcpyAsync(L_end, &init[1], 4, cudaMemcpyHostToDevice, st));
-      WPBR_CUDA(cudaMemcpyAsync(L_node, &init[2], 4, cudaMemcpyHostToDevice, st));
-      nlarge = 1;
-    } else {
-      uint32_t init[3] = {0u, T - 1, 0u};
-      WPBR_CUDA(cudaMemcpyAsync(B.small_start.p, &init[0], 4, cudaMemcpyHostToDevice, st));
-      WPBR_CUDA(cudaMemcpyAsync(B.small_end.p, &init[1], 4, cudaMemcpyHostToDevice, st));
-      WPBR_CUDA(cudaMemcpyAsync(B.small_node.p, &init[2], 4, cudaMemcpyHostToDevice, st));
-      h_counters[2] = 1;
-    }
-    WPBR_CUDA(cudaMemcpyAsync(B.counters.p, h_counters, sizeof(h_counters), cudaMemcpyHostToDevice, st));
-    const unsigned gT = div_up(T, kB);
-    const unsigned gS = div_up(maxseg, kB);
-    // Level counts live in two device words (this level's and the next's);
-    // each level's next count is also copied into a small pinned ring. Level
-    // L is queued as soon as level L - 2's copy shows that level L - 1 has
-    // large segments, so the GPU always has the next level queued instead of
-    // idling through a host round trip per level; the level after the last
-    // one is queued too and finds no segment.
-    WPBR_CUDA(B.nseg.ensure(2));
-    WPBR_CUDA(cudaMemcpyAsync(B.nseg.p, &nlarge, 4, cudaMemcpyHostToDevice, st));
-    if (!B.h_nseg) WPBR_CUDA(cudaMallocHost((void**)&B.h_nseg, sizeof(uint32_t) * BvhState::kLevelRing));
-    for (cudaEvent_t& ev : B.lev_ev)
-      if (!ev) WPBR_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    int level = 0;
-    while (nlarge > 0) {  // level 0 has a large segment; later levels end on the ring's counts
-      if (level >= 2) {
-        const int r = (level - 2) % BvhState::kLevelRing;
-        WPBR_CUDA(cudaEventSynchronize(B.lev_ev[r]));
-        if (B.h_nseg[r] == 0) break;  // level - 1 had no large segment
-      }
-      if (level >= 100000) return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: SAH level limit");
-      const uint32_t* nseg = B.nseg.p + (level & 1);
-      uint32_t* nseg_next = B.nseg.p + ((level + 1) & 1);
-      SegLevel L{L_start, L_end, L_node};
-      k_pos_seg<<<gT, kB, 0, st>>>(T, nseg, L_start, L_end, B.pos_seg.p);
-      k_seg_init<<<gS, kB, 0, st>>>(nseg, B.seg_benc.p, B.seg_cenc.p, B.seg_bucket_cnt.p, B.seg_bucket_enc.p);
-      k_seg_reduce<<<gT, kB, 0, st>>>(A, B.cur.p, B.pos_seg.p, B.seg_benc.p, B.seg_cenc.p);
-      k_seg_bucket<<<gT, kB, 0, st>>>(A, B.cur.p, B.pos_seg.p, B.seg_cenc.p, B.bucket.p, B.seg_bucket_cnt.p,
-                                      B.seg_bucket_enc.p);
-      k_seg_split<<<gS, kB, 0, st>>>(
-          nseg, maxseg, L, B.seg_benc.p, B.seg_cenc.p, B.seg_bucket_cnt.p, B.seg_bucket_enc.p, B.seg_k.p, B.seg_dim.p,
-          B.seg_mid.p, B.seg_a.p, B.seg_b.p, B.counters.p, B.sah_axis.p, B.nb_lo.p, B.nb_hi.p, B.child0.p,
-          B.child1.p, B.parent.p, B.flags.p, B.small_start.p, B.small_end.p, B.small_node.p, N2);
-      k_part_flags<<<gT, kB, 0, st>>>(T, B.pos_seg.p, B.bucket.p, B.seg_k.p, B.seg_dim.p, B.ft.p);
-      WPBR_CUDA(scan_exclusive_pair(B.ft.p, B.ftscan.p, T, B.scan_tmp, st));
-      k_part_ranks<<<gT, kB, 0, st>>>(T, L, B.pos_seg.p, B.ft.p, B.ftscan.p, B.posF.p, B.posT.p);
-      k_part_scatter<<<gT, kB, 0, st>>>(T, L, B.pos_seg.p, B.ft.p, B.ftscan.p, B.posF.p, B.posT.p, B.cur.p,
-                                        B.nxt.p);
-      std::swap(B.cur, B.nxt);
-      // next level list (ordered by start)
-      WPBR_CUDA(scan_exclusive(B.flags.p, B.flags.p, maxseg, B.scan_tmp, st));
-      k_seg_children<<<gS, kB, 0, st>>>(nseg, maxseg, nseg_next, L, B.seg_mid.p, B.seg_a.p, B.seg_b.p, B.flags.p,
-                                        B.cur.p, B.troot.p, B.child0.p, B.child1.p, B.parent.p, Nx_start, Nx_end,
-                                        Nx_node, N2);
-      const int r = level % BvhState::kLevelRing;
-      WPBR_CUDA(cudaMemcpyAsync(B.h_nseg + r, nseg_next, 4, cudaMemcpyDeviceToHost, st));
-      WPBR_CUDA(cudaEventRecord(B.lev_ev[r], st));
-      ++level;
-      std::swap(L_start, Nx_start);
-      std::swap(L_end, Nx_end);
-      std::swap(L_node, Nx_node);
-    }
-    WPBR_CUDA(cudaMemcpyAsync(h_counters, B.counters.p, sizeof(h_counters), cudaMemcpyDeviceToHost, st));
-    WPBR_CUDA(cudaStreamSynchronize(st));
-    uint32_t nsmall = h_counters[2];
-    if (nsmall > 0)
-      k_small_sah<<<div_up((uint64_t)nsmall * 32, kB), kB, 0, st>>>(
-          A, nsmall, B.small_start.p, B.small_end.p, B.small_node.p, B.cur.p, B.counters.p, B.sah_axis.p, B.nb_lo.p,
-          B.nb_hi.p, B.child0.p, B.child1.p, B.parent.p, N2, ctx->d_err.p);
-    WPBR_CUDA(cudaMemcpyAsync(h_counters, B.counters.p, sizeof(h_counters), cudaMemcpyDeviceToHost, st));
-    WPBR_CUDA(cudaStreamSynchronize(st));
-    nsah = h_counters[0];
-    if (nsah != T - 1) return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: SAH node count mismatch");
-    k_sah_sizes<<<div_up(T, kB), kB, 0, st>>>(T, B.troot.p, B.parent.p, B.visits.p, B.size.p, B.child0.p,
-                                              B.child1.p, root, ctx->d_err.p);
+    C.sdec = B.seg_dec.p;
+    C.sbest = B.seg_best.p;
+    C.segpre = B.seg_pre.p;
+    C.btot = B.chunk_tot.p;
+    C.lvl = B.lvl.p;
+    C.small_start = B.small_start.p;
+    C.small_end = B.small_end.p;
+    C.small_node = B.small_node.p;
+    C.counters = B.counters.p;
+    C.root_out = B.dinfo.p + kInfoRoot;
+    C.bar = B.bar.p;
+    C.err = ctx->d_err.p;
+    void* args[] = {&C};
+    WPBR_CUDA(cudaLaunchCooperativeKernel((const void*)k_sah_levels, dim3((unsigned)(per_sm * sms)),
+                                          dim3(kCoopBlock), args, 0, st));
+    SahArgs A{N, B.troot.p, B.nb_lo.p, B.nb_hi.p};
+    k_small_sah<<<persistent_grid((const void*)k_small_sah, kB), kB, 0, st>>>(
+        A, B.counters.p + 2, B.small_start.p, B.small_end.p, B.small_node.p, B.cur.p, B.counters.p, B.sah_axis.p,
+        B.nb_lo.p, B.nb_hi.p, B.child0.p, B.child1.p, B.parent.p, N2, ctx->d_err.p);
+    k_sah_sizes<<<g, kB, 0, st>>>(B.dinfo.p, B.troot.p, B.parent.p, B.visits.p, B.size.p, B.child0.p, B.child1.p,
+                                  ctx->d_err.p);
   }
   // A9
-  uint32_t M = 0;
-  WPBR_CUDA(cudaMemcpyAsync(&M, B.size.p + root, 4, cudaMemcpyDeviceToHost, st));
-  WPBR_CUDA(cudaStreamSynchronize(st));
-  B.M = M;
-  WPBR_CUDA(B.lin_node.ensure((size_t)3 * M));
-  WPBR_CUDA(B.lin_bounds.ensure((size_t)6 * M));
-  WPBR_CUDA(B.is_int.ensure(M));
-  WPBR_CUDA(B.int_index.ensure(M));
+  WPBR_CUDA(cudaMemsetAsync(B.is_int.p, 0, sizeof(uint32_t) * N2, st));
   WPBR_CUDA(cudaMemsetAsync(B.depth_max.p, 0, 4, st));
-  k_flatten<<<div_up(N2 + nsah, kB), kB, 0, st>>>(N, nsah, root, M, B.skey, B.tid.p, B.tstart.p, B.tsize.p, B.rng_lo.p,
-                                                   B.rng_hi.p, B.child0.p, B.parent.p, B.size.p, B.sah_axis.p,
-                                                   B.nb_lo.p, B.nb_hi.p, B.lin_node.p, B.lin_bounds.p, B.is_int.p,
-                                                   B.depth_max.p, ctx->d_err.p);
-  WPBR_CUDA(scan_exclusive(B.is_int.p, B.int_index.p, M, B.scan_tmp, st));
-  uint32_t last_int = 0, last_idx = 0, depth = 0;
-  uint32_t node0[3];
-  float b0[6];
-  WPBR_CUDA(cudaMemcpyAsync(&last_int, B.is_int.p + M - 1, 4, cudaMemcpyDeviceToHost, st));
-  WPBR_CUDA(cudaMemcpyAsync(&last_idx, B.int_index.p + M - 1, 4, cudaMemcpyDeviceToHost, st));
-  WPBR_CUDA(cudaMemcpyAsync(&depth, B.depth_max.p, 4, cudaMemcpyDeviceToHost, st));
-  WPBR_CUDA(cudaMemcpyAsync(node0, B.lin_node.p, 12, cudaMemcpyDeviceToHost, st));
-  WPBR_CUDA(cudaMemcpyAsync(b0, B.lin_bounds.p, 24, cudaMemcpyDeviceToHost, st));
-  WPBR_CUDA(cudaStreamSynchronize(st));
-  B.n_int = last_int + last_idx;
-  B.max_depth = depth;
-  WPBR_CUDA(B.nodes2.ensure(B.n_int ? B.n_int : 1));
-  WPBR_CUDA(B.prims.ensure((size_t)3 * N));
-  if (B.n_int) {
-    WPBR_CUDA(B.int_kids.ensure(B.n_int));
-    WPBR_CUDA(B.int_slot.ensure(B.n_int));
-    k_int_kids<<<div_up(M, kB), kB, 0, st>>>(M, B.lin_node.p, B.is_int.p, B.int_index.p, B.int_kids.p);
-    WPBR_CUDA(scan_exclusive(B.int_kids.p, B.int_kids.p, B.n_int, B.scan_tmp, st));
-    k_int_slots<<<div_up(M, kB), kB, 0, st>>>(M, B.lin_node.p, B.is_int.p, B.int_index.p, B.int_kids.p,
-                                              B.int_slot.p);
-    k_node2<<<div_up(M, kB), kB, 0, st>>>(M, B.lin_node.p, B.lin_bounds.p, B.is_int.p, B.int_index.p,
-                                          B.int_slot.p, B.nodes2.p);
-  }
+  k_flatten<<<div_up((uint64_t)N2 + N, kB), kB, 0, st>>>(N, B.dinfo.p, B.skey, B.tid.p, B.tstart.p, B.tsize.p,
+                                                          B.rng_lo.p, B.rng_hi.p, B.child0.p, B.parent.p, B.size.p,
+                                                          B.sah_axis.p, B.nb_lo.p, B.nb_hi.p, B.lin_node.p,
+                                                          B.lin_bounds.p, B.is_int.p, B.depth_max.p, ctx->d_err.p);
+  WPBR_CUDA(scan_exclusive(B.is_int.p, B.int_index.p, N2, B.scan_tmp, st));
+  WPBR_CUDA(cudaMemsetAsync(B.int_kids.p, 0, sizeof(uint32_t) * N, st));
+  const unsigned g2 = div_up(N2, kB);
+  k_int_kids<<<g2, kB, 0, st>>>(B.dinfo.p, B.lin_node.p, B.is_int.p, B.int_index.p, B.int_kids.p);
+  WPBR_CUDA(scan_exclusive(B.int_kids.p, B.int_kids.p, N, B.scan_tmp, st));
+  k_int_slots<<<g2, kB, 0, st>>>(B.dinfo.p, B.lin_node.p, B.is_int.p, B.int_index.p, B.int_kids.p, B.int_slot.p);
+  k_node2<<<g2, kB, 0, st>>>(B.dinfo.p, B.lin_node.p, B.lin_bounds.p, B.is_int.p, B.int_index.p, B.int_slot.p,
+                             B.nodes2.p, B.nodes_split.p);
   k_prims<<<g, kB, 0, st>>>(S, B.sprim, B.prims.p);
-  WPBR_CUDA(cudaGetLastError());
   // leaf-split layout (the default binary traversal); a tree whose root is a
   // leaf keeps the reference layout
-  uint32_t n_split = 0, split_d = 0;
-  if (B.n_int) {
-    WPBR_CUDA(B.counters.ensure(8));
-    WPBR_CUDA(B.split_cnt.ensure(2 * (size_t)B.n_int));
-    WPBR_CUDA(B.split_off.ensure(2 * (size_t)B.n_int));
-    WPBR_CUDA(cudaMemsetAsync(B.counters.p + 6, 0, 4, st));
-    k_split_count<<<div_up(2 * (size_t)B.n_int, kB), kB, 0, st>>>(B.n_int, B.nodes2.p, B.split_cnt.p,
-                                                                  B.counters.p + 6);
-    WPBR_CUDA(scan_exclusive(B.split_cnt.p, B.split_off.p, 2 * B.n_int, B.scan_tmp, st));
-    uint32_t lastc = 0, lasto = 0;
-    WPBR_CUDA(cudaMemcpyAsync(&lastc, B.split_cnt.p + 2 * B.n_int - 1, 4, cudaMemcpyDeviceToHost, st));
-    WPBR_CUDA(cudaMemcpyAsync(&lasto, B.split_off.p + 2 * B.n_int - 1, 4, cudaMemcpyDeviceToHost, st));
-    WPBR_CUDA(cudaMemcpyAsync(&split_d, B.counters.p + 6, 4, cudaMemcpyDeviceToHost, st));
-    WPBR_CUDA(cudaStreamSynchronize(st));
-    n_split = lastc + lasto;
-    if (n_split) {
-      if ((uint64_t)B.n_int + n_split > 0x7FFFFFFFull) return set_err(ctx, WPBR_ERR_OOM, "bvh_build: leaf split too large");
-      WPBR_CUDA(B.nodes_split.ensure((size_t)B.n_int + n_split));
-      WPBR_CUDA(cudaMemcpyAsync(B.nodes_split.p, B.nodes2.p, sizeof(Node2) * (size_t)B.n_int,
-                                cudaMemcpyDeviceToDevice, st));
-      k_split_emit<<<div_up(2 * (size_t)B.n_int, kB), kB, 0, st>>>(B.n_int, B.nodes2.p, B.split_off.p, B.sprim,
-                                                                   B.pb_lo.p, B.pb_hi.p, N, B.nodes_split.p,
-                                                                   B.n_int + n_split, ctx->d_err.p);
-      WPBR_CUDA(cudaGetLastError());
-    } else {
-      split_d = 0;
-    }
+  WPBR_CUDA(cudaMemsetAsync(B.counters.p + 6, 0, 4, st));
+  k_split_count<<<g2, kB, 0, st>>>(B.dinfo.p, B.is_int.p, B.int_index.p, B.nodes2.p, B.split_cnt.p, N2,
+                                   B.counters.p + 6);
+  WPBR_CUDA(scan_exclusive(B.split_cnt.p, B.split_off.p, N2, B.scan_tmp, st));
+  k_split_emit<<<g2, kB, 0, st>>>(B.dinfo.p, B.is_int.p, B.int_index.p, B.nodes2.p, B.split_cnt.p, B.split_off.p,
+                                  B.sprim, B.pb_lo.p, B.pb_hi.p, N, B.nodes_split.p, (uint32_t)split_cap,
+                                  ctx->d_err.p);
+  k_build_summary<<<1, 32, 0, st>>>(B.dinfo.p, B.is_int.p, B.int_index.p, B.split_cnt.p, B.split_off.p,
+                                    B.counters.p, B.depth_max.p, B.lin_node.p, B.lin_bounds.p, ctx->d_err.p);
+  WPBR_CUDA(cudaGetLastError());
+  WPBR_CUDA(cudaMemcpyAsync(B.h_info, B.dinfo.p + kInfoSum, sizeof(uint32_t) * kSumWords, cudaMemcpyDeviceToHost,
+                            st));
+  WPBR_CUDA(cudaStreamSynchronize(st));
+  const uint32_t* o = B.h_info;
+  const uint32_t T = o[0], M = o[1], n_int = o[2], nsah = o[6], derr = o[7];
+  uint32_t n_split = o[3], split_d = o[4];
+  const uint32_t depth = o[5];
+  if (derr) return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: device invariant violated");
+  if (T == 0 || nsah != T - 1) return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: SAH node count mismatch");
+  if ((uint64_t)n_int + n_split > split_cap || M == 0 || M >= N2)
+    return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: tree sizes out of range");
+  B.T = T;
+  B.M = M;
+  B.n_int = n_int;
+  B.max_depth = depth;
+  if (!n_int || !n_split) {
+    n_split = 0;
+    split_d = 0;
   }
   BvhView v{};
   v.nodes = n_split ? B.nodes_split.p : B.nodes2.p;
   v.nodes_ref = B.nodes2.p;
-  v.n_ref_int = B.n_int;
+  v.n_ref_int = n_int;
   v.ref_depth = depth;
   v.prims = B.prims.p;
   v.empty = 0;
+  const uint32_t* node0 = o + 8;
   bool root_leaf = node0[1] > 0;
   v.root_ref = root_leaf ? ~(int)node0[0] : 0;
   v.root_count = root_leaf ? node0[1] : 0;
   for (int k = 0; k < 3; ++k) {
-    v.root_lo[k] = b0[k];
-    v.root_hi[k] = b0[3 + k];
+    memcpy(&v.root_lo[k], o + 11 + k, 4);
+    memcpy(&v.root_hi[k], o + 14 + k, 4);
   }
   v.max_depth = depth + split_d;
   v.stack_cap = kDefaultStackCap;
   v.step_cap = kDefaultStepCap;
   v.n_prims = N;
-  v.n_int = B.n_int + n_split;
+  v.n_int = n_int + n_split;
   B.view = v;
-  uint32_t derr = 0;
-  WPBR_CUDA(cudaMemcpyAsync(&derr, ctx->d_err.p, 4, cudaMemcpyDeviceToHost, st));
-  WPBR_CUDA(cudaStreamSynchronize(st));
-  if (derr) return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: device invariant violated");
   B.built = true;
   return WPBR_OK;
 }

@@ -137,12 +137,12 @@ void bvh_release(wpbr_ctx* ctx, bool keep_traversal) {
   B.flags.release(); B.tid.release(); B.tstart.release(); B.tsize.release(); B.troot.release();
   B.rng_lo.release(); B.rng_hi.release(); B.child0.release(); B.child1.release(); B.parent.release();
   B.visits.release(); B.size.release(); B.nb_lo.release(); B.nb_hi.release();
-  B.cur.release(); B.nxt.release(); B.pos_seg.release(); B.bucket.release(); B.fl.release();
-  B.ft.release(); B.ftscan.release(); B.posF.release(); B.posT.release();
-  B.seg_a.release(); B.seg_b.release(); B.seg_start.release(); B.seg_end.release(); B.seg_node.release();
-  B.seg_k.release(); B.seg_mid.release(); B.seg_dim.release(); B.seg_benc.release(); B.seg_cenc.release();
-  B.seg_bucket_cnt.release(); B.seg_bucket_enc.release(); B.small_start.release(); B.small_end.release();
-  B.small_node.release(); B.counters.release(); B.nseg.release(); B.sah_axis.release(); B.lin_node.release();
+  B.cur.release(); B.nxt.release(); B.seg_of.release(); B.posF.release(); B.posT.release(); B.rnk.release();
+  B.pos_lo.release(); B.pos_hi.release(); B.bucket.release(); B.ftl.release();
+  B.seg_start.release(); B.seg_end.release(); B.seg_node.release(); B.seg_acc.release(); B.seg_bk.release();
+  B.seg_best.release(); B.seg_dec.release(); B.seg_pre.release(); B.chunk_tot.release(); B.lvl.release();
+  B.bar.release(); B.small_start.release(); B.small_end.release();
+  B.small_node.release(); B.counters.release(); B.dinfo.release(); B.sah_axis.release(); B.lin_node.release();
   B.lin_bounds.release(); B.is_int.release(); B.int_index.release(); B.depth_max.release();
   B.int_kids.release(); B.int_slot.release();
   B.split_cnt.release(); B.split_off.release();
@@ -217,9 +217,7 @@ WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
   ctx->marg_func.release(); ctx->marg_cdf.release(); ctx->marg_int.release(); ctx->env_lum.release();
   ctx->tex_texels.release(); ctx->tex_levels.release(); ctx->tex_info.release(); ctx->tex_gauss.release();
   bvh_release(ctx, false);
-  if (ctx->bvh.h_nseg) cudaFreeHost(ctx->bvh.h_nseg);
-  for (cudaEvent_t& ev : ctx->bvh.lev_ev)
-    if (ev) cudaEventDestroy(ev);
+  if (ctx->bvh.h_info) cudaFreeHost(ctx->bvh.h_info);
   RenderState& R = ctx->rs;
   R.acc.release(); R.hit_prim.release(); R.shadow_rays.release(); R.shadow_hit.release(); R.pstate.release();
   R.Lbuf.release(); R.pfilm.release(); R.pass_dev.release(); R.counters.release();

@@ -66,16 +66,19 @@ struct BvhState {
   DevBuf<uint32_t> rng_lo, rng_hi, child0, child1;  // unified-id arrays
   DevBuf<uint32_t> parent, visits, size;            // size 2N+T
   DevBuf<float4> nb_lo, nb_hi;                      // node bounds, unified ids
-  // SAH
-  DevBuf<uint32_t> cur, nxt, pos_seg, bucket, fl, posF, posT;
-  DevBuf<unsigned long long> ft, ftscan;  // partition flags (true << 32 | false) and their prefix sums
-  DevBuf<uint32_t> seg_a, seg_b, seg_start, seg_end, seg_node, seg_k, seg_mid, seg_dim;
-  DevBuf<uint32_t> seg_benc, seg_cenc, seg_bucket_cnt, seg_bucket_enc;
+  // SAH (k_sah_levels): per position, two buffers each (cur / nxt hold the roots)
+  DevBuf<uint32_t> cur, nxt, seg_of, posF, posT, rnk;
+  DevBuf<float4> pos_lo, pos_hi;
+  DevBuf<uint8_t> bucket;
+  DevBuf<unsigned long long> ftl;  // prefix of the partition flags (true << 32 | false) within each chunk
+  // per large segment, two sets (a level's and the next level's)
+  DevBuf<uint32_t> seg_start, seg_end, seg_node, seg_acc, seg_bk, seg_best;
+  DevBuf<uint4> seg_dec;
+  DevBuf<unsigned long long> seg_pre, chunk_tot;  // children prefixes per segment, totals per chunk
+  DevBuf<uint32_t> lvl, bar;                      // level words, grid barrier
   DevBuf<uint32_t> small_start, small_end, small_node, counters;
-  DevBuf<uint32_t> nseg;  // large-segment counts of the current and the next SAH level
-  static constexpr int kLevelRing = 4;
-  uint32_t* h_nseg = nullptr;  // pinned copies of each level's next count (a ring)
-  cudaEvent_t lev_ev[kLevelRing] = {};
+  DevBuf<uint32_t> dinfo;       // sizes found on the device (treelets, root, nodes, summary)
+  uint32_t* h_info = nullptr;   // pinned copy of dinfo's summary
   DevBuf<uint32_t> sah_axis;
   // flattened tree (CSceneTreeLBVH) + traversal layout
   DevBuf<uint32_t> lin_node;  // M*3: offset, n_shapes, axis
