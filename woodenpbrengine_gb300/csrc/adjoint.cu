@@ -381,11 +381,6 @@ __global__ void __launch_bounds__(kTB) k_adj_eval(PassCtx P, AdjView A, const fl
   Lb[pix] = make_float4(L.r, L.g, L.b, 0.0f);
 }
 
-__global__ void k_adj_film(uint32_t W, uint32_t H, const float2* pf, const float4* Lb, float4* acc) {
-  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= W * H) return;
-  film_gather(W, H, pix % W, pix / W, pf, Lb, acc);
-}
 
 // dLoss/dL of a sample: the transpose of the tile-clipped film gather.
 __device__ RGB3 film_adjoint(uint32_t W, uint32_t H, uint32_t pix, float2 f, const float4* gpix) {
@@ -757,7 +752,8 @@ wpbr_status adjoint_forward(wpbr_ctx* ctx, const float* target, float* image, do
     wpbr_status s = replay_pass(ctx, P, A, p);
     if (s != WPBR_OK) return s;
     k_adj_eval<<<div_up(n, kTB), kTB, 0, st>>>(P, A, J.state.p, J.shadow_hit.p, J.Lb.p);
-    k_adj_film<<<div_up(n, kTB), kTB, 0, st>>>(J.W, J.H, J.pf.p, J.Lb.p, J.acc.p);
+    k_film_tiles<<<dim3(div_up(J.W, kFilmTile), div_up(J.H, kFilmTile)), kFilmThreadsRGB, 0, st>>>(
+        J.W, J.H, J.pf.p, J.Lb.p, J.acc.p);
   }
   const float* d_target = nullptr;
   if (target) {

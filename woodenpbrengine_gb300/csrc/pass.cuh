@@ -260,32 +260,76 @@ __device__ __forceinline__ uint32_t light_prim(const wpbr_light& lt) {
 
 // JobAccumalateLIFromSamples (CSFilm.cpp:70-122) as a gather: each pixel
 // sums, in the reference's row-major sample order, the Mitchell-weighted
-// samples of its 32x32 tile whose splat footprint covers it.
-__device__ void film_gather(uint32_t W, uint32_t H, uint32_t x, uint32_t y, const float2* pf, const float4* Lb,
-                            float4* acc) {
-  uint32_t tx0 = (x / 32) * 32, ty0 = (y / 32) * 32;
-  uint32_t tx1 = min(tx0 + 31, W - 1), ty1 = min(ty0 + 31, H - 1);
+// samples of its 32x32 tile whose splat footprint covers it. A block takes
+// kFilmTile x kFilmTile pixels and first stages the samples of its halo in
+// shared memory, once each: the sample's value, its splat footprint clipped
+// to its own 32x32 tile (bit masks over the five pixel columns and rows it
+// can reach: a pixel of another tile is never inside it, so the clip by the
+// pixel's tile and the clip by the sample's agree), and the Mitchell factors
+// of those columns and rows. A pixel's weight is then the product of the same
+// two factors, in the same order, as one computed per (pixel, sample) pair,
+// so the film is bit-identical to that gather.
+constexpr int kFilmTile = 16;
+constexpr int kFilmHalo = kFilmTile + 4;
+constexpr int kFilmThreadsRGB = kFilmTile * kFilmTile;
+__global__ void __launch_bounds__(kFilmThreadsRGB) k_film_tiles(uint32_t W, uint32_t H, const float2* pf,
+                                                                 const float4* Lb, float4* acc) {
+  __shared__ float4 s_L[kFilmHalo * kFilmHalo];
+  __shared__ float s_mx[kFilmHalo * kFilmHalo][5], s_my[kFilmHalo * kFilmHalo][5];
+  __shared__ uint32_t s_mask[kFilmHalo * kFilmHalo];  // bits 0-4: columns sx-2..sx+2; 5-9: rows; 10: black
+  const int bx0 = (int)blockIdx.x * kFilmTile, by0 = (int)blockIdx.y * kFilmTile;
+  for (int h = (int)threadIdx.x; h < kFilmHalo * kFilmHalo; h += kFilmThreadsRGB) {
+    const int sx = bx0 - 2 + h % kFilmHalo, sy = by0 - 2 + h / kFilmHalo;
+    uint32_t m = 0;
+    if (sx >= 0 && sy >= 0 && sx < (int)W && sy < (int)H) {
+      const int tx0 = (sx / 32) * 32, ty0 = (sy / 32) * 32;
+      const int tx1 = min(tx0 + 31, (int)W - 1), ty1 = min(ty0 + 31, (int)H - 1);
+      const size_t sp = (size_t)sy * W + sx;
+      const float2 f = pf[sp];
+      const float dx0 = f.x - 0.5f, dy0 = f.y - 0.5f;
+      int pminx = (int)ceilf(dx0 - 2.0f), pmaxx = (int)floorf(dx0 + 2.0f);
+      int pminy = (int)ceilf(dy0 - 2.0f), pmaxy = (int)floorf(dy0 + 2.0f);
+      pminx = max(pminx, tx0);
+      pminy = max(pminy, ty0);
+      pmaxx = min(pmaxx, tx1);
+      pmaxy = min(pmaxy, ty1);
+#pragma unroll
+      for (int d = 0; d < 5; ++d) {
+        const int x = sx - 2 + d, y = sy - 2 + d;
+        if (x >= pminx && x <= pmaxx) {
+          m |= 1u << d;
+          s_mx[h][d] = mitchell1(((float)x - f.x) / 2.0f);
+        }
+        if (y >= pminy && y <= pmaxy) {
+          m |= 1u << (5 + d);
+          s_my[h][d] = mitchell1(((float)y - f.y) / 2.0f);
+        }
+      }
+      const float4 c = Lb[sp];
+      s_L[h] = c;
+      if (rblack(RGB3{c.x, c.y, c.z})) m |= 1u << 10;
+    }
+    s_mask[h] = m;
+  }
+  __syncthreads();
+  const int lx = (int)threadIdx.x % kFilmTile, ly = (int)threadIdx.x / kFilmTile;
+  const uint32_t x = (uint32_t)(bx0 + lx), y = (uint32_t)(by0 + ly);
+  if (x >= W || y >= H) return;
   float4 a = acc[(size_t)y * W + x];
   RGB3 L{a.x, a.y, a.z};
   float ws = a.w;
-  int sy0 = max((int)ty0, (int)y - 2), sy1 = min((int)ty1, (int)y + 2);
-  int sx0 = max((int)tx0, (int)x - 2), sx1 = min((int)tx1, (int)x + 2);
-  for (int sy = sy0; sy <= sy1; ++sy)
-    for (int sx = sx0; sx <= sx1; ++sx) {
-      size_t sp = (size_t)sy * W + sx;
-      float2 f = pf[sp];
-      float dx0 = f.x - 0.5f, dy0 = f.y - 0.5f;
-      int pminx = (int)ceilf(dx0 - 2.0f), pmaxx = (int)floorf(dx0 + 2.0f);
-      int pminy = (int)ceilf(dy0 - 2.0f), pmaxy = (int)floorf(dy0 + 2.0f);
-      pminx = max(pminx, (int)tx0);
-      pminy = max(pminy, (int)ty0);
-      pmaxx = min(pmaxx, (int)tx1);
-      pmaxy = min(pmaxy, (int)ty1);
-      if ((int)x < pminx || (int)x > pmaxx || (int)y < pminy || (int)y > pmaxy) continue;
-      float w = mitchell1(((float)x - f.x) / 2.0f) * mitchell1(((float)y - f.y) / 2.0f);
-      float4 s = Lb[sp];
-      RGB3 c{s.x, s.y, s.z};
-      if (!rblack(c)) L = radd(L, rmuls(c, w));
+  // the neighbours sy = y-2..y+2 (outer), sx = x-2..x+2 (inner); this pixel
+  // is column 4 - dx and row 4 - dy of a neighbour's reach
+  for (int dy = 0; dy < 5; ++dy)
+    for (int dx = 0; dx < 5; ++dx) {
+      const int h = (ly + dy) * kFilmHalo + (lx + dx);
+      const uint32_t m = s_mask[h];
+      if (!((m >> (4 - dx)) & 1u) || !((m >> (9 - dy)) & 1u)) continue;
+      const float w = s_mx[h][4 - dx] * s_my[h][4 - dy];
+      if (!(m & (1u << 10))) {
+        const float4 c = s_L[h];
+        L = radd(L, rmuls(RGB3{c.x, c.y, c.z}, w));
+      }
       ws = ws + w;
     }
   acc[(size_t)y * W + x] = make_float4(L.r, L.g, L.b, ws);

@@ -241,11 +241,6 @@ __global__ void kj_film_pack(PassCtx P, Staged G, float2* pf, float4* Lb) {
   Lb[pix] = make_float4(L.r, L.g, L.b, 0.0f);
 }
 
-__global__ void k_film(uint32_t W, uint32_t H, const float2* pf, const float4* Lb, float4* acc) {
-  uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= W * H) return;
-  film_gather(W, H, pix % W, pix / W, pf, Lb, acc);
-}
 
 // ============================== fused pass ==================================
 // Compact per-pixel state written by k_spawn and read by k_finish.
@@ -568,7 +563,8 @@ wpbr_status render_pass_launch(wpbr_ctx* ctx) {
     WPBR_CUDA(spectral_finish_launch(ctx, order));
   } else {
     k_finish<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pstate.p, R.shadow_hit.p, R.Lbuf.p, order);
-    k_film<<<div_up(n, kTB), kTB, 0, st>>>(R.W, R.H, R.pfilm.p, R.Lbuf.p, (float4*)R.acc.p);
+    k_film_tiles<<<dim3(div_up(R.W, kFilmTile), div_up(R.H, kFilmTile)), kFilmThreadsRGB, 0, st>>>(
+        R.W, R.H, R.pfilm.p, R.Lbuf.p, (float4*)R.acc.p);
   }
   WPBR_CUDA(cudaGetLastError());
   return WPBR_OK;
@@ -668,7 +664,8 @@ wpbr_status job_run(wpbr_ctx* ctx, uint32_t job, uint32_t pass) {
     case WPBR_JOB_INTEGRATE_BSDF: kj_integrate_bsdf<<<g, kTB, 0, st>>>(P, G); break;
     case WPBR_JOB_FILM_ACCUMULATE:
       kj_film_pack<<<g, kTB, 0, st>>>(P, G, R.pfilm.p, R.Lbuf.p);
-      k_film<<<g, kTB, 0, st>>>(R.W, R.H, R.pfilm.p, R.Lbuf.p, (float4*)R.acc.p);
+      k_film_tiles<<<dim3(div_up(R.W, kFilmTile), div_up(R.H, kFilmTile)), kFilmThreadsRGB, 0, st>>>(
+          R.W, R.H, R.pfilm.p, R.Lbuf.p, (float4*)R.acc.p);
       break;
   }
   WPBR_CUDA(cudaGetLastError());

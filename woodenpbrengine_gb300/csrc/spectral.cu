@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(128, 12) k_sfinish(PassCtx P, SpecCtx C, const
   st_bins(C.L + (size_t)pix * kSpecN + b0, L);
 }
 
-// Tile-clipped Mitchell gather of film_gather, 64 bins per sample. A block
+// Tile-clipped Mitchell gather of k_film_tiles, 64 bins per sample. A block
 // handles an 8x8 pixel tile (inside one 32x32 film tile): it stages the
 // 12x12 halo of sample spectra (those inside the film tile's clipped window)
 // in shared memory with asynchronous copies, computes the 64 x 25 neighbour
