@@ -63,7 +63,7 @@ __device__ __forceinline__ bool finite3(RGB3 c) { return isfinite(c.r) && isfini
 
 // ---- sample generation with the sampling parameters --------------------------
 __global__ void __launch_bounds__(kTB, WPBR_ADJ_SPAWN_MIN_BLOCKS) k_adj_spawn(PassCtx P, AdjView A, const uint32_t* pass_dev,
-                                                   const uint32_t* hit_prim, float4* state, float4* rays, float2* pf) {
+                                                   const uint32_t* hit_prim, float4* state, ShadowQueue sq, float2* pf) {
   uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= P.W * P.H) return;
   uint32_t pass = *pass_dev;
@@ -73,12 +73,9 @@ __global__ void __launch_bounds__(kTB, WPBR_ADJ_SPAWN_MIN_BLOCKS) k_adj_spawn(Pa
   RayD r = camera_ray(P.S.cam, fx, fy);
   uint32_t prim = hit_prim[pix];
   float4* st = state + (size_t)pix * kAdjF4;
-  float4* ry = rays + (size_t)pix * 4;
-  const float4 off = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
   if (prim == kNoHit || P.S.nlights == 0) {
     st[0] = make_float4(r.d.x, r.d.y, r.d.z, __uint_as_float(prim == kNoHit ? 0u : AF_HIT));
     st[1] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0xFFFFFFFFu));  // no light: nothing to shade
-    ry[0] = off; ry[1] = off; ry[2] = off; ry[3] = off;
     return;
   }
   uint32_t flags = AF_HIT;
@@ -102,30 +99,17 @@ __global__ void __launch_bounds__(kTB, WPBR_ADJ_SPAWN_MIN_BLOCKS) k_adj_spawn(Pa
   } else {
     env_li_sample(A.env_s, P.S.quirks, u0, u1, &wi, &li, &lpdf, &ok, uvs);
   }
-  if (ok && !rblack(li)) {
-    flags |= AF_TRACE_L;
-    V3 o = add(s.p, mul(wi, (float)0.1));
-    ry[0] = make_float4(o.x, o.y, o.z, 0.0f);
-    ry[1] = make_float4(wi.x, wi.y, wi.z, inf_());
-  } else {
-    ry[0] = off;
-    ry[1] = off;
-  }
+  const bool trace_l = ok && !rblack(li);
+  if (trace_l) flags |= AF_TRACE_L;
+  sq.push(trace_l, 2 * pix, add(s.p, mul(wi, (float)0.1)), wi);
   wpbr_rng::sample2d(P.rs, pix, pass, wpbr_rng::DIM_BSDF, &u0, &u1);
   V3 bwi_l;
   float bpdf;
   bool valid;
   bsdf_sample(ms, wo_l, u0, u1, &bwi_l, &bpdf, &valid);
   V3 bwi = to_world(fr, bwi_l);
-  if (valid) {
-    flags |= AF_TRACE_B;
-    V3 o = add(s.p, mul(bwi, (float)0.01));
-    ry[2] = make_float4(o.x, o.y, o.z, 0.0f);
-    ry[3] = make_float4(bwi.x, bwi.y, bwi.z, inf_());
-  } else {
-    ry[2] = off;
-    ry[3] = off;
-  }
+  if (valid) flags |= AF_TRACE_B;
+  sq.push(valid, 2 * pix + 1, add(s.p, mul(bwi, (float)0.01)), bwi);
   V3 wi_l = to_local(fr, wi);
   st[0] = make_float4(wo_l.x, wo_l.y, wo_l.z, __uint_as_float(flags));
   st[1] = make_float4(wi_l.x, wi_l.y, wi_l.z, __uint_as_float(li_idx));
@@ -574,11 +558,13 @@ wpbr_status replay_pass(wpbr_ctx* ctx, const PassCtx& P, const AdjView& A, uint3
   cudaStream_t st = ctx->stream;
   uint32_t n = J.W * J.H;
   WPBR_CUDA(cudaMemcpyAsync(J.pass_dev.p, &pass, 4, cudaMemcpyHostToDevice, st));
-  WPBR_CUDA(cudaMemsetAsync(J.counters.p, 0, 2 * sizeof(uint32_t), st));
+  WPBR_CUDA(cudaMemsetAsync(J.counters.p, 0, 3 * sizeof(uint32_t), st));
   launch_traversal<false>(P.S, P.Bv, CameraSrc{P, J.pass_dev.p}, PrimSink{J.hit_prim.p}, n, J.counters.p, P.err, st);
-  k_adj_spawn<<<div_up(n, kTB), kTB, 0, st>>>(P, A, J.pass_dev.p, J.hit_prim.p, J.state.p, J.rays.p, J.pf.p);
-  launch_traversal<false>(P.S, P.Bv, BufferSrc{J.rays.p}, PrimSink{J.shadow_hit.p}, 2 * n, J.counters.p + 1, P.err,
-                          st);
+  // shadow rays: the spawn queues the ones it traces (counter word 2), the traversal walks the queue
+  const ShadowQueue sq{J.rays.p, J.shadow_map.p, J.counters.p + 2};
+  k_adj_spawn<<<div_up(n, kTB), kTB, 0, st>>>(P, A, J.pass_dev.p, J.hit_prim.p, J.state.p, sq, J.pf.p);
+  launch_traversal<false>(P.S, P.Bv, QueueSrc{sq.rays, sq.count}, MapSink{J.shadow_hit.p, sq.map}, 2 * n,
+                          J.counters.p + 1, P.err, st);
   WPBR_CUDA(cudaGetLastError());
   return WPBR_OK;
 }
@@ -648,8 +634,9 @@ wpbr_status adjoint_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t s
   WPBR_CUDA(J.image.ensure(n * 3));
   WPBR_CUDA(J.hit_prim.ensure(n));
   WPBR_CUDA(J.shadow_hit.ensure(2 * n));
+  WPBR_CUDA(J.shadow_map.ensure(2 * n));
   WPBR_CUDA(J.pass_dev.ensure(1));
-  WPBR_CUDA(J.counters.ensure(2));
+  WPBR_CUDA(J.counters.ensure(3));
   WPBR_CUDA(cudaStreamSynchronize(st));
   J.ready = true;
   J.param_gen += 1;

@@ -219,7 +219,8 @@ WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
   bvh_release(ctx, false);
   if (ctx->bvh.h_info) cudaFreeHost(ctx->bvh.h_info);
   RenderState& R = ctx->rs;
-  R.acc.release(); R.hit_prim.release(); R.shadow_rays.release(); R.shadow_hit.release(); R.pstate.release();
+  R.acc.release(); R.hit_prim.release(); R.shadow_rays.release(); R.shadow_hit.release(); R.shadow_map.release();
+  R.pstate.release();
   R.Lbuf.release(); R.pfilm.release(); R.pass_dev.release(); R.counters.release();
   R.spec_mats.release(); R.spec_le.release(); R.spec_L.release(); R.spec_acc.release();
   ctx->io_rays.release(); ctx->io_hits.release(); ctx->io_stats.release();

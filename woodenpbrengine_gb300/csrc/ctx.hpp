@@ -92,6 +92,10 @@ struct BvhState {
   BvhView view{};
 };
 
+// Words of RenderState::counters (zeroed at the start of every pass).
+constexpr uint32_t kQueueCounter = 24;
+constexpr uint32_t kPassCounters = 25;
+
 struct RenderState {
   bool ready = false;
   uint32_t spp = 0, seed = 0, stream = 0;
@@ -99,7 +103,8 @@ struct RenderState {
   DevBuf<float> acc;  // W*H*4 (L rgb, weight)
   // fused-path per-pixel state
   DevBuf<uint32_t> hit_prim;
-  DevBuf<float4> shadow_rays;   // 2 rays (2 float4 each) per pixel
+  DevBuf<float4> shadow_rays;   // the pass's queued shadow rays (2 float4 each), at most 2 per pixel
+  DevBuf<uint32_t> shadow_map;  // result slot (2 * pixel + branch) of each queued shadow ray
   DevBuf<uint32_t> shadow_hit;  // 2 per pixel
   DevBuf<float4> pstate;        // compact shading state, kStateF4 per pixel
   DevBuf<float4> Lbuf;          // per pixel L (xyz) + pFilm packed in w? separate:
@@ -111,8 +116,9 @@ struct RenderState {
   cudaGraphExec_t graph = nullptr;
   uint64_t graph_key = 0;
   DevBuf<uint32_t> pass_dev;  // pass index read by the captured kernels
-  DevBuf<uint32_t> counters;  // ray-fetch counters of the pass's traversal launches, then the
-                              // per-category pixel counts and cursors of the material-sorted order
+  DevBuf<uint32_t> counters;  // kPassCounters words: ray-fetch counters of the pass's two traversal
+                              // launches, the per-category pixel counts and cursors of the
+                              // material-sorted order, and (kQueueCounter) the queued shadow rays
   DevBuf<uint32_t> order;     // the pass's pixels grouped by material category (k_cat_scatter)
   // Sampled64 mode: material / light spectra, per-pixel sample spectra, film spectra
   DevBuf<float> spec_mats, spec_le, spec_L, spec_acc;
@@ -138,14 +144,15 @@ struct AdjState {
   DevBuf<double> g_mat, g_scalar;
   DevBuf<float4> state, rays, Lb, acc, gpix;
   DevBuf<float2> pf;
-  DevBuf<uint32_t> hit_prim, shadow_hit, pass_dev, counters;
+  DevBuf<uint32_t> hit_prim, shadow_hit, shadow_map, pass_dev, counters;  // counters: 2 ray fetches, queued shadow rays
   void release() {
     mats_s.release(); mats_e.release(); rgb_s.release(); rgb_e.release();
     s_func.release(); s_cdf.release(); s_int.release(); s_mfunc.release(); s_mcdf.release(); s_mint.release();
     e_func.release(); e_cdf.release(); e_int.release(); e_mfunc.release(); e_mcdf.release(); e_mint.release();
     mat_prm.release(); env_prm.release(); target.release(); image.release(); g_env.release(); g_func.release();
     g_mat.release(); g_scalar.release(); state.release(); rays.release(); Lb.release(); acc.release();
-    gpix.release(); pf.release(); hit_prim.release(); shadow_hit.release(); pass_dev.release(); counters.release();
+    gpix.release(); pf.release(); hit_prim.release(); shadow_hit.release(); shadow_map.release(); pass_dev.release();
+    counters.release();
     ready = false;
   }
 };

@@ -335,10 +335,38 @@ __global__ void __launch_bounds__(kFilmThreadsRGB) k_film_tiles(uint32_t W, uint
   acc[(size_t)y * W + x] = make_float4(L.r, L.g, L.b, ws);
 }
 
+// Shadow rays of a pass, queued densely: a kernel that decides per pixel
+// whether to trace a ray pushes only the rays it traces (one atomic per warp
+// and call) with the slot of their result (2 * pixel + branch), and the
+// traversal walks just the queue, so its warps do not refill lanes with
+// empty slots. All lanes that reach a push call it, each with its own
+// `want`.
+struct ShadowQueue {
+  float4* rays;     // 2 float4 per queued ray
+  uint32_t* map;    // result slot of each queued ray
+  uint32_t* count;  // rays queued in this pass (zeroed before the pass)
+  __device__ __forceinline__ void push(bool want, uint32_t slot, V3 o, V3 d) const {
+    const uint32_t act = __activemask();
+    const uint32_t m = __ballot_sync(act, want);
+    if (!m) return;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t leader = __ffs(m) - 1u;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(act, base, leader);
+    if (!want) return;
+    const uint32_t q = base + __popc(m & ((1u << lane) - 1u));
+    rays[2 * (size_t)q] = make_float4(o.x, o.y, o.z, 0.0f);
+    rays[2 * (size_t)q + 1] = make_float4(d.x, d.y, d.z, inf_());
+    map[q] = slot;
+  }
+};
+
 // Camera rays generated inside the persistent traversal's ray source.
 struct CameraSrc {
   PassCtx P;
   const uint32_t* pass_dev;
+  __device__ __forceinline__ uint32_t limit(uint32_t n) const { return n; }
   __device__ __forceinline__ void load(uint32_t pix, float4* o, float4* d) const {
     float fx, fy;
     camera_sample(P, pix, *pass_dev, &fx, &fy);

@@ -249,7 +249,7 @@ enum : uint32_t { SF_VALID = 1u, SF_TRACE_L = 2u, SF_TRACE_B = 4u, SF_HIT = 8u, 
 
 template <bool TEX>
 __global__ void __launch_bounds__(kTB, TEX ? WPBR_SPAWN_TEX_MIN_BLOCKS : WPBR_SPAWN_MIN_BLOCKS) k_spawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
-                                               float4* state, float4* rays, float4* Lb, float2* pf,
+                                               float4* state, ShadowQueue sq, float4* Lb, float2* pf,
                                                const uint32_t* order) {
   uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= P.W * P.H) return;
@@ -262,13 +262,10 @@ __global__ void __launch_bounds__(kTB, TEX ? WPBR_SPAWN_TEX_MIN_BLOCKS : WPBR_SP
   RayD r = camera_ray(P.S.cam, fx, fy);
   uint32_t prim = hit_prim[pix];
   float4* st = state + (size_t)pix * kStateF4;
-  float4* ry = rays + (size_t)pix * 4;
-  const float4 off = make_float4(0.0f, 0.0f, 0.0f, -1.0f);  // tmax < 0: nothing to trace
   RGB3 L = rgb1(0.0f);
   uint32_t flags = 0;
   if (prim == kNoHit || P.S.nlights == 0) {
     if (prim == kNoHit && P.S.has_env) L = radd(L, env_le(P.S.env, r.d));
-    ry[0] = off; ry[1] = off; ry[2] = off; ry[3] = off;
     st[4] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(flags));
     Lb[pix] = make_float4(L.r, L.g, L.b, 0.0f);
     return;
@@ -286,15 +283,9 @@ __global__ void __launch_bounds__(kTB, TEX ? WPBR_SPAWN_TEX_MIN_BLOCKS : WPBR_SP
   uint32_t li_idx = pick_light(P, pix, pass);
   const wpbr_light& lt = P.S.lights[li_idx];
   LightSample ls = sample_light(P, lt, s.p, pix, pass);
-  if (ls.ok && !rblack(ls.li)) {
-    flags |= SF_TRACE_L;
-    V3 o = add(s.p, mul(ls.wi, (float)0.1));
-    ry[0] = make_float4(o.x, o.y, o.z, 0.0f);
-    ry[1] = make_float4(ls.wi.x, ls.wi.y, ls.wi.z, inf_());
-  } else {
-    ry[0] = off;
-    ry[1] = off;
-  }
+  const bool trace_l = ls.ok && !rblack(ls.li);
+  if (trace_l) flags |= SF_TRACE_L;
+  sq.push(trace_l, 2 * pix, add(s.p, mul(ls.wi, (float)0.1)), ls.wi);
   float u0, u1;
   wpbr_rng::sample2d(P.rs, pix, pass, wpbr_rng::DIM_BSDF, &u0, &u1);
   V3 bwi_l;
@@ -302,15 +293,8 @@ __global__ void __launch_bounds__(kTB, TEX ? WPBR_SPAWN_TEX_MIN_BLOCKS : WPBR_SP
   bool valid;
   RGB3 bf = bsdf_sample(m, wo_l, u0, u1, &bwi_l, &bpdf, &valid);
   V3 bwi = to_world(fr, bwi_l);
-  if (valid) {
-    flags |= SF_VALID | SF_TRACE_B;
-    V3 o = add(s.p, mul(bwi, (float)0.01));
-    ry[2] = make_float4(o.x, o.y, o.z, 0.0f);
-    ry[3] = make_float4(bwi.x, bwi.y, bwi.z, inf_());
-  } else {
-    ry[2] = off;
-    ry[3] = off;
-  }
+  if (valid) flags |= SF_VALID | SF_TRACE_B;
+  sq.push(valid, 2 * pix + 1, add(s.p, mul(bwi, (float)0.01)), bwi);
   V3 wi_l = to_local(fr, ls.wi);
   st[0] = make_float4(ls.li.r, ls.li.g, ls.li.b, ls.pdf);
   st[1] = make_float4(wi_l.x, wi_l.y, wi_l.z, __uint_as_float(li_idx));
@@ -485,6 +469,8 @@ wpbr_status env_preprocess(wpbr_ctx* ctx) {
   return env_distribution_build(ctx, ctx->env_rgb.p, d, &ctx->env_marg_int);
 }
 
+static_assert(kQueueCounter == 2 + 2 * kPixCats, "pass counters: fetches, categories, then the queue");
+
 wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t stream) {
   if (!ctx->has_scene) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render_setup: no scene");
   if (!ctx->bvh.built) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render_setup: BVH not built");
@@ -502,12 +488,13 @@ wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t st
   WPBR_CUDA(R.acc.ensure(n * 4));
   WPBR_CUDA(R.hit_prim.ensure(n));
   WPBR_CUDA(R.shadow_rays.ensure(n * 4));
+  WPBR_CUDA(R.shadow_map.ensure(n * 2));
   WPBR_CUDA(R.shadow_hit.ensure(n * 2));
   WPBR_CUDA(R.pstate.ensure(n * kStateF4));
   WPBR_CUDA(R.Lbuf.ensure(n));
   WPBR_CUDA(R.pfilm.ensure(n));
   WPBR_CUDA(R.pass_dev.ensure(1));
-  WPBR_CUDA(R.counters.ensure(2 + 2 * kPixCats));  // allocated before any graph capture
+  WPBR_CUDA(R.counters.ensure(kPassCounters));  // allocated before any graph capture
   WPBR_CUDA(R.order.ensure(n));
   WPBR_CUDA(cudaMemsetAsync(R.acc.p, 0, n * 4 * sizeof(float), ctx->stream));
   if (ctx->spectrum == WPBR_SPECTRUM_SAMPLED64) {
@@ -529,9 +516,11 @@ wpbr_status render_pass_launch(wpbr_ctx* ctx) {
   uint32_t n = R.W * R.H;
   cudaStream_t st = ctx->stream;
   const uint32_t* pass_ptr = R.pass_ptr ? R.pass_ptr : R.pass_dev.p;
-  WPBR_CUDA(R.counters.ensure(2 + 2 * kPixCats));
+  WPBR_CUDA(R.counters.ensure(kPassCounters));
+  WPBR_CUDA(R.shadow_map.ensure((size_t)2 * n));
   WPBR_CUDA(R.order.ensure(n));
-  WPBR_CUDA(cudaMemsetAsync(R.counters.p, 0, (2 + 2 * kPixCats) * sizeof(uint32_t), st));
+  WPBR_CUDA(cudaMemsetAsync(R.counters.p, 0, kPassCounters * sizeof(uint32_t), st));
+  const ShadowQueue sq{R.shadow_rays.p, R.shadow_map.p, R.counters.p + kQueueCounter};
   bool spectral = ctx->spectrum == WPBR_SPECTRUM_SAMPLED64;
   launch_traversal<false>(P.S, P.Bv, CameraSrc{P, pass_ptr}, PrimSink{R.hit_prim.p}, n, R.counters.p, P.err, st,
                           R.trace_grid);
@@ -548,17 +537,18 @@ wpbr_status render_pass_launch(wpbr_ctx* ctx) {
     WPBR_CUDA(spectral_spawn_launch(ctx, pass_ptr, order));
   else
     (ctx->has_metal ? k_spawn<true> : k_spawn<false>)<<<div_up(n, kTB), kTB, 0, st>>>(
-        P, pass_ptr, R.hit_prim.p, R.pstate.p, R.shadow_rays.p, R.Lbuf.p, R.pfilm.p, order);
+        P, pass_ptr, R.hit_prim.p, R.pstate.p, sq, R.Lbuf.p, R.pfilm.p, order);
   // shadow rays: unoccluded iff no hit or the closest hit is the sampled
   // light's primitive; with environment lights only that is "no hit", which
   // the any-hit traversal decides with the same primitive tests, stopping at
   // the first hit (the stored id is then some hit, never a light's)
+  // (the spawn queued only the rays it traces; the traversal walks the queue)
+  const QueueSrc qsrc{sq.rays, sq.count};
+  const MapSink qsink{R.shadow_hit.p, sq.map};
   if (ctx->env_lights_only)
-    launch_traversal<true>(P.S, P.Bv, BufferSrc{R.shadow_rays.p}, PrimSink{R.shadow_hit.p}, 2 * n,
-                           R.counters.p + 1, P.err, st, R.trace_grid);
+    launch_traversal<true>(P.S, P.Bv, qsrc, qsink, 2 * n, R.counters.p + 1, P.err, st, R.trace_grid);
   else
-    launch_traversal<false>(P.S, P.Bv, BufferSrc{R.shadow_rays.p}, PrimSink{R.shadow_hit.p}, 2 * n,
-                            R.counters.p + 1, P.err, st, R.trace_grid);
+    launch_traversal<false>(P.S, P.Bv, qsrc, qsink, 2 * n, R.counters.p + 1, P.err, st, R.trace_grid);
   if (spectral) {
     WPBR_CUDA(spectral_finish_launch(ctx, order));
   } else {
@@ -593,7 +583,7 @@ static uint64_t pass_graph_key(const wpbr_ctx* ctx) {
   mix(((uint64_t)R.W << 32) | R.H);
   mix((uint64_t)R.trace_grid);
   mix((uint64_t)ctx->spectrum | ((uint64_t)ctx->quirks << 8));
-  const void* ptrs[] = {R.acc.p,    R.hit_prim.p, R.shadow_rays.p,     R.shadow_hit.p,      R.pstate.p,
+  const void* ptrs[] = {R.acc.p,    R.hit_prim.p, R.shadow_rays.p,     R.shadow_hit.p,      R.shadow_map.p, R.pstate.p,
                         R.Lbuf.p,   R.pfilm.p,    R.pass_dev.p,        R.counters.p,        R.pass_ptr, R.order.p,
                         ctx->d_err.p, ctx->bvh.view.nodes,
                         ctx->bvh.view.prims, R.spec_mats.p, R.spec_le.p, R.spec_L.p, R.spec_acc.p};

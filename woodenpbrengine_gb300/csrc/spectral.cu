@@ -136,7 +136,7 @@ __device__ __forceinline__ FScalars f_scalars(const wpbr_material& m, float d_wh
 
 template <bool TEX>
 __global__ void __launch_bounds__(kTB, TEX ? WPBR_SPAWN_TEX_MIN_BLOCKS : WPBR_SPAWN_MIN_BLOCKS) k_sspawn(PassCtx P, const uint32_t* pass_dev, const uint32_t* hit_prim,
-                                                float4* state, float4* rays, float2* pf, const uint32_t* order) {
+                                                float4* state, ShadowQueue sq, float2* pf, const uint32_t* order) {
   uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= P.W * P.H) return;
   uint32_t pix = order ? order[slot] : slot;  // material-sorted (large films)
@@ -148,9 +148,6 @@ __global__ void __launch_bounds__(kTB, TEX ? WPBR_SPAWN_TEX_MIN_BLOCKS : WPBR_SP
   RayD r = camera_ray(P.S.cam, fx, fy);
   uint32_t prim = hit_prim[pix];
   float4* st = state + (size_t)pix * kSpecStateF4;
-  float4* ry = rays + (size_t)pix * 4;
-  const float4 off = make_float4(0.0f, 0.0f, 0.0f, -1.0f);  // tmax < 0: nothing to trace
-  ry[0] = off; ry[1] = off; ry[2] = off; ry[3] = off;
   uint32_t nl = P.S.nlights;
   if (prim == kNoHit || nl == 0) {
     uint32_t flags = 0, env_light = 0;
@@ -213,9 +210,7 @@ __global__ void __launch_bounds__(kTB, TEX ? WPBR_SPAWN_TEX_MIN_BLOCKS : WPBR_SP
       float w = power_heuristic(lpdf, bpdf);
       s0.w = w / lpdf;
       s1 = make_float4(F.c, F.kf, F.fcos, 0.0f);
-      V3 o = add(si.p, mul(wi, (float)0.1));
-      ry[0] = make_float4(o.x, o.y, o.z, 0.0f);
-      ry[1] = make_float4(wi.x, wi.y, wi.z, inf_());
+      sq.push(true, 2 * pix, add(si.p, mul(wi, (float)0.1)), wi);
     }
   }
   // ---- BSDF-sampling branch
@@ -268,9 +263,7 @@ __global__ void __launch_bounds__(kTB, TEX ? WPBR_SPAWN_TEX_MIN_BLOCKS : WPBR_SP
       float w = (bpdf == 1.0f) ? 1.0f : power_heuristic(bpdf, blpdf);
       s1.w = w / bpdf;
       s2 = make_float4(F.c, F.kf, F.fcos, 0.0f);
-      V3 o = add(si.p, mul(wi_w, (float)0.01));
-      ry[2] = make_float4(o.x, o.y, o.z, 0.0f);
-      ry[3] = make_float4(wi_w.x, wi_w.y, wi_w.z, inf_());
+      sq.push(true, 2 * pix + 1, add(si.p, mul(wi_w, (float)0.01)), wi_w);
     }
   }
   s0.x = __uint_as_float(flags);
@@ -624,8 +617,9 @@ static PassCtx spec_pass_ctx(wpbr_ctx* ctx) {
 cudaError_t spectral_spawn_launch(wpbr_ctx* ctx, const uint32_t* pass_ptr, const uint32_t* order) {
   RenderState& R = ctx->rs;
   uint32_t n = R.W * R.H;
-  (ctx->has_metal ? k_sspawn<true> : k_sspawn<false>)<<<div_up(n, kTB), kTB, 0, ctx->stream>>>(spec_pass_ctx(ctx), pass_ptr, R.hit_prim.p, R.pstate.p,
-                                                     R.shadow_rays.p, R.pfilm.p, order);
+  const ShadowQueue sq{R.shadow_rays.p, R.shadow_map.p, R.counters.p + kQueueCounter};
+  (ctx->has_metal ? k_sspawn<true> : k_sspawn<false>)<<<div_up(n, kTB), kTB, 0, ctx->stream>>>(
+      spec_pass_ctx(ctx), pass_ptr, R.hit_prim.p, R.pstate.p, sq, R.pfilm.p, order);
   return cudaGetLastError();
 }
 

@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
   bool active = false;
   bool exhausted = false;
   uint32_t guard = 0;
+  n = src.limit(n);  // a queue source reads its length from device memory
 
   while (true) {
     // ---- refill idle lanes ------------------------------------------------
@@ -407,6 +408,21 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
 // ---- ray sources and hit sinks -------------------------------------------------
 struct BufferSrc {
   const float4* rays;  // 2 float4 per ray: (o, unused), (d, tmax)
+  __device__ __forceinline__ uint32_t limit(uint32_t n) const { return n; }
+  __device__ __forceinline__ void load(uint32_t i, float4* o, float4* d) const {
+    *o = __ldg(&rays[2 * (size_t)i]);
+    *d = __ldg(&rays[2 * (size_t)i + 1]);
+  }
+};
+// The rays a kernel queued (ShadowQueue): as many as *count says, at most
+// the launch's n.
+struct QueueSrc {
+  const float4* rays;
+  const uint32_t* count;
+  __device__ __forceinline__ uint32_t limit(uint32_t n) const {
+    const uint32_t c = *count;
+    return c < n ? c : n;
+  }
   __device__ __forceinline__ void load(uint32_t i, float4* o, float4* d) const {
     *o = __ldg(&rays[2 * (size_t)i]);
     *d = __ldg(&rays[2 * (size_t)i + 1]);
@@ -428,6 +444,7 @@ struct HitSink4 {
 struct PermSrc {
   const float4* rays;
   const uint32_t* perm;
+  __device__ __forceinline__ uint32_t limit(uint32_t n) const { return n; }
   __device__ __forceinline__ void load(uint32_t i, float4* o, float4* d) const {
     size_t j = __ldg(&perm[i]);
     *o = __ldg(&rays[2 * j]);
@@ -449,6 +466,15 @@ struct PrimSink {
   uint32_t* prims;
   __device__ __forceinline__ void store(uint32_t i, const HitRec& h) const { prims[i] = h.prim; }
 };
+// Hit primitive of queued ray i at the result slot the queue recorded for it.
+struct MapSink {
+  static constexpr int kMinBlocks = 8;
+  static constexpr bool kCollide = false;
+  uint32_t* prims;
+  const uint32_t* map;
+  __device__ __forceinline__ void store(uint32_t i, const HitRec& h) const { prims[__ldg(&map[i])] = h.prim; }
+};
+
 
 // Launches the traversal whose stack fits the tree: a lane's stack never
 // holds more entries than the tree is deep, so trees shallower than 60
