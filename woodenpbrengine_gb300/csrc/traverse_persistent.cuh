@@ -460,6 +460,10 @@ struct PermHitSink4 {
     hits[__ldg(&perm[i])] = make_float4(h.t, __uint_as_float(h.prim), h.b1, h.b2);
   }
 };
+// The render passes' camera (PrimSink) and shadow-queue (MapSink) traversals
+// at 8 resident blocks per SM. 1080p full frame x 16 spp, camera/shadow
+// blocks: 8/8 1,815 Msamples/s, 8/10 1,786, 8/12 1,772, 10/10 1,739, 12/12
+// 1,688 (textured metal and the 256x256 frame in the same order).
 struct PrimSink {
   static constexpr int kMinBlocks = 8;
   static constexpr bool kCollide = false;
