@@ -260,6 +260,7 @@ __global__ void k_morton(uint32_t N, const float4* cen, const uint32_t* cb_enc, 
 constexpr int kRadixItems = 8;
 constexpr int kRadixTile = kB * kRadixItems;
 
+// Block histograms of one pass (digit-major, block-minor).
 __global__ void k_radix_hist(const uint32_t* keys, uint32_t n, int shift, uint32_t dmask, uint32_t* hist,
                              uint32_t nblocks) {
   __shared__ uint32_t cnt[256];
@@ -274,45 +275,97 @@ __global__ void k_radix_hist(const uint32_t* keys, uint32_t n, int shift, uint32
   hist[threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
 }
 
-__global__ void k_radix_scatter(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout,
-                                uint32_t n, int shift, uint32_t dmask, const uint32_t* offs, uint32_t nblocks) {
-  __shared__ uint32_t s_off[256];
-  __shared__ uint32_t s_wcnt[kB / 32][256];
-  __shared__ uint32_t s_round[256];
-  s_off[threadIdx.x] = offs[threadIdx.x * nblocks + blockIdx.x];
+// Stable scatter of one pass over tiles of kRadixTile keys. Warp w owns the
+// tile's keys [w * 256, (w + 1) * 256) and takes them 32 at a time (lane l,
+// round k: key w * 256 + 32 k + l): a __match_any_sync rank within the round
+// plus the warp's running count of that digit (a warp-private row of counters
+// in shared memory, updated by each digit group's first lane) ranks every key
+// among the warp's keys of its digit. One block-wide pass then turns the
+// warps' counts into offsets, warps in order, so the keys of one digit keep
+// the tile's order, which is the input order. The keys go through a tile
+// sorted by digit in shared memory, so each digit's run leaves the block as
+// consecutive writes.
+__global__ void __launch_bounds__(kB) k_radix_scatter(const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                                                      uint32_t* vout, uint32_t n, int shift, uint32_t dmask,
+                                                      const uint32_t* offs, uint32_t nblocks) {
+  __shared__ uint32_t s_wc[kB / 32][256];  // per warp and digit: keys, then the warp's offset in the block
+  __shared__ uint32_t s_off[256];          // global start of each digit's run of this tile
+  __shared__ uint32_t s_lst[256];          // start of each digit in the sorted tile
+  __shared__ uint32_t s_wsum[kB / 32];
+  __shared__ uint32_t s_key[kRadixTile], s_val[kRadixTile];
   const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
   const uint32_t lt = (1u << lane) - 1u;
-  uint32_t base = blockIdx.x * kRadixTile;
-  for (int r = 0; r < kRadixItems; ++r) {
-    for (int q = 0; q < kB / 32; ++q) s_wcnt[q][threadIdx.x] = 0;
-    __syncthreads();
-    uint32_t i = base + r * kB + threadIdx.x;
-    bool valid = i < n;
-    uint32_t key = valid ? kin[i] : 0u;
-    uint32_t val = valid ? vin[i] : 0u;
-    uint32_t d = valid ? ((key >> shift) & dmask) : (256u + lane);
-    uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
-    uint32_t rank = __popc(peers & lt);
-    if (valid && rank == 0) s_wcnt[w][d] = __popc(peers);
-    __syncthreads();
-    {
-      uint32_t dd = threadIdx.x, acc = 0;
-      for (int q = 0; q < kB / 32; ++q) {
-        uint32_t c = s_wcnt[q][dd];
-        s_wcnt[q][dd] = acc;
-        acc += c;
-      }
-      s_round[dd] = acc;
+#pragma unroll
+  for (int q = 0; q < kB / 32; ++q) s_wc[q][threadIdx.x] = 0;
+  s_off[threadIdx.x] = offs[threadIdx.x * nblocks + blockIdx.x];
+  __syncthreads();
+  const uint32_t base = blockIdx.x * kRadixTile + w * (32 * kRadixItems);
+  uint32_t key[kRadixItems], val[kRadixItems], rk[kRadixItems];
+#pragma unroll
+  for (int k = 0; k < kRadixItems; ++k) {
+    const uint32_t i = base + k * 32 + lane;
+    key[k] = i < n ? kin[i] : 0u;
+    val[k] = i < n ? vin[i] : 0u;
+  }
+  uint32_t* wc = s_wc[w];
+#pragma unroll
+  for (int k = 0; k < kRadixItems; ++k) {
+    const bool valid = base + k * 32 + lane < n;
+    const uint32_t d = valid ? ((key[k] >> shift) & dmask) : (256u + lane);
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+    const uint32_t leader = __ffs(peers) - 1;
+    uint32_t before = 0;
+    if (valid && lane == leader) {
+      before = wc[d];
+      wc[d] = before + __popc(peers);
     }
-    __syncthreads();
-    if (valid) {
-      uint32_t pos = s_off[d] + s_wcnt[w][d] + rank;
-      kout[pos] = key;
-      vout[pos] = val;
+    before = __shfl_sync(0xFFFFFFFFu, before, leader);
+    rk[k] = before + __popc(peers & lt);
+    __syncwarp();
+  }
+  __syncthreads();
+  {  // per digit: the warps' offsets in the block, then the digit's start in the sorted tile
+    const uint32_t d = threadIdx.x;
+    uint32_t acc = 0;
+#pragma unroll
+    for (int q = 0; q < kB / 32; ++q) {
+      const uint32_t c = s_wc[q][d];
+      s_wc[q][d] = acc;
+      acc += c;
     }
+    uint32_t x = acc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+      if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) s_wsum[w] = x;
     __syncthreads();
-    s_off[threadIdx.x] += s_round[threadIdx.x];
-    __syncthreads();
+    uint32_t wb = 0;
+    for (uint32_t q = 0; q < w; ++q) wb += s_wsum[q];
+    s_lst[d] = wb + x - acc;
+  }
+  __syncthreads();
+  // the tile sorted by digit in shared memory, then each digit's run written
+  // to its global position by consecutive threads
+#pragma unroll
+  for (int k = 0; k < kRadixItems; ++k) {
+    if (base + k * 32 + lane < n) {
+      const uint32_t d = (key[k] >> shift) & dmask;
+      const uint32_t lp = s_lst[d] + wc[d] + rk[k];
+      s_key[lp] = key[k];
+      s_val[lp] = val[k];
+    }
+  }
+  __syncthreads();
+  const uint32_t tile0 = blockIdx.x * kRadixTile;
+  const uint32_t tile_n = min((uint32_t)kRadixTile, n - tile0);
+  for (uint32_t t = threadIdx.x; t < tile_n; t += kB) {
+    const uint32_t kt = s_key[t];
+    const uint32_t d = (kt >> shift) & dmask;
+    const uint32_t pos = s_off[d] + (t - s_lst[d]);
+    kout[pos] = kt;
+    vout[pos] = s_val[t];
   }
 }
 
