@@ -259,8 +259,11 @@ __global__ void k_morton(uint32_t N, const float4* cen, const uint32_t* cb_enc, 
 // ---------------------------------------------------------------------------
 constexpr int kRadixItems = 8;
 constexpr int kRadixTile = kB * kRadixItems;
+static_assert(kRadixTile == (int)kSortTile, "the sort's tile size is shared with the key producers");
 
-// Block histograms of one pass (digit-major, block-minor).
+// Block histograms of one pass (digit-major, block-minor). A warp whose 32
+// keys share one digit adds them with one atomic (coherent rays' origins
+// often do), the others key by key.
 __global__ void k_radix_hist(const uint32_t* keys, uint32_t n, int shift, uint32_t dmask, uint32_t* hist,
                              uint32_t nblocks) {
   __shared__ uint32_t cnt[256];
@@ -269,7 +272,13 @@ __global__ void k_radix_hist(const uint32_t* keys, uint32_t n, int shift, uint32
   uint32_t base = blockIdx.x * kRadixTile;
   for (int k = 0; k < kRadixItems; ++k) {
     uint32_t i = base + threadIdx.x + k * kB;
-    if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & dmask], 1u);
+    const bool valid = i < n;
+    const uint32_t d = valid ? (keys[i] >> shift) & dmask : 0xFFFFFFFFu;
+    if (__all_sync(0xFFFFFFFFu, d == __shfl_sync(0xFFFFFFFFu, d, 0) && valid)) {
+      if (lane_id() == 0) atomicAdd(&cnt[d], 32u);
+    } else if (valid) {
+      atomicAdd(&cnt[d], 1u);
+    }
   }
   __syncthreads();
   hist[threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
@@ -1877,7 +1886,7 @@ uint32_t radix_sort_launches(uint32_t n, int bits) {
 // pair that holds the result.
 cudaError_t radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t n, int bits,
                              DevBuf<uint32_t>& hist, DevBuf<uint32_t>& scan_tmp, cudaStream_t st, uint32_t** kres,
-                             uint32_t** vres) {
+                             uint32_t** vres, bool first_hist) {
   uint32_t nblk = div_up(n, kRadixTile);
   cudaError_t e = hist.ensure((size_t)256 * nblk);
   if (e != cudaSuccess) return e;
@@ -1885,7 +1894,7 @@ cudaError_t radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t*
   for (int shift = 0; shift < bits && n > 1; shift += 8) {
     int w = bits - shift < 8 ? bits - shift : 8;
     uint32_t dmask = (1u << w) - 1u;
-    k_radix_hist<<<nblk, kB, 0, st>>>(kin, n, shift, dmask, hist.p, nblk);
+    if (shift > 0 || !first_hist) k_radix_hist<<<nblk, kB, 0, st>>>(kin, n, shift, dmask, hist.p, nblk);
     e = scan_exclusive(hist.p, hist.p, 256 * nblk, scan_tmp, st);
     if (e != cudaSuccess) return e;
     k_radix_scatter<<<nblk, kB, 0, st>>>(kin, vin, kout, vout, n, shift, dmask, hist.p, nblk);

@@ -254,9 +254,14 @@ wpbr_status set_err(wpbr_ctx* ctx, wpbr_status st, const std::string& msg);
 wpbr_status cuda_err(wpbr_ctx* ctx, cudaError_t e, const char* what);
 SceneView scene_view(const wpbr_ctx* ctx);
 wpbr_status bvh_build(wpbr_ctx* ctx);
+// Keys per block of the radix sort's kernels (its histograms are kept per
+// tile of this many keys, digit-major).
+constexpr uint32_t kSortTile = 2048;
+// first_hist: the first pass's tile histograms are already in hist (written
+// by the kernel that produced the keys).
 cudaError_t radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t n, int bits,
                              DevBuf<uint32_t>& hist, DevBuf<uint32_t>& scan_tmp, cudaStream_t st, uint32_t** kres,
-                             uint32_t** vres);
+                             uint32_t** vres, bool first_hist = false);
 // Traces on `stream` (the context's when null) with scratch set `scratch`.
 wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* d_hits, uint32_t mode,
                        uint32_t* d_stats, int scratch = 0, cudaStream_t stream = nullptr);

@@ -39,17 +39,40 @@ __device__ __forceinline__ uint32_t spread10(uint32_t v) {
   v = (v | (v << 2)) & 0x09249249u;
   return v;
 }
-__global__ void k_ray_keys(const float4* rays, uint32_t n, float3 lo, float3 scale, uint32_t cells, uint32_t* keys,
-                           uint32_t* idx) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float4 o = __ldg(&rays[2 * (size_t)i]);
-  float q[3] = {(o.x - lo.x) * scale.x, (o.y - lo.y) * scale.y, (o.z - lo.z) * scale.z};
-  float top = (float)(cells - 1);
-  uint32_t c[3];
-  for (int k = 0; k < 3; ++k) c[k] = q[k] > 0.0f ? (q[k] < top ? (uint32_t)q[k] : cells - 1) : 0u;
-  keys[i] = spread10(c[0]) | (spread10(c[1]) << 1) | (spread10(c[2]) << 2);
-  idx[i] = i;
+// One block per kSortTile rays: the keys, their indices, and the tile's
+// histogram of the sort's first digit (the low 8 bits), in the layout of the
+// sort's own histogram kernel (digit-major, tile-minor), which the sort then
+// skips. A warp whose 32 keys share that digit adds them with one atomic.
+constexpr int kKeyBlock = 256;
+__global__ void __launch_bounds__(kKeyBlock) k_ray_keys(const float4* rays, uint32_t n, float3 lo, float3 scale,
+                                                        uint32_t cells, uint32_t* keys, uint32_t* idx,
+                                                        uint32_t* hist, uint32_t ntiles) {
+  __shared__ uint32_t cnt[256];
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const float top = (float)(cells - 1);
+  const uint32_t base = blockIdx.x * kSortTile;
+  for (uint32_t k = 0; k < kSortTile / kKeyBlock; ++k) {
+    const uint32_t i = base + k * kKeyBlock + threadIdx.x;
+    uint32_t d = 0xFFFFFFFFu;
+    if (i < n) {
+      float4 o = __ldg(&rays[2 * (size_t)i]);
+      float q[3] = {(o.x - lo.x) * scale.x, (o.y - lo.y) * scale.y, (o.z - lo.z) * scale.z};
+      uint32_t c[3];
+      for (int a = 0; a < 3; ++a) c[a] = q[a] > 0.0f ? (q[a] < top ? (uint32_t)q[a] : cells - 1) : 0u;
+      const uint32_t key = spread10(c[0]) | (spread10(c[1]) << 1) | (spread10(c[2]) << 2);
+      keys[i] = key;
+      idx[i] = i;
+      d = key & 0xFFu;
+    }
+    if (__all_sync(0xFFFFFFFFu, d == __shfl_sync(0xFFFFFFFFu, d, 0) && d != 0xFFFFFFFFu)) {
+      if ((threadIdx.x & 31u) == 0) atomicAdd(&cnt[d], 32u);
+    } else if (d != 0xFFFFFFFFu) {
+      atomicAdd(&cnt[d], 1u);
+    }
+  }
+  __syncthreads();
+  hist[threadIdx.x * ntiles + blockIdx.x] = cnt[threadIdx.x];
 }
 
 template <bool ANY, bool STATS>
@@ -72,7 +95,8 @@ uint32_t trace_launches(const wpbr_ctx* ctx, uint64_t n, bool stats) {
   if (n == 0) return 0;
   if (stats) return 1;
   const BvhView Bv = traversal_view(ctx);
-  if (ctx->ray_sort && n >= kRaySortMin && !Bv.empty) return 2 + radix_sort_launches((uint32_t)n, 3 * (int)ctx->ray_sort);
+  // the key kernel also counts the sort's first digit, so the sort skips one histogram launch
+  if (ctx->ray_sort && n >= kRaySortMin && !Bv.empty) return 1 + radix_sort_launches((uint32_t)n, 3 * (int)ctx->ray_sort);
   return 1;
 }
 
@@ -111,11 +135,15 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
           float cells = (float)(1u << b);
           float3 sc = make_float3(ex[0] > 0.0f ? cells / ex[0] : 0.0f, ex[1] > 0.0f ? cells / ex[1] : 0.0f,
                                   ex[2] > 0.0f ? cells / ex[2] : 0.0f);
-          k_ray_keys<<<div_up(n, 256), 256, 0, st>>>(d_rays, (uint32_t)n, lo, sc, 1u << b, X.k0.p,
-                                                              X.v0.p);
+          const uint32_t ntiles = div_up(n, kSortTile);
+          e = X.hist.ensure((size_t)256 * ntiles);
           uint32_t *kr = nullptr, *vr = nullptr;
-          e = radix_sort_pairs(X.k0.p, X.v0.p, X.k1.p, X.v1.p, (uint32_t)n, 3 * (int)b,
-                               X.hist, X.scan, st, &kr, &vr);
+          if (e == cudaSuccess) {
+            k_ray_keys<<<ntiles, kKeyBlock, 0, st>>>(d_rays, (uint32_t)n, lo, sc, 1u << b, X.k0.p, X.v0.p, X.hist.p,
+                                                     ntiles);
+            e = radix_sort_pairs(X.k0.p, X.v0.p, X.k1.p, X.v1.p, (uint32_t)n, 3 * (int)b, X.hist, X.scan, st, &kr,
+                                 &vr, true);
+          }
           perm = vr;
         }
       }
