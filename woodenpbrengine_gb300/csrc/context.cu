@@ -219,6 +219,12 @@ WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
   bvh_release(ctx, false);
   if (ctx->bvh.h_info) cudaFreeHost(ctx->bvh.h_info);
   RenderState& R = ctx->rs;
+  if (R.ggraph) cudaGraphExecDestroy(R.ggraph);
+  for (uint32_t g = 0; g < RenderState::kMaxGroup; ++g) {
+    if (R.gstream[g]) cudaStreamDestroy(R.gstream[g]);
+    if (R.gjoin[g]) cudaEventDestroy(R.gjoin[g]);
+  }
+  if (R.gfork) cudaEventDestroy(R.gfork);
   R.acc.release(); R.hit_prim.release(); R.shadow_rays.release(); R.shadow_hit.release(); R.shadow_map.release();
   R.pstate.release();
   R.Lbuf.release(); R.pfilm.release(); R.pass_dev.release(); R.counters.release();
@@ -719,10 +725,8 @@ WPBR_API wpbr_status wpbr_render_pass(wpbr_ctx* ctx, uint32_t pass) {
 WPBR_API wpbr_status wpbr_render(wpbr_ctx* ctx) {
   if (!ctx) return WPBR_ERR_INVALID_ARG;
   if (!ctx->rs.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render: render_setup not called");
-  for (uint32_t p = 0; p < ctx->rs.spp; ++p) {
-    wpbr_status s = render_pass_fused(ctx, p);
-    if (s != WPBR_OK) return s;
-  }
+  wpbr_status s = render_frame(ctx);  // every pass, small films a group of passes at a time
+  if (s != WPBR_OK) return s;
   return spectral_resolve(ctx);  // Sampled64: the film's toRGB, once per frame
 }
 

@@ -125,6 +125,14 @@ struct RenderState {
   bool spec_dirty = false;  // Sampled64 passes ran since the last toRGB of the film
   const uint32_t* pass_ptr = nullptr;  // shared pass index (batches); null: pass_dev
   uint32_t trace_grid = 0;             // persistent traversal grid cap (0: full)
+  // pass groups (render_frame, small RGB films): kMaxGroup branches of one
+  // fork/join graph, each on its own stream, state slice and pass index word
+  static constexpr uint32_t kMaxGroup = 8;
+  uint32_t group = 0;  // passes per group of the captured group graph
+  cudaGraphExec_t ggraph = nullptr;
+  uint64_t ggraph_key = 0;
+  cudaStream_t gstream[kMaxGroup] = {};
+  cudaEvent_t gfork = nullptr, gjoin[kMaxGroup] = {};
 };
 
 // State of the differentiable estimator (adjoint.cu): sampling (_s) and
@@ -275,6 +283,7 @@ wpbr_status env_distribution_build(wpbr_ctx* ctx, const float4* rgb, const EnvDi
 wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t stream);
 wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass);
 wpbr_status render_pass_launch(wpbr_ctx* ctx);
+wpbr_status render_frame(wpbr_ctx* ctx);
 wpbr_status spectral_setup(wpbr_ctx* ctx);
 // Sampled64 pieces of render_pass_launch: the scalar spawn (replaces the
 // RGB spawn) and the per-bin finish + film (replace the RGB finish + film).

@@ -8,6 +8,7 @@
 //    sample generation (spawn), one traversal launch for both shadow rays,
 //    MIS finish, film gather — five kernels per sample pass, captured once as
 //    a CUDA graph that reads the pass index from device memory.
+#include <algorithm>
 #include <cstring>
 
 #include "common.cuh"
@@ -506,58 +507,76 @@ wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t st
 }
 
 
-// Launches the five kernels of one sample pass on the context's stream. The
-// pass index is read from device memory (R.pass_ptr, shared across the scenes
-// of a batch, else R.pass_dev); R.trace_grid caps the persistent traversal
-// grids (0: one full wave of resident blocks).
-wpbr_status render_pass_launch(wpbr_ctx* ctx) {
+namespace {
+// The kernels of one sample pass on stream `st` over state slice g of a pass
+// group (per-pixel arrays offset by g films, counters by g sets), reading the
+// pass index at pass_ptr; with_film appends the film gather.
+wpbr_status pass_kernels(wpbr_ctx* ctx, uint32_t g, const uint32_t* pass_ptr, cudaStream_t st, uint32_t grid,
+                         bool with_film) {
   RenderState& R = ctx->rs;
   PassCtx P = make_pass_ctx(ctx);
-  uint32_t n = R.W * R.H;
-  cudaStream_t st = ctx->stream;
-  const uint32_t* pass_ptr = R.pass_ptr ? R.pass_ptr : R.pass_dev.p;
-  WPBR_CUDA(R.counters.ensure(kPassCounters));
-  WPBR_CUDA(R.shadow_map.ensure((size_t)2 * n));
-  WPBR_CUDA(R.order.ensure(n));
-  WPBR_CUDA(cudaMemsetAsync(R.counters.p, 0, kPassCounters * sizeof(uint32_t), st));
-  const ShadowQueue sq{R.shadow_rays.p, R.shadow_map.p, R.counters.p + kQueueCounter};
+  const uint32_t n = R.W * R.H;
+  const size_t o = (size_t)g * n;
+  uint32_t* counters = R.counters.p + (size_t)g * kPassCounters;
+  uint32_t* hit_prim = R.hit_prim.p + o;
+  float4* pstate = R.pstate.p + o * kStateF4;
+  float4* Lbuf = R.Lbuf.p + o;
+  float2* pfilm = R.pfilm.p + o;
+  uint32_t* shadow_hit = R.shadow_hit.p + 2 * o;
+  uint32_t* order_buf = R.order.p + o;
+  WPBR_CUDA(cudaMemsetAsync(counters, 0, kPassCounters * sizeof(uint32_t), st));
+  const ShadowQueue sq{R.shadow_rays.p + 4 * o, R.shadow_map.p + 2 * o, counters + kQueueCounter};
   bool spectral = ctx->spectrum == WPBR_SPECTRUM_SAMPLED64;
-  launch_traversal<false>(P.S, P.Bv, CameraSrc{P, pass_ptr}, PrimSink{R.hit_prim.p}, n, R.counters.p, P.err, st,
-                          R.trace_grid);
+  launch_traversal<false>(P.S, P.Bv, CameraSrc{P, pass_ptr}, PrimSink{hit_prim}, n, counters, P.err, st, grid);
   // the pixels in material-sorted order for the spawn and finish kernels
   const uint32_t* order = nullptr;
   if (n >= kSortMinPixels) {
-    uint32_t* cat_counts = R.counters.p + 2;
-    k_cat_count<<<div_up(n, kCatBlock), kCatBlock, 0, st>>>(P.S, n, R.hit_prim.p, cat_counts);
-    k_cat_scatter<<<div_up(n, kCatBlock), kCatBlock, 0, st>>>(P.S, n, R.hit_prim.p, cat_counts,
-                                                              cat_counts + kPixCats, R.order.p, P.err);
-    order = R.order.p;
+    uint32_t* cat_counts = counters + 2;
+    k_cat_count<<<div_up(n, kCatBlock), kCatBlock, 0, st>>>(P.S, n, hit_prim, cat_counts);
+    k_cat_scatter<<<div_up(n, kCatBlock), kCatBlock, 0, st>>>(P.S, n, hit_prim, cat_counts, cat_counts + kPixCats,
+                                                              order_buf, P.err);
+    order = order_buf;
   }
   if (spectral)
     WPBR_CUDA(spectral_spawn_launch(ctx, pass_ptr, order));
   else
-    (ctx->has_metal ? k_spawn<true> : k_spawn<false>)<<<div_up(n, kTB), kTB, 0, st>>>(
-        P, pass_ptr, R.hit_prim.p, R.pstate.p, sq, R.Lbuf.p, R.pfilm.p, order);
+    (ctx->has_metal ? k_spawn<true> : k_spawn<false>)<<<div_up(n, kTB), kTB, 0, st>>>(P, pass_ptr, hit_prim, pstate,
+                                                                                      sq, Lbuf, pfilm, order);
   // shadow rays: unoccluded iff no hit or the closest hit is the sampled
   // light's primitive; with environment lights only that is "no hit", which
   // the any-hit traversal decides with the same primitive tests, stopping at
   // the first hit (the stored id is then some hit, never a light's)
   // (the spawn queued only the rays it traces; the traversal walks the queue)
   const QueueSrc qsrc{sq.rays, sq.count};
-  const MapSink qsink{R.shadow_hit.p, sq.map};
+  const MapSink qsink{shadow_hit, sq.map};
   if (ctx->env_lights_only)
-    launch_traversal<true>(P.S, P.Bv, qsrc, qsink, 2 * n, R.counters.p + 1, P.err, st, R.trace_grid);
+    launch_traversal<true>(P.S, P.Bv, qsrc, qsink, 2 * n, counters + 1, P.err, st, grid);
   else
-    launch_traversal<false>(P.S, P.Bv, qsrc, qsink, 2 * n, R.counters.p + 1, P.err, st, R.trace_grid);
+    launch_traversal<false>(P.S, P.Bv, qsrc, qsink, 2 * n, counters + 1, P.err, st, grid);
   if (spectral) {
     WPBR_CUDA(spectral_finish_launch(ctx, order));
   } else {
-    k_finish<<<div_up(n, kTB), kTB, 0, st>>>(P, R.pstate.p, R.shadow_hit.p, R.Lbuf.p, order);
-    k_film_tiles<<<dim3(div_up(R.W, kFilmTile), div_up(R.H, kFilmTile)), kFilmThreadsRGB, 0, st>>>(
-        R.W, R.H, R.pfilm.p, R.Lbuf.p, (float4*)R.acc.p);
+    k_finish<<<div_up(n, kTB), kTB, 0, st>>>(P, pstate, shadow_hit, Lbuf, order);
+    if (with_film)
+      k_film_tiles<<<dim3(div_up(R.W, kFilmTile), div_up(R.H, kFilmTile)), kFilmThreadsRGB, 0, st>>>(
+          R.W, R.H, pfilm, Lbuf, (float4*)R.acc.p);
   }
   WPBR_CUDA(cudaGetLastError());
   return WPBR_OK;
+}
+}  // namespace
+
+// Launches the five kernels of one sample pass on the context's stream. The
+// pass index is read from device memory (R.pass_ptr, shared across the scenes
+// of a batch, else R.pass_dev); R.trace_grid caps the persistent traversal
+// grids (0: one full wave of resident blocks).
+wpbr_status render_pass_launch(wpbr_ctx* ctx) {
+  RenderState& R = ctx->rs;
+  const uint32_t n = R.W * R.H;
+  WPBR_CUDA(R.counters.ensure(kPassCounters));
+  WPBR_CUDA(R.shadow_map.ensure((size_t)2 * n));
+  WPBR_CUDA(R.order.ensure(n));
+  return pass_kernels(ctx, 0, R.pass_ptr ? R.pass_ptr : R.pass_dev.p, ctx->stream, R.trace_grid, true);
 }
 
 uint32_t persistent_full_grid() {
@@ -622,6 +641,101 @@ wpbr_status render_pass_fused(wpbr_ctx* ctx, uint32_t pass) {
     if (!R.graph_ok) return render_pass_launch(ctx);
   }
   WPBR_CUDA(cudaGraphLaunch(R.graph, st));
+  return WPBR_OK;
+}
+
+// Passes per group for a frame: small films leave most of the GPU idle in one
+// pass (its traversals hold a few tens of thousands of rays), so the passes
+// of a group run as concurrent branches until a group holds about 2^18 rays;
+// the size divides spp, so every group is whole.
+uint32_t group_size(uint32_t n, uint32_t spp) {
+  uint32_t k = (uint32_t)std::min<uint64_t>(RenderState::kMaxGroup, ((1ull << 18) + n - 1) / n);
+  k = std::min(k, spp);
+  while (k > 1 && spp % k) --k;
+  return std::max(k, 1u);
+}
+
+// A whole frame (every pass of render_setup's spp) through the fused pass.
+// Films of RGB frames that fit a group of several passes render a group at a
+// time: one fork/join graph whose K branches run the pass kernels of passes
+// base .. base + K - 1 on their own streams, state slices and pass index
+// words (each traversal capped at a K-th of the resident grid), then the K
+// film gathers in pass order on the context's stream. Every pass computes
+// what it computes alone, and the film adds the passes in the same order, so
+// the film is identical to spp calls of render_pass_fused.
+wpbr_status render_frame(wpbr_ctx* ctx) {
+  RenderState& R = ctx->rs;
+  if (!R.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render: render_setup not called");
+  const uint32_t n = R.W * R.H;
+  const uint32_t K = (ctx->spectrum == WPBR_SPECTRUM_RGB && !R.pass_ptr) ? group_size(n, R.spp) : 1u;
+  if (K <= 1) {
+    for (uint32_t p = 0; p < R.spp; ++p) {
+      wpbr_status s = render_pass_fused(ctx, p);
+      if (s != WPBR_OK) return s;
+    }
+    return WPBR_OK;
+  }
+  cudaStream_t st = ctx->stream;
+  const size_t kn = (size_t)K * n;
+  WPBR_CUDA(R.hit_prim.ensure(kn));
+  WPBR_CUDA(R.pstate.ensure(kn * kStateF4));
+  WPBR_CUDA(R.Lbuf.ensure(kn));
+  WPBR_CUDA(R.pfilm.ensure(kn));
+  WPBR_CUDA(R.shadow_rays.ensure(4 * kn));
+  WPBR_CUDA(R.shadow_map.ensure(2 * kn));
+  WPBR_CUDA(R.shadow_hit.ensure(2 * kn));
+  WPBR_CUDA(R.order.ensure(kn));
+  WPBR_CUDA(R.counters.ensure((size_t)K * kPassCounters));
+  WPBR_CUDA(R.pass_dev.ensure(K));
+  for (uint32_t g = 0; g < K; ++g)
+    if (!R.gstream[g]) WPBR_CUDA(cudaStreamCreateWithFlags(&R.gstream[g], cudaStreamNonBlocking));
+  if (!R.gfork) WPBR_CUDA(cudaEventCreateWithFlags(&R.gfork, cudaEventDisableTiming));
+  for (uint32_t g = 0; g < K; ++g)
+    if (!R.gjoin[g]) WPBR_CUDA(cudaEventCreateWithFlags(&R.gjoin[g], cudaEventDisableTiming));
+  const uint64_t key = pass_graph_key(ctx) * 0x100000001B3ull + K;
+  if (R.ggraph && (R.ggraph_key != key || R.group != K)) {
+    cudaGraphExecDestroy(R.ggraph);
+    R.ggraph = nullptr;
+  }
+  if (!R.ggraph) {
+    const uint32_t full = persistent_full_grid();
+    const uint32_t grid = std::max(1u, full / K);
+    cudaGraph_t gr = nullptr;
+    WPBR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    wpbr_status s = WPBR_OK;
+    cudaError_t e = cudaEventRecord(R.gfork, st);
+    for (uint32_t g = 0; g < K && e == cudaSuccess && s == WPBR_OK; ++g) {
+      e = cudaStreamWaitEvent(R.gstream[g], R.gfork, 0);
+      if (e != cudaSuccess) break;
+      s = pass_kernels(ctx, g, R.pass_dev.p + g, R.gstream[g], grid, false);
+      if (s != WPBR_OK) break;
+      e = cudaEventRecord(R.gjoin[g], R.gstream[g]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, R.gjoin[g], 0);
+    }
+    for (uint32_t g = 0; g < K && e == cudaSuccess && s == WPBR_OK; ++g)
+      k_film_tiles<<<dim3(div_up(R.W, kFilmTile), div_up(R.H, kFilmTile)), kFilmThreadsRGB, 0, st>>>(
+          R.W, R.H, R.pfilm.p + (size_t)g * n, R.Lbuf.p + (size_t)g * n, (float4*)R.acc.p);
+    cudaError_t e2 = cudaStreamEndCapture(st, &gr);
+    if (s == WPBR_OK && e == cudaSuccess && e2 == cudaSuccess && gr) e = cudaGraphInstantiate(&R.ggraph, gr, 0);
+    if (gr) cudaGraphDestroy(gr);
+    if (s != WPBR_OK) {
+      cudaGetLastError();
+      return s;
+    }
+    if (e != cudaSuccess || e2 != cudaSuccess || !R.ggraph) {
+      cudaGetLastError();
+      R.ggraph = nullptr;
+      return set_err(ctx, WPBR_ERR_CUDA, "render: pass-group graph capture failed");
+    }
+    R.ggraph_key = key;
+    R.group = K;
+  }
+  uint32_t passes[RenderState::kMaxGroup];
+  for (uint32_t base = 0; base < R.spp; base += K) {
+    for (uint32_t g = 0; g < K; ++g) passes[g] = base + g;
+    WPBR_CUDA(cudaMemcpyAsync(R.pass_dev.p, passes, sizeof(uint32_t) * K, cudaMemcpyHostToDevice, st));
+    WPBR_CUDA(cudaGraphLaunch(R.ggraph, st));
+  }
   return WPBR_OK;
 }
 
