@@ -90,6 +90,11 @@ def parse():
                    help="Sampled64 case for ncu: config 2 (level 8) at W x H, one 2-spp frame")
     p.add_argument("--profile-build", action="store_true",
                    help="LBVH build case for ncu: 8 builds of the 1,310,720-triangle mesh (3 warm-up, 5 timed)")
+    p.add_argument("--profile-collide", action="store_true",
+                   help="collide case for ncu: one build of the microbenchmark mesh (45 launches), then three "
+                        "closest-hit collides of all 8,388,608 rays on resident buffers (16 launches each)")
+    p.add_argument("--profile-frame", action="store_true",
+                   help="render case for ncu: config 2 (level 8) at 1920x1080, two 8-spp frames")
     return p.parse_args()
 
 
@@ -674,6 +679,59 @@ def run_spectral_profile_case(res):
     print(json.dumps({"profile_case": "Sampled64 config 2, %dx%d, 2 spp" % tuple(res)}))
 
 
+def run_collide_profile_case():
+    """One build of the microbenchmark mesh, then three closest-hit collides
+    of the whole ray set through wpbr_collide_device (each: ray keys, the
+    ray-order sort, the traversal)."""
+    import torch
+
+    from __graft_entry__ import build
+
+    build()
+    import woodenpbrengine_gb300 as W
+
+    g = W.SceneGen(1, 0, (RES, RES), level=LEVEL, rays=True)
+    rays = g.rays()
+    n = rays.shape[0]
+    ctx = W.Context(0)
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    ctx.upload(g.desc)
+    ctx.build()
+    d_rays = torch.from_numpy(rays).to("cuda")
+    d_hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        ctx.collide_device(d_rays.data_ptr(), n, d_hits.data_ptr(), W.TRACE_CLOSEST)
+    torch.cuda.synchronize()
+    ctx.check_device_errors()
+    ctx.close()
+    print(json.dumps({"profile_case": "closest hit, %d rays, 3 collides after one build" % n}))
+
+
+def run_frame_profile_case():
+    """Two 8-spp frames of the full-frame scene (config 2, level 8) at
+    1920x1080 through the graph-captured RGB pass."""
+    import torch
+
+    from __graft_entry__ import build
+
+    build()
+    import woodenpbrengine_gb300 as W
+
+    g = W.SceneGen(2, 0, (1920, 1080), level=LEVEL)
+    ctx = W.Context(0)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload(g.desc)
+    ctx.build()
+    for _ in range(2):
+        ctx.render_setup(8, seed=0)
+        ctx.render()
+    torch.cuda.synchronize()
+    ctx.check_device_errors()
+    ctx.close()
+    print(json.dumps({"profile_case": "config 2, 1920x1080, two 8-spp frames"}))
+
+
 def run_build_profile_case():
     """Eight LBVH builds of the 1,310,720-triangle microbenchmark mesh (three
     warm-up builds, then five timed back to back on the context's stream)."""
@@ -704,6 +762,12 @@ def main():
     args = parse()
     if args.profile_build:
         run_build_profile_case()
+        return
+    if args.profile_collide:
+        run_collide_profile_case()
+        return
+    if args.profile_frame:
+        run_frame_profile_case()
         return
     if args.profile_spectral:
         run_spectral_profile_case(args.profile_spectral)
