@@ -330,6 +330,13 @@ WPBR_API wpbr_status wpbr_adjoint_backward_device(wpbr_ctx* ctx, float* d_grad_m
  * WPBR_ERR_TRAVERSAL_LIMIT; nothing traps and the context stays usable.
  * Applies to later launches (pass graphs are recaptured). */
 WPBR_API wpbr_status wpbr_set_traversal_limits(wpbr_ctx* ctx, uint32_t max_stack_entries, uint32_t max_loop_steps);
+/* The order wpbr_collide traces a batch of n rays in when it sorts them
+ * (batches of 2^18 rays and more, wpbr_set_ray_sort > 0): keys[i] is the
+ * Morton code of ray i's origin cell (3 x bits-per-axis bits over the scene
+ * bounds) and perm[j] the input index of the j-th ray traced, a stable sort of
+ * the keys. rays as for wpbr_collide (host); any n below 2^32 - 1. */
+WPBR_API wpbr_status wpbr_debug_ray_order(wpbr_ctx* ctx, const float* rays, uint64_t n, uint32_t* keys,
+                                          uint32_t* perm);
 /* Process-wide device-allocation fault injection: with n >= 0 the library's
  * next n device allocations succeed and every later one fails (cudaMalloc is
  * not called), so the call that needed it returns WPBR_ERR_OOM; n < 0 (the

@@ -136,6 +136,35 @@ def test_ray_reordering_keeps_hits(W, ctx):
     ctx.check_device_errors()
 
 
+@pytest.mark.parametrize("bits", [8, 5, 10])
+def test_ray_order_is_a_stable_sort(W, ctx, bits):
+    # the radix sort behind the ray order (one pass per 8-bit digit; 15 bits
+    # end on a 7-bit digit, 30 bits take four passes): for
+    # whole, ragged, one-tile and tiny batches, in the generator's order and
+    # shuffled, the trace order is the stable sort of the origin keys
+    g = W.SceneGen(1, 0, (512, 512), level=6, rays=True)
+    ctx.set_quirks(0)
+    ctx.upload(g.desc)
+    ctx.build()
+    rays = g.rays()
+    shuffled = rays[np.random.default_rng(3).permutation(rays.shape[0])]
+    ctx.set_ray_sort(bits)
+    try:
+        for rs in (rays, shuffled):
+            for n in (rs.shape[0], 3 * 2048 + 5, 2048, 2, 1):
+                keys, perm = ctx.debug_ray_order(rs[:n])
+                assert int(keys.max()) < 1 << (3 * bits)
+                assert np.array_equal(perm, np.argsort(keys, kind="stable").astype(np.uint32))
+        # identical origins share a key (the coherent half has one origin)
+        o = rays[:, :3]
+        same = np.all(o == o[0], axis=1)
+        keys, _ = ctx.debug_ray_order(rays)
+        assert same.sum() > 1 and np.all(keys[same] == keys[0])
+    finally:
+        ctx.set_ray_sort(8)
+    ctx.check_device_errors()
+
+
 def test_chunked_host_collide_matches_device_collide(W, ctx):
     # host-buffer batches of 2^22 rays and more are copied and traced in
     # chunks whose copies overlap the neighbouring chunks' traversal; the

@@ -106,6 +106,7 @@ _SIGS = {
     "wpbr_batch_check_device_errors": (C.c_int, [_VP]),
     "wpbr_set_traversal_limits": (C.c_int, [_VP, C.c_uint32, C.c_uint32]),
     "wpbr_debug_fail_allocations": (None, [C.c_int64]),
+    "wpbr_debug_ray_order": (C.c_int, [_VP, _FP, C.c_uint64, _UP, _UP]),
 }
 SORT_NOALLOC_MAX_KEYS = 1 << 20
 EXPORTED = sorted(_SIGS)
@@ -303,6 +304,15 @@ class Context:
         ms, c = C.c_float(), C.c_uint32()
         self._check(lib().wpbr_kernel_timing(self._h, C.byref(ms), C.byref(c)), "kernel_timing")
         return ms.value, c.value
+
+    def debug_ray_order(self, rays):
+        """(keys in input order, trace order) of a sorted collide of rays (n, 8)."""
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        keys = np.zeros(n, np.uint32)
+        perm = np.zeros(n, np.uint32)
+        self._check(lib().wpbr_debug_ray_order(self._h, _fp(rays), n, _up(keys), _up(perm)), "debug_ray_order")
+        return keys, perm
 
     def collide_device(self, d_rays, n, d_hits, mode=TRACE_CLOSEST):
         self._check(lib().wpbr_collide_device(self._h, d_rays, n, d_hits, mode), "collide_device")

@@ -114,6 +114,31 @@ __global__ void k_scan_add(V* out, uint32_t n, const V* boff) {
   if (i < n) out[i] += boff[i / kScanTile];
 }
 
+// The second launch of a two-level scan: one block per scan tile adds the
+// sum of the tile sums before it, reduced here from the unscanned sums (at
+// most kScanTile of them) instead of by a scan launch of its own.
+template <class V>
+__global__ void __launch_bounds__(kScanBlock) k_scan_add_tiles(V* out, uint32_t n, const V* bsum) {
+  __shared__ V wsum[kScanBlock / 32];
+  const uint32_t j = blockIdx.x;
+  if (j == 0) return;  // block-uniform: the first tile is already final
+  V part = 0;
+  for (uint32_t t = threadIdx.x; t < j; t += kScanBlock) part += bsum[t];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xFFFFFFFFu, part, o);
+  if (lane_id() == 0) wsum[threadIdx.x >> 5] = part;
+  __syncthreads();
+  V off = 0;
+#pragma unroll
+  for (int q = 0; q < kScanBlock / 32; ++q) off += wsum[q];
+  const uint32_t base = j * kScanTile;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const uint32_t i = base + threadIdx.x + k * kScanBlock;
+    if (i < n) out[i] += off;
+  }
+}
+
 template <class V>
 cudaError_t scan_exclusive_t(const V* in, V* out, uint32_t n, V* tmp, size_t tmp_n, cudaStream_t s) {
   struct Lvl {
@@ -140,6 +165,12 @@ cudaError_t scan_exclusive_t(const V* in, V* out, uint32_t n, V* tmp, size_t tmp
     m = nb;
     if (L >= 8) return cudaErrorInvalidValue;
   }
+  if (L == 2) {  // the tile sums fit one tile: two launches
+    const uint32_t nb = div_up(n, kScanTile);
+    k_scan_tile<V><<<nb, kScanBlock, 0, s>>>(in, out, n, lv[0].sums);
+    k_scan_add_tiles<V><<<nb, kScanBlock, 0, s>>>(out, n, lv[0].sums);
+    return cudaGetLastError();
+  }
   for (int i = 0; i < L; ++i) {
     uint32_t nb = div_up(lv[i].n, kScanTile);
     k_scan_tile<V><<<nb, kScanBlock, 0, s>>>(lv[i].in, lv[i].out, lv[i].n, lv[i].sums);
@@ -164,7 +195,7 @@ uint32_t scan_launches(uint32_t n) {
   if (n == 0) return 0;
   uint32_t levels = 1;
   for (uint32_t m = n; m > (uint32_t)kScanTile; m = div_up(m, kScanTile)) ++levels;
-  return 2 * levels - 1;
+  return levels == 2 ? 2 : 2 * levels - 1;
 }
 
 cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, DevBuf<uint32_t>& tmp, cudaStream_t s) {
@@ -261,19 +292,29 @@ constexpr int kRadixItems = 8;
 constexpr int kRadixTile = kB * kRadixItems;
 static_assert(kRadixTile == (int)kSortTile, "the sort's tile size is shared with the key producers");
 
-// Block histograms of one pass (digit-major, block-minor). A warp whose 32
-// keys share one digit adds them with one atomic (coherent rays' origins
-// often do), the others key by key.
+// Block histograms of one pass (digit-major, block-minor). Each thread
+// loads its kRadixItems keys before it counts any (eight loads in flight: the
+// kernel reads memory at a rate bound by loads in flight, and the shared
+// atomics would otherwise order each load after the previous count). A warp
+// whose 32 keys share one digit adds them with one atomic (coherent rays'
+// origins often do), the others key by key.
 __global__ void k_radix_hist(const uint32_t* keys, uint32_t n, int shift, uint32_t dmask, uint32_t* hist,
                              uint32_t nblocks) {
   __shared__ uint32_t cnt[256];
   cnt[threadIdx.x] = 0;
-  __syncthreads();
-  uint32_t base = blockIdx.x * kRadixTile;
+  const uint32_t base = blockIdx.x * kRadixTile;
+  uint32_t key[kRadixItems];
+#pragma unroll
   for (int k = 0; k < kRadixItems; ++k) {
-    uint32_t i = base + threadIdx.x + k * kB;
+    const uint32_t i = base + threadIdx.x + k * kB;
+    key[k] = i < n ? keys[i] : 0u;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kRadixItems; ++k) {
+    const uint32_t i = base + threadIdx.x + k * kB;
     const bool valid = i < n;
-    const uint32_t d = valid ? (keys[i] >> shift) & dmask : 0xFFFFFFFFu;
+    const uint32_t d = valid ? (key[k] >> shift) & dmask : 0xFFFFFFFFu;
     if (__all_sync(0xFFFFFFFFu, d == __shfl_sync(0xFFFFFFFFu, d, 0) && valid)) {
       if (lane_id() == 0) atomicAdd(&cnt[d], 32u);
     } else if (valid) {
@@ -314,7 +355,7 @@ __global__ void __launch_bounds__(kB) k_radix_scatter(const uint32_t* kin, const
   for (int k = 0; k < kRadixItems; ++k) {
     const uint32_t i = base + k * 32 + lane;
     key[k] = i < n ? kin[i] : 0u;
-    val[k] = i < n ? vin[i] : 0u;
+    val[k] = i < n ? (vin ? vin[i] : i) : 0u;  // no values: the pass sorts the keys' positions
   }
   uint32_t* wc = s_wc[w];
 #pragma unroll
@@ -1883,21 +1924,26 @@ uint32_t radix_sort_launches(uint32_t n, int bits) {
 
 // Stable LSD radix sort of (key, value) pairs by key bits [0, bits), 8 bits
 // per pass (the build's sort kernels); *kres / *vres point at the buffer
-// pair that holds the result.
+// pair that holds the result. index_values: the values are the keys' input
+// positions, made by the first pass (v0 is then only a ping-pong buffer).
 cudaError_t radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t n, int bits,
                              DevBuf<uint32_t>& hist, DevBuf<uint32_t>& scan_tmp, cudaStream_t st, uint32_t** kres,
-                             uint32_t** vres, bool first_hist) {
+                             uint32_t** vres, bool first_hist, bool index_values) {
   uint32_t nblk = div_up(n, kRadixTile);
+  *kres = k0;
+  *vres = v0;
+  if (n <= 1) return index_values && n == 1 ? cudaMemsetAsync(v0, 0, sizeof(uint32_t), st) : cudaSuccess;
   cudaError_t e = hist.ensure((size_t)256 * nblk);
   if (e != cudaSuccess) return e;
   uint32_t *kin = k0, *vin = v0, *kout = k1, *vout = v1;
-  for (int shift = 0; shift < bits && n > 1; shift += 8) {
+  for (int shift = 0; shift < bits; shift += 8) {
     int w = bits - shift < 8 ? bits - shift : 8;
     uint32_t dmask = (1u << w) - 1u;
     if (shift > 0 || !first_hist) k_radix_hist<<<nblk, kB, 0, st>>>(kin, n, shift, dmask, hist.p, nblk);
     e = scan_exclusive(hist.p, hist.p, 256 * nblk, scan_tmp, st);
     if (e != cudaSuccess) return e;
-    k_radix_scatter<<<nblk, kB, 0, st>>>(kin, vin, kout, vout, n, shift, dmask, hist.p, nblk);
+    k_radix_scatter<<<nblk, kB, 0, st>>>(kin, (shift == 0 && index_values) ? nullptr : vin, kout, vout, n, shift,
+                                         dmask, hist.p, nblk);
     std::swap(kin, kout);
     std::swap(vin, vout);
   }

@@ -171,6 +171,11 @@ WPBR_API wpbr_status wpbr_set_traversal_limits(wpbr_ctx* ctx, uint32_t max_stack
   return WPBR_OK;
 }
 
+WPBR_API wpbr_status wpbr_debug_ray_order(wpbr_ctx* ctx, const float* rays, uint64_t n, uint32_t* keys,
+                                          uint32_t* perm) {
+  if (!ctx || (n && (!rays || !keys || !perm))) return WPBR_ERR_INVALID_ARG;
+  return ray_order_debug(ctx, rays, n, keys, perm);
+}
 WPBR_API void wpbr_debug_fail_allocations(int64_t n) { g_alloc_budget.store(n < 0 ? -1 : (long long)n); }
 
 WPBR_API wpbr_status wpbr_create(int device, wpbr_ctx** out) {

@@ -266,10 +266,11 @@ wpbr_status bvh_build(wpbr_ctx* ctx);
 // tile of this many keys, digit-major).
 constexpr uint32_t kSortTile = 2048;
 // first_hist: the first pass's tile histograms are already in hist (written
-// by the kernel that produced the keys).
+// by the kernel that produced the keys); index_values: sort the keys'
+// positions (v0 need not be filled).
 cudaError_t radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uint32_t n, int bits,
                              DevBuf<uint32_t>& hist, DevBuf<uint32_t>& scan_tmp, cudaStream_t st, uint32_t** kres,
-                             uint32_t** vres, bool first_hist = false);
+                             uint32_t** vres, bool first_hist = false, bool index_values = false);
 // Traces on `stream` (the context's when null) with scratch set `scratch`.
 wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* d_hits, uint32_t mode,
                        uint32_t* d_stats, int scratch = 0, cudaStream_t stream = nullptr);
@@ -310,6 +311,7 @@ cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, DevBuf
 uint32_t scan_launches(uint32_t n);
 uint32_t radix_sort_launches(uint32_t n, int bits);
 uint32_t trace_launches(const wpbr_ctx* ctx, uint64_t n, bool stats);
+wpbr_status ray_order_debug(wpbr_ctx* ctx, const float* rays, uint64_t n, uint32_t* keys, uint32_t* perm);
 }  // namespace wpbr
 
 #define WPBR_CUDA(call)                                          \

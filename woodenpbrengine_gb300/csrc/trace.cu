@@ -39,30 +39,38 @@ __device__ __forceinline__ uint32_t spread10(uint32_t v) {
   v = (v | (v << 2)) & 0x09249249u;
   return v;
 }
-// One block per kSortTile rays: the keys, their indices, and the tile's
-// histogram of the sort's first digit (the low 8 bits), in the layout of the
-// sort's own histogram kernel (digit-major, tile-minor), which the sort then
-// skips. A warp whose 32 keys share that digit adds them with one atomic.
+// One block per kSortTile rays: the keys, and the tile's histogram of the
+// sort's first digit (the low 8 bits), in the layout of the sort's own
+// histogram kernel (digit-major, tile-minor), which the sort then skips. A
+// thread loads its rays' origins before it counts any (its loads in flight
+// together); a warp whose 32 keys share the digit adds them with one atomic.
+// The sort's first pass makes the indices itself.
 constexpr int kKeyBlock = 256;
+constexpr int kKeyItems = (int)kSortTile / kKeyBlock;
 __global__ void __launch_bounds__(kKeyBlock) k_ray_keys(const float4* rays, uint32_t n, float3 lo, float3 scale,
-                                                        uint32_t cells, uint32_t* keys, uint32_t* idx,
-                                                        uint32_t* hist, uint32_t ntiles) {
+                                                        uint32_t cells, uint32_t* keys, uint32_t* hist,
+                                                        uint32_t ntiles) {
   __shared__ uint32_t cnt[256];
   cnt[threadIdx.x] = 0;
-  __syncthreads();
   const float top = (float)(cells - 1);
   const uint32_t base = blockIdx.x * kSortTile;
-  for (uint32_t k = 0; k < kSortTile / kKeyBlock; ++k) {
+  float4 o[kKeyItems];
+#pragma unroll
+  for (int k = 0; k < kKeyItems; ++k) {
+    const uint32_t i = base + k * kKeyBlock + threadIdx.x;
+    o[k] = i < n ? __ldg(&rays[2 * (size_t)i]) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kKeyItems; ++k) {
     const uint32_t i = base + k * kKeyBlock + threadIdx.x;
     uint32_t d = 0xFFFFFFFFu;
     if (i < n) {
-      float4 o = __ldg(&rays[2 * (size_t)i]);
-      float q[3] = {(o.x - lo.x) * scale.x, (o.y - lo.y) * scale.y, (o.z - lo.z) * scale.z};
+      float q[3] = {(o[k].x - lo.x) * scale.x, (o[k].y - lo.y) * scale.y, (o[k].z - lo.z) * scale.z};
       uint32_t c[3];
       for (int a = 0; a < 3; ++a) c[a] = q[a] > 0.0f ? (q[a] < top ? (uint32_t)q[a] : cells - 1) : 0u;
       const uint32_t key = spread10(c[0]) | (spread10(c[1]) << 1) | (spread10(c[2]) << 2);
       keys[i] = key;
-      idx[i] = i;
       d = key & 0xFFu;
     }
     if (__all_sync(0xFFFFFFFFu, d == __shfl_sync(0xFFFFFFFFu, d, 0) && d != 0xFFFFFFFFu)) {
@@ -73,6 +81,35 @@ __global__ void __launch_bounds__(kKeyBlock) k_ray_keys(const float4* rays, uint
   }
   __syncthreads();
   hist[threadIdx.x * ntiles + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// The ray order of a batch: keys with the first digit's tile histograms,
+// then the rest of the stable LSD sort of the ray indices; *perm receives
+// sorted position -> input index. keys_host, when given, receives the keys
+// in input order (a testing aid).
+cudaError_t ray_order(wpbr_ctx* ctx, wpbr_ctx::TraceScratch& X, const BvhView& Bv, const float4* d_rays, uint32_t n,
+                      cudaStream_t st, const uint32_t** perm, uint32_t* keys_host) {
+  cudaError_t e = cudaSuccess;
+  for (DevBuf<uint32_t>* b : {&X.k0, &X.v0, &X.k1, &X.v1})
+    if (e == cudaSuccess) e = b->ensure(n);
+  if (e != cudaSuccess) return e;
+  const float3 lo = make_float3(Bv.root_lo[0], Bv.root_lo[1], Bv.root_lo[2]);
+  const float ex[3] = {Bv.root_hi[0] - Bv.root_lo[0], Bv.root_hi[1] - Bv.root_lo[1], Bv.root_hi[2] - Bv.root_lo[2]};
+  const uint32_t b = ctx->ray_sort;  // bits per axis
+  const int key_bits = 3 * (int)b;
+  const float cells = (float)(1u << b);
+  const float3 sc = make_float3(ex[0] > 0.0f ? cells / ex[0] : 0.0f, ex[1] > 0.0f ? cells / ex[1] : 0.0f,
+                                ex[2] > 0.0f ? cells / ex[2] : 0.0f);
+  const uint32_t ntiles = div_up(n, kSortTile);
+  e = X.hist.ensure((size_t)256 * ntiles);
+  if (e != cudaSuccess) return e;
+  k_ray_keys<<<ntiles, kKeyBlock, 0, st>>>(d_rays, n, lo, sc, 1u << b, X.k0.p, X.hist.p, ntiles);
+  if (keys_host) e = cudaMemcpyAsync(keys_host, X.k0.p, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+  uint32_t *kr = nullptr, *vr = nullptr;
+  if (e == cudaSuccess)
+    e = radix_sort_pairs(X.k0.p, X.v0.p, X.k1.p, X.v1.p, n, key_bits, X.hist, X.scan, st, &kr, &vr, true, true);
+  *perm = vr;
+  return e;
 }
 
 template <bool ANY, bool STATS>
@@ -117,36 +154,16 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
                                  : launch<false, true>(S, Br, d_rays, n, d_hits, d_stats, ctx->d_err.p, st);
   } else {
     if (n >= 0xFFFFFFFFull) return set_err(ctx, WPBR_ERR_INVALID_ARG, "collide: more than 2^32-1 rays per call");
-    e = X.counter.ensure(4);
+    // large batches are traced in the order of their origins' Morton cells:
+    // neighbouring rays of a warp then share nodes (hits are per ray, so the
+    // order does not change them)
+    const bool sorted = ctx->ray_sort && n >= kRaySortMin && !Bv.empty;
+    e = X.counter.ensure(1);
     if (e == cudaSuccess) {
       uint32_t* c = X.counter.p;
       e = cudaMemsetAsync(c, 0, sizeof(uint32_t), st);
-      // large batches are traced in the order of their origins' Morton cells:
-      // neighbouring rays of a warp then share nodes (hits are per ray, so the
-      // order does not change them)
       const uint32_t* perm = nullptr;
-      if (e == cudaSuccess && ctx->ray_sort && n >= kRaySortMin && !Bv.empty) {
-        for (DevBuf<uint32_t>* b : {&X.k0, &X.v0, &X.k1, &X.v1})
-          if (e == cudaSuccess) e = b->ensure(n);
-        if (e == cudaSuccess) {
-          float3 lo = make_float3(Bv.root_lo[0], Bv.root_lo[1], Bv.root_lo[2]);
-          float ex[3] = {Bv.root_hi[0] - Bv.root_lo[0], Bv.root_hi[1] - Bv.root_lo[1], Bv.root_hi[2] - Bv.root_lo[2]};
-          uint32_t b = ctx->ray_sort;  // bits per axis
-          float cells = (float)(1u << b);
-          float3 sc = make_float3(ex[0] > 0.0f ? cells / ex[0] : 0.0f, ex[1] > 0.0f ? cells / ex[1] : 0.0f,
-                                  ex[2] > 0.0f ? cells / ex[2] : 0.0f);
-          const uint32_t ntiles = div_up(n, kSortTile);
-          e = X.hist.ensure((size_t)256 * ntiles);
-          uint32_t *kr = nullptr, *vr = nullptr;
-          if (e == cudaSuccess) {
-            k_ray_keys<<<ntiles, kKeyBlock, 0, st>>>(d_rays, (uint32_t)n, lo, sc, 1u << b, X.k0.p, X.v0.p, X.hist.p,
-                                                     ntiles);
-            e = radix_sort_pairs(X.k0.p, X.v0.p, X.k1.p, X.v1.p, (uint32_t)n, 3 * (int)b, X.hist, X.scan, st, &kr,
-                                 &vr, true);
-          }
-          perm = vr;
-        }
-      }
+      if (e == cudaSuccess && sorted) e = ray_order(ctx, X, Bv, d_rays, (uint32_t)n, st, &perm, nullptr);
       // optional CUDA events around the traversal launch (wpbr_set_kernel_timing)
       int slot = -1;
       if (e == cudaSuccess && ctx->kernel_timing && ctx->timed < wpbr_ctx::kTimedMax) {
@@ -180,6 +197,26 @@ wpbr_status trace_rays(wpbr_ctx* ctx, const float4* d_rays, uint64_t n, float4* 
     }
   }
   if (e != cudaSuccess) return cuda_err(ctx, e, "collide kernel");
+  return WPBR_OK;
+}
+
+wpbr_status ray_order_debug(wpbr_ctx* ctx, const float* rays, uint64_t n, uint32_t* keys, uint32_t* perm) {
+  if (!ctx->bvh.built) return set_err(ctx, WPBR_ERR_NOT_BUILT, "ray order: BVH not built");
+  if (n == 0) return WPBR_OK;
+  const BvhView Bv = traversal_view(ctx);
+  if (!ctx->ray_sort || Bv.empty || n >= 0xFFFFFFFFull)
+    return set_err(ctx, WPBR_ERR_INVALID_ARG, "ray order: sorting off, empty scene or 2^32-1 rays and more");
+  cudaStream_t st = ctx->stream;
+  wpbr_ctx::TraceScratch& X = ctx->tscr[0];
+  DevBuf<float4> d_rays;
+  cudaError_t e = d_rays.ensure(2 * n);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_rays.p, rays, n * 32, cudaMemcpyHostToDevice, st);
+  const uint32_t* d_perm = nullptr;
+  if (e == cudaSuccess) e = ray_order(ctx, X, Bv, d_rays.p, (uint32_t)n, st, &d_perm, keys);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(perm, d_perm, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  d_rays.release();
+  if (e != cudaSuccess) return cuda_err(ctx, e, "ray order");
   return WPBR_OK;
 }
 

@@ -27,13 +27,12 @@ constexpr int kPersistBlock = 128;
 #define WPBR_REFILL_MIN 20
 #endif
 // Resident blocks per SM each traversal instantiation is compiled for
-// (Sink::kMinBlocks): the collide kernels (full hit records) run best at 12
-// (40 registers, some spilled; on the 8.4M-ray microbenchmark 10 blocks at 48
-// registers were 1.4% faster than 8, and with the packed stack entries 12
-// blocks 0.8% faster than 10 for closest hit, 0.4% slower for any-hit; 9
-// blocks 1.2% slower; 14 were 19% slower before); the render passes' kernels
-// (camera rays generated in the source, prim-id sinks) at 8 (64 registers),
-// where 10 cost them 5%.
+// (Sink::kMinBlocks): 8 (64 registers, next to no spilling) for the collide
+// kernels, whose lowest 8 stack entries live in shared memory, and for the
+// render passes' kernels (camera rays generated in the source, prim-id
+// sinks), where 10 cost 5%. With the whole stack in local memory the collide
+// kernels had run best at 12 blocks (40 registers, registers and stack
+// entries spilled to local memory, 2.1 M-ray launch: 63 M local loads).
 
 // Ray data the warp's lanes read when they test primitives for another lane:
 // a triangle test reads the first two float4s (two 16-byte shared loads), a
@@ -129,6 +128,64 @@ struct TravStack<STACK, false> {
     return true;
   }
 };
+// The same stack with its lowest KS entries in shared memory (the block's
+// entries stored entry-major, so a warp's 32 lanes touch consecutive words)
+// and the rest in local memory. The collide kernels keep 8 entries there
+// (12 KB per block). 8.4M-ray microbenchmark, closest-hit step / any-hit
+// step, ms: all local at 12 blocks 4.307 / 3.963; 8 shared entries at 8
+// blocks 4.228 / 3.855, 10 at 8 4.232 / 3.858, 12 at 8 4.258 / 3.871, 14 at 8
+// (7 blocks fit) 4.476 / 4.079, none at 8 4.351 / 3.975; 6 or 8 at 9 blocks
+// 4.27 / 3.91; 4-8 at 12 blocks 4.56-4.72 (the L1 left is too small), 12 at
+// 7 blocks 4.437; hits identical in every case.
+template <int STACK, int KS>
+struct TravStackSh {
+  unsigned long long* s_tr;  // this lane's column: entry i at s_tr[i * kPersistBlock]
+  uint32_t* s_c;
+  unsigned long long tr[STACK - KS];
+  uint32_t c[STACK - KS];
+  __device__ __forceinline__ void put(int i, int ref, uint32_t cnt, float t) {
+    const unsigned long long e = ((unsigned long long)__float_as_uint(t) << 32) | (uint32_t)ref;
+    if (i < KS) {
+      s_tr[i * kPersistBlock] = e;
+      s_c[i * kPersistBlock] = cnt;
+    } else {
+      tr[i - KS] = e;
+      c[i - KS] = cnt;
+    }
+  }
+  __device__ __forceinline__ bool take(int i, float limit, int* ref, uint32_t* cnt) const {
+    const unsigned long long e = i < KS ? s_tr[i * kPersistBlock] : tr[i - KS];
+    if (__uint_as_float((uint32_t)(e >> 32)) > limit) return false;
+    *ref = (int)(uint32_t)e;
+    *cnt = i < KS ? s_c[i * kPersistBlock] : c[i - KS];
+    return true;
+  }
+};
+#ifndef WPBR_SHARED_STACK
+#define WPBR_SHARED_STACK 8
+#endif
+// The render passes' kernels keep their stacks in local memory: 4, 8 or 12
+// shared entries changed the 1080p full frame by -0.5, +0.2 and -1.4 %, the
+// textured-metal frame by -1.0, -0.9 and -1.3 %.
+#ifndef WPBR_SHARED_STACK_RENDER
+#define WPBR_SHARED_STACK_RENDER 0
+#endif
+template <int STACK, bool PACKED, int KS>
+struct StackSel {
+  using type = TravStackSh<STACK, KS>;
+};
+template <int STACK, bool PACKED>
+struct StackSel<STACK, PACKED, 0> {
+  using type = TravStack<STACK, PACKED>;
+};
+template <int STACK, int KS>
+__device__ __forceinline__ void stack_bind(TravStackSh<STACK, KS>& st, unsigned long long* tr, uint32_t* c) {
+  st.s_tr = tr;
+  st.s_c = c;
+}
+template <int STACK, bool PACKED>
+__device__ __forceinline__ void stack_bind(TravStack<STACK, PACKED>&, unsigned long long*, uint32_t*) {}
+
 // Pops until an entry whose entry distance does not exceed the best hit by
 // more than the pruning margin; kEnd when the stack runs out.
 template <class Stack>
@@ -149,6 +206,9 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
   __shared__ unsigned long long s_key[kPersistBlock / 32][32];
   __shared__ uint32_t s_hprim[kPersistBlock / 32][32];  // primitive and barycentrics of s_key's hit
   __shared__ float2 s_hbary[kPersistBlock / 32][32];
+  constexpr int KS = Sink::kCollide ? WPBR_SHARED_STACK : WPBR_SHARED_STACK_RENDER;
+  __shared__ unsigned long long s_stk_tr[KS > 0 ? KS : 1][kPersistBlock];
+  __shared__ uint32_t s_stk_c[KS > 0 ? KS : 1][kPersistBlock];
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t wid = threadIdx.x >> 5;
   const uint32_t lt_mask = (1u << lane) - 1u;
@@ -167,7 +227,8 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
   int lref = kEnd;
   uint32_t lcnt = 0;
   int sp = 0;
-  TravStack<STACK, Sink::kCollide> stk;
+  typename StackSel<STACK, Sink::kCollide, KS>::type stk;
+  stack_bind(stk, &s_stk_tr[0][threadIdx.x], &s_stk_c[0][threadIdx.x]);
   uint32_t rid = 0;
   bool active = false;
   bool exhausted = false;
@@ -252,13 +313,10 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
             ref = kEnd;
             break;
           }
-          int far_ref = first1 ? m.x : m.y;
-          stk.put(sp, far_ref, first1 ? c0n : c1n, first1 ? t0 : t1);
+          // (an L2 prefetch of the far child's record here, -1.1 % with the
+          // stack in local memory, cost 1.5 % once the kernels were issue-bound)
+          stk.put(sp, first1 ? m.x : m.y, first1 ? c0n : c1n, first1 ? t0 : t1);
           ++sp;
-          // collide kernels: start the far child's record on its way to L2
-          // now, so that a later pop finds it there (8.4M rays: -1.1 %)
-          if (Sink::kCollide && far_ref >= 0 && (uint32_t)far_ref < Bv.n_int)
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(Bv.nodes + far_ref));
           ref = first1 ? m.y : m.x;
           cnt = first1 ? c1n : c0n;
         } else if (h0) {
@@ -406,12 +464,17 @@ __global__ void __launch_bounds__(kPersistBlock, Sink::kMinBlocks) k_trace_persi
 }
 
 // ---- ray sources and hit sinks -------------------------------------------------
+// The collide kernels load each ray and store each hit once: the
+// cache-streaming forms leave L2 to the tree (8.4M rays, 268 MB of rays and
+// 134 MB of hits against a 93 MB tree: closest-hit step -0.2 %).
+__device__ __forceinline__ float4 ray_load(const float4* p) { return __ldcs(p); }
+__device__ __forceinline__ void hit_store(float4* p, float4 v) { __stcs(p, v); }
 struct BufferSrc {
   const float4* rays;  // 2 float4 per ray: (o, unused), (d, tmax)
   __device__ __forceinline__ uint32_t limit(uint32_t n) const { return n; }
   __device__ __forceinline__ void load(uint32_t i, float4* o, float4* d) const {
-    *o = __ldg(&rays[2 * (size_t)i]);
-    *d = __ldg(&rays[2 * (size_t)i + 1]);
+    *o = ray_load(&rays[2 * (size_t)i]);
+    *d = ray_load(&rays[2 * (size_t)i + 1]);
   }
 };
 // The rays a kernel queued (ShadowQueue): as many as *count says, at most
@@ -429,14 +492,14 @@ struct QueueSrc {
   }
 };
 #ifndef WPBR_COLLIDE_BLOCKS
-#define WPBR_COLLIDE_BLOCKS 12
+#define WPBR_COLLIDE_BLOCKS 8
 #endif
 struct HitSink4 {
   static constexpr int kMinBlocks = WPBR_COLLIDE_BLOCKS;
   static constexpr bool kCollide = true;
   float4* hits;
   __device__ __forceinline__ void store(uint32_t i, const HitRec& h) const {
-    hits[i] = make_float4(h.t, __uint_as_float(h.prim), h.b1, h.b2);
+    hit_store(&hits[i], make_float4(h.t, __uint_as_float(h.prim), h.b1, h.b2));
   }
 };
 // Rays visited in the order of a permutation (sorted position -> input
@@ -447,8 +510,8 @@ struct PermSrc {
   __device__ __forceinline__ uint32_t limit(uint32_t n) const { return n; }
   __device__ __forceinline__ void load(uint32_t i, float4* o, float4* d) const {
     size_t j = __ldg(&perm[i]);
-    *o = __ldg(&rays[2 * j]);
-    *d = __ldg(&rays[2 * j + 1]);
+    *o = ray_load(&rays[2 * j]);
+    *d = ray_load(&rays[2 * j + 1]);
   }
 };
 struct PermHitSink4 {
@@ -457,7 +520,7 @@ struct PermHitSink4 {
   float4* hits;
   const uint32_t* perm;
   __device__ __forceinline__ void store(uint32_t i, const HitRec& h) const {
-    hits[__ldg(&perm[i])] = make_float4(h.t, __uint_as_float(h.prim), h.b1, h.b2);
+    hit_store(&hits[__ldg(&perm[i])], make_float4(h.t, __uint_as_float(h.prim), h.b1, h.b2));
   }
 };
 // The render passes' camera (PrimSink) and shadow-queue (MapSink) traversals
