@@ -1414,12 +1414,74 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
   }
 }
 
+// An SAH node over the two roots in lanes p and p + 1 (warp-uniform call).
+// The centroid bounds' minimum along their longest axis is one root's
+// centroid, which falls in bucket 0, and the other lies at t = 1, bucket 11
+// (both in bucket 0 when the centroids coincide along that axis, or the
+// extent is not finite): every split then has the same two sides, so every
+// cost is the same float and the sequential first-minimum picks split 0 —
+// the root in bucket 0 goes left, which std::partition reaches by swapping
+// the pair when the first root is the one in bucket 11. The bounds, centroid
+// bounds, axis and buckets are computed exactly as the general step does;
+// any other bucket pair returns false and is left to the general step.
+__device__ bool sah_pair(const SahArgs& A, uint32_t p, uint32_t nd, uint32_t N2, uint32_t& item, V3& lo, V3& hi,
+                         uint32_t* sah_axis, float4* nb_lo, float4* nb_hi, uint32_t* child0, uint32_t* child1,
+                         uint32_t* parent) {
+  const uint32_t FULL = 0xFFFFFFFFu, lane = lane_id();
+  const uint32_t it0 = __shfl_sync(FULL, item, p), it1 = __shfl_sync(FULL, item, p + 1);
+  const V3 lo0{__shfl_sync(FULL, lo.x, p), __shfl_sync(FULL, lo.y, p), __shfl_sync(FULL, lo.z, p)};
+  const V3 hi0{__shfl_sync(FULL, hi.x, p), __shfl_sync(FULL, hi.y, p), __shfl_sync(FULL, hi.z, p)};
+  const V3 lo1{__shfl_sync(FULL, lo.x, p + 1), __shfl_sync(FULL, lo.y, p + 1), __shfl_sync(FULL, lo.z, p + 1)};
+  const V3 hi1{__shfl_sync(FULL, hi.x, p + 1), __shfl_sync(FULL, hi.y, p + 1), __shfl_sync(FULL, hi.z, p + 1)};
+  auto emin = [](float a, float b) { return fdec(min(fenc(a), fenc(b))); };
+  auto emax = [](float a, float b) { return fdec(max(fenc(a), fenc(b))); };
+  const Bounds bb{V3{emin(lo0.x, lo1.x), emin(lo0.y, lo1.y), emin(lo0.z, lo1.z)},
+                  V3{emax(hi0.x, hi1.x), emax(hi0.y, hi1.y), emax(hi0.z, hi1.z)}};
+  const V3 c0 = mul(add(lo0, hi0), 0.5f), c1 = mul(add(lo1, hi1), 0.5f);
+  const Bounds cb{V3{emin(c0.x, c1.x), emin(c0.y, c1.y), emin(c0.z, c1.z)},
+                  V3{emax(c0.x, c1.x), emax(c0.y, c1.y), emax(c0.z, c1.z)}};
+  const int dim = bmax_extent(cb);
+  const uint32_t b0 = sah_bucket(lo0, hi0, cb, dim), b1 = sah_bucket(lo1, hi1, cb, dim);
+  bool swap;
+  if (b0 == 0u && (b1 == 11u || b1 == 0u))
+    swap = false;
+  else if (b0 == 11u && b1 == 0u)
+    swap = true;
+  else
+    return false;
+  if (swap) {
+    if (lane == p) {
+      item = it1;
+      lo = lo1;
+      hi = hi1;
+    } else if (lane == p + 1) {
+      item = it0;
+      lo = lo0;
+      hi = hi0;
+    }
+  }
+  if (lane == 0) {
+    const uint32_t me = N2 + nd;
+    sah_axis[nd] = (uint32_t)dim;
+    nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
+    nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
+    const uint32_t r0 = A.troot[swap ? it1 : it0], r1 = A.troot[swap ? it0 : it1];
+    child0[me] = r0;
+    parent[r0] = (me << 1) | 0u;
+    child1[me] = r1;
+    parent[r1] = (me << 1) | 1u;
+  }
+  return true;
+}
+
 // Segments of 2..32 roots: the whole SAH recursion inside one warp. Bounds
 // by warp reductions, buckets by shared-memory atomics, the split decision by
 // warp_sah_split, the two-pointer partition by ballots. Each segment's n - 2
-// new SAH node ids are reserved with one atomic. A persistent grid of warps
-// walks the queue, whose length it reads from *nsmall_p (the cooperative
-// levels fill the queue on the device).
+// new SAH node ids are reserved with one atomic. Nodes over two roots (about
+// half of them) are finished by sah_pair within the step that creates them
+// instead of a step of their own. A persistent grid of warps walks the
+// queue, whose length it reads from *nsmall_p (the cooperative levels fill
+// the queue on the device).
 __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t* sm_start, const uint32_t* sm_end,
                             const uint32_t* sm_node, uint32_t* cur, uint32_t* counters, uint32_t* sah_axis,
                             float4* nb_lo, float4* nb_hi, uint32_t* child0, uint32_t* child1, uint32_t* parent,
@@ -1446,12 +1508,14 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
     id_base = __shfl_sync(FULL, id_base, 0);
     uint32_t* stk = sh_stack[w];
     __syncwarp();
-    if (lane == 0) {
+    int sp = 1;
+    if (n == 2 && sah_pair(A, 0, sm_node[seg], N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent)) {
+      sp = 0;
+    } else if (lane == 0) {
       stk[0] = 0;
       stk[1] = n - 1;
       stk[2] = sm_node[seg];
     }
-    int sp = 1;
     __syncwarp();
     uint32_t guard = 0;
     while (sp > 0) {
@@ -1534,28 +1598,43 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
       uint32_t ln = mid - a, rn = b - mid + 1;
       uint32_t litem = __shfl_sync(FULL, item, a);
       uint32_t ritem = __shfl_sync(FULL, item, b);
+      // the children's node ids (lane 0 keeps the running count); children of
+      // two roots are finished here
+      uint32_t cl = 0, cr = 0;
+      if (lane == 0) {
+        if (ln > 1) cl = id_base + id_next++;
+        if (rn > 1) cr = id_base + id_next++;
+      }
+      cl = __shfl_sync(FULL, cl, 0);
+      cr = __shfl_sync(FULL, cr, 0);
+      const bool lpair =
+          ln == 2 && sah_pair(A, a, cl, N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent);
+      const bool rpair =
+          rn == 2 && sah_pair(A, mid, cr, N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent);
       if (lane == 0) {
         if (ln == 1) {
           uint32_t r = A.troot[litem];
           child0[me] = r;
           parent[r] = (me << 1) | 0u;
         } else {
-          uint32_t cl = id_base + id_next++;
           child0[me] = N2 + cl;
           parent[N2 + cl] = (me << 1) | 0u;
-          stk[3 * sp] = a; stk[3 * sp + 1] = mid - 1; stk[3 * sp + 2] = cl;
-          ++sp;
+          if (!lpair) {
+            stk[3 * sp] = a; stk[3 * sp + 1] = mid - 1; stk[3 * sp + 2] = cl;
+            ++sp;
+          }
         }
         if (rn == 1) {
           uint32_t r = A.troot[ritem];
           child1[me] = r;
           parent[r] = (me << 1) | 1u;
         } else {
-          uint32_t cr = id_base + id_next++;
           child1[me] = N2 + cr;
           parent[N2 + cr] = (me << 1) | 1u;
-          stk[3 * sp] = mid; stk[3 * sp + 1] = b; stk[3 * sp + 2] = cr;
-          ++sp;
+          if (!rpair) {
+            stk[3 * sp] = mid; stk[3 * sp + 1] = b; stk[3 * sp + 2] = cr;
+            ++sp;
+          }
         }
       }
       sp = __shfl_sync(FULL, sp, 0);
