@@ -39,6 +39,9 @@ namespace {
 constexpr uint32_t kTreeletMask = 0b00111111111111000000000000000000u;  // SLBVH.cpp:301
 constexpr int kLeafMax = 30;                                          // SLBVH.cpp:356
 constexpr uint32_t kSmallSeg = 32;
+// Segments of kSmallSeg + 1 .. kMedSeg treelet roots take their SAH levels in
+// one block (k_medium_sah) instead of the cooperative grid.
+constexpr uint32_t kMedSeg = 4096;
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr int kB = 256;
 
@@ -691,7 +694,8 @@ __device__ __forceinline__ uint32_t sah_bucket(const V3& lo, const V3& hi, const
 //       order) or the small-segment queue;
 //   E   the swap: each pair trades places, the next level's position arrays
 //       are written, and single-root children are linked.
-// Segments of 2..32 roots go to the warp-local queue (k_small_sah). A tile is
+// Segments of 33..kMedSeg roots go to the block-local queue (k_medium_sah),
+// segments of 2..32 roots to the warp-local queue (k_small_sah). A tile is
 // kCoopBlock consecutive positions. Every grid barrier is bounded: past the
 // limit the kernel sets the error word and an abort flag, and every block
 // leaves at its next barrier. Indices derived from scanned values are checked
@@ -736,12 +740,15 @@ struct CoopSah {
   unsigned long long* segpre;  // (large << 32 | new-node) children before the segment, within its chunk
   unsigned long long* btot;    // per block: its chunk's flag totals and children totals
   // level words, two sets: [0] large segments, [1] SAH nodes allocated before
-  // the level, [2] small segments queued before the level
+  // the level
   uint32_t* lvl;
   uint32_t* small_start;
   uint32_t* small_end;
   uint32_t* small_node;
-  uint32_t* counters;  // [0] SAH nodes allocated, [2] small segments queued
+  uint32_t* med_start;
+  uint32_t* med_end;
+  uint32_t* med_node;
+  uint32_t* counters;  // [0] SAH nodes allocated, [2] small segments queued, [3] medium segments queued
   uint32_t* root_out;  // unified id of the tree's root
   uint32_t* bar;       // grid barrier: [0] arrivals, [1] generation, [2] abort
   uint32_t* err;
@@ -899,18 +906,23 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
       *C.root_out = T == 1 ? C.troot[0] : kNone;
       C.counters[0] = 0u;
       C.counters[2] = 0u;
+      C.counters[3] = 0u;
     }
     return;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *C.root_out = C.N2;  // SAH node 0
-  if (T <= kSmallSeg) {
+  if (T <= kMedSeg) {  // the root segment is small or medium: no cooperative level
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < T; p += gridDim.x * blockDim.x) C.item[0][p] = p;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-      C.small_start[0] = 0u;
-      C.small_end[0] = T - 1;
-      C.small_node[0] = 0u;
+      uint32_t* st = T <= kSmallSeg ? C.small_start : C.med_start;
+      uint32_t* en = T <= kSmallSeg ? C.small_end : C.med_end;
+      uint32_t* nd = T <= kSmallSeg ? C.small_node : C.med_node;
+      st[0] = 0u;
+      en[0] = T - 1;
+      nd[0] = 0u;
       C.counters[0] = 1u;
-      C.counters[2] = 1u;
+      C.counters[2] = T <= kSmallSeg ? 1u : 0u;
+      C.counters[3] = T <= kSmallSeg ? 0u : 1u;
     }
     return;
   }
@@ -928,7 +940,8 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
     init_segment(C.sacc[0], C.sbk[0]);
     C.lvl[0] = 1u;  // one large segment
     C.lvl[1] = 1u;  // the root is SAH node 0
-    C.lvl[2] = 0u;
+    C.counters[2] = 0u;  // the queues fill by atomics
+    C.counters[3] = 0u;
   }
   if (!coop_sync(C.bar, C.err)) return;
 
@@ -1174,7 +1187,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
             if (p[k] == g.a) {
               const uint32_t ln = g.mid - g.a, rn = g.b - g.mid + 1;
               nn = (uint32_t)(ln >= 2) + (uint32_t)(rn >= 2);
-              nl = (uint32_t)(ln > kSmallSeg) + (uint32_t)(rn > kSmallSeg);
+              nl = (uint32_t)(ln > kMedSeg) + (uint32_t)(rn > kMedSeg);
             }
           }
           v1[k] = ((unsigned long long)fT << 32) | (unsigned long long)fF;
@@ -1232,12 +1245,11 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
     block_scan_pairs(C.btot, gridDim.x, s_bp1, s_bp2, &s_w1[0][0], &s_w2[0][0], s_tot);
     {
       const unsigned long long gtot1 = s_tot[0], gtot2 = s_tot[1];
-      const uint32_t node_base = __ldcg(Lc + 1), small_base = __ldcg(Lc + 2);
+      const uint32_t node_base = __ldcg(Lc + 1);
       if (blockIdx.x == 0 && threadIdx.x == 0) {  // the next level's words
         const uint32_t tot_nn = (uint32_t)(gtot2 & 0xFFFFFFFFull), tot_nl = (uint32_t)(gtot2 >> 32);
         Ln[0] = tot_nl;
         Ln[1] = node_base + tot_nn;
-        Ln[2] = small_base + (tot_nn - tot_nl);
       }
       for (uint32_t base = c0; base < c1; base += kBatch) {
         batch_segments(seg_of, base, c1, nseg, p, s, sl);
@@ -1295,30 +1307,32 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
           C.sah_axis[nd] = (uint32_t)bmax_extent(cb);
           C.nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
           C.nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
-          uint32_t node = node_base + nn_pre, segn = nl_pre, small = small_base + (nn_pre - nl_pre);
+          uint32_t node = node_base + nn_pre, segn = nl_pre;
           uint32_t cseg[2] = {kNone, kNone};
           const uint32_t ca[2] = {a, mid}, cb_[2] = {mid - 1, b}, cn[2] = {ln, rn};
           for (int q = 0; q < 2; ++q) {
             if (cn[q] < 2) continue;  // a single root: linked in phase E
             const uint32_t id = node++;
-            if (id >= T || (cn[q] > kSmallSeg ? segn >= C.maxseg : small >= T)) {
+            // large children stay in the levels; medium and small ones are
+            // queued (in any order: each is finished on its own)
+            const bool large = cn[q] > kMedSeg, med = !large && cn[q] > kSmallSeg;
+            const uint32_t z = large ? segn++ : atomicAdd(C.counters + (med ? 3 : 2), 1u);
+            if (id >= T || z >= (large || med ? C.maxseg : T)) {
               atomicOr(C.err, kErrBuild);
               continue;
             }
             (q ? C.child1 : C.child0)[me] = C.N2 + id;
             C.parent[C.N2 + id] = (me << 1) | (uint32_t)q;
-            if (cn[q] > kSmallSeg) {
-              const uint32_t z = segn++;
+            if (large) {
               cseg[q] = z;
               C.sa[nx][z] = ca[q];
               C.sb[nx][z] = cb_[q];
               C.snode[nx][z] = id;
               init_segment(C.sacc[nx] + (size_t)z * kSegWords, C.sbk[nx] + (size_t)z * kBucketWords);
             } else {
-              const uint32_t z = small++;
-              C.small_start[z] = ca[q];
-              C.small_end[z] = cb_[q];
-              C.small_node[z] = id;
+              (med ? C.med_start : C.small_start)[z] = ca[q];
+              (med ? C.med_end : C.small_end)[z] = cb_[q];
+              (med ? C.med_node : C.small_node)[z] = id;
             }
           }
           C.sdec[sv].z = cseg[0];
@@ -1408,9 +1422,370 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
   if (par == 1u)
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < T; p += gridDim.x * blockDim.x)
       C.item[0][p] = __ldcg(C.item[1] + p);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    C.counters[0] = __ldcg(C.lvl + 8 * par + 1);
-    C.counters[2] = __ldcg(C.lvl + 8 * par + 2);
+  if (blockIdx.x == 0 && threadIdx.x == 0) C.counters[0] = __ldcg(C.lvl + 8 * par + 1);
+}
+
+// ---------------------------------------------------------------------------
+// A8, segments of 33..kMedSeg treelet roots: all their SAH levels in one
+// block, with the segment's positions, bounds and buckets in shared memory and
+// block barriers between the phases. Each level runs the cooperative kernel's
+// phases over every sub-segment of more than 32 roots at once: bounds and
+// centroid bounds (order-preserving encodings, warp-reduced where a warp's
+// positions share a sub-segment), buckets with per-sub-segment bucket counts
+// and bounds, one warp_sah_split per sub-segment, the two-pointer partition
+// of std::partition (the r-th "false" root from the left trades places with
+// the r-th "true" one from the right, ranks from a block scan of the flags),
+// and the children: single roots are linked, sub-segments of 2..32 roots go
+// to the warp-local queue (as global positions), larger ones to the next
+// level. New SAH node ids come from the shared counter; queue order does not
+// matter. The positions are written back for the warp-local pass.
+// ---------------------------------------------------------------------------
+constexpr int kMedBlock = 1024;
+constexpr uint32_t kMedSlots = 128;  // sub-segments of more than 32 roots in one level
+static_assert(kMedSeg / (kSmallSeg + 1) <= kMedSlots, "a level of a medium segment fits the slots");
+static_assert(kMedSeg == 4 * kMedBlock, "the flag scan takes four positions per thread");
+constexpr uint16_t kNoSub = 0xFFFFu;
+// dynamic shared memory layout (bytes)
+constexpr size_t kMedOffIt = 0;                                       // u32 item per position
+constexpr size_t kMedOffPre = kMedOffIt + 4 * kMedSeg;                // u32 flag prefix per position (+1)
+constexpr size_t kMedOffBnd = kMedOffPre + 4 * (kMedSeg + 32);        // f32 lo xyz, hi xyz per position
+constexpr size_t kMedOffAcc = kMedOffBnd + 24 * (size_t)kMedSeg;     // u32 kSegWords per slot
+constexpr size_t kMedOffBk = kMedOffAcc + 4 * kMedSlots * kSegWords;  // u32 kBucketWords per slot
+constexpr size_t kMedOffTab = kMedOffBk + 4 * kMedSlots * kBucketWords;  // u32 slot tables
+constexpr int kMedTabs = 13;
+constexpr size_t kMedOffPos = kMedOffTab + 4 * kMedTabs * kMedSlots;  // u16 posF, posT
+constexpr size_t kMedOffSid = kMedOffPos + 4 * (size_t)kMedSeg;      // u16 sub-segment per position
+constexpr size_t kMedOffBkt = kMedOffSid + 2 * (size_t)kMedSeg;      // u8 bucket per position
+constexpr size_t kMedOffMisc = kMedOffBkt + kMedSeg;                   // u32 warp sums, counters
+constexpr size_t kMedSmem = kMedOffMisc + 4 * 64;
+static_assert(kMedSmem <= 227 * 1024, "the medium SAH's shared memory fits one block");
+
+struct MedArgs {
+  uint32_t N, N2;
+  const uint32_t* troot;
+  float4* nb_lo;
+  float4* nb_hi;
+  uint32_t* child0;
+  uint32_t* child1;
+  uint32_t* parent;
+  uint32_t* sah_axis;
+  uint32_t* cur;  // positions after the cooperative levels
+  const uint32_t* med_start;
+  const uint32_t* med_end;
+  const uint32_t* med_node;
+  uint32_t* small_start;
+  uint32_t* small_end;
+  uint32_t* small_node;
+  uint32_t* counters;  // [0] SAH nodes allocated, [2] small segments queued, [3] medium segments queued
+  uint32_t* err;
+};
+
+__global__ void __launch_bounds__(kMedBlock, 1) k_medium_sah(MedArgs M) {
+  extern __shared__ __align__(16) unsigned char s_med[];
+  uint32_t* s_it = (uint32_t*)(s_med + kMedOffIt);
+  uint32_t* s_pre = (uint32_t*)(s_med + kMedOffPre);
+  float* s_bnd = (float*)(s_med + kMedOffBnd);  // [6][kMedSeg]
+  uint32_t* s_acc = (uint32_t*)(s_med + kMedOffAcc);
+  uint32_t* s_bkc = (uint32_t*)(s_med + kMedOffBk);
+  uint32_t* tab = (uint32_t*)(s_med + kMedOffTab);
+  uint32_t* s_sa = tab;
+  uint32_t* s_sb = tab + kMedSlots;
+  uint32_t* s_snode = tab + 2 * kMedSlots;
+  uint32_t* s_best = tab + 3 * kMedSlots;
+  uint32_t* s_spt = tab + 4 * kMedSlots;
+  uint32_t* s_mid = tab + 5 * kMedSlots;
+  uint32_t* s_nsw = tab + 6 * kMedSlots;  // pairs that trade places
+  uint32_t* s_cl = tab + 7 * kMedSlots;   // next-level slot of each child (kNone: not large)
+  uint32_t* s_cr = tab + 8 * kMedSlots;
+  uint32_t* s_na = tab + 9 * kMedSlots;   // next level's slots
+  uint32_t* s_nb = tab + 10 * kMedSlots;
+  uint32_t* s_nnode = tab + 11 * kMedSlots;
+  uint32_t* s_dim = tab + 12 * kMedSlots;
+  uint16_t* s_posF = (uint16_t*)(s_med + kMedOffPos);
+  uint16_t* s_posT = s_posF + kMedSeg;
+  uint16_t* s_sid = (uint16_t*)(s_med + kMedOffSid);
+  uint8_t* s_bkt = (uint8_t*)(s_med + kMedOffBkt);
+  uint32_t* s_misc = (uint32_t*)(s_med + kMedOffMisc);  // [0..31] warp sums, [32] active, [33] next active
+  const uint32_t FULL = 0xFFFFFFFFu;
+  const uint32_t t = threadIdx.x, lane = lane_id(), wid = t >> 5;
+  const uint32_t nmed = M.counters[3];
+  for (uint32_t seg = blockIdx.x; seg < nmed; seg += gridDim.x) {
+    const uint32_t start = M.med_start[seg], end = M.med_end[seg];
+    const uint32_t n = end - start + 1;
+    if (end < start || end >= M.N || n <= kSmallSeg || n > kMedSeg) {  // block-uniform
+      if (t == 0) atomicOr(M.err, kErrBuild);
+      continue;
+    }
+    for (uint32_t i = t; i < n; i += kMedBlock) {
+      const uint32_t it = M.cur[start + i];
+      const uint32_t r = M.troot[it];
+      const float4 l = M.nb_lo[r], h = M.nb_hi[r];
+      s_it[i] = it;
+      s_bnd[i] = l.x;
+      s_bnd[kMedSeg + i] = l.y;
+      s_bnd[2 * kMedSeg + i] = l.z;
+      s_bnd[3 * kMedSeg + i] = h.x;
+      s_bnd[4 * kMedSeg + i] = h.y;
+      s_bnd[5 * kMedSeg + i] = h.z;
+      s_sid[i] = 0;
+    }
+    if (t == 0) {
+      s_sa[0] = 0;
+      s_sb[0] = n - 1;
+      s_snode[0] = M.med_node[seg];
+      s_misc[32] = 1;
+    }
+    __syncthreads();
+    const uint32_t nw = div_up_d(n, 32) * 32;  // positions rounded up to whole warps
+    for (uint32_t level = 0;; ++level) {
+      const uint32_t nact = s_misc[32];
+      if (nact == 0) break;
+      if (level > kMedSeg || nact > kMedSlots) {  // block-uniform
+        if (t == 0) atomicOr(M.err, level > kMedSeg ? kErrLoopLimit : kErrBuild);
+        break;
+      }
+      for (uint32_t k = t; k < nact * kSegWords; k += kMedBlock)
+        s_acc[k] = (((k % kSegWords) / 3) % 2 == 0) ? 0xFFFFFFFFu : 0u;
+      for (uint32_t k = t; k < nact * kBucketWords; k += kMedBlock)
+        s_bkc[k] = (k % 7 == 0) ? 0u : ((k % 7) <= 3 ? 0xFFFFFFFFu : 0u);
+      if (t == 0) s_misc[33] = 0;
+      __syncthreads();
+      // A: bounds and centroid bounds of every sub-segment
+      for (uint32_t i = t; i < nw; i += kMedBlock) {
+        const uint32_t sk = i < n ? (uint32_t)s_sid[i] : (uint32_t)kNoSub;
+        uint32_t e[12];
+        if (sk != kNoSub) {
+          const V3 lo{s_bnd[i], s_bnd[kMedSeg + i], s_bnd[2 * kMedSeg + i]};
+          const V3 hi{s_bnd[3 * kMedSeg + i], s_bnd[4 * kMedSeg + i], s_bnd[5 * kMedSeg + i]};
+          const V3 c = mul(add(lo, hi), 0.5f);
+          e[0] = fenc(lo.x); e[1] = fenc(lo.y); e[2] = fenc(lo.z);
+          e[3] = fenc(hi.x); e[4] = fenc(hi.y); e[5] = fenc(hi.z);
+          e[6] = fenc(c.x); e[7] = fenc(c.y); e[8] = fenc(c.z);
+          e[9] = e[6]; e[10] = e[7]; e[11] = e[8];
+        } else {
+#pragma unroll
+          for (int q = 0; q < 12; ++q) e[q] = ((q / 3) % 2 == 0) ? 0xFFFFFFFFu : 0u;
+        }
+        const uint32_t s0 = __shfl_sync(FULL, sk, 0);
+        if (s0 != kNoSub && __all_sync(FULL, sk == s0)) {  // one sub-segment across the warp
+#pragma unroll
+          for (int q = 0; q < 12; ++q)
+            e[q] = ((q / 3) % 2 == 0) ? __reduce_min_sync(FULL, e[q]) : __reduce_max_sync(FULL, e[q]);
+          if (lane == 0) {
+            uint32_t* r = s_acc + s0 * kSegWords;
+            for (int q = 0; q < 12; ++q) {
+              if ((q / 3) % 2 == 0)
+                atomicMin(r + q, e[q]);
+              else
+                atomicMax(r + q, e[q]);
+            }
+          }
+        } else if (sk != kNoSub) {
+          uint32_t* r = s_acc + sk * kSegWords;
+          for (int q = 0; q < 12; ++q) {
+            if ((q / 3) % 2 == 0)
+              atomicMin(r + q, e[q]);
+            else
+              atomicMax(r + q, e[q]);
+          }
+        }
+      }
+      __syncthreads();
+      for (uint32_t j = t; j < nact; j += kMedBlock) s_dim[j] = (uint32_t)bmax_extent(dec_bounds(s_acc + j * kSegWords + 6));
+      __syncthreads();
+      // B: buckets, bucket counts and bounds
+      for (uint32_t i = t; i < n; i += kMedBlock) {
+        const uint32_t sk = s_sid[i];
+        if (sk == kNoSub) continue;
+        const V3 lo{s_bnd[i], s_bnd[kMedSeg + i], s_bnd[2 * kMedSeg + i]};
+        const V3 hi{s_bnd[3 * kMedSeg + i], s_bnd[4 * kMedSeg + i], s_bnd[5 * kMedSeg + i]};
+        const Bounds cb = dec_bounds(s_acc + sk * kSegWords + 6);
+        const uint32_t ib = sah_bucket(lo, hi, cb, (int)s_dim[sk]);
+        s_bkt[i] = (uint8_t)ib;
+        uint32_t* d = s_bkc + sk * kBucketWords + ib * 7;
+        atomicAdd(d, 1u);
+        atomicMin(d + 1, fenc(lo.x));
+        atomicMin(d + 2, fenc(lo.y));
+        atomicMin(d + 3, fenc(lo.z));
+        atomicMax(d + 4, fenc(hi.x));
+        atomicMax(d + 5, fenc(hi.y));
+        atomicMax(d + 6, fenc(hi.z));
+      }
+      __syncthreads();
+      // C: one decision per sub-segment, one warp each
+      for (uint32_t j = wid; j < nact; j += kMedBlock / 32) {
+        const uint32_t* bk = s_bkc + j * kBucketWords;
+        uint32_t cj = 0;
+        Bounds bj = bempty();
+        if (lane < 12) {
+          cj = bk[lane * 7];
+          if (cj) bj = dec_bounds(bk + lane * 7 + 1);
+        }
+        const Bounds bb = dec_bounds(s_acc + j * kSegWords);
+        uint32_t kv;
+        const int bv = warp_sah_split(cj, bj, barea(bb), &kv);
+        if (lane == 0) {
+          const uint32_t a = s_sa[j], b = s_sb[j], cnt = b - a + 1;
+          s_best[j] = (uint32_t)bv;
+          s_spt[j] = a + kv;
+          s_mid[j] = (kv == cnt) ? a + cnt / 2 : a + kv;
+        }
+      }
+      __syncthreads();
+      // partition flags, block scan of (true << 16 | false) over positions
+      // 4t .. 4t + 3
+      {
+        uint32_t v[4], sum = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const uint32_t i = 4 * t + q;
+          v[q] = 0;
+          if (i < n) {
+            const uint32_t sk = s_sid[i];
+            if (sk != kNoSub) {
+              const bool pred = s_bkt[i] <= s_best[sk];
+              const uint32_t spt = s_spt[sk];
+              v[q] = (i < spt && !pred) ? 1u : ((i >= spt && pred) ? (1u << 16) : 0u);
+            }
+          }
+          sum += v[q];
+        }
+        uint32_t x = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(FULL, x, o);
+          if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) s_misc[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+          const uint32_t ws = s_misc[lane];
+          uint32_t y = ws;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t z = __shfl_up_sync(FULL, y, o);
+            if (lane >= (uint32_t)o) y += z;
+          }
+          s_misc[lane] = y - ws;
+        }
+        __syncthreads();
+        uint32_t run = s_misc[wid] + x - sum;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const uint32_t i = 4 * t + q;
+          if (i <= n) s_pre[i] = run;  // s_pre[n]: the total
+          run += v[q];
+        }
+        if (t == kMedBlock - 1) s_pre[4 * kMedBlock] = run;  // the total when n = 4 * kMedBlock
+      }
+      __syncthreads();
+      // select tables: the r-th false from the left and the r-th true from
+      // the right of each sub-segment
+      for (uint32_t i = t; i < n; i += kMedBlock) {
+        const uint32_t sk = s_sid[i];
+        if (sk == kNoSub) continue;
+        const uint32_t a = s_sa[sk], b = s_sb[sk], spt = s_spt[sk];
+        const bool pred = s_bkt[i] <= s_best[sk];
+        if (i < spt && !pred) {
+          const uint32_t r = (s_pre[i] & 0xFFFFu) - (s_pre[a] & 0xFFFFu);
+          if (a + r <= b) s_posF[a + r] = (uint16_t)i;
+        } else if (i >= spt && pred) {
+          const uint32_t r = (s_pre[b + 1] >> 16) - (s_pre[i] >> 16) - 1u;
+          if (a + r <= b) s_posT[a + r] = (uint16_t)i;
+        }
+      }
+      for (uint32_t j = t; j < nact; j += kMedBlock) {
+        const uint32_t a = s_sa[j], b = s_sb[j];
+        const uint32_t nf = (s_pre[b + 1] & 0xFFFFu) - (s_pre[a] & 0xFFFFu);
+        const uint32_t nt = (s_pre[b + 1] >> 16) - (s_pre[a] >> 16);
+        if (nf != nt) atomicOr(M.err, kErrBuild);
+        s_nsw[j] = min(nf, nt);
+      }
+      __syncthreads();
+      // E: the pairs trade places
+      for (uint32_t k = t; k < n; k += kMedBlock) {
+        const uint32_t sk = s_sid[k];
+        if (sk == kNoSub) continue;
+        const uint32_t r = k - s_sa[sk];
+        if (r >= s_nsw[sk]) continue;
+        const uint32_t pf = s_posF[k], pt = s_posT[k];
+        if (pf >= n || pt >= n) {
+          atomicOr(M.err, kErrBuild);
+          continue;
+        }
+        const uint32_t ti = s_it[pf];
+        s_it[pf] = s_it[pt];
+        s_it[pt] = ti;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          const float f = s_bnd[q * kMedSeg + pf];
+          s_bnd[q * kMedSeg + pf] = s_bnd[q * kMedSeg + pt];
+          s_bnd[q * kMedSeg + pt] = f;
+        }
+      }
+      __syncthreads();
+      // the sub-segments' SAH nodes and their children
+      for (uint32_t j = t; j < nact; j += kMedBlock) {
+        const uint32_t a = s_sa[j], b = s_sb[j], mid = s_mid[j];
+        const uint32_t nd = s_snode[j], me = M.N2 + nd;
+        const Bounds bb = dec_bounds(s_acc + j * kSegWords);
+        M.sah_axis[nd] = s_dim[j];
+        M.nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
+        M.nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
+        const uint32_t ca[2] = {a, mid}, ce[2] = {mid - 1, b};
+        uint32_t slot[2] = {kNone, kNone};
+        for (int q = 0; q < 2; ++q) {
+          const uint32_t cn = ce[q] + 1 - ca[q];
+          uint32_t* cref = q ? M.child1 : M.child0;
+          if (cn == 1) {
+            const uint32_t r = M.troot[s_it[ca[q]]];
+            cref[me] = r;
+            M.parent[r] = (me << 1) | (uint32_t)q;
+            continue;
+          }
+          const uint32_t id = atomicAdd(M.counters, 1u);
+          const bool large = cn > kSmallSeg;
+          const uint32_t z = large ? atomicAdd(s_misc + 33, 1u) : atomicAdd(M.counters + 2, 1u);
+          if (id >= M.N || z >= (large ? kMedSlots : M.N)) {
+            atomicOr(M.err, kErrBuild);
+            continue;
+          }
+          cref[me] = M.N2 + id;
+          M.parent[M.N2 + id] = (me << 1) | (uint32_t)q;
+          if (large) {
+            s_na[z] = ca[q];
+            s_nb[z] = ce[q];
+            s_nnode[z] = id;
+            slot[q] = z;
+          } else {
+            M.small_start[z] = start + ca[q];
+            M.small_end[z] = start + ce[q];
+            M.small_node[z] = id;
+          }
+        }
+        s_cl[j] = slot[0];
+        s_cr[j] = slot[1];
+      }
+      __syncthreads();
+      // the next level's sub-segment of every position, and its slots
+      for (uint32_t k = t; k < n; k += kMedBlock) {
+        const uint32_t sk = s_sid[k];
+        if (sk == kNoSub) continue;
+        const uint32_t z = k < s_mid[sk] ? s_cl[sk] : s_cr[sk];
+        s_sid[k] = z < kMedSlots ? (uint16_t)z : kNoSub;
+      }
+      __syncthreads();
+      const uint32_t nnext = s_misc[33];
+      for (uint32_t j = t; j < nnext && j < kMedSlots; j += kMedBlock) {
+        s_sa[j] = s_na[j];
+        s_sb[j] = s_nb[j];
+        s_snode[j] = s_nnode[j];
+      }
+      if (t == 0) s_misc[32] = min(nnext, kMedSlots);
+      __syncthreads();
+    }
+    for (uint32_t i = t; i < n; i += kMedBlock) M.cur[start + i] = s_it[i];
+    __syncthreads();
   }
 }
 
@@ -2121,6 +2496,9 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   WPBR_CUDA(B.chunk_tot.ensure(2 * (size_t)kMaxCoopGrid));
   WPBR_CUDA(B.lvl.ensure(16));
   WPBR_CUDA(B.bar.ensure(4));
+  WPBR_CUDA(B.med_start.ensure(maxseg));
+  WPBR_CUDA(B.med_end.ensure(maxseg));
+  WPBR_CUDA(B.med_node.ensure(maxseg));
   WPBR_CUDA(B.small_start.ensure(N));
   WPBR_CUDA(B.small_end.ensure(N));
   WPBR_CUDA(B.small_node.ensure(N));
@@ -2234,6 +2612,9 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
     C.small_start = B.small_start.p;
     C.small_end = B.small_end.p;
     C.small_node = B.small_node.p;
+    C.med_start = B.med_start.p;
+    C.med_end = B.med_end.p;
+    C.med_node = B.med_node.p;
     C.counters = B.counters.p;
     C.root_out = B.dinfo.p + kInfoRoot;
     C.bar = B.bar.p;
@@ -2241,6 +2622,12 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
     void* args[] = {&C};
     WPBR_CUDA(cudaLaunchCooperativeKernel((const void*)k_sah_levels, dim3((unsigned)(per_sm * sms)),
                                           dim3(kCoopBlock), args, 0, st));
+    WPBR_CUDA(cudaFuncSetAttribute((const void*)k_medium_sah, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kMedSmem));
+    MedArgs Md{N, N2, B.troot.p, B.nb_lo.p, B.nb_hi.p, B.child0.p, B.child1.p, B.parent.p, B.sah_axis.p, B.cur.p,
+               B.med_start.p, B.med_end.p, B.med_node.p, B.small_start.p, B.small_end.p, B.small_node.p,
+               B.counters.p, ctx->d_err.p};
+    k_medium_sah<<<(unsigned)sms, kMedBlock, kMedSmem, st>>>(Md);
     SahArgs A{N, B.troot.p, B.nb_lo.p, B.nb_hi.p};
     k_small_sah<<<persistent_grid((const void*)k_small_sah, kB), kB, 0, st>>>(
         A, B.counters.p + 2, B.small_start.p, B.small_end.p, B.small_node.p, B.cur.p, B.counters.p, B.sah_axis.p,
