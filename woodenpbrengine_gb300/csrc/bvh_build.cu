@@ -41,7 +41,12 @@ constexpr int kLeafMax = 30;                                          // SLBVH.c
 constexpr uint32_t kSmallSeg = 32;
 // Segments of kSmallSeg + 1 .. kMedSeg treelet roots take their SAH levels in
 // one block (k_medium_sah) instead of the cooperative grid.
-constexpr uint32_t kMedSeg = 4096;
+// 1.31M-triangle build, device ms: 1024 1.775 (4 blocks of 256 per SM),
+// 2048 1.718 (2 of 512), 4096 1.691 (1 of 1024).
+#ifndef WPBR_MED_SEG
+#define WPBR_MED_SEG 4096
+#endif
+constexpr uint32_t kMedSeg = WPBR_MED_SEG;
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr int kB = 256;
 
@@ -576,6 +581,7 @@ struct SahArgs {
   const uint32_t* troot;
   const float4* nb_lo;
   const float4* nb_hi;
+  uint32_t* sah_rng;  // per SAH node: its first final position and one past its last
 };
 
 __device__ __forceinline__ void item_bounds(const SahArgs& A, uint32_t item, V3* lo, V3* hi) {
@@ -719,6 +725,7 @@ struct CoopSah {
   uint32_t* child1;
   uint32_t* parent;
   uint32_t* sah_axis;
+  uint32_t* sah_rng;  // per SAH node: first position, one past the last (positions of a segment never change)
   // per position (two buffers each, swapped every level)
   uint32_t* item[2];
   uint32_t* seg_of[2];
@@ -907,6 +914,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
       C.counters[0] = 0u;
       C.counters[2] = 0u;
       C.counters[3] = 0u;
+      C.counters[4] = 0u;
     }
     return;
   }
@@ -923,6 +931,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
       C.counters[0] = 1u;
       C.counters[2] = T <= kSmallSeg ? 1u : 0u;
       C.counters[3] = T <= kSmallSeg ? 0u : 1u;
+      C.counters[4] = 0u;
     }
     return;
   }
@@ -942,6 +951,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
     C.lvl[1] = 1u;  // the root is SAH node 0
     C.counters[2] = 0u;  // the queues fill by atomics
     C.counters[3] = 0u;
+    C.counters[4] = 0u;
   }
   if (!coop_sync(C.bar, C.err)) return;
 
@@ -1305,6 +1315,8 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
           Bounds bb = dec_bounds_cg(sacc + (size_t)sv * kSegWords);
           Bounds cb = dec_bounds_cg(sacc + (size_t)sv * kSegWords + 6);
           C.sah_axis[nd] = (uint32_t)bmax_extent(cb);
+          C.sah_rng[2 * nd] = a;
+          C.sah_rng[2 * nd + 1] = b + 1;
           C.nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
           C.nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
           uint32_t node = node_base + nn_pre, segn = nl_pre;
@@ -1440,8 +1452,9 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
 // level. New SAH node ids come from the shared counter; queue order does not
 // matter. The positions are written back for the warp-local pass.
 // ---------------------------------------------------------------------------
-constexpr int kMedBlock = 1024;
-constexpr uint32_t kMedSlots = 128;  // sub-segments of more than 32 roots in one level
+constexpr int kMedBlock = (int)kMedSeg / 4;
+constexpr uint32_t kMedSlots = kMedSeg / 32;  // sub-segments of more than 32 roots in one level
+constexpr int kMedPerSM = 4096 / (int)kMedSeg;  // resident blocks per SM (shared memory)
 static_assert(kMedSeg / (kSmallSeg + 1) <= kMedSlots, "a level of a medium segment fits the slots");
 static_assert(kMedSeg == 4 * kMedBlock, "the flag scan takes four positions per thread");
 constexpr uint16_t kNoSub = 0xFFFFu;
@@ -1452,13 +1465,13 @@ constexpr size_t kMedOffBnd = kMedOffPre + 4 * (kMedSeg + 32);        // f32 lo 
 constexpr size_t kMedOffAcc = kMedOffBnd + 24 * (size_t)kMedSeg;     // u32 kSegWords per slot
 constexpr size_t kMedOffBk = kMedOffAcc + 4 * kMedSlots * kSegWords;  // u32 kBucketWords per slot
 constexpr size_t kMedOffTab = kMedOffBk + 4 * kMedSlots * kBucketWords;  // u32 slot tables
-constexpr int kMedTabs = 13;
+constexpr int kMedTabs = 12;
 constexpr size_t kMedOffPos = kMedOffTab + 4 * kMedTabs * kMedSlots;  // u16 posF, posT
 constexpr size_t kMedOffSid = kMedOffPos + 4 * (size_t)kMedSeg;      // u16 sub-segment per position
 constexpr size_t kMedOffBkt = kMedOffSid + 2 * (size_t)kMedSeg;      // u8 bucket per position
 constexpr size_t kMedOffMisc = kMedOffBkt + kMedSeg;                   // u32 warp sums, counters
 constexpr size_t kMedSmem = kMedOffMisc + 4 * 64;
-static_assert(kMedSmem <= 227 * 1024, "the medium SAH's shared memory fits one block");
+static_assert(kMedPerSM * (kMedSmem + 1024) <= 228 * 1024, "the medium SAH blocks fit one SM");
 
 struct MedArgs {
   uint32_t N, N2;
@@ -1469,6 +1482,7 @@ struct MedArgs {
   uint32_t* child1;
   uint32_t* parent;
   uint32_t* sah_axis;
+  uint32_t* sah_rng;
   uint32_t* cur;  // positions after the cooperative levels
   const uint32_t* med_start;
   const uint32_t* med_end;
@@ -1476,11 +1490,12 @@ struct MedArgs {
   uint32_t* small_start;
   uint32_t* small_end;
   uint32_t* small_node;
-  uint32_t* counters;  // [0] SAH nodes allocated, [2] small segments queued, [3] medium segments queued
+  uint32_t* counters;  // [0] SAH nodes allocated, [2] small segments queued, [3] medium segments queued,
+                       // [4] medium segments taken
   uint32_t* err;
 };
 
-__global__ void __launch_bounds__(kMedBlock, 1) k_medium_sah(MedArgs M) {
+__global__ void __launch_bounds__(kMedBlock, kMedPerSM) k_medium_sah(MedArgs M) {
   extern __shared__ __align__(16) unsigned char s_med[];
   uint32_t* s_it = (uint32_t*)(s_med + kMedOffIt);
   uint32_t* s_pre = (uint32_t*)(s_med + kMedOffPre);
@@ -1500,7 +1515,6 @@ __global__ void __launch_bounds__(kMedBlock, 1) k_medium_sah(MedArgs M) {
   uint32_t* s_na = tab + 9 * kMedSlots;   // next level's slots
   uint32_t* s_nb = tab + 10 * kMedSlots;
   uint32_t* s_nnode = tab + 11 * kMedSlots;
-  uint32_t* s_dim = tab + 12 * kMedSlots;
   uint16_t* s_posF = (uint16_t*)(s_med + kMedOffPos);
   uint16_t* s_posT = s_posF + kMedSeg;
   uint16_t* s_sid = (uint16_t*)(s_med + kMedOffSid);
@@ -1509,7 +1523,14 @@ __global__ void __launch_bounds__(kMedBlock, 1) k_medium_sah(MedArgs M) {
   const uint32_t FULL = 0xFFFFFFFFu;
   const uint32_t t = threadIdx.x, lane = lane_id(), wid = t >> 5;
   const uint32_t nmed = M.counters[3];
-  for (uint32_t seg = blockIdx.x; seg < nmed; seg += gridDim.x) {
+  for (;;) {
+    // segments taken in turn from a counter, so that blocks that drew small
+    // segments take more (the barrier first: every thread has read the last one)
+    __syncthreads();
+    if (t == 0) s_misc[38] = atomicAdd(M.counters + 4, 1u);
+    __syncthreads();
+    const uint32_t seg = s_misc[38];
+    if (seg >= nmed) break;  // block-uniform
     const uint32_t start = M.med_start[seg], end = M.med_end[seg];
     const uint32_t n = end - start + 1;
     if (end < start || end >= M.N || n <= kSmallSeg || n > kMedSeg) {  // block-uniform
@@ -1535,6 +1556,10 @@ __global__ void __launch_bounds__(kMedBlock, 1) k_medium_sah(MedArgs M) {
       s_snode[0] = M.med_node[seg];
       s_misc[32] = 1;
     }
+    // the accumulators of a level's slots are reset by the phase before it
+    for (uint32_t k = t; k < kSegWords; k += kMedBlock) s_acc[k] = (((k % kSegWords) / 3) % 2 == 0) ? 0xFFFFFFFFu : 0u;
+    for (uint32_t k = t; k < kBucketWords; k += kMedBlock)
+      s_bkc[k] = (k % 7 == 0) ? 0u : ((k % 7) <= 3 ? 0xFFFFFFFFu : 0u);
     __syncthreads();
     const uint32_t nw = div_up_d(n, 32) * 32;  // positions rounded up to whole warps
     for (uint32_t level = 0;; ++level) {
@@ -1544,12 +1569,6 @@ __global__ void __launch_bounds__(kMedBlock, 1) k_medium_sah(MedArgs M) {
         if (t == 0) atomicOr(M.err, level > kMedSeg ? kErrLoopLimit : kErrBuild);
         break;
       }
-      for (uint32_t k = t; k < nact * kSegWords; k += kMedBlock)
-        s_acc[k] = (((k % kSegWords) / 3) % 2 == 0) ? 0xFFFFFFFFu : 0u;
-      for (uint32_t k = t; k < nact * kBucketWords; k += kMedBlock)
-        s_bkc[k] = (k % 7 == 0) ? 0u : ((k % 7) <= 3 ? 0xFFFFFFFFu : 0u);
-      if (t == 0) s_misc[33] = 0;
-      __syncthreads();
       // A: bounds and centroid bounds of every sub-segment
       for (uint32_t i = t; i < nw; i += kMedBlock) {
         const uint32_t sk = i < n ? (uint32_t)s_sid[i] : (uint32_t)kNoSub;
@@ -1591,8 +1610,6 @@ __global__ void __launch_bounds__(kMedBlock, 1) k_medium_sah(MedArgs M) {
         }
       }
       __syncthreads();
-      for (uint32_t j = t; j < nact; j += kMedBlock) s_dim[j] = (uint32_t)bmax_extent(dec_bounds(s_acc + j * kSegWords + 6));
-      __syncthreads();
       // B: buckets, bucket counts and bounds
       for (uint32_t i = t; i < n; i += kMedBlock) {
         const uint32_t sk = s_sid[i];
@@ -1600,7 +1617,7 @@ __global__ void __launch_bounds__(kMedBlock, 1) k_medium_sah(MedArgs M) {
         const V3 lo{s_bnd[i], s_bnd[kMedSeg + i], s_bnd[2 * kMedSeg + i]};
         const V3 hi{s_bnd[3 * kMedSeg + i], s_bnd[4 * kMedSeg + i], s_bnd[5 * kMedSeg + i]};
         const Bounds cb = dec_bounds(s_acc + sk * kSegWords + 6);
-        const uint32_t ib = sah_bucket(lo, hi, cb, (int)s_dim[sk]);
+        const uint32_t ib = sah_bucket(lo, hi, cb, bmax_extent(cb));
         s_bkt[i] = (uint8_t)ib;
         uint32_t* d = s_bkc + sk * kBucketWords + ib * 7;
         atomicAdd(d, 1u);
@@ -1613,6 +1630,7 @@ __global__ void __launch_bounds__(kMedBlock, 1) k_medium_sah(MedArgs M) {
       }
       __syncthreads();
       // C: one decision per sub-segment, one warp each
+      if (t == 0) s_misc[33] = 0;  // the next level's slots (counted by the children phase)
       for (uint32_t j = wid; j < nact; j += kMedBlock / 32) {
         const uint32_t* bk = s_bkc + j * kBucketWords;
         uint32_t cj = 0;
@@ -1724,28 +1742,34 @@ __global__ void __launch_bounds__(kMedBlock, 1) k_medium_sah(MedArgs M) {
         }
       }
       __syncthreads();
-      // the sub-segments' SAH nodes and their children
+      // the sub-segments' SAH nodes and their children (one reservation of
+      // SAH node ids and one of warp-local queue entries per sub-segment)
       for (uint32_t j = t; j < nact; j += kMedBlock) {
         const uint32_t a = s_sa[j], b = s_sb[j], mid = s_mid[j];
         const uint32_t nd = s_snode[j], me = M.N2 + nd;
         const Bounds bb = dec_bounds(s_acc + j * kSegWords);
-        M.sah_axis[nd] = s_dim[j];
+        M.sah_axis[nd] = (uint32_t)bmax_extent(dec_bounds(s_acc + j * kSegWords + 6));
+        M.sah_rng[2 * nd] = start + a;
+        M.sah_rng[2 * nd + 1] = start + b + 1;
         M.nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
         M.nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
-        const uint32_t ca[2] = {a, mid}, ce[2] = {mid - 1, b};
-        uint32_t slot[2] = {kNone, kNone};
+        const uint32_t ca[2] = {a, mid}, ce[2] = {mid - 1, b}, cn[2] = {mid - a, b - mid + 1};
+        const uint32_t nids = (uint32_t)(cn[0] >= 2) + (uint32_t)(cn[1] >= 2);
+        const uint32_t nsm = (uint32_t)(cn[0] >= 2 && cn[0] <= kSmallSeg) + (uint32_t)(cn[1] >= 2 && cn[1] <= kSmallSeg);
+        const uint32_t id0 = nids ? atomicAdd(M.counters, nids) : 0u;
+        const uint32_t q0 = nsm ? atomicAdd(M.counters + 2, nsm) : 0u;
+        uint32_t nid = 0, nq = 0, slot[2] = {kNone, kNone};
         for (int q = 0; q < 2; ++q) {
-          const uint32_t cn = ce[q] + 1 - ca[q];
           uint32_t* cref = q ? M.child1 : M.child0;
-          if (cn == 1) {
+          if (cn[q] == 1) {
             const uint32_t r = M.troot[s_it[ca[q]]];
             cref[me] = r;
             M.parent[r] = (me << 1) | (uint32_t)q;
             continue;
           }
-          const uint32_t id = atomicAdd(M.counters, 1u);
-          const bool large = cn > kSmallSeg;
-          const uint32_t z = large ? atomicAdd(s_misc + 33, 1u) : atomicAdd(M.counters + 2, 1u);
+          const uint32_t id = id0 + nid++;
+          const bool large = cn[q] > kSmallSeg;
+          const uint32_t z = large ? atomicAdd(s_misc + 33, 1u) : q0 + nq++;
           if (id >= M.N || z >= (large ? kMedSlots : M.N)) {
             atomicOr(M.err, kErrBuild);
             continue;
@@ -1767,6 +1791,12 @@ __global__ void __launch_bounds__(kMedBlock, 1) k_medium_sah(MedArgs M) {
         s_cr[j] = slot[1];
       }
       __syncthreads();
+      const uint32_t nnext = min(s_misc[33], kMedSlots);
+      // the next level's accumulators
+      for (uint32_t k = t; k < nnext * kSegWords; k += kMedBlock)
+        s_acc[k] = (((k % kSegWords) / 3) % 2 == 0) ? 0xFFFFFFFFu : 0u;
+      for (uint32_t k = t; k < nnext * kBucketWords; k += kMedBlock)
+        s_bkc[k] = (k % 7 == 0) ? 0u : ((k % 7) <= 3 ? 0xFFFFFFFFu : 0u);
       // the next level's sub-segment of every position, and its slots
       for (uint32_t k = t; k < n; k += kMedBlock) {
         const uint32_t sk = s_sid[k];
@@ -1774,14 +1804,12 @@ __global__ void __launch_bounds__(kMedBlock, 1) k_medium_sah(MedArgs M) {
         const uint32_t z = k < s_mid[sk] ? s_cl[sk] : s_cr[sk];
         s_sid[k] = z < kMedSlots ? (uint16_t)z : kNoSub;
       }
-      __syncthreads();
-      const uint32_t nnext = s_misc[33];
-      for (uint32_t j = t; j < nnext && j < kMedSlots; j += kMedBlock) {
+      for (uint32_t j = t; j < nnext; j += kMedBlock) {
         s_sa[j] = s_na[j];
         s_sb[j] = s_nb[j];
         s_snode[j] = s_nnode[j];
       }
-      if (t == 0) s_misc[32] = min(nnext, kMedSlots);
+      if (t == 0) s_misc[32] = nnext;
       __syncthreads();
     }
     for (uint32_t i = t; i < n; i += kMedBlock) M.cur[start + i] = s_it[i];
@@ -1799,7 +1827,7 @@ __global__ void __launch_bounds__(kMedBlock, 1) k_medium_sah(MedArgs M) {
 // the pair when the first root is the one in bucket 11. The bounds, centroid
 // bounds, axis and buckets are computed exactly as the general step does;
 // any other bucket pair returns false and is left to the general step.
-__device__ bool sah_pair(const SahArgs& A, uint32_t p, uint32_t nd, uint32_t N2, uint32_t& item, V3& lo, V3& hi,
+__device__ bool sah_pair(const SahArgs& A, uint32_t base, uint32_t p, uint32_t nd, uint32_t N2, uint32_t& item, V3& lo, V3& hi,
                          uint32_t* sah_axis, float4* nb_lo, float4* nb_hi, uint32_t* child0, uint32_t* child1,
                          uint32_t* parent) {
   const uint32_t FULL = 0xFFFFFFFFu, lane = lane_id();
@@ -1838,6 +1866,8 @@ __device__ bool sah_pair(const SahArgs& A, uint32_t p, uint32_t nd, uint32_t N2,
   if (lane == 0) {
     const uint32_t me = N2 + nd;
     sah_axis[nd] = (uint32_t)dim;
+    A.sah_rng[2 * nd] = base + p;
+    A.sah_rng[2 * nd + 1] = base + p + 2;
     nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
     nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
     const uint32_t r0 = A.troot[swap ? it1 : it0], r1 = A.troot[swap ? it0 : it1];
@@ -1884,7 +1914,7 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
     uint32_t* stk = sh_stack[w];
     __syncwarp();
     int sp = 1;
-    if (n == 2 && sah_pair(A, 0, sm_node[seg], N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent)) {
+    if (n == 2 && sah_pair(A, base, 0, sm_node[seg], N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent)) {
       sp = 0;
     } else if (lane == 0) {
       stk[0] = 0;
@@ -1967,6 +1997,8 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
       uint32_t me = N2 + nd;
       if (lane == 0) {
         sah_axis[nd] = (uint32_t)dim;
+        A.sah_rng[2 * nd] = base + a;
+        A.sah_rng[2 * nd + 1] = base + b + 1;
         nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
         nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
       }
@@ -1983,9 +2015,9 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
       cl = __shfl_sync(FULL, cl, 0);
       cr = __shfl_sync(FULL, cr, 0);
       const bool lpair =
-          ln == 2 && sah_pair(A, a, cl, N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent);
+          ln == 2 && sah_pair(A, base, a, cl, N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent);
       const bool rpair =
-          rn == 2 && sah_pair(A, mid, cr, N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent);
+          rn == 2 && sah_pair(A, base, mid, cr, N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent);
       if (lane == 0) {
         if (ln == 1) {
           uint32_t r = A.troot[litem];
@@ -2020,26 +2052,29 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
   }
 }
 
-// Subtree node counts of SAH nodes, bottom-up from the treelet roots.
-__global__ void k_sah_sizes(const uint32_t* info, const uint32_t* troot, const uint32_t* parent, uint32_t* visits,
-                            uint32_t* size, const uint32_t* child0, const uint32_t* child1, uint32_t* err) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t T = info[kInfoT], root = info[kInfoRoot];
-  if (t >= T) return;
-  uint32_t cur = troot[t];
-  uint32_t guard = 0;
-  while (cur != root) {
-    if (++guard > (1u << 22)) {
-      atomicOr(err, kErrLoopLimit);
-      return;
-    }
-    uint32_t p = parent[cur] >> 1;
-    __threadfence();
-    if (atomicAdd(&visits[p], 1u) == 0u) return;
-    __threadfence();
-    size[p] = 1u + __ldcg(&size[child0[p]]) + __ldcg(&size[child1[p]]);
-    cur = p;
+// Subtree node counts of SAH nodes. The roots under an SAH node fill the
+// range of final positions its segment had when it was made (the levels only
+// permute roots within a segment), so its count is its cnt - 1 SAH nodes
+// plus the treelet sizes over that range: per position the treelet size of
+// its root (zero past T), scanned, then one difference per SAH node.
+__global__ void k_pos_tsize(const uint32_t* info, const uint32_t* cur, const uint32_t* troot, const uint32_t* size,
+                            uint32_t* tpos, uint32_t n) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t T = info[kInfoT];
+  tpos[p] = p < T ? size[troot[cur[p]]] : 0u;
+}
+__global__ void k_sah_sizes(const uint32_t* info, const uint32_t* rng, const uint32_t* tpre, uint32_t* size,
+                            uint32_t N2, uint32_t* err) {
+  const uint32_t nd = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t T = info[kInfoT];
+  if (T < 2 || nd >= T - 1) return;
+  const uint32_t a = rng[2 * nd], e = rng[2 * nd + 1];
+  if (a + 2 > e || e > T) {
+    atomicOr(err, kErrBuild);
+    return;
   }
+  size[N2 + nd] = (e - a - 1u) + (tpre[e] - tpre[a]);
 }
 
 // ---------------------------------------------------------------------------
@@ -2496,6 +2531,8 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   WPBR_CUDA(B.chunk_tot.ensure(2 * (size_t)kMaxCoopGrid));
   WPBR_CUDA(B.lvl.ensure(16));
   WPBR_CUDA(B.bar.ensure(4));
+  WPBR_CUDA(B.sah_rng.ensure(2 * (size_t)N));
+  WPBR_CUDA(B.tpos.ensure((size_t)N + 1));
   WPBR_CUDA(B.med_start.ensure(maxseg));
   WPBR_CUDA(B.med_end.ensure(maxseg));
   WPBR_CUDA(B.med_node.ensure(maxseg));
@@ -2584,6 +2621,7 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
     C.child1 = B.child1.p;
     C.parent = B.parent.p;
     C.sah_axis = B.sah_axis.p;
+    C.sah_rng = B.sah_rng.p;
     C.item[0] = B.cur.p;
     C.item[1] = B.nxt.p;
     C.seg_of[0] = B.seg_of.p;
@@ -2624,16 +2662,17 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
                                           dim3(kCoopBlock), args, 0, st));
     WPBR_CUDA(cudaFuncSetAttribute((const void*)k_medium_sah, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)kMedSmem));
-    MedArgs Md{N, N2, B.troot.p, B.nb_lo.p, B.nb_hi.p, B.child0.p, B.child1.p, B.parent.p, B.sah_axis.p, B.cur.p,
+    MedArgs Md{N, N2, B.troot.p, B.nb_lo.p, B.nb_hi.p, B.child0.p, B.child1.p, B.parent.p, B.sah_axis.p, B.sah_rng.p, B.cur.p,
                B.med_start.p, B.med_end.p, B.med_node.p, B.small_start.p, B.small_end.p, B.small_node.p,
                B.counters.p, ctx->d_err.p};
-    k_medium_sah<<<(unsigned)sms, kMedBlock, kMedSmem, st>>>(Md);
-    SahArgs A{N, B.troot.p, B.nb_lo.p, B.nb_hi.p};
+    k_medium_sah<<<kMedPerSM * (unsigned)sms, kMedBlock, kMedSmem, st>>>(Md);
+    SahArgs A{N, B.troot.p, B.nb_lo.p, B.nb_hi.p, B.sah_rng.p};
     k_small_sah<<<persistent_grid((const void*)k_small_sah, kB), kB, 0, st>>>(
         A, B.counters.p + 2, B.small_start.p, B.small_end.p, B.small_node.p, B.cur.p, B.counters.p, B.sah_axis.p,
         B.nb_lo.p, B.nb_hi.p, B.child0.p, B.child1.p, B.parent.p, N2, ctx->d_err.p);
-    k_sah_sizes<<<g, kB, 0, st>>>(B.dinfo.p, B.troot.p, B.parent.p, B.visits.p, B.size.p, B.child0.p, B.child1.p,
-                                  ctx->d_err.p);
+    k_pos_tsize<<<div_up(N + 1, kB), kB, 0, st>>>(B.dinfo.p, B.cur.p, B.troot.p, B.size.p, B.tpos.p, N + 1);
+    WPBR_CUDA(scan_exclusive(B.tpos.p, B.tpos.p, N + 1, B.scan_tmp, st));
+    k_sah_sizes<<<g, kB, 0, st>>>(B.dinfo.p, B.sah_rng.p, B.tpos.p, B.size.p, N2, ctx->d_err.p);
   }
   // A9
   WPBR_CUDA(cudaMemsetAsync(B.is_int.p, 0, sizeof(uint32_t) * N2, st));
