@@ -576,12 +576,20 @@ __global__ void k_refit(uint32_t N, const uint32_t* skey, const uint32_t* sprim,
 // ---------------------------------------------------------------------------
 // A8: segmented SAH over treelet roots
 // ---------------------------------------------------------------------------
+// Where a node sits on its path from the root: (depth << 16) | the number of
+// steps into a child 0. With a node's first final position a, its preorder
+// index is that count + a + the treelet nodes of the roots before a (every
+// subtree's roots fill a range of positions, child 0's range first).
+__device__ __forceinline__ uint32_t ld_child(uint32_t ld, int q) { return ld + (1u << 16) + (q == 0 ? 1u : 0u); }
+
 struct SahArgs {
   uint32_t N;
   const uint32_t* troot;
   const float4* nb_lo;
   const float4* nb_hi;
   uint32_t* sah_rng;  // per SAH node: its first final position and one past its last
+  uint32_t* sah_ld;   // per SAH node: ld_child's packed depth and child-0 steps
+  uint32_t* t_ld;     // per treelet: the same for its root
 };
 
 __device__ __forceinline__ void item_bounds(const SahArgs& A, uint32_t item, V3* lo, V3* hi) {
@@ -589,18 +597,6 @@ __device__ __forceinline__ void item_bounds(const SahArgs& A, uint32_t item, V3*
   float4 l = A.nb_lo[r], h = A.nb_hi[r];
   *lo = V3{l.x, l.y, l.z};
   *hi = V3{h.x, h.y, h.z};
-}
-
-// Bounds of another lane (shuffled component by component).
-__device__ __forceinline__ Bounds shfl_bounds_up(const Bounds& b, uint32_t o) {
-  const uint32_t F = 0xFFFFFFFFu;
-  return Bounds{V3{__shfl_up_sync(F, b.lo.x, o), __shfl_up_sync(F, b.lo.y, o), __shfl_up_sync(F, b.lo.z, o)},
-                V3{__shfl_up_sync(F, b.hi.x, o), __shfl_up_sync(F, b.hi.y, o), __shfl_up_sync(F, b.hi.z, o)}};
-}
-__device__ __forceinline__ Bounds shfl_bounds_down(const Bounds& b, uint32_t o) {
-  const uint32_t F = 0xFFFFFFFFu;
-  return Bounds{V3{__shfl_down_sync(F, b.lo.x, o), __shfl_down_sync(F, b.lo.y, o), __shfl_down_sync(F, b.lo.z, o)},
-                V3{__shfl_down_sync(F, b.hi.x, o), __shfl_down_sync(F, b.hi.y, o), __shfl_down_sync(F, b.hi.z, o)}};
 }
 
 __device__ __forceinline__ Bounds dec_bounds(const uint32_t* e) {
@@ -614,41 +610,48 @@ __device__ __forceinline__ Bounds dec_bounds_cg(const uint32_t* e) {
 }
 
 // Split decision of JobBuildUpperSAH (SLBVH.cpp:504-538) by one warp: lane
-// j < 12 holds bucket j's count and bounds. Shuffle scans give every lane the
-// union and count of buckets 0..j (prefix) and j..11 (suffix), lane i < 11
-// costs split i from lane i's prefix and lane i+1's suffix (the unions of the
-// non-empty buckets on each side, as the reference's two inner loops form
-// them), and the sequential first-minimum rule is a lexicographic (cost,
-// split) reduction: a NaN never wins, and a NaN at split 0 keeps split 0.
-// Min and max of finite coordinates do not depend on the grouping; only a
-// zero's sign could, which no area or cost sees. Returns the split bucket
-// (warp-uniform); *k_out receives the count of buckets 0..best.
+// j < 12 holds bucket j's count and bounds. One width-16 shuffle scan gives
+// lanes 0..11 the union and count of buckets 0..j (prefix) and lanes 16..27,
+// which hold the buckets in reverse order, those of buckets 11-m..11
+// (suffix); lane i < 11 costs split i from its prefix and the suffix of
+// bucket i+1 (lane 26 - i): the unions of the non-empty buckets on each side,
+// as the reference's two inner loops form them. The sequential first-minimum
+// rule is a lexicographic (cost, split) reduction: a NaN never wins, and a NaN
+// at split 0 keeps split 0. Min and max of finite coordinates do not depend
+// on the grouping or operand order; only a zero's sign could, which no area
+// or cost sees. Returns the split bucket (warp-uniform); *k_out receives the
+// count of buckets 0..best.
 __device__ int warp_sah_split(uint32_t cj, const Bounds& bj, float area_all, uint32_t* k_out) {
   const uint32_t FULL = 0xFFFFFFFFu;
   const uint32_t lane = lane_id();
-  Bounds pre = (lane < 12 && cj) ? bj : bempty();
-  Bounds suf = pre;
-  uint32_t npre = lane < 12 ? cj : 0u, nsuf = npre;
+  const uint32_t src = lane < 16 ? lane : 27u - lane;  // lane 16 + m takes bucket 11 - m
+  const bool holds = lane < 12 || (lane >= 16 && lane < 28);
+  const uint32_t c = __shfl_sync(FULL, cj, src & 31u);
+  const Bounds b{V3{__shfl_sync(FULL, bj.lo.x, src & 31u), __shfl_sync(FULL, bj.lo.y, src & 31u),
+                    __shfl_sync(FULL, bj.lo.z, src & 31u)},
+                 V3{__shfl_sync(FULL, bj.hi.x, src & 31u), __shfl_sync(FULL, bj.hi.y, src & 31u),
+                    __shfl_sync(FULL, bj.hi.z, src & 31u)}};
+  Bounds acc = (holds && c) ? b : bempty();
+  uint32_t nacc = holds ? c : 0u;
 #pragma unroll
   for (uint32_t o = 1; o < 16; o <<= 1) {
-    Bounds u = shfl_bounds_up(pre, o);
-    uint32_t nu = __shfl_up_sync(FULL, npre, o);
-    Bounds v = shfl_bounds_down(suf, o);
-    uint32_t nv = __shfl_down_sync(FULL, nsuf, o);
-    if (lane >= o) {
-      pre = bunion(u, pre);
-      npre += nu;
-    }
-    if (lane + o < 12) {
-      suf = bunion(suf, v);
-      nsuf += nv;
+    const Bounds u{V3{__shfl_up_sync(FULL, acc.lo.x, o, 16), __shfl_up_sync(FULL, acc.lo.y, o, 16),
+                      __shfl_up_sync(FULL, acc.lo.z, o, 16)},
+                   V3{__shfl_up_sync(FULL, acc.hi.x, o, 16), __shfl_up_sync(FULL, acc.hi.y, o, 16),
+                      __shfl_up_sync(FULL, acc.hi.z, o, 16)}};
+    const uint32_t nu = __shfl_up_sync(FULL, nacc, o, 16);
+    if ((lane & 15u) >= o) {
+      acc = bunion(u, acc);
+      nacc += nu;
     }
   }
-  Bounds b1 = shfl_bounds_down(suf, 1);
-  uint32_t n1 = __shfl_down_sync(FULL, nsuf, 1);
+  const uint32_t rs = lane < 11 ? 26u - lane : lane;  // the suffix of bucket lane + 1
+  const Bounds b1{V3{__shfl_sync(FULL, acc.lo.x, rs), __shfl_sync(FULL, acc.lo.y, rs), __shfl_sync(FULL, acc.lo.z, rs)},
+                  V3{__shfl_sync(FULL, acc.hi.x, rs), __shfl_sync(FULL, acc.hi.y, rs), __shfl_sync(FULL, acc.hi.z, rs)}};
+  const uint32_t n1 = __shfl_sync(FULL, nacc, rs);
   float cost = 0.0f;
   if (lane < 11) {
-    float l = (npre == 0) ? 0.0f : (float)npre * barea(pre);
+    float l = (nacc == 0) ? 0.0f : (float)nacc * barea(acc);
     float r = (n1 == 0) ? 0.0f : (float)n1 * barea(b1);
     cost = (float)(0.125 + (double)((l + r) / area_all));
   }
@@ -665,7 +668,7 @@ __device__ int warp_sah_split(uint32_t cj, const Bounds& bj, float area_all, uin
     }
   }
   int best = isnan(c0) ? 0 : (int)bi;
-  *k_out = __shfl_sync(FULL, npre, best);
+  *k_out = __shfl_sync(FULL, nacc, best);
   return best;
 }
 
@@ -726,6 +729,8 @@ struct CoopSah {
   uint32_t* parent;
   uint32_t* sah_axis;
   uint32_t* sah_rng;  // per SAH node: first position, one past the last (positions of a segment never change)
+  uint32_t* sah_ld;   // per SAH node: packed depth and child-0 steps
+  uint32_t* t_ld;     // per treelet: the same for its root
   // per position (two buffers each, swapped every level)
   uint32_t* item[2];
   uint32_t* seg_of[2];
@@ -740,6 +745,7 @@ struct CoopSah {
   uint32_t* sa[2];
   uint32_t* sb[2];
   uint32_t* snode[2];
+  uint32_t* sld[2];   // the segment node's packed depth and child-0 steps
   uint32_t* sacc[2];  // kSegWords per segment
   uint32_t* sbk[2];   // kBucketWords per segment
   uint4* sdec;        // partition point, mid, left and right child segment (kNone: not large)
@@ -755,6 +761,8 @@ struct CoopSah {
   uint32_t* med_start;
   uint32_t* med_end;
   uint32_t* med_node;
+  uint32_t* med_ld;
+  uint32_t* small_ld;
   uint32_t* counters;  // [0] SAH nodes allocated, [2] small segments queued, [3] medium segments queued
   uint32_t* root_out;  // unified id of the tree's root
   uint32_t* bar;       // grid barrier: [0] arrivals, [1] generation, [2] abort
@@ -867,7 +875,7 @@ __device__ __forceinline__ void init_segment(uint32_t* acc, uint32_t* bk) {
 struct SlotSeg {
   uint32_t s, a, b, node;
   uint32_t spt, mid, best, kk;
-  uint32_t cl, cr;
+  uint32_t cl, cr, ld;
   unsigned long long ga, ge;  // global flag prefixes at a and at b + 1 (phase C2)
   float cb[6];                // centroid bounds lo xyz, hi xyz (phase B)
 };
@@ -911,6 +919,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
   if (T <= 1) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       *C.root_out = T == 1 ? C.troot[0] : kNone;
+      if (T == 1) C.t_ld[0] = 0u;
       C.counters[0] = 0u;
       C.counters[2] = 0u;
       C.counters[3] = 0u;
@@ -928,6 +937,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
       st[0] = 0u;
       en[0] = T - 1;
       nd[0] = 0u;
+      (T <= kSmallSeg ? C.small_ld : C.med_ld)[0] = 0u;
       C.counters[0] = 1u;
       C.counters[2] = T <= kSmallSeg ? 1u : 0u;
       C.counters[3] = T <= kSmallSeg ? 0u : 1u;
@@ -946,6 +956,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
     C.sa[0][0] = 0u;
     C.sb[0][0] = T - 1;
     C.snode[0][0] = 0u;
+    C.sld[0][0] = 0u;
     init_segment(C.sacc[0], C.sbk[0]);
     C.lvl[0] = 1u;  // one large segment
     C.lvl[1] = 1u;  // the root is SAH node 0
@@ -1317,6 +1328,8 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
           C.sah_axis[nd] = (uint32_t)bmax_extent(cb);
           C.sah_rng[2 * nd] = a;
           C.sah_rng[2 * nd + 1] = b + 1;
+          const uint32_t ldm = __ldcg(C.sld[par] + sv);
+          C.sah_ld[nd] = ldm;
           C.nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
           C.nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
           uint32_t node = node_base + nn_pre, segn = nl_pre;
@@ -1340,11 +1353,13 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
               C.sa[nx][z] = ca[q];
               C.sb[nx][z] = cb_[q];
               C.snode[nx][z] = id;
+              C.sld[nx][z] = ld_child(ldm, q);
               init_segment(C.sacc[nx] + (size_t)z * kSegWords, C.sbk[nx] + (size_t)z * kBucketWords);
             } else {
               (med ? C.med_start : C.small_start)[z] = ca[q];
               (med ? C.med_end : C.small_end)[z] = cb_[q];
               (med ? C.med_node : C.small_node)[z] = id;
+              (med ? C.med_ld : C.small_ld)[z] = ld_child(ldm, q);
             }
           }
           C.sdec[sv].z = cseg[0];
@@ -1374,6 +1389,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
             g.cr = dec.w;
             g.best = __ldcg(C.sbest + g.s);
             g.node = __ldcg(snode + g.s);
+            g.ld = __ldcg(C.sld[par] + g.s);
             if (!(g.a <= g.b && g.b < T)) {
               atomicOr(C.err, kErrBuild);
               g.s = kNone;
@@ -1416,11 +1432,13 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
             uint32_t r = C.troot[it[k]];
             C.child0[me] = r;
             C.parent[r] = (me << 1) | 0u;
+            C.t_ld[it[k]] = ld_child(g.ld, 0);
           }
           if (dst == g.b && g.b - g.mid + 1 == 1) {
             uint32_t r = C.troot[it[k]];
             C.child1[me] = r;
             C.parent[r] = (me << 1) | 1u;
+            C.t_ld[it[k]] = ld_child(g.ld, 1);
           }
         }
         __syncthreads();
@@ -1465,7 +1483,7 @@ constexpr size_t kMedOffBnd = kMedOffPre + 4 * (kMedSeg + 32);        // f32 lo 
 constexpr size_t kMedOffAcc = kMedOffBnd + 24 * (size_t)kMedSeg;     // u32 kSegWords per slot
 constexpr size_t kMedOffBk = kMedOffAcc + 4 * kMedSlots * kSegWords;  // u32 kBucketWords per slot
 constexpr size_t kMedOffTab = kMedOffBk + 4 * kMedSlots * kBucketWords;  // u32 slot tables
-constexpr int kMedTabs = 12;
+constexpr int kMedTabs = 14;
 constexpr size_t kMedOffPos = kMedOffTab + 4 * kMedTabs * kMedSlots;  // u16 posF, posT
 constexpr size_t kMedOffSid = kMedOffPos + 4 * (size_t)kMedSeg;      // u16 sub-segment per position
 constexpr size_t kMedOffBkt = kMedOffSid + 2 * (size_t)kMedSeg;      // u8 bucket per position
@@ -1487,9 +1505,13 @@ struct MedArgs {
   const uint32_t* med_start;
   const uint32_t* med_end;
   const uint32_t* med_node;
+  const uint32_t* med_ld;
   uint32_t* small_start;
   uint32_t* small_end;
   uint32_t* small_node;
+  uint32_t* small_ld;
+  uint32_t* sah_ld;
+  uint32_t* t_ld;
   uint32_t* counters;  // [0] SAH nodes allocated, [2] small segments queued, [3] medium segments queued,
                        // [4] medium segments taken
   uint32_t* err;
@@ -1515,6 +1537,8 @@ __global__ void __launch_bounds__(kMedBlock, kMedPerSM) k_medium_sah(MedArgs M) 
   uint32_t* s_na = tab + 9 * kMedSlots;   // next level's slots
   uint32_t* s_nb = tab + 10 * kMedSlots;
   uint32_t* s_nnode = tab + 11 * kMedSlots;
+  uint32_t* s_ld = tab + 12 * kMedSlots;  // packed depth and child-0 steps of the slot's node
+  uint32_t* s_nld = tab + 13 * kMedSlots;
   uint16_t* s_posF = (uint16_t*)(s_med + kMedOffPos);
   uint16_t* s_posT = s_posF + kMedSeg;
   uint16_t* s_sid = (uint16_t*)(s_med + kMedOffSid);
@@ -1554,6 +1578,7 @@ __global__ void __launch_bounds__(kMedBlock, kMedPerSM) k_medium_sah(MedArgs M) 
       s_sa[0] = 0;
       s_sb[0] = n - 1;
       s_snode[0] = M.med_node[seg];
+      s_ld[0] = M.med_ld[seg];
       s_misc[32] = 1;
     }
     // the accumulators of a level's slots are reset by the phase before it
@@ -1751,6 +1776,8 @@ __global__ void __launch_bounds__(kMedBlock, kMedPerSM) k_medium_sah(MedArgs M) 
         M.sah_axis[nd] = (uint32_t)bmax_extent(dec_bounds(s_acc + j * kSegWords + 6));
         M.sah_rng[2 * nd] = start + a;
         M.sah_rng[2 * nd + 1] = start + b + 1;
+        const uint32_t ldm = s_ld[j];
+        M.sah_ld[nd] = ldm;
         M.nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
         M.nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
         const uint32_t ca[2] = {a, mid}, ce[2] = {mid - 1, b}, cn[2] = {mid - a, b - mid + 1};
@@ -1765,6 +1792,7 @@ __global__ void __launch_bounds__(kMedBlock, kMedPerSM) k_medium_sah(MedArgs M) 
             const uint32_t r = M.troot[s_it[ca[q]]];
             cref[me] = r;
             M.parent[r] = (me << 1) | (uint32_t)q;
+            M.t_ld[s_it[ca[q]]] = ld_child(ldm, q);
             continue;
           }
           const uint32_t id = id0 + nid++;
@@ -1780,11 +1808,13 @@ __global__ void __launch_bounds__(kMedBlock, kMedPerSM) k_medium_sah(MedArgs M) 
             s_na[z] = ca[q];
             s_nb[z] = ce[q];
             s_nnode[z] = id;
+            s_nld[z] = ld_child(ldm, q);
             slot[q] = z;
           } else {
             M.small_start[z] = start + ca[q];
             M.small_end[z] = start + ce[q];
             M.small_node[z] = id;
+            M.small_ld[z] = ld_child(ldm, q);
           }
         }
         s_cl[j] = slot[0];
@@ -1808,6 +1838,7 @@ __global__ void __launch_bounds__(kMedBlock, kMedPerSM) k_medium_sah(MedArgs M) 
         s_sa[j] = s_na[j];
         s_sb[j] = s_nb[j];
         s_snode[j] = s_nnode[j];
+        s_ld[j] = s_nld[j];
       }
       if (t == 0) s_misc[32] = nnext;
       __syncthreads();
@@ -1827,7 +1858,7 @@ __global__ void __launch_bounds__(kMedBlock, kMedPerSM) k_medium_sah(MedArgs M) 
 // the pair when the first root is the one in bucket 11. The bounds, centroid
 // bounds, axis and buckets are computed exactly as the general step does;
 // any other bucket pair returns false and is left to the general step.
-__device__ bool sah_pair(const SahArgs& A, uint32_t base, uint32_t p, uint32_t nd, uint32_t N2, uint32_t& item, V3& lo, V3& hi,
+__device__ bool sah_pair(const SahArgs& A, uint32_t base, uint32_t p, uint32_t nd, uint32_t ld, uint32_t N2, uint32_t& item, V3& lo, V3& hi,
                          uint32_t* sah_axis, float4* nb_lo, float4* nb_hi, uint32_t* child0, uint32_t* child1,
                          uint32_t* parent) {
   const uint32_t FULL = 0xFFFFFFFFu, lane = lane_id();
@@ -1868,6 +1899,9 @@ __device__ bool sah_pair(const SahArgs& A, uint32_t base, uint32_t p, uint32_t n
     sah_axis[nd] = (uint32_t)dim;
     A.sah_rng[2 * nd] = base + p;
     A.sah_rng[2 * nd + 1] = base + p + 2;
+    A.sah_ld[nd] = ld;
+    A.t_ld[swap ? it1 : it0] = ld_child(ld, 0);
+    A.t_ld[swap ? it0 : it1] = ld_child(ld, 1);
     nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
     nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
     const uint32_t r0 = A.troot[swap ? it1 : it0], r1 = A.troot[swap ? it0 : it1];
@@ -1888,12 +1922,12 @@ __device__ bool sah_pair(const SahArgs& A, uint32_t base, uint32_t p, uint32_t n
 // queue, whose length it reads from *nsmall_p (the cooperative levels fill
 // the queue on the device).
 __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t* sm_start, const uint32_t* sm_end,
-                            const uint32_t* sm_node, uint32_t* cur, uint32_t* counters, uint32_t* sah_axis,
+                            const uint32_t* sm_node, const uint32_t* sm_ld, uint32_t* cur, uint32_t* counters, uint32_t* sah_axis,
                             float4* nb_lo, float4* nb_hi, uint32_t* child0, uint32_t* child1, uint32_t* parent,
                             uint32_t N2, uint32_t* err) {
   __shared__ uint32_t sh_bcnt[kB / 32][12];
   __shared__ uint32_t sh_benc[kB / 32][12 * 6];
-  __shared__ uint32_t sh_stack[kB / 32][3 * 64];
+  __shared__ uint32_t sh_stack[kB / 32][4 * 64];
   const uint32_t FULL = 0xFFFFFFFFu;
   const uint32_t w = threadIdx.x >> 5, lane = lane_id();
   const uint32_t nsmall = *nsmall_p;
@@ -1914,12 +1948,15 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
     uint32_t* stk = sh_stack[w];
     __syncwarp();
     int sp = 1;
-    if (n == 2 && sah_pair(A, base, 0, sm_node[seg], N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent)) {
+    const uint32_t ld0 = sm_ld[seg];
+    if (n == 2 &&
+        sah_pair(A, base, 0, sm_node[seg], ld0, N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent)) {
       sp = 0;
     } else if (lane == 0) {
       stk[0] = 0;
       stk[1] = n - 1;
       stk[2] = sm_node[seg];
+      stk[3] = ld0;
     }
     __syncwarp();
     uint32_t guard = 0;
@@ -1929,7 +1966,7 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
         break;
       }
       --sp;
-      uint32_t a = stk[3 * sp], b = stk[3 * sp + 1], nd = stk[3 * sp + 2];
+      uint32_t a = stk[4 * sp], b = stk[4 * sp + 1], nd = stk[4 * sp + 2], ld = stk[4 * sp + 3];
       __syncwarp();
       bool act = lane >= a && lane <= b;
       uint32_t cnt = b - a + 1;
@@ -1999,6 +2036,7 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
         sah_axis[nd] = (uint32_t)dim;
         A.sah_rng[2 * nd] = base + a;
         A.sah_rng[2 * nd + 1] = base + b + 1;
+        A.sah_ld[nd] = ld;
         nb_lo[me] = make_float4(bb.lo.x, bb.lo.y, bb.lo.z, 0.0f);
         nb_hi[me] = make_float4(bb.hi.x, bb.hi.y, bb.hi.z, 0.0f);
       }
@@ -2015,19 +2053,20 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
       cl = __shfl_sync(FULL, cl, 0);
       cr = __shfl_sync(FULL, cr, 0);
       const bool lpair =
-          ln == 2 && sah_pair(A, base, a, cl, N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent);
+          ln == 2 && sah_pair(A, base, a, cl, ld_child(ld, 0), N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent);
       const bool rpair =
-          rn == 2 && sah_pair(A, base, mid, cr, N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent);
+          rn == 2 && sah_pair(A, base, mid, cr, ld_child(ld, 1), N2, item, lo, hi, sah_axis, nb_lo, nb_hi, child0, child1, parent);
       if (lane == 0) {
         if (ln == 1) {
           uint32_t r = A.troot[litem];
           child0[me] = r;
           parent[r] = (me << 1) | 0u;
+          A.t_ld[litem] = ld_child(ld, 0);
         } else {
           child0[me] = N2 + cl;
           parent[N2 + cl] = (me << 1) | 0u;
           if (!lpair) {
-            stk[3 * sp] = a; stk[3 * sp + 1] = mid - 1; stk[3 * sp + 2] = cl;
+            stk[4 * sp] = a; stk[4 * sp + 1] = mid - 1; stk[4 * sp + 2] = cl; stk[4 * sp + 3] = ld_child(ld, 0);
             ++sp;
           }
         }
@@ -2035,11 +2074,12 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
           uint32_t r = A.troot[ritem];
           child1[me] = r;
           parent[r] = (me << 1) | 1u;
+          A.t_ld[ritem] = ld_child(ld, 1);
         } else {
           child1[me] = N2 + cr;
           parent[N2 + cr] = (me << 1) | 1u;
           if (!rpair) {
-            stk[3 * sp] = mid; stk[3 * sp + 1] = b; stk[3 * sp + 2] = cr;
+            stk[4 * sp] = mid; stk[4 * sp + 1] = b; stk[4 * sp + 2] = cr; stk[4 * sp + 3] = ld_child(ld, 1);
             ++sp;
           }
         }
@@ -2058,11 +2098,19 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
 // plus the treelet sizes over that range: per position the treelet size of
 // its root (zero past T), scanned, then one difference per SAH node.
 __global__ void k_pos_tsize(const uint32_t* info, const uint32_t* cur, const uint32_t* troot, const uint32_t* size,
-                            uint32_t* tpos, uint32_t n) {
+                            uint32_t* tpos, uint32_t* tinv, uint32_t n) {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   const uint32_t T = info[kInfoT];
-  tpos[p] = p < T ? size[troot[cur[p]]] : 0u;
+  uint32_t v = 0;
+  if (p < T && T > 1) {
+    const uint32_t t = cur[p];
+    if (t < T) {
+      v = size[troot[t]];
+      tinv[t] = p;  // the final position of treelet t
+    }
+  }
+  tpos[p] = v;
 }
 __global__ void k_sah_sizes(const uint32_t* info, const uint32_t* rng, const uint32_t* tpre, uint32_t* size,
                             uint32_t N2, uint32_t* err) {
@@ -2084,11 +2132,13 @@ __global__ void k_flatten(uint32_t N, uint32_t* info, const uint32_t* skey, cons
                           const uint32_t* tstart, const uint32_t* tsize, const uint32_t* rng_lo,
                           const uint32_t* rng_hi, const uint32_t* child0, const uint32_t* parent,
                           const uint32_t* size, const uint32_t* sah_axis, const float4* nb_lo, const float4* nb_hi,
-                          uint32_t* lin_node, float* lin_bounds, uint32_t* is_int, uint32_t* depth_max,
-                          uint32_t* err) {
+                          const uint32_t* sah_ld, const uint32_t* sah_rng, const uint32_t* t_ld,
+                          const uint32_t* tinv, const uint32_t* tpre, uint32_t* lin_node, float* lin_bounds,
+                          uint32_t* is_int, uint32_t* depth_max, uint32_t* err) {
   uint32_t X = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t N2 = 2 * N;
-  const uint32_t nsah = info[kInfoT] - 1u, root = info[kInfoRoot];
+  const uint32_t T = info[kInfoT];
+  const uint32_t nsah = T - 1u, root = info[kInfoRoot];
   const uint32_t M = root < N2 + N ? size[root] : kNone;
   if (M > N2) {  // a flattened tree has at most 2N - 1 nodes
     if (X == 0) {
@@ -2100,11 +2150,10 @@ __global__ void k_flatten(uint32_t N, uint32_t* info, const uint32_t* skey, cons
   if (X == 0) info[kInfoM] = M;
   if (X >= N2 + nsah) return;
   uint32_t kind;  // 0 radix interior, 1 leaf, 2 SAH
-  uint32_t lo = 0, hi = 0;
+  uint32_t lo = 0, hi = 0, t = 0, troot_ = 0;
   if (X >= N2) {
     kind = 2;
   } else {
-    uint32_t t;
     if (X < N) {
       if (X + 1 >= N) return;
       t = tid[X];
@@ -2115,23 +2164,47 @@ __global__ void k_flatten(uint32_t N, uint32_t* info, const uint32_t* skey, cons
       lo = hi = X - N;
       t = tid[lo];
     }
-    uint32_t troot_ = treelet_root(t, tstart, tsize, N);
+    troot_ = treelet_root(t, tstart, tsize, N);
     if (X != troot_) {
       uint32_t p = parent[X] >> 1;
       if (!ref_interior(p, N, rng_lo, rng_hi, skey)) return;
     }
     kind = ref_interior(X, N, rng_lo, rng_hi, skey) ? 0u : 1u;
   }
-  uint32_t idx = 0, depth = 0, cur = X;
-  while (cur != root) {
-    if (++depth > (1u << 22)) {
-      atomicOr(err, kErrLoopLimit);
+  // the preorder index: an SAH node or a treelet root takes it from its
+  // recorded child-0 steps and depth (ld_child), its first position and the
+  // treelet nodes before that position; a treelet's other nodes walk up to
+  // their treelet root
+  uint32_t idx = 0, depth = 0;
+  if (kind == 2) {
+    const uint32_t nd = X - N2, ld = sah_ld[nd], a = sah_rng[2 * nd];
+    if (a >= T) {
+      atomicOr(err, kErrBuild);
       return;
     }
-    uint32_t pw = parent[cur];
-    uint32_t p = pw >> 1;
-    idx += (pw & 1u) ? 1u + size[child0[p]] : 1u;
-    cur = p;
+    idx = (ld & 0xFFFFu) + a + tpre[a];
+    depth = ld >> 16;
+  } else {
+    uint32_t cur = X;
+    while (cur != troot_) {
+      if (++depth > (1u << 22)) {
+        atomicOr(err, kErrLoopLimit);
+        return;
+      }
+      uint32_t pw = parent[cur];
+      uint32_t p = pw >> 1;
+      idx += (pw & 1u) ? 1u + size[child0[p]] : 1u;
+      cur = p;
+    }
+    if (T > 1) {  // one treelet: its root is the tree's root
+      const uint32_t pos = tinv[t], ld = t_ld[t];
+      if (pos >= T) {
+        atomicOr(err, kErrBuild);
+        return;
+      }
+      idx += (ld & 0xFFFFu) + pos + tpre[pos];
+      depth += ld >> 16;
+    }
   }
   if (idx >= M) {
     atomicOr(err, kErrBuild);
@@ -2532,6 +2605,12 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   WPBR_CUDA(B.lvl.ensure(16));
   WPBR_CUDA(B.bar.ensure(4));
   WPBR_CUDA(B.sah_rng.ensure(2 * (size_t)N));
+  WPBR_CUDA(B.sah_ld.ensure(N));
+  WPBR_CUDA(B.t_ld.ensure(N));
+  WPBR_CUDA(B.tinv.ensure(N));
+  WPBR_CUDA(B.seg_ld.ensure(2 * (size_t)maxseg));
+  WPBR_CUDA(B.med_ld.ensure(maxseg));
+  WPBR_CUDA(B.small_ld.ensure(N));
   WPBR_CUDA(B.tpos.ensure((size_t)N + 1));
   WPBR_CUDA(B.med_start.ensure(maxseg));
   WPBR_CUDA(B.med_end.ensure(maxseg));
@@ -2622,6 +2701,10 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
     C.parent = B.parent.p;
     C.sah_axis = B.sah_axis.p;
     C.sah_rng = B.sah_rng.p;
+    C.sah_ld = B.sah_ld.p;
+    C.t_ld = B.t_ld.p;
+    C.med_ld = B.med_ld.p;
+    C.small_ld = B.small_ld.p;
     C.item[0] = B.cur.p;
     C.item[1] = B.nxt.p;
     C.seg_of[0] = B.seg_of.p;
@@ -2639,6 +2722,7 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
       C.sa[q] = B.seg_start.p + (size_t)q * maxseg;
       C.sb[q] = B.seg_end.p + (size_t)q * maxseg;
       C.snode[q] = B.seg_node.p + (size_t)q * maxseg;
+      C.sld[q] = B.seg_ld.p + (size_t)q * maxseg;
       C.sacc[q] = B.seg_acc.p + (size_t)q * maxseg * kSegWords;
       C.sbk[q] = B.seg_bk.p + (size_t)q * maxseg * kBucketWords;
     }
@@ -2663,14 +2747,15 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
     WPBR_CUDA(cudaFuncSetAttribute((const void*)k_medium_sah, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)kMedSmem));
     MedArgs Md{N, N2, B.troot.p, B.nb_lo.p, B.nb_hi.p, B.child0.p, B.child1.p, B.parent.p, B.sah_axis.p, B.sah_rng.p, B.cur.p,
-               B.med_start.p, B.med_end.p, B.med_node.p, B.small_start.p, B.small_end.p, B.small_node.p,
-               B.counters.p, ctx->d_err.p};
+               B.med_start.p, B.med_end.p, B.med_node.p, B.med_ld.p, B.small_start.p, B.small_end.p, B.small_node.p,
+               B.small_ld.p, B.sah_ld.p, B.t_ld.p, B.counters.p, ctx->d_err.p};
     k_medium_sah<<<kMedPerSM * (unsigned)sms, kMedBlock, kMedSmem, st>>>(Md);
-    SahArgs A{N, B.troot.p, B.nb_lo.p, B.nb_hi.p, B.sah_rng.p};
+    SahArgs A{N, B.troot.p, B.nb_lo.p, B.nb_hi.p, B.sah_rng.p, B.sah_ld.p, B.t_ld.p};
     k_small_sah<<<persistent_grid((const void*)k_small_sah, kB), kB, 0, st>>>(
-        A, B.counters.p + 2, B.small_start.p, B.small_end.p, B.small_node.p, B.cur.p, B.counters.p, B.sah_axis.p,
+        A, B.counters.p + 2, B.small_start.p, B.small_end.p, B.small_node.p, B.small_ld.p, B.cur.p, B.counters.p,
+        B.sah_axis.p,
         B.nb_lo.p, B.nb_hi.p, B.child0.p, B.child1.p, B.parent.p, N2, ctx->d_err.p);
-    k_pos_tsize<<<div_up(N + 1, kB), kB, 0, st>>>(B.dinfo.p, B.cur.p, B.troot.p, B.size.p, B.tpos.p, N + 1);
+    k_pos_tsize<<<div_up(N + 1, kB), kB, 0, st>>>(B.dinfo.p, B.cur.p, B.troot.p, B.size.p, B.tpos.p, B.tinv.p, N + 1);
     WPBR_CUDA(scan_exclusive(B.tpos.p, B.tpos.p, N + 1, B.scan_tmp, st));
     k_sah_sizes<<<g, kB, 0, st>>>(B.dinfo.p, B.sah_rng.p, B.tpos.p, B.size.p, N2, ctx->d_err.p);
   }
@@ -2679,7 +2764,8 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   WPBR_CUDA(cudaMemsetAsync(B.depth_max.p, 0, 4, st));
   k_flatten<<<div_up((uint64_t)N2 + N, kB), kB, 0, st>>>(N, B.dinfo.p, B.skey, B.tid.p, B.tstart.p, B.tsize.p,
                                                           B.rng_lo.p, B.rng_hi.p, B.child0.p, B.parent.p, B.size.p,
-                                                          B.sah_axis.p, B.nb_lo.p, B.nb_hi.p, B.lin_node.p,
+                                                          B.sah_axis.p, B.nb_lo.p, B.nb_hi.p, B.sah_ld.p,
+                                                          B.sah_rng.p, B.t_ld.p, B.tinv.p, B.tpos.p, B.lin_node.p,
                                                           B.lin_bounds.p, B.is_int.p, B.depth_max.p, ctx->d_err.p);
   WPBR_CUDA(scan_exclusive(B.is_int.p, B.int_index.p, N2, B.scan_tmp, st));
   WPBR_CUDA(cudaMemsetAsync(B.int_kids.p, 0, sizeof(uint32_t) * N, st));
