@@ -511,6 +511,15 @@ __device__ __forceinline__ uint32_t treelet_root(uint32_t t, const uint32_t* tst
   return tsize[t] >= 2 ? tstart[t] : N + tstart[t];
 }
 
+// An arrival count with acquire-release ordering: the arriving thread's
+// earlier writes are visible to the thread whose increment reads its value,
+// and that thread's later reads see them.
+__device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t* a) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(a) : "memory");
+  return old;
+}
+
 // Ref leaves compute their bounds; the second child to finish builds each
 // parent (atomic arrival counter), up to the treelet root.
 __global__ void k_refit(uint32_t N, const uint32_t* skey, const uint32_t* sprim, const uint32_t* tid,
@@ -557,9 +566,7 @@ __global__ void k_refit(uint32_t N, const uint32_t* skey, const uint32_t* sprim,
       return;
     }
     uint32_t p = parent[cur] >> 1;
-    __threadfence();
-    if (atomicAdd(&visits[p], 1u) == 0u) return;
-    __threadfence();
+    if (arrive_acq_rel(&visits[p]) == 0u) return;
     uint32_t c0 = child0[p], c1 = child1[p];
     float4 a0 = __ldcg(&nb_lo[c0]), a1 = __ldcg(&nb_lo[c1]);
     float4 b0 = __ldcg(&nb_hi[c0]), b1 = __ldcg(&nb_hi[c1]);
