@@ -931,6 +931,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
       C.counters[2] = 0u;
       C.counters[3] = 0u;
       C.counters[4] = 0u;
+      C.counters[5] = 0u;
     }
     return;
   }
@@ -949,6 +950,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
       C.counters[2] = T <= kSmallSeg ? 1u : 0u;
       C.counters[3] = T <= kSmallSeg ? 0u : 1u;
       C.counters[4] = 0u;
+      C.counters[5] = 0u;
     }
     return;
   }
@@ -970,6 +972,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
     C.counters[2] = 0u;  // the queues fill by atomics
     C.counters[3] = 0u;
     C.counters[4] = 0u;
+    C.counters[5] = 0u;
   }
   if (!coop_sync(C.bar, C.err)) return;
 
@@ -1520,7 +1523,7 @@ struct MedArgs {
   uint32_t* sah_ld;
   uint32_t* t_ld;
   uint32_t* counters;  // [0] SAH nodes allocated, [2] small segments queued, [3] medium segments queued,
-                       // [4] medium segments taken
+                       // [4] medium segments taken, [5] small segments taken
   uint32_t* err;
 };
 
@@ -1926,8 +1929,9 @@ __device__ bool sah_pair(const SahArgs& A, uint32_t base, uint32_t p, uint32_t n
 // new SAH node ids are reserved with one atomic. Nodes over two roots (about
 // half of them) are finished by sah_pair within the step that creates them
 // instead of a step of their own. A persistent grid of warps walks the
-// queue, whose length it reads from *nsmall_p (the cooperative levels fill
-// the queue on the device).
+// queue, whose length it reads from *nsmall_p (the cooperative and
+// block-local levels fill the queue on the device), each warp taking the
+// next segment from counters[5].
 __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t* sm_start, const uint32_t* sm_end,
                             const uint32_t* sm_node, const uint32_t* sm_ld, uint32_t* cur, uint32_t* counters, uint32_t* sah_axis,
                             float4* nb_lo, float4* nb_hi, uint32_t* child0, uint32_t* child1, uint32_t* parent,
@@ -1938,8 +1942,13 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
   const uint32_t FULL = 0xFFFFFFFFu;
   const uint32_t w = threadIdx.x >> 5, lane = lane_id();
   const uint32_t nsmall = *nsmall_p;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; seg < nsmall; seg += nwarps) {
+  for (;;) {
+    // segments (2 to 32 roots) taken in turn from a counter, which keeps the
+    // warps' loads even
+    uint32_t seg = 0;
+    if (lane == 0) seg = atomicAdd(counters + 5, 1u);
+    seg = __shfl_sync(FULL, seg, 0);
+    if (seg >= nsmall) break;
     const uint32_t base = sm_start[seg];
     const uint32_t n = sm_end[seg] - base + 1;
     if (n < 2 || n > kSmallSeg || sm_end[seg] >= A.N) {
