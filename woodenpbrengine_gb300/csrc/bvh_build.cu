@@ -932,6 +932,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
       C.counters[3] = 0u;
       C.counters[4] = 0u;
       C.counters[5] = 0u;
+      C.counters[7] = 0u;
     }
     return;
   }
@@ -951,6 +952,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
       C.counters[3] = T <= kSmallSeg ? 0u : 1u;
       C.counters[4] = 0u;
       C.counters[5] = 0u;
+      C.counters[7] = 0u;
     }
     return;
   }
@@ -973,6 +975,7 @@ __global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
     C.counters[3] = 0u;
     C.counters[4] = 0u;
     C.counters[5] = 0u;
+    C.counters[7] = 0u;
   }
   if (!coop_sync(C.bar, C.err)) return;
 
@@ -1523,7 +1526,7 @@ struct MedArgs {
   uint32_t* sah_ld;
   uint32_t* t_ld;
   uint32_t* counters;  // [0] SAH nodes allocated, [2] small segments queued, [3] medium segments queued,
-                       // [4] medium segments taken, [5] small segments taken
+                       // [4], [7] medium segments taken (two passes), [5] small segments taken
   uint32_t* err;
 };
 
@@ -1557,16 +1560,22 @@ __global__ void __launch_bounds__(kMedBlock, kMedPerSM) k_medium_sah(MedArgs M) 
   const uint32_t FULL = 0xFFFFFFFFu;
   const uint32_t t = threadIdx.x, lane = lane_id(), wid = t >> 5;
   const uint32_t nmed = M.counters[3];
-  for (;;) {
+  for (uint32_t pass = 0; pass < 2;) {
     // segments taken in turn from a counter, so that blocks that drew small
-    // segments take more (the barrier first: every thread has read the last one)
+    // segments take more; the first pass takes those of more than kMedSeg / 2
+    // roots and the second the others, so the last to run are the shorter
+    // ones (the barrier first: every thread has read the last number)
     __syncthreads();
-    if (t == 0) s_misc[38] = atomicAdd(M.counters + 4, 1u);
+    if (t == 0) s_misc[38] = atomicAdd(M.counters + (pass == 0 ? 4 : 7), 1u);
     __syncthreads();
     const uint32_t seg = s_misc[38];
-    if (seg >= nmed) break;  // block-uniform
+    if (seg >= nmed) {  // block-uniform
+      ++pass;
+      continue;
+    }
     const uint32_t start = M.med_start[seg], end = M.med_end[seg];
     const uint32_t n = end - start + 1;
+    if ((n > kMedSeg / 2) != (pass == 0)) continue;  // the other pass's segment
     if (end < start || end >= M.N || n <= kSmallSeg || n > kMedSeg) {  // block-uniform
       if (t == 0) atomicOr(M.err, kErrBuild);
       continue;
