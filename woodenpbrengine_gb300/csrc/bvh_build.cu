@@ -526,14 +526,18 @@ __global__ void k_refit(uint32_t N, const uint32_t* skey, const uint32_t* sprim,
                         const uint32_t* tstart, const uint32_t* tsize, const uint32_t* rng_lo, const uint32_t* rng_hi,
                         const uint32_t* child0, const uint32_t* child1, const uint32_t* parent, uint32_t* visits,
                         uint32_t* size, float4* nb_lo, float4* nb_hi, const float4* pb_lo, const float4* pb_hi,
-                        uint32_t* troot, uint32_t* err) {
+                        uint32_t* troot, uint8_t* role, uint32_t* err) {
   uint32_t X = blockIdx.x * blockDim.x + threadIdx.x;
   if (X >= 2 * N) return;
+  // role of X in the flattened tree (read by k_flatten): 0 none, 1 ref leaf,
+  // 2 ref interior
   uint32_t lo, hi, t;
   if (X < N) {
-    if (X + 1 >= N) return;
-    t = tid[X];
-    if (tid[X + 1] != t) return;  // not an internal node
+    t = X + 1 < N ? tid[X] : kNone;
+    if (X + 1 >= N || tid[X + 1] != t) {  // not an internal node
+      role[X] = 0;
+      return;
+    }
     lo = rng_lo[X];
     hi = rng_hi[X];
   } else {
@@ -544,9 +548,16 @@ __global__ void k_refit(uint32_t N, const uint32_t* skey, const uint32_t* sprim,
   bool is_root = (X == root);
   if (!is_root) {
     uint32_t p = parent[X] >> 1;
-    if (!ref_interior(p, N, rng_lo, rng_hi, skey)) return;  // inside a leaf
+    if (!ref_interior(p, N, rng_lo, rng_hi, skey)) {  // inside a leaf
+      role[X] = 0;
+      return;
+    }
   }
-  if (ref_interior(X, N, rng_lo, rng_hi, skey)) return;  // interior: built by its children
+  if (ref_interior(X, N, rng_lo, rng_hi, skey)) {  // interior: built by its children
+    role[X] = 2;
+    return;
+  }
+  role[X] = 1;
   // ref leaf: union of its primitives' bounds in sorted order
   float4 l = pb_lo[sprim[lo]], h = pb_hi[sprim[lo]];
   V3 blo{l.x, l.y, l.z}, bhi{h.x, h.y, h.z};
@@ -717,9 +728,16 @@ __device__ __forceinline__ uint32_t sah_bucket(const V3& lo, const V3& hi, const
 // leaves at its next barrier. Indices derived from scanned values are checked
 // before use.
 // ---------------------------------------------------------------------------
-constexpr int kCoopBlock = 512;
+// 1.31M-triangle build, device ms: 512 threads (2 blocks per SM) 1.588,
+// 1024 (1 per SM, half the grid barrier's arrivals) 1.575.
+#ifndef WPBR_COOP_BLOCK
+#define WPBR_COOP_BLOCK 1024
+#endif
+constexpr int kCoopBlock = WPBR_COOP_BLOCK;
+constexpr int kCoopPerSM = 1024 / kCoopBlock;  // resident blocks per SM (64 registers a thread)
 constexpr int kCoopWarps = kCoopBlock / 32;
-constexpr uint32_t kMaxCoopGrid = 2 * kCoopBlock;  // blocks of the cooperative grid (chunk prefixes in shared memory)
+constexpr uint32_t kMaxCoopGrid = 1024;  // blocks of the cooperative grid (chunk prefixes in shared memory)
+static_assert(kMaxCoopGrid <= 2 * kCoopBlock, "block_scan_pairs scans two entries a thread");
 constexpr uint32_t kSpinLimit = 1u << 24;   // barrier polls (100 ns apart) before giving up
 constexpr uint32_t kSegWords = 12;          // bounds lo/hi, centroid bounds lo/hi (encoded)
 constexpr uint32_t kBucketWords = 12 * 7;   // per bucket: count, lo xyz, hi xyz (encoded)
@@ -888,8 +906,8 @@ struct SlotSeg {
 };
 constexpr int kBatchTiles = 4;
 constexpr uint32_t kBatch = kBatchTiles * kCoopBlock;
-constexpr uint32_t kSlots = 64;
-static_assert(2 + (kBatch - 2) / (kSmallSeg + 1) <= kSlots, "a batch meets at most kSlots large segments");
+constexpr uint32_t kSlots = 8;
+static_assert(2 + (kBatch - 2) / (kMedSeg + 1) <= kSlots, "a batch meets at most kSlots large segments");
 
 // Positions of the block's batch starting at `base` (k-th tile of the batch:
 // base + k * kCoopBlock + thread) and their segments; marks the slots the
@@ -910,7 +928,7 @@ __device__ __forceinline__ void batch_segments(const uint32_t* seg_of, uint32_t 
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kCoopBlock, 2) k_sah_levels(CoopSah C) {
+__global__ void __launch_bounds__(kCoopBlock, kCoopPerSM) k_sah_levels(CoopSah C) {
   __shared__ SlotSeg sl[kSlots];
   __shared__ uint32_t s_acc[kSlots * kSegWords];
   __shared__ uint32_t s_bk[kSlots * kBucketWords];
@@ -2158,8 +2176,8 @@ __global__ void k_flatten(uint32_t N, uint32_t* info, const uint32_t* skey, cons
                           const uint32_t* rng_hi, const uint32_t* child0, const uint32_t* parent,
                           const uint32_t* size, const uint32_t* sah_axis, const float4* nb_lo, const float4* nb_hi,
                           const uint32_t* sah_ld, const uint32_t* sah_rng, const uint32_t* t_ld,
-                          const uint32_t* tinv, const uint32_t* tpre, uint32_t* lin_node, float* lin_bounds,
-                          uint32_t* is_int, uint32_t* depth_max, uint32_t* err) {
+                          const uint32_t* tinv, const uint32_t* tpre, const uint8_t* role, uint32_t* lin_node,
+                          float* lin_bounds, uint32_t* is_int, uint32_t* depth_max, uint32_t* err) {
   uint32_t X = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t N2 = 2 * N;
   const uint32_t T = info[kInfoT];
@@ -2179,10 +2197,10 @@ __global__ void k_flatten(uint32_t N, uint32_t* info, const uint32_t* skey, cons
   if (X >= N2) {
     kind = 2;
   } else {
+    const uint32_t r = role[X];  // as the refit classified X
+    if (r == 0u) return;
     if (X < N) {
-      if (X + 1 >= N) return;
       t = tid[X];
-      if (tid[X + 1] != t) return;
       lo = rng_lo[X];
       hi = rng_hi[X];
     } else {
@@ -2190,11 +2208,7 @@ __global__ void k_flatten(uint32_t N, uint32_t* info, const uint32_t* skey, cons
       t = tid[lo];
     }
     troot_ = treelet_root(t, tstart, tsize, N);
-    if (X != troot_) {
-      uint32_t p = parent[X] >> 1;
-      if (!ref_interior(p, N, rng_lo, rng_hi, skey)) return;
-    }
-    kind = ref_interior(X, N, rng_lo, rng_hi, skey) ? 0u : 1u;
+    kind = r == 2u ? 0u : 1u;
   }
   // the preorder index: an SAH node or a treelet root takes it from its
   // recorded child-0 steps and depth (ld_child), its first position and the
@@ -2630,6 +2644,7 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   WPBR_CUDA(B.lvl.ensure(16));
   WPBR_CUDA(B.bar.ensure(4));
   WPBR_CUDA(B.sah_rng.ensure(2 * (size_t)N));
+  WPBR_CUDA(B.role.ensure(2 * (size_t)N));
   WPBR_CUDA(B.sah_ld.ensure(N));
   WPBR_CUDA(B.t_ld.ensure(N));
   WPBR_CUDA(B.tinv.ensure(N));
@@ -2699,7 +2714,8 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
                                                B.child0.p, B.child1.p, B.parent.p);
   k_refit<<<div_up(2 * N, kB), kB, 0, st>>>(N, B.skey, B.sprim, B.tid.p, B.tstart.p, B.tsize.p, B.rng_lo.p,
                                             B.rng_hi.p, B.child0.p, B.child1.p, B.parent.p, B.visits.p, B.size.p,
-                                            B.nb_lo.p, B.nb_hi.p, B.pb_lo.p, B.pb_hi.p, B.troot.p, ctx->d_err.p);
+                                            B.nb_lo.p, B.nb_hi.p, B.pb_lo.p, B.pb_hi.p, B.troot.p, B.role.p,
+                                            ctx->d_err.p);
   // A8: the large segments' levels in one cooperative launch, then the
   // warp-local SAH of the small segments
   {
@@ -2709,7 +2725,7 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
     WPBR_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     WPBR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sah_levels, kCoopBlock, 0));
     if (!coop || per_sm < 1) return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: cooperative launch unavailable");
-    if (per_sm > 2) per_sm = 2;
+    if (per_sm > kCoopPerSM) per_sm = kCoopPerSM;
     if ((uint32_t)(per_sm * sms) > kMaxCoopGrid) per_sm = (int)(kMaxCoopGrid / (uint32_t)sms);
     if (per_sm < 1) return set_err(ctx, WPBR_ERR_CUDA, "bvh_build: too many SMs for the cooperative grid");
     WPBR_CUDA(cudaMemsetAsync(B.bar.p, 0, sizeof(uint32_t) * 4, st));
@@ -2790,7 +2806,7 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   k_flatten<<<div_up((uint64_t)N2 + N, kB), kB, 0, st>>>(N, B.dinfo.p, B.skey, B.tid.p, B.tstart.p, B.tsize.p,
                                                           B.rng_lo.p, B.rng_hi.p, B.child0.p, B.parent.p, B.size.p,
                                                           B.sah_axis.p, B.nb_lo.p, B.nb_hi.p, B.sah_ld.p,
-                                                          B.sah_rng.p, B.t_ld.p, B.tinv.p, B.tpos.p, B.lin_node.p,
+                                                          B.sah_rng.p, B.t_ld.p, B.tinv.p, B.tpos.p, B.role.p, B.lin_node.p,
                                                           B.lin_bounds.p, B.is_int.p, B.depth_max.p, ctx->d_err.p);
   WPBR_CUDA(scan_exclusive(B.is_int.p, B.int_index.p, N2, B.scan_tmp, st));
   WPBR_CUDA(cudaMemsetAsync(B.int_kids.p, 0, sizeof(uint32_t) * N, st));

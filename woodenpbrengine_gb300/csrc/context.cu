@@ -143,7 +143,7 @@ void bvh_release(wpbr_ctx* ctx, bool keep_traversal) {
   B.seg_best.release(); B.seg_dec.release(); B.seg_pre.release(); B.chunk_tot.release(); B.lvl.release();
   B.bar.release(); B.small_start.release(); B.small_end.release();
   B.small_node.release(); B.med_start.release(); B.med_end.release(); B.med_node.release(); B.sah_rng.release(); B.tpos.release(); B.sah_ld.release(); B.t_ld.release(); B.tinv.release(); B.seg_ld.release();
-  B.med_ld.release(); B.small_ld.release(); B.counters.release(); B.dinfo.release(); B.sah_axis.release(); B.lin_node.release();
+  B.med_ld.release(); B.small_ld.release(); B.role.release(); B.counters.release(); B.dinfo.release(); B.sah_axis.release(); B.lin_node.release();
   B.lin_bounds.release(); B.is_int.release(); B.int_index.release(); B.depth_max.release();
   B.int_kids.release(); B.int_slot.release();
   B.split_cnt.release(); B.split_off.release();

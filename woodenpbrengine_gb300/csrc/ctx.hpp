@@ -80,6 +80,7 @@ struct BvhState {
   DevBuf<uint32_t> med_start, med_end, med_node;  // segments of 33..4096 treelet roots
   DevBuf<uint32_t> sah_rng, tpos;  // SAH node position ranges; treelet sizes by position, scanned
   DevBuf<uint32_t> sah_ld, t_ld, tinv, seg_ld, med_ld, small_ld;  // depths and child-0 steps; treelet positions
+  DevBuf<uint8_t> role;  // per radix node: 0 outside the flattened tree, 1 ref leaf, 2 ref interior
   DevBuf<uint32_t> dinfo;       // sizes found on the device (treelets, root, nodes, summary)
   uint32_t* h_info = nullptr;   // pinned copy of dinfo's summary
   DevBuf<uint32_t> sah_axis;
