@@ -931,6 +931,8 @@ __device__ __forceinline__ void batch_segments(const uint32_t* seg_of, uint32_t 
 __global__ void __launch_bounds__(kCoopBlock, kCoopPerSM) k_sah_levels(CoopSah C) {
   __shared__ SlotSeg sl[kSlots];
   __shared__ uint32_t s_acc[kSlots * kSegWords];
+  __shared__ uint32_t s_nacc[2 * kSlots * kSegWords];  // phase E: the next level's bounds by child segment
+  __shared__ uint32_t s_nid[2 * kSlots];
   __shared__ uint32_t s_bk[kSlots * kBucketWords];
   __shared__ unsigned long long s_w1[kBatchTiles][kCoopWarps], s_w2[kBatchTiles][kCoopWarps];
   __shared__ unsigned long long s_t1[kBatchTiles], s_t2[kBatchTiles];
@@ -1025,88 +1027,91 @@ __global__ void __launch_bounds__(kCoopBlock, kCoopPerSM) k_sah_levels(CoopSah C
     }
     uint32_t p[kBatchTiles], s[kBatchTiles];
 
-    // ---- A: segment bounds and centroid bounds ----
-    for (uint32_t base = c0; base < c1; base += kBatch) {
-      batch_segments(seg_of, base, c1, nseg, p, s, sl);
-      for (uint32_t k = threadIdx.x; k < kSlots * kSegWords; k += blockDim.x)
-        s_acc[k] = (((k % kSegWords) / 3) % 2 == 0) ? 0xFFFFFFFFu : 0u;
-      __syncthreads();
-      float4 l[kBatchTiles], h[kBatchTiles];
-#pragma unroll
-      for (int k = 0; k < kBatchTiles; ++k)
-        if (s[k] != kNone) {
-          l[k] = __ldcg(plo + p[k]);
-          h[k] = __ldcg(phi + p[k]);
-        }
-#pragma unroll 1
-      for (int k = 0; k < kBatchTiles; ++k) {
-        const uint32_t sk = s[k];
-        if (!__any_sync(FULL, sk != kNone)) continue;
-        uint32_t e[12];
-        if (sk != kNone) {
-          V3 lo{l[k].x, l[k].y, l[k].z}, hi{h[k].x, h[k].y, h[k].z};
-          V3 c = mul(add(lo, hi), 0.5f);
-          e[0] = fenc(lo.x); e[1] = fenc(lo.y); e[2] = fenc(lo.z);
-          e[3] = fenc(hi.x); e[4] = fenc(hi.y); e[5] = fenc(hi.z);
-          e[6] = fenc(c.x); e[7] = fenc(c.y); e[8] = fenc(c.z);
-          e[9] = e[6]; e[10] = e[7]; e[11] = e[8];
-        } else {
-#pragma unroll
-          for (int q = 0; q < 12; ++q) e[q] = ((q / 3) % 2 == 0) ? 0xFFFFFFFFu : 0u;
-        }
-        const uint32_t s0 = __shfl_sync(FULL, sk, 0);
-        if (__all_sync(FULL, sk == s0)) {  // one segment across the warp
-#pragma unroll
-          for (int q = 0; q < 12; ++q)
-            e[q] = ((q / 3) % 2 == 0) ? __reduce_min_sync(FULL, e[q]) : __reduce_max_sync(FULL, e[q]);
-          if (lane == 0) {
-            uint32_t* r = s_acc + (s0 & (kSlots - 1)) * kSegWords;
-            for (int q = 0; q < 12; ++q) {
-              if ((q / 3) % 2 == 0)
-                atomicMin(r + q, e[q]);
-              else
-                atomicMax(r + q, e[q]);
+    // ---- A: segment bounds and centroid bounds (the root level; later
+    // levels' come from the swap phase before them) ----
+    if (level == 0) {
+      for (uint32_t base = c0; base < c1; base += kBatch) {
+        batch_segments(seg_of, base, c1, nseg, p, s, sl);
+        for (uint32_t k = threadIdx.x; k < kSlots * kSegWords; k += blockDim.x)
+          s_acc[k] = (((k % kSegWords) / 3) % 2 == 0) ? 0xFFFFFFFFu : 0u;
+        __syncthreads();
+        float4 l[kBatchTiles], h[kBatchTiles];
+  #pragma unroll
+        for (int k = 0; k < kBatchTiles; ++k)
+          if (s[k] != kNone) {
+            l[k] = __ldcg(plo + p[k]);
+            h[k] = __ldcg(phi + p[k]);
+          }
+  #pragma unroll 1
+        for (int k = 0; k < kBatchTiles; ++k) {
+          const uint32_t sk = s[k];
+          if (!__any_sync(FULL, sk != kNone)) continue;
+          uint32_t e[12];
+          if (sk != kNone) {
+            V3 lo{l[k].x, l[k].y, l[k].z}, hi{h[k].x, h[k].y, h[k].z};
+            V3 c = mul(add(lo, hi), 0.5f);
+            e[0] = fenc(lo.x); e[1] = fenc(lo.y); e[2] = fenc(lo.z);
+            e[3] = fenc(hi.x); e[4] = fenc(hi.y); e[5] = fenc(hi.z);
+            e[6] = fenc(c.x); e[7] = fenc(c.y); e[8] = fenc(c.z);
+            e[9] = e[6]; e[10] = e[7]; e[11] = e[8];
+          } else {
+  #pragma unroll
+            for (int q = 0; q < 12; ++q) e[q] = ((q / 3) % 2 == 0) ? 0xFFFFFFFFu : 0u;
+          }
+          const uint32_t s0 = __shfl_sync(FULL, sk, 0);
+          if (__all_sync(FULL, sk == s0)) {  // one segment across the warp
+  #pragma unroll
+            for (int q = 0; q < 12; ++q)
+              e[q] = ((q / 3) % 2 == 0) ? __reduce_min_sync(FULL, e[q]) : __reduce_max_sync(FULL, e[q]);
+            if (lane == 0) {
+              uint32_t* r = s_acc + (s0 & (kSlots - 1)) * kSegWords;
+              for (int q = 0; q < 12; ++q) {
+                if ((q / 3) % 2 == 0)
+                  atomicMin(r + q, e[q]);
+                else
+                  atomicMax(r + q, e[q]);
+              }
+            }
+          } else {  // runs of one segment meet at the run's first lane
+  #pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              uint32_t so = __shfl_down_sync(FULL, sk, o);
+              bool take = (lane + o < 32) && (so == sk) && (sk != kNone);
+  #pragma unroll
+              for (int q = 0; q < 12; ++q) {
+                uint32_t y = __shfl_down_sync(FULL, e[q], o);
+                if (take) e[q] = ((q / 3) % 2 == 0) ? min(e[q], y) : max(e[q], y);
+              }
+            }
+            uint32_t sp = __shfl_up_sync(FULL, sk, 1);
+            if (sk != kNone && (lane == 0 || sp != sk)) {
+              uint32_t* r = s_acc + (sk & (kSlots - 1)) * kSegWords;
+              for (int q = 0; q < 12; ++q) {
+                if ((q / 3) % 2 == 0)
+                  atomicMin(r + q, e[q]);
+                else
+                  atomicMax(r + q, e[q]);
+              }
             }
           }
-        } else {  // runs of one segment meet at the run's first lane
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            uint32_t so = __shfl_down_sync(FULL, sk, o);
-            bool take = (lane + o < 32) && (so == sk) && (sk != kNone);
-#pragma unroll
-            for (int q = 0; q < 12; ++q) {
-              uint32_t y = __shfl_down_sync(FULL, e[q], o);
-              if (take) e[q] = ((q / 3) % 2 == 0) ? min(e[q], y) : max(e[q], y);
-            }
-          }
-          uint32_t sp = __shfl_up_sync(FULL, sk, 1);
-          if (sk != kNone && (lane == 0 || sp != sk)) {
-            uint32_t* r = s_acc + (sk & (kSlots - 1)) * kSegWords;
-            for (int q = 0; q < 12; ++q) {
-              if ((q / 3) % 2 == 0)
-                atomicMin(r + q, e[q]);
-              else
-                atomicMax(r + q, e[q]);
-            }
-          }
         }
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < kSlots * kSegWords; k += blockDim.x) {
+          const uint32_t seg = sl[k / kSegWords].s;
+          if (seg == kNone) continue;
+          const uint32_t v = s_acc[k];
+          const bool mn = ((k % kSegWords) / 3) % 2 == 0;
+          if (v == (mn ? 0xFFFFFFFFu : 0u)) continue;
+          uint32_t* dst = sacc + (size_t)seg * kSegWords + (k % kSegWords);
+          if (mn)
+            atomicMin(dst, v);
+          else
+            atomicMax(dst, v);
+        }
+        __syncthreads();
       }
-      __syncthreads();
-      for (uint32_t k = threadIdx.x; k < kSlots * kSegWords; k += blockDim.x) {
-        const uint32_t seg = sl[k / kSegWords].s;
-        if (seg == kNone) continue;
-        const uint32_t v = s_acc[k];
-        const bool mn = ((k % kSegWords) / 3) % 2 == 0;
-        if (v == (mn ? 0xFFFFFFFFu : 0u)) continue;
-        uint32_t* dst = sacc + (size_t)seg * kSegWords + (k % kSegWords);
-        if (mn)
-          atomicMin(dst, v);
-        else
-          atomicMax(dst, v);
-      }
-      __syncthreads();
+      if (!coop_sync(C.bar, C.err)) return;
     }
-    if (!coop_sync(C.bar, C.err)) return;
 
     // ---- B: buckets ----
     for (uint32_t base = c0; base < c1; base += kBatch) {
@@ -1427,6 +1432,9 @@ __global__ void __launch_bounds__(kCoopBlock, kCoopPerSM) k_sah_levels(CoopSah C
             }
           }
         }
+        for (uint32_t k = threadIdx.x; k < 2 * kSlots * kSegWords; k += blockDim.x)
+          s_nacc[k] = (((k % kSegWords) / 3) % 2 == 0) ? 0xFFFFFFFFu : 0u;
+        if (threadIdx.x < 2 * kSlots) s_nid[threadIdx.x] = kNone;
         __syncthreads();
         uint32_t it[kBatchTiles];
 #pragma unroll
@@ -1434,43 +1442,89 @@ __global__ void __launch_bounds__(kCoopBlock, kCoopPerSM) k_sah_levels(CoopSah C
 #pragma unroll 1
         for (int k = 0; k < kBatchTiles; ++k) {
           const uint32_t pk = p[k];
-          if (pk >= c1) continue;
-          if (s[k] == kNone) {
+          uint32_t cs = kNone;  // the large child segment the root lands in
+          float4 lv = make_float4(0.0f, 0.0f, 0.0f, 0.0f), hv = lv;
+          if (pk < c1 && s[k] == kNone) {
             item_n[pk] = it[k];
             seg_n[pk] = kNone;
-            continue;
+          } else if (pk < c1 && sl[s[k] & (kSlots - 1)].s != kNone) {
+            const SlotSeg& g = sl[s[k] & (kSlots - 1)];
+            const bool pred = __ldcg(C.bucket + pk) <= g.best;
+            const bool fF = pk < g.spt && !pred, fT = pk >= g.spt && pred;
+            uint32_t dst = pk;
+            const uint32_t n = g.b - g.a + 1;
+            if (fF || fT) {  // the r-th false (from the left) and the r-th true (from the right) trade places
+              const uint32_t r = __ldcg(C.rnk + pk);
+              dst = r < n ? __ldcg((fF ? C.posT : C.posF) + g.a + r) : kNone;
+            }
+            if (dst < g.a || dst > g.b) {
+              atomicOr(C.err, kErrBuild);
+            } else {
+              item_n[dst] = it[k];
+              lv = __ldcg(plo + pk);
+              hv = __ldcg(phi + pk);
+              C.plo[nx][dst] = lv;
+              C.phi[nx][dst] = hv;
+              cs = dst < g.mid ? g.cl : g.cr;
+              seg_n[dst] = cs;
+              const uint32_t me = C.N2 + g.node;
+              if (dst == g.a && g.mid - g.a == 1) {
+                uint32_t r = C.troot[it[k]];
+                C.child0[me] = r;
+                C.parent[r] = (me << 1) | 0u;
+                C.t_ld[it[k]] = ld_child(g.ld, 0);
+              }
+              if (dst == g.b && g.b - g.mid + 1 == 1) {
+                uint32_t r = C.troot[it[k]];
+                C.child1[me] = r;
+                C.parent[r] = (me << 1) | 1u;
+                C.t_ld[it[k]] = ld_child(g.ld, 1);
+              }
+            }
           }
-          const SlotSeg& g = sl[s[k] & (kSlots - 1)];
-          if (g.s == kNone) continue;
-          const bool pred = __ldcg(C.bucket + pk) <= g.best;
-          const bool fF = pk < g.spt && !pred, fT = pk >= g.spt && pred;
-          uint32_t dst = pk;
-          const uint32_t n = g.b - g.a + 1;
-          if (fF || fT) {  // the r-th false (from the left) and the r-th true (from the right) trade places
-            const uint32_t r = __ldcg(C.rnk + pk);
-            dst = r < n ? __ldcg((fF ? C.posT : C.posF) + g.a + r) : kNone;
+          // the next level's bounds and centroid bounds of the child segment:
+          // the lanes of one child reduce together, their first lane adds
+          // to the batch's slot (children of a batch's segments have
+          // consecutive ids, at most 2 * kSlots of them)
+          if (__any_sync(FULL, cs != kNone)) {
+            const uint32_t peers = __match_any_sync(FULL, cs);
+            if (cs != kNone) {
+              const V3 lo{lv.x, lv.y, lv.z}, hi{hv.x, hv.y, hv.z};
+              const V3 c = mul(add(lo, hi), 0.5f);
+              uint32_t e[12];
+              e[0] = fenc(lo.x); e[1] = fenc(lo.y); e[2] = fenc(lo.z);
+              e[3] = fenc(hi.x); e[4] = fenc(hi.y); e[5] = fenc(hi.z);
+              e[6] = fenc(c.x); e[7] = fenc(c.y); e[8] = fenc(c.z);
+              e[9] = e[6]; e[10] = e[7]; e[11] = e[8];
+#pragma unroll
+              for (int q = 0; q < 12; ++q)
+                e[q] = ((q / 3) % 2 == 0) ? __reduce_min_sync(peers, e[q]) : __reduce_max_sync(peers, e[q]);
+              if (lane == (uint32_t)(__ffs(peers) - 1)) {
+                const uint32_t z = cs & (2 * kSlots - 1);
+                s_nid[z] = cs;
+                uint32_t* r = s_nacc + z * kSegWords;
+                for (int q = 0; q < 12; ++q) {
+                  if ((q / 3) % 2 == 0)
+                    atomicMin(r + q, e[q]);
+                  else
+                    atomicMax(r + q, e[q]);
+                }
+              }
+            }
           }
-          if (dst < g.a || dst > g.b) {
-            atomicOr(C.err, kErrBuild);
-            continue;
-          }
-          item_n[dst] = it[k];
-          C.plo[nx][dst] = __ldcg(plo + pk);
-          C.phi[nx][dst] = __ldcg(phi + pk);
-          seg_n[dst] = dst < g.mid ? g.cl : g.cr;
-          const uint32_t me = C.N2 + g.node;
-          if (dst == g.a && g.mid - g.a == 1) {
-            uint32_t r = C.troot[it[k]];
-            C.child0[me] = r;
-            C.parent[r] = (me << 1) | 0u;
-            C.t_ld[it[k]] = ld_child(g.ld, 0);
-          }
-          if (dst == g.b && g.b - g.mid + 1 == 1) {
-            uint32_t r = C.troot[it[k]];
-            C.child1[me] = r;
-            C.parent[r] = (me << 1) | 1u;
-            C.t_ld[it[k]] = ld_child(g.ld, 1);
-          }
+        }
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < 2 * kSlots * kSegWords; k += blockDim.x) {
+          const uint32_t cs = s_nid[k / kSegWords];
+          if (cs == kNone) continue;
+          const uint32_t v = s_nacc[k];
+          const bool mn = ((k % kSegWords) / 3) % 2 == 0;
+          if (v == (mn ? 0xFFFFFFFFu : 0u)) continue;
+          uint32_t* dst = C.sacc[nx] + (size_t)cs * kSegWords + (k % kSegWords);
+          if (mn)
+            atomicMin(dst, v);
+          else
+            atomicMax(dst, v);
         }
         __syncthreads();
       }
