@@ -68,14 +68,21 @@ __device__ __forceinline__ uint32_t div_up_d(uint32_t a, uint32_t b) { return (u
 // 64-bit words that pack two 32-bit counts whose sums stay below 2^32 (no
 // carry crosses the halves, so one scan gives both prefix sums)
 // ---------------------------------------------------------------------------
+// The scanned values come from an input functor: an array, or values made
+// on the fly by the scan's first launch (no launch of their own).
 template <class V>
-__global__ void k_scan_tile(const V* in, V* out, uint32_t n, V* bsum) {
+struct ArrayIn {
+  const V* p;
+  __device__ __forceinline__ V operator()(uint32_t i) const { return p[i]; }
+};
+template <class V, class In>
+__global__ void k_scan_tile(In in, V* out, uint32_t n, V* bsum) {
   __shared__ V sh[kScanTile];
   __shared__ V wsum[kScanBlock / 32];
   const uint32_t base = blockIdx.x * kScanTile;
   for (int k = 0; k < kScanItems; ++k) {
     uint32_t i = base + threadIdx.x + k * kScanBlock;
-    sh[threadIdx.x + k * kScanBlock] = i < n ? in[i] : V(0);
+    sh[threadIdx.x + k * kScanBlock] = i < n ? in(i) : V(0);
   }
   __syncthreads();
   V v[kScanItems];
@@ -147,10 +154,10 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_add_tiles(V* out, uint32_t 
   }
 }
 
-template <class V>
-cudaError_t scan_exclusive_t(const V* in, V* out, uint32_t n, V* tmp, size_t tmp_n, cudaStream_t s) {
+template <class V, class In>
+cudaError_t scan_exclusive_t(In in, V* out, uint32_t n, V* tmp, size_t tmp_n, cudaStream_t s) {
   struct Lvl {
-    const V* in;
+    const V* in;  // levels above the first: the sums below
     V* out;
     uint32_t n;
     V* sums;
@@ -158,7 +165,7 @@ cudaError_t scan_exclusive_t(const V* in, V* out, uint32_t n, V* tmp, size_t tmp
   Lvl lv[8];
   int L = 0;
   size_t off = 0;
-  const V* cin = in;
+  const V* cin = nullptr;
   V* cout = out;
   uint32_t m = n;
   while (true) {
@@ -173,15 +180,15 @@ cudaError_t scan_exclusive_t(const V* in, V* out, uint32_t n, V* tmp, size_t tmp
     m = nb;
     if (L >= 8) return cudaErrorInvalidValue;
   }
+  const uint32_t nb0 = div_up(n, kScanTile);
+  k_scan_tile<V, In><<<nb0, kScanBlock, 0, s>>>(in, out, n, lv[0].sums);
   if (L == 2) {  // the tile sums fit one tile: two launches
-    const uint32_t nb = div_up(n, kScanTile);
-    k_scan_tile<V><<<nb, kScanBlock, 0, s>>>(in, out, n, lv[0].sums);
-    k_scan_add_tiles<V><<<nb, kScanBlock, 0, s>>>(out, n, lv[0].sums);
+    k_scan_add_tiles<V><<<nb0, kScanBlock, 0, s>>>(out, n, lv[0].sums);
     return cudaGetLastError();
   }
-  for (int i = 0; i < L; ++i) {
+  for (int i = 1; i < L; ++i) {
     uint32_t nb = div_up(lv[i].n, kScanTile);
-    k_scan_tile<V><<<nb, kScanBlock, 0, s>>>(lv[i].in, lv[i].out, lv[i].n, lv[i].sums);
+    k_scan_tile<V, ArrayIn<V>><<<nb, kScanBlock, 0, s>>>(ArrayIn<V>{lv[i].in}, lv[i].out, lv[i].n, lv[i].sums);
   }
   for (int i = L - 2; i >= 0; --i) {
     k_scan_add<V><<<div_up(lv[i].n, 256), 256, 0, s>>>(lv[i].out, lv[i].n, lv[i].sums);
@@ -206,13 +213,20 @@ uint32_t scan_launches(uint32_t n) {
   return levels == 2 ? 2 : 2 * levels - 1;
 }
 
-cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, DevBuf<uint32_t>& tmp, cudaStream_t s) {
+namespace {
+template <class In>
+cudaError_t scan_exclusive_in(In in, uint32_t* out, uint32_t n, DevBuf<uint32_t>& tmp, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   // tmp layout: level-1 sums, level-2 sums, ...
   size_t need = scan_tmp_need(n);
   cudaError_t e = tmp.ensure(need + 8);
   if (e != cudaSuccess) return e;
-  return scan_exclusive_t(in, out, n, tmp.p, need + 8, s);
+  return scan_exclusive_t<uint32_t, In>(in, out, n, tmp.p, need + 8, s);
+}
+}  // namespace
+
+cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, DevBuf<uint32_t>& tmp, cudaStream_t s) {
+  return scan_exclusive_in(ArrayIn<uint32_t>{in}, out, n, tmp, s);
 }
 
 namespace {
@@ -430,17 +444,21 @@ __global__ void __launch_bounds__(kB) k_radix_scatter(const uint32_t* kin, const
 // ---------------------------------------------------------------------------
 // treelets (top 12 bits of the code)
 // ---------------------------------------------------------------------------
-__global__ void k_treelet_flags(const uint32_t* skey, uint32_t N, uint32_t* flags) {
+// A treelet starts where the top 12 bits of the code change (the scan's input).
+struct TreeletFlagIn {
+  const uint32_t* skey;
+  __device__ __forceinline__ uint32_t operator()(uint32_t i) const {
+    return (i == 0 || ((skey[i] ^ skey[i - 1]) & kTreeletMask) != 0) ? 1u : 0u;
+  }
+};
+__global__ void k_treelet_ids(const uint32_t* skey, uint32_t* tid, uint32_t* tstart, uint32_t N, uint32_t* info) {
+  const TreeletFlagIn flag{skey};
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
-  flags[i] = (i == 0 || ((skey[i] ^ skey[i - 1]) & kTreeletMask) != 0) ? 1u : 0u;
-}
-__global__ void k_treelet_ids(const uint32_t* flags, uint32_t* tid, uint32_t* tstart, uint32_t N, uint32_t* info) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
-  uint32_t t = tid[i] + flags[i] - 1u;  // inclusive - 1
+  const uint32_t f = flag(i);
+  uint32_t t = tid[i] + f - 1u;  // inclusive - 1
   tid[i] = t;
-  if (flags[i]) tstart[t] = i;
+  if (f) tstart[t] = i;
   if (i == N - 1) info[kInfoT] = t + 1u;
 }
 __global__ void k_treelet_sizes(const uint32_t* tstart, uint32_t* tsize, const uint32_t* info, uint32_t N) {
@@ -952,6 +970,7 @@ __global__ void __launch_bounds__(kCoopBlock, kCoopPerSM) k_sah_levels(CoopSah C
       C.counters[3] = 0u;
       C.counters[4] = 0u;
       C.counters[5] = 0u;
+      C.counters[1] = 0u;
       C.counters[7] = 0u;
     }
     return;
@@ -972,6 +991,7 @@ __global__ void __launch_bounds__(kCoopBlock, kCoopPerSM) k_sah_levels(CoopSah C
       C.counters[3] = T <= kSmallSeg ? 0u : 1u;
       C.counters[4] = 0u;
       C.counters[5] = 0u;
+      C.counters[1] = 0u;
       C.counters[7] = 0u;
     }
     return;
@@ -995,6 +1015,7 @@ __global__ void __launch_bounds__(kCoopBlock, kCoopPerSM) k_sah_levels(CoopSah C
     C.counters[3] = 0u;
     C.counters[4] = 0u;
     C.counters[5] = 0u;
+    C.counters[1] = 0u;
     C.counters[7] = 0u;
   }
   if (!coop_sync(C.bar, C.err)) return;
@@ -1598,7 +1619,7 @@ struct MedArgs {
   uint32_t* sah_ld;
   uint32_t* t_ld;
   uint32_t* counters;  // [0] SAH nodes allocated, [2] small segments queued, [3] medium segments queued,
-                       // [4], [7] medium segments taken (two passes), [5] small segments taken
+                       // [4], [7] medium segments taken (two passes), [5], [1] small segments taken
   uint32_t* err;
 };
 
@@ -2012,7 +2033,7 @@ __device__ bool sah_pair(const SahArgs& A, uint32_t base, uint32_t p, uint32_t n
 // instead of a step of their own. A persistent grid of warps walks the
 // queue, whose length it reads from *nsmall_p (the cooperative and
 // block-local levels fill the queue on the device), each warp taking the
-// next segment from counters[5].
+// next segment from counters[5] (then counters[1]).
 __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t* sm_start, const uint32_t* sm_end,
                             const uint32_t* sm_node, const uint32_t* sm_ld, uint32_t* cur, uint32_t* counters, uint32_t* sah_axis,
                             float4* nb_lo, float4* nb_hi, uint32_t* child0, uint32_t* child1, uint32_t* parent,
@@ -2023,13 +2044,18 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
   const uint32_t FULL = 0xFFFFFFFFu;
   const uint32_t w = threadIdx.x >> 5, lane = lane_id();
   const uint32_t nsmall = *nsmall_p;
-  for (;;) {
+  for (uint32_t pass = 0; pass < 2;) {
     // segments (2 to 32 roots) taken in turn from a counter, which keeps the
-    // warps' loads even
+    // warps' loads even; those of more than 16 roots first (pass 0), so the
+    // last to run are the shorter ones
     uint32_t seg = 0;
-    if (lane == 0) seg = atomicAdd(counters + 5, 1u);
+    if (lane == 0) seg = atomicAdd(counters + (pass == 0 ? 5 : 1), 1u);
     seg = __shfl_sync(FULL, seg, 0);
-    if (seg >= nsmall) break;
+    if (seg >= nsmall) {
+      ++pass;
+      continue;
+    }
+    if ((sm_end[seg] - sm_start[seg] + 1 > kSmallSeg / 2) != (pass == 0)) continue;
     const uint32_t base = sm_start[seg];
     const uint32_t n = sm_end[seg] - base + 1;
     if (n < 2 || n > kSmallSeg || sm_end[seg] >= A.N) {
@@ -2194,21 +2220,24 @@ __global__ void k_small_sah(SahArgs A, const uint32_t* nsmall_p, const uint32_t*
 // permute roots within a segment), so its count is its cnt - 1 SAH nodes
 // plus the treelet sizes over that range: per position the treelet size of
 // its root (zero past T), scanned, then one difference per SAH node.
-__global__ void k_pos_tsize(const uint32_t* info, const uint32_t* cur, const uint32_t* troot, const uint32_t* size,
-                            uint32_t* tpos, uint32_t* tinv, uint32_t n) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const uint32_t T = info[kInfoT];
-  uint32_t v = 0;
-  if (p < T && T > 1) {
-    const uint32_t t = cur[p];
-    if (t < T) {
-      v = size[troot[t]];
-      tinv[t] = p;  // the final position of treelet t
+struct PosTsizeIn {
+  const uint32_t* info;
+  const uint32_t* cur;
+  const uint32_t* troot;
+  const uint32_t* size;
+  uint32_t* tinv;  // the final position of each treelet, written on the way
+  __device__ __forceinline__ uint32_t operator()(uint32_t p) const {
+    const uint32_t T = info[kInfoT];
+    if (p < T && T > 1) {
+      const uint32_t t = cur[p];
+      if (t < T) {
+        tinv[t] = p;
+        return size[troot[t]];
+      }
     }
+    return 0u;
   }
-  tpos[p] = v;
-}
+};
 __global__ void k_sah_sizes(const uint32_t* info, const uint32_t* rng, const uint32_t* tpre, uint32_t* size,
                             uint32_t N2, uint32_t* err) {
   const uint32_t nd = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2662,7 +2691,6 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   WPBR_CUDA(B.v1.ensure(N));
   const uint32_t nblk = div_up(N, kRadixTile);
   WPBR_CUDA(B.hist.ensure((size_t)256 * nblk));
-  WPBR_CUDA(B.flags.ensure(N));
   WPBR_CUDA(B.tid.ensure(N));
   WPBR_CUDA(B.tstart.ensure(N));
   WPBR_CUDA(B.tsize.ensure(N));
@@ -2756,9 +2784,8 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   B.skey = kin;
   B.sprim = vin;
   // treelets
-  k_treelet_flags<<<g, kB, 0, st>>>(B.skey, N, B.flags.p);
-  WPBR_CUDA(scan_exclusive(B.flags.p, B.tid.p, N, B.scan_tmp, st));
-  k_treelet_ids<<<g, kB, 0, st>>>(B.flags.p, B.tid.p, B.tstart.p, N, B.dinfo.p);
+  WPBR_CUDA(scan_exclusive_in(TreeletFlagIn{B.skey}, B.tid.p, N, B.scan_tmp, st));
+  k_treelet_ids<<<g, kB, 0, st>>>(B.skey, B.tid.p, B.tstart.p, N, B.dinfo.p);
   k_treelet_sizes<<<g, kB, 0, st>>>(B.tstart.p, B.tsize.p, B.dinfo.p, N);
   // A7
   WPBR_CUDA(cudaMemsetAsync(B.visits.p, 0, sizeof(uint32_t) * NU, st));
@@ -2850,8 +2877,8 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
         A, B.counters.p + 2, B.small_start.p, B.small_end.p, B.small_node.p, B.small_ld.p, B.cur.p, B.counters.p,
         B.sah_axis.p,
         B.nb_lo.p, B.nb_hi.p, B.child0.p, B.child1.p, B.parent.p, N2, ctx->d_err.p);
-    k_pos_tsize<<<div_up(N + 1, kB), kB, 0, st>>>(B.dinfo.p, B.cur.p, B.troot.p, B.size.p, B.tpos.p, B.tinv.p, N + 1);
-    WPBR_CUDA(scan_exclusive(B.tpos.p, B.tpos.p, N + 1, B.scan_tmp, st));
+    WPBR_CUDA(scan_exclusive_in(PosTsizeIn{B.dinfo.p, B.cur.p, B.troot.p, B.size.p, B.tinv.p}, B.tpos.p, N + 1,
+                                B.scan_tmp, st));
     k_sah_sizes<<<g, kB, 0, st>>>(B.dinfo.p, B.sah_rng.p, B.tpos.p, B.size.p, N2, ctx->d_err.p);
   }
   // A9
