@@ -2476,35 +2476,46 @@ __host__ __device__ inline uint32_t split_depth(uint32_t c) {
 
 // Records each child slot of the reference layout adds (slot s = 2 * record + child).
 // Slots past the tree's 2 * n_int (up to n_slots, the scanned length) count 0.
-__global__ void k_split_count(const uint32_t* info, const uint32_t* is_int, const uint32_t* int_index,
-                              const Node2* nodes, uint32_t* cnt, uint32_t n_slots, uint32_t* max_d) {
-  uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n_slots) return;
-  const uint32_t n_int = n_int_of(info, is_int, int_index);
-  if (s >= 2 * n_int) {
-    cnt[s] = 0u;
-    return;
-  }
-  int4 m = nodes[s >> 1].meta;
-  int ref = (s & 1) ? m.y : m.x;
-  uint32_t c = (s & 1) ? ((uint32_t)m.w & 0x3FFFFFFFu) : (uint32_t)m.z;
-  uint32_t d = ref < 0 ? split_depth(c) : 0u;
-  cnt[s] = d ? (1u << d) - 1u : 0u;
-  if (d) atomicMax(max_d, d);
+// Range-tree records of the last child slot of n_int interior records.
+__device__ __forceinline__ uint32_t last_slot_split_count(const Node2* nodes, uint32_t n_int) {
+  const int4 ml = nodes[n_int - 1].meta;
+  const uint32_t dl = ml.y < 0 ? split_depth((uint32_t)ml.w & 0x3FFFFFFFu) : 0u;
+  return dl ? (1u << dl) - 1u : 0u;
 }
+
+// Range-tree records of child slot s (0 for an interior child or a leaf too
+// small or too large to split), and the deepest range tree in *max_d: the
+// input of the scan that places the records (made inside the scan).
+struct SplitCountIn {
+  const uint32_t* info;
+  const uint32_t* is_int;
+  const uint32_t* int_index;
+  const Node2* nodes;
+  uint32_t* max_d;
+  __device__ __forceinline__ uint32_t operator()(uint32_t s) const {
+    const uint32_t n_int = n_int_of(info, is_int, int_index);
+    if (s >= 2 * n_int) return 0u;
+    int4 m = nodes[s >> 1].meta;
+    int ref = (s & 1) ? m.y : m.x;
+    uint32_t c = (s & 1) ? ((uint32_t)m.w & 0x3FFFFFFFu) : (uint32_t)m.z;
+    uint32_t d = ref < 0 ? split_depth(c) : 0u;
+    if (d) atomicMax(max_d, d);
+    return d ? (1u << d) - 1u : 0u;
+  }
+};
 
 // One thread per child slot: redirects the slot to its range tree and writes
 // the tree's records (boxes = union of the primitive bounds of each range).
 // out holds a copy of the reference layout's n_int records on entry and has
 // room for n_cap records.
 __global__ void k_split_emit(const uint32_t* info, const uint32_t* is_int, const uint32_t* int_index,
-                             const Node2* nodes, const uint32_t* cnt, const uint32_t* off, const uint32_t* sprim,
+                             const Node2* nodes, const uint32_t* off, const uint32_t* sprim,
                              const float4* pb_lo, const float4* pb_hi, uint32_t n_prims, Node2* out, uint32_t n_cap,
                              uint32_t* err) {
   uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t n_int = n_int_of(info, is_int, int_index);
   if (s >= 2 * n_int) return;
-  const uint32_t n_split = off[2 * n_int - 1] + cnt[2 * n_int - 1];
+  const uint32_t n_split = off[2 * n_int - 1] + last_slot_split_count(nodes, n_int);
   const uint32_t n_out = (uint64_t)n_int + n_split <= n_cap ? n_int + n_split : 0u;
   uint32_t i = s >> 1, k = s & 1;
   int4 m = nodes[i].meta;
@@ -2577,7 +2588,7 @@ __global__ void k_split_emit(const uint32_t* info, const uint32_t* is_int, const
 // tree depth, SAH nodes, the error word, the root's record and bounds.
 constexpr uint32_t kSumWords = 17;
 __global__ void k_build_summary(uint32_t* info, const uint32_t* is_int, const uint32_t* int_index,
-                                const uint32_t* split_cnt, const uint32_t* split_off, const uint32_t* counters,
+                                const Node2* nodes, const uint32_t* split_off, const uint32_t* counters,
                                 const uint32_t* depth_max, const uint32_t* lin_node, const float* lin_bounds,
                                 const uint32_t* err) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
@@ -2586,7 +2597,7 @@ __global__ void k_build_summary(uint32_t* info, const uint32_t* is_int, const ui
   o[0] = info[kInfoT];
   o[1] = info[kInfoM];
   o[2] = n_int;
-  o[3] = n_int ? split_off[2 * n_int - 1] + split_cnt[2 * n_int - 1] : 0u;
+  o[3] = n_int ? split_off[2 * n_int - 1] + last_slot_split_count(nodes, n_int) : 0u;
   o[4] = counters[6];
   o[5] = *depth_max;
   o[6] = counters[0];
@@ -2753,7 +2764,6 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   WPBR_CUDA(B.nodes2.ensure(N));
   WPBR_CUDA(B.nodes_split.ensure(split_cap));
   WPBR_CUDA(B.prims.ensure((size_t)3 * N));
-  WPBR_CUDA(B.split_cnt.ensure(N2));
   WPBR_CUDA(B.split_off.ensure(N2));
   if (!B.h_info) WPBR_CUDA(cudaMallocHost((void**)&B.h_info, sizeof(uint32_t) * kInfoWords));
 
@@ -2901,13 +2911,12 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   // leaf-split layout (the default binary traversal); a tree whose root is a
   // leaf keeps the reference layout
   WPBR_CUDA(cudaMemsetAsync(B.counters.p + 6, 0, 4, st));
-  k_split_count<<<g2, kB, 0, st>>>(B.dinfo.p, B.is_int.p, B.int_index.p, B.nodes2.p, B.split_cnt.p, N2,
-                                   B.counters.p + 6);
-  WPBR_CUDA(scan_exclusive(B.split_cnt.p, B.split_off.p, N2, B.scan_tmp, st));
-  k_split_emit<<<g2, kB, 0, st>>>(B.dinfo.p, B.is_int.p, B.int_index.p, B.nodes2.p, B.split_cnt.p, B.split_off.p,
+  WPBR_CUDA(scan_exclusive_in(SplitCountIn{B.dinfo.p, B.is_int.p, B.int_index.p, B.nodes2.p, B.counters.p + 6},
+                              B.split_off.p, N2, B.scan_tmp, st));
+  k_split_emit<<<g2, kB, 0, st>>>(B.dinfo.p, B.is_int.p, B.int_index.p, B.nodes2.p, B.split_off.p,
                                   B.sprim, B.pb_lo.p, B.pb_hi.p, N, B.nodes_split.p, (uint32_t)split_cap,
                                   ctx->d_err.p);
-  k_build_summary<<<1, 32, 0, st>>>(B.dinfo.p, B.is_int.p, B.int_index.p, B.split_cnt.p, B.split_off.p,
+  k_build_summary<<<1, 32, 0, st>>>(B.dinfo.p, B.is_int.p, B.int_index.p, B.nodes2.p, B.split_off.p,
                                     B.counters.p, B.depth_max.p, B.lin_node.p, B.lin_bounds.p, ctx->d_err.p);
   WPBR_CUDA(cudaGetLastError());
   WPBR_CUDA(cudaMemcpyAsync(B.h_info, B.dinfo.p + kInfoSum, sizeof(uint32_t) * kSumWords, cudaMemcpyDeviceToHost,

@@ -146,7 +146,7 @@ void bvh_release(wpbr_ctx* ctx, bool keep_traversal) {
   B.med_ld.release(); B.small_ld.release(); B.role.release(); B.counters.release(); B.dinfo.release(); B.sah_axis.release(); B.lin_node.release();
   B.lin_bounds.release(); B.is_int.release(); B.int_index.release(); B.depth_max.release();
   B.int_kids.release(); B.int_slot.release();
-  B.split_cnt.release(); B.split_off.release();
+  B.split_off.release();
   if (!keep_traversal) {
     B.nodes2.release();
     B.nodes_split.release();

@@ -91,7 +91,7 @@ struct BvhState {
   DevBuf<uint32_t> int_kids, int_slot;  // traversal-layout order of the interior nodes
   DevBuf<Node2> nodes2;
   DevBuf<Node2> nodes_split;             // leaf-split layout: nodes2 + the records splitting large leaves
-  DevBuf<uint32_t> split_cnt, split_off;  // records per child slot, and their offsets
+  DevBuf<uint32_t> split_off;  // offsets of each child slot's range-tree records
   DevBuf<float4> prims;
   BvhView view{};
 };
