@@ -461,11 +461,10 @@ __global__ void k_treelet_ids(const uint32_t* skey, uint32_t* tid, uint32_t* tst
   if (f) tstart[t] = i;
   if (i == N - 1) info[kInfoT] = t + 1u;
 }
-__global__ void k_treelet_sizes(const uint32_t* tstart, uint32_t* tsize, const uint32_t* info, uint32_t N) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+// Primitives of treelet t: from its start to the next treelet's (T treelets).
+__device__ __forceinline__ uint32_t treelet_size(uint32_t t, const uint32_t* tstart, const uint32_t* info, uint32_t N) {
   const uint32_t T = info[kInfoT];
-  if (t >= T) return;
-  tsize[t] = (t + 1 < T ? tstart[t + 1] : N) - tstart[t];
+  return (t + 1 < T ? tstart[t + 1] : N) - tstart[t];
 }
 
 // ---------------------------------------------------------------------------
@@ -482,13 +481,13 @@ struct KarrasCtx {
   }
 };
 
-__global__ void k_karras(const uint32_t* skey, const uint32_t* tid, const uint32_t* tstart, const uint32_t* tsize,
+__global__ void k_karras(const uint32_t* skey, const uint32_t* tid, const uint32_t* tstart, const uint32_t* info,
                          uint32_t N, uint32_t* rng_lo, uint32_t* rng_hi, uint32_t* child0, uint32_t* child1,
                          uint32_t* parent) {
   int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   if (i >= (int)N - 1) return;
   uint32_t t = tid[i];
-  KarrasCtx K{skey, tstart[t], tstart[t] + tsize[t] - 1};
+  KarrasCtx K{skey, tstart[t], tstart[t] + treelet_size(t, tstart, info, N) - 1};
   if ((uint32_t)i == K.te) return;  // last primitive of the treelet: no internal node here
   int d = (K.delta(i, i + 1) - K.delta(i, i - 1)) > 0 ? 1 : -1;
   int dmin = K.delta(i, i - d);
@@ -525,8 +524,8 @@ __device__ __forceinline__ bool ref_interior(uint32_t x, uint32_t N, const uint3
 }
 
 // treelet root of the treelet containing sorted position p
-__device__ __forceinline__ uint32_t treelet_root(uint32_t t, const uint32_t* tstart, const uint32_t* tsize, uint32_t N) {
-  return tsize[t] >= 2 ? tstart[t] : N + tstart[t];
+__device__ __forceinline__ uint32_t treelet_root(uint32_t t, const uint32_t* tstart, const uint32_t* info, uint32_t N) {
+  return treelet_size(t, tstart, info, N) >= 2 ? tstart[t] : N + tstart[t];
 }
 
 // An arrival count with acquire-release ordering: the arriving thread's
@@ -541,7 +540,7 @@ __device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t* a) {
 // Ref leaves compute their bounds; the second child to finish builds each
 // parent (atomic arrival counter), up to the treelet root.
 __global__ void k_refit(uint32_t N, const uint32_t* skey, const uint32_t* sprim, const uint32_t* tid,
-                        const uint32_t* tstart, const uint32_t* tsize, const uint32_t* rng_lo, const uint32_t* rng_hi,
+                        const uint32_t* tstart, const uint32_t* info, const uint32_t* rng_lo, const uint32_t* rng_hi,
                         const uint32_t* child0, const uint32_t* child1, const uint32_t* parent, uint32_t* visits,
                         uint32_t* size, float4* nb_lo, float4* nb_hi, const float4* pb_lo, const float4* pb_hi,
                         uint32_t* troot, uint8_t* role, uint32_t* err) {
@@ -562,7 +561,7 @@ __global__ void k_refit(uint32_t N, const uint32_t* skey, const uint32_t* sprim,
     lo = hi = X - N;
     t = tid[lo];
   }
-  uint32_t root = treelet_root(t, tstart, tsize, N);
+  uint32_t root = treelet_root(t, tstart, info, N);
   bool is_root = (X == root);
   if (!is_root) {
     uint32_t p = parent[X] >> 1;
@@ -2255,7 +2254,7 @@ __global__ void k_sah_sizes(const uint32_t* info, const uint32_t* rng, const uin
 // A9: flattenBVHTree — depth-first preorder index of every reference node
 // ---------------------------------------------------------------------------
 __global__ void k_flatten(uint32_t N, uint32_t* info, const uint32_t* skey, const uint32_t* tid,
-                          const uint32_t* tstart, const uint32_t* tsize, const uint32_t* rng_lo,
+                          const uint32_t* tstart, const uint32_t* rng_lo,
                           const uint32_t* rng_hi, const uint32_t* child0, const uint32_t* parent,
                           const uint32_t* size, const uint32_t* sah_axis, const float4* nb_lo, const float4* nb_hi,
                           const uint32_t* sah_ld, const uint32_t* sah_rng, const uint32_t* t_ld,
@@ -2290,7 +2289,7 @@ __global__ void k_flatten(uint32_t N, uint32_t* info, const uint32_t* skey, cons
       lo = hi = X - N;
       t = tid[lo];
     }
-    troot_ = treelet_root(t, tstart, tsize, N);
+    troot_ = treelet_root(t, tstart, info, N);
     kind = r == 2u ? 0u : 1u;
   }
   // the preorder index: an SAH node or a treelet root takes it from its
@@ -2704,7 +2703,6 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   WPBR_CUDA(B.hist.ensure((size_t)256 * nblk));
   WPBR_CUDA(B.tid.ensure(N));
   WPBR_CUDA(B.tstart.ensure(N));
-  WPBR_CUDA(B.tsize.ensure(N));
   WPBR_CUDA(B.troot.ensure(N));
   WPBR_CUDA(B.rng_lo.ensure(N));
   WPBR_CUDA(B.rng_hi.ensure(N));
@@ -2796,14 +2794,13 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   // treelets
   WPBR_CUDA(scan_exclusive_in(TreeletFlagIn{B.skey}, B.tid.p, N, B.scan_tmp, st));
   k_treelet_ids<<<g, kB, 0, st>>>(B.skey, B.tid.p, B.tstart.p, N, B.dinfo.p);
-  k_treelet_sizes<<<g, kB, 0, st>>>(B.tstart.p, B.tsize.p, B.dinfo.p, N);
   // A7
   WPBR_CUDA(cudaMemsetAsync(B.visits.p, 0, sizeof(uint32_t) * NU, st));
   WPBR_CUDA(cudaMemsetAsync(B.parent.p, 0xFF, sizeof(uint32_t) * NU, st));
   if (N > 1)
-    k_karras<<<div_up(N - 1, kB), kB, 0, st>>>(B.skey, B.tid.p, B.tstart.p, B.tsize.p, N, B.rng_lo.p, B.rng_hi.p,
+    k_karras<<<div_up(N - 1, kB), kB, 0, st>>>(B.skey, B.tid.p, B.tstart.p, B.dinfo.p, N, B.rng_lo.p, B.rng_hi.p,
                                                B.child0.p, B.child1.p, B.parent.p);
-  k_refit<<<div_up(2 * N, kB), kB, 0, st>>>(N, B.skey, B.sprim, B.tid.p, B.tstart.p, B.tsize.p, B.rng_lo.p,
+  k_refit<<<div_up(2 * N, kB), kB, 0, st>>>(N, B.skey, B.sprim, B.tid.p, B.tstart.p, B.dinfo.p, B.rng_lo.p,
                                             B.rng_hi.p, B.child0.p, B.child1.p, B.parent.p, B.visits.p, B.size.p,
                                             B.nb_lo.p, B.nb_hi.p, B.pb_lo.p, B.pb_hi.p, B.troot.p, B.role.p,
                                             ctx->d_err.p);
@@ -2894,7 +2891,7 @@ static wpbr_status bvh_build_tree(wpbr_ctx* ctx) {
   // A9
   WPBR_CUDA(cudaMemsetAsync(B.is_int.p, 0, sizeof(uint32_t) * N2, st));
   WPBR_CUDA(cudaMemsetAsync(B.depth_max.p, 0, 4, st));
-  k_flatten<<<div_up((uint64_t)N2 + N, kB), kB, 0, st>>>(N, B.dinfo.p, B.skey, B.tid.p, B.tstart.p, B.tsize.p,
+  k_flatten<<<div_up((uint64_t)N2 + N, kB), kB, 0, st>>>(N, B.dinfo.p, B.skey, B.tid.p, B.tstart.p,
                                                           B.rng_lo.p, B.rng_hi.p, B.child0.p, B.parent.p, B.size.p,
                                                           B.sah_axis.p, B.nb_lo.p, B.nb_hi.p, B.sah_ld.p,
                                                           B.sah_rng.p, B.t_ld.p, B.tinv.p, B.tpos.p, B.role.p, B.lin_node.p,

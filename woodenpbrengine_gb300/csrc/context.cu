@@ -134,7 +134,7 @@ void bvh_release(wpbr_ctx* ctx, bool keep_traversal) {
   BvhState& B = ctx->bvh;
   B.pb_lo.release(); B.pb_hi.release(); B.centroid.release(); B.codes.release(); B.cb_enc.release();
   B.k0.release(); B.k1.release(); B.v0.release(); B.v1.release(); B.hist.release(); B.scan_tmp.release();
-  B.tid.release(); B.tstart.release(); B.tsize.release(); B.troot.release();
+  B.tid.release(); B.tstart.release(); B.troot.release();
   B.rng_lo.release(); B.rng_hi.release(); B.child0.release(); B.child1.release(); B.parent.release();
   B.visits.release(); B.size.release(); B.nb_lo.release(); B.nb_hi.release();
   B.cur.release(); B.nxt.release(); B.seg_of.release(); B.posF.release(); B.posT.release(); B.rnk.release();

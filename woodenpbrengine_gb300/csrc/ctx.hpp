@@ -62,7 +62,7 @@ struct BvhState {
   uint32_t* skey = nullptr;   // sorted codes (points into k0/k1)
   uint32_t* sprim = nullptr;  // sorted primitive ids
   // treelets / Karras
-  DevBuf<uint32_t> tid, tstart, tsize, troot;
+  DevBuf<uint32_t> tid, tstart, troot;
   DevBuf<uint32_t> rng_lo, rng_hi, child0, child1;  // unified-id arrays
   DevBuf<uint32_t> parent, visits, size;            // size 2N+T
   DevBuf<float4> nb_lo, nb_hi;                      // node bounds, unified ids
