@@ -14,13 +14,17 @@
 //                                                reference's leaf rule (n < 30 or equal codes),
 //                                                bottom-up bounds (k_refit)
 //   JobBuildUpperSAH                             level-synchronous segmented 12-bucket SAH over
-//                                                treelet roots, every level in one cooperative
-//                                                launch (k_sah_levels), std::partition's
-//                                                two-pointer swap order reproduced with ranks;
-//                                                segments of <= 32 roots finish in one warp
+//                                                treelet roots: the levels of segments of more
+//                                                than 4,096 roots in one cooperative launch
+//                                                (k_sah_levels), std::partition's two-pointer
+//                                                swap order reproduced with ranks; segments of
+//                                                33..4,096 roots in one block each
+//                                                (k_medium_sah), of <= 32 in one warp each
 //                                                (k_small_sah)
-//   flattenBVHTree                               preorder index by walking up subtree sizes
-//                                                (k_flatten), then k_node2 / k_prims
+//   flattenBVHTree                               subtree sizes from each SAH node's position
+//                                                range (k_sah_sizes), preorder index from the
+//                                                recorded depth and child-0 steps (k_flatten),
+//                                                then k_node2 / k_prims
 //
 // Unified node ids: [0, N-1) radix-tree internal nodes, [N, 2N) single
 // primitives (sorted position + N), [2N, 2N + T) SAH nodes.
