@@ -36,6 +36,33 @@ def test_spectral_film_matches_oracle(W, O, ctx, config, res, level, quirks):
     ctx.set_quirks(0)
 
 
+@pytest.mark.parametrize("spp", [3, 4, 6, 8])
+def test_spectral_frame_in_pass_groups(W, O, ctx, spp):
+    # wpbr_render runs Sampled64 frames in groups of 4 or 2 sequential passes
+    # (whichever divides spp, else one at a time), gathering each group's
+    # samples into the film at once, in pass order: the film is the oracle's
+    g = W.SceneGen(2, 0, (44, 28), level=4)
+    ctx.set_quirks(0)
+    ctx.set_spectrum(W.SPECTRUM_SAMPLED64)
+    try:
+        ctx.upload(g.desc)
+        ctx.build()
+        ctx.render_setup(spp, seed=5, stream=3)
+        ctx.render()
+        L, w = ctx.film(44, 28)
+        Lo, wo = O.OracleScene(g.desc).render_spectral(44, 28, spp, 5, 3)
+        assert np.array_equal(w, wo)
+        assert _same_nan_aware(L, Lo)
+        # a second frame on the same context reuses the group graph
+        ctx.render_setup(spp, seed=5, stream=3)
+        ctx.render()
+        L2, w2 = ctx.film(44, 28)
+        assert np.array_equal(w2, wo) and _same_nan_aware(L2, Lo)
+    finally:
+        ctx.set_spectrum(W.SPECTRUM_RGB)
+    ctx.check_device_errors()
+
+
 def test_back_to_rgb_after_spectral(W, O, ctx):
     g = W.SceneGen(0, 0, (32, 32))
     ctx.set_quirks(0)

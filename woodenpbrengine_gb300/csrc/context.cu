@@ -226,6 +226,7 @@ WPBR_API void wpbr_destroy(wpbr_ctx* ctx) {
   if (ctx->bvh.h_info) cudaFreeHost(ctx->bvh.h_info);
   RenderState& R = ctx->rs;
   if (R.ggraph) cudaGraphExecDestroy(R.ggraph);
+  if (R.sgraph) cudaGraphExecDestroy(R.sgraph);
   for (uint32_t g = 0; g < RenderState::kMaxGroup; ++g) {
     if (R.gstream[g]) cudaStreamDestroy(R.gstream[g]);
     if (R.gjoin[g]) cudaEventDestroy(R.gjoin[g]);

@@ -135,6 +135,11 @@ struct RenderState {
   uint32_t group = 0;  // passes per group of the captured group graph
   cudaGraphExec_t ggraph = nullptr;
   uint64_t ggraph_key = 0;
+  // Sampled64 frames: one graph of `sgroup` sequential passes (sample slots
+  // 0 .. sgroup - 1) and one film gather over them
+  cudaGraphExec_t sgraph = nullptr;
+  uint64_t sgraph_key = 0;
+  uint32_t sgroup = 0;
   cudaStream_t gstream[kMaxGroup] = {};
   cudaEvent_t gfork = nullptr, gjoin[kMaxGroup] = {};
 };
@@ -293,8 +298,11 @@ wpbr_status spectral_setup(wpbr_ctx* ctx);
 // Sampled64 pieces of render_pass_launch: the scalar spawn (replaces the
 // RGB spawn) and the per-bin finish + film (replace the RGB finish + film).
 // `order`: the material-sorted pixel order (null: film order).
-cudaError_t spectral_spawn_launch(wpbr_ctx* ctx, const uint32_t* pass_ptr, const uint32_t* order);
-cudaError_t spectral_finish_launch(wpbr_ctx* ctx, const uint32_t* order);
+// Sample slots: a Sampled64 frame writes `slots` passes' film positions and
+// spectra side by side and gathers them into the film at once.
+cudaError_t spectral_slots(wpbr_ctx* ctx, uint32_t slots);
+cudaError_t spectral_spawn_launch(wpbr_ctx* ctx, const uint32_t* pass_ptr, const uint32_t* order, uint32_t slot);
+cudaError_t spectral_finish_launch(wpbr_ctx* ctx, const uint32_t* order, uint32_t slot, uint32_t film_slots);
 wpbr_status spectral_resolve(wpbr_ctx* ctx);
 // float4 per pixel of the fused pass's state buffer (RenderState::pstate);
 // the RGB and the Sampled64 spawn records both fit in it.

@@ -510,9 +510,11 @@ wpbr_status render_setup(wpbr_ctx* ctx, uint32_t spp, uint32_t seed, uint32_t st
 namespace {
 // The kernels of one sample pass on stream `st` over state slice g of a pass
 // group (per-pixel arrays offset by g films, counters by g sets), reading the
-// pass index at pass_ptr; with_film appends the film gather.
+// pass index at pass_ptr; with_film appends the film gather. Sampled64
+// passes write sample slot spec_slot and, when spec_film > 0, gather slots
+// 0 .. spec_film - 1 into the film.
 wpbr_status pass_kernels(wpbr_ctx* ctx, uint32_t g, const uint32_t* pass_ptr, cudaStream_t st, uint32_t grid,
-                         bool with_film) {
+                         bool with_film, uint32_t spec_slot = 0, uint32_t spec_film = 1) {
   RenderState& R = ctx->rs;
   PassCtx P = make_pass_ctx(ctx);
   const uint32_t n = R.W * R.H;
@@ -538,7 +540,7 @@ wpbr_status pass_kernels(wpbr_ctx* ctx, uint32_t g, const uint32_t* pass_ptr, cu
     order = order_buf;
   }
   if (spectral)
-    WPBR_CUDA(spectral_spawn_launch(ctx, pass_ptr, order));
+    WPBR_CUDA(spectral_spawn_launch(ctx, pass_ptr, order, spec_slot));
   else
     (ctx->has_metal ? k_spawn<true> : k_spawn<false>)<<<div_up(n, kTB), kTB, 0, st>>>(P, pass_ptr, hit_prim, pstate,
                                                                                       sq, Lbuf, pfilm, order);
@@ -554,7 +556,7 @@ wpbr_status pass_kernels(wpbr_ctx* ctx, uint32_t g, const uint32_t* pass_ptr, cu
   else
     launch_traversal<false>(P.S, P.Bv, qsrc, qsink, 2 * n, counters + 1, P.err, st, grid);
   if (spectral) {
-    WPBR_CUDA(spectral_finish_launch(ctx, order));
+    WPBR_CUDA(spectral_finish_launch(ctx, order, spec_slot, spec_film));
   } else {
     k_finish<<<div_up(n, kTB), kTB, 0, st>>>(P, pstate, shadow_hit, Lbuf, order);
     if (with_film)
@@ -655,6 +657,57 @@ uint32_t group_size(uint32_t n, uint32_t spp) {
   return std::max(k, 1u);
 }
 
+// A Sampled64 frame in groups of J sequential passes: one graph runs the J
+// passes, each writing its film positions and spectra to its own sample
+// slot, then one film gather adds the J slots in pass order (each pass's
+// neighbours in row-major order), so the film is identical to J one-pass
+// gathers while the 64-bin accumulator is read and written once per group.
+static wpbr_status spectral_frame(wpbr_ctx* ctx, uint32_t J) {
+  RenderState& R = ctx->rs;
+  cudaStream_t st = ctx->stream;
+  const uint32_t n = R.W * R.H;
+  WPBR_CUDA(spectral_slots(ctx, J));
+  WPBR_CUDA(R.pass_dev.ensure(J));
+  WPBR_CUDA(R.counters.ensure(kPassCounters));
+  WPBR_CUDA(R.shadow_map.ensure((size_t)2 * n));
+  WPBR_CUDA(R.order.ensure(n));
+  const uint64_t key = pass_graph_key(ctx) * 0x100000001B3ull + 0x5300u + J;
+  if (R.sgraph && (R.sgraph_key != key || R.sgroup != J)) {
+    cudaGraphExecDestroy(R.sgraph);
+    R.sgraph = nullptr;
+  }
+  if (!R.sgraph) {
+    cudaGraph_t gr = nullptr;
+    WPBR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    wpbr_status s = WPBR_OK;
+    for (uint32_t j = 0; j < J && s == WPBR_OK; ++j)
+      s = pass_kernels(ctx, 0, R.pass_dev.p + j, st, R.trace_grid, false, j, j + 1 == J ? J : 0);
+    cudaError_t e2 = cudaStreamEndCapture(st, &gr);
+    cudaError_t e = cudaSuccess;
+    if (s == WPBR_OK && e2 == cudaSuccess && gr) e = cudaGraphInstantiate(&R.sgraph, gr, 0);
+    if (gr) cudaGraphDestroy(gr);
+    if (s != WPBR_OK) {
+      cudaGetLastError();
+      return s;
+    }
+    if (e != cudaSuccess || e2 != cudaSuccess || !R.sgraph) {
+      cudaGetLastError();
+      R.sgraph = nullptr;
+      return set_err(ctx, WPBR_ERR_CUDA, "render: Sampled64 pass-group graph capture failed");
+    }
+    R.sgraph_key = key;
+    R.sgroup = J;
+  }
+  R.spec_dirty = true;
+  uint32_t passes[4];
+  for (uint32_t base = 0; base < R.spp; base += J) {
+    for (uint32_t j = 0; j < J; ++j) passes[j] = base + j;
+    WPBR_CUDA(cudaMemcpyAsync(R.pass_dev.p, passes, sizeof(uint32_t) * J, cudaMemcpyHostToDevice, st));
+    WPBR_CUDA(cudaGraphLaunch(R.sgraph, st));
+  }
+  return WPBR_OK;
+}
+
 // A whole frame (every pass of render_setup's spp) through the fused pass.
 // Films of RGB frames that fit a group of several passes render a group at a
 // time: one fork/join graph whose K branches run the pass kernels of passes
@@ -667,6 +720,10 @@ wpbr_status render_frame(wpbr_ctx* ctx) {
   RenderState& R = ctx->rs;
   if (!R.ready) return set_err(ctx, WPBR_ERR_NOT_BUILT, "render: render_setup not called");
   const uint32_t n = R.W * R.H;
+  if (ctx->spectrum == WPBR_SPECTRUM_SAMPLED64 && !R.pass_ptr) {
+    const uint32_t J = R.spp % 4 == 0 ? 4u : (R.spp % 2 == 0 ? 2u : 1u);
+    if (J > 1) return spectral_frame(ctx, J);
+  }
   const uint32_t K = (ctx->spectrum == WPBR_SPECTRUM_RGB && !R.pass_ptr) ? group_size(n, R.spp) : 1u;
   if (K <= 1) {
     for (uint32_t p = 0; p < R.spp; ++p) {

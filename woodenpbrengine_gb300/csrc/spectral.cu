@@ -424,8 +424,13 @@ constexpr int kHalo = kFT + 4;            // staged samples per side
 constexpr int kSStride = kSpecN + 4;      // floats per staged sample (float4-aligned, bank-skewed)
 constexpr int kFilmThreads = kFT * kFT * 4;
 constexpr int kFilmBins = kSpecN / 4;
+// npass passes' samples (pass j's film positions at pf + j * W * H and
+// spectra at L + j * W * H * 64) are added in pass order, each pass's
+// neighbours in row-major order, to an accumulator held in registers: the
+// same sums as npass one-pass gathers, with one read and one write of the
+// 64-bin accumulator.
 __global__ void __launch_bounds__(kFilmThreads, 4) k_sfilm(uint32_t W, uint32_t H, const float2* pf, const float* L,
-                                                        float* acc, float4* accw) {
+                                                        uint32_t npass, float* acc, float4* accw) {
   __shared__ __align__(16) float S[kHalo * kHalo * kSStride];
   __shared__ float wt[kFT * kFT * 25];
   __shared__ uint32_t vmask[kFT * kFT];
@@ -434,89 +439,101 @@ __global__ void __launch_bounds__(kFilmThreads, 4) k_sfilm(uint32_t W, uint32_t 
   const int bx0 = (int)blockIdx.x * kFT, by0 = (int)blockIdx.y * kFT;
   const int tx0 = (bx0 / 32) * 32, ty0 = (by0 / 32) * 32;
   const int tx1 = min(tx0 + 31, (int)W - 1), ty1 = min(ty0 + 31, (int)H - 1);
-  // halo spectra: asynchronous 16-byte global-to-shared copies (cp.async),
-  // zero-filled outside the film tile's clipped window; they land while the
-  // weights are computed
-  for (int i = tid; i < kHalo * kHalo * 16; i += kFilmThreads) {
-    int h = i / 16, c = i % 16;
-    int sy = by0 - 2 + h / kHalo, sx = bx0 - 2 + h % kHalo;
-    bool in = sy >= ty0 && sy <= ty1 && sx >= tx0 && sx <= tx1;
-    const float* src = in ? L + ((size_t)sy * W + sx) * kSpecN + 4 * c : L;
-    uint32_t dst = (uint32_t)__cvta_generic_to_shared(S + h * kSStride + 4 * c);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(in ? 16 : 0) : "memory");
-  }
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-  if (tid < kFT * kFT) vmask[tid] = 0u;
-  __syncthreads();
-  // neighbour weights: entry p * 25 + k is neighbour k (row-major in the 5x5 window) of pixel p
-  for (int e = tid; e < kFT * kFT * 25; e += kFilmThreads) {
-    int p = e / 25, k = e % 25;
-    int x = bx0 + p % kFT, y = by0 + p / kFT;
-    int sx = x - 2 + k % 5, sy = y - 2 + k / 5;
-    float w = 0.0f;
-    if (x < (int)W && y < (int)H && sx >= tx0 && sx <= tx1 && sy >= ty0 && sy <= ty1) {
-      float2 f = pf[(size_t)sy * W + sx];
-      float dx0 = f.x - 0.5f, dy0 = f.y - 0.5f;
-      int pminx = (int)ceilf(dx0 - 2.0f), pmaxx = (int)floorf(dx0 + 2.0f);
-      int pminy = (int)ceilf(dy0 - 2.0f), pmaxy = (int)floorf(dy0 + 2.0f);
-      pminx = max(pminx, tx0);
-      pminy = max(pminy, ty0);
-      pmaxx = min(pmaxx, tx1);
-      pmaxy = min(pmaxy, ty1);
-      if (!(x < pminx || x > pmaxx || y < pminy || y > pmaxy)) {
-        w = mitchell1(((float)x - f.x) / 2.0f) * mitchell1(((float)y - f.y) / 2.0f);
-        atomicOr(&vmask[p], 1u << k);
-      }
-    }
-    wt[e] = w;
-  }
-  asm volatile("cp.async.wait_all;\n" ::: "memory");
-  __syncthreads();
-  // each sample's black flag, 16 threads (a half-warp) per sample
-  for (int i = tid; i < kHalo * kHalo * 16; i += kFilmThreads) {
-    int h = i / 16, c = i % 16;
-    float4 v = *reinterpret_cast<const float4*>(S + h * kSStride + 4 * c);
-    bool nz = v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f;
-    uint32_t bal = __ballot_sync(0xFFFFFFFFu, nz);
-    if (c == 0) black[h] = ((bal >> (threadIdx.x & 16u)) & 0xFFFFu) == 0u;
-  }
-  __syncthreads();
   const int p = tid / 4, q = tid % 4;
   const int lx = p % kFT, ly = p / kFT;
   const int x = bx0 + lx, y = by0 + ly;
-  if (x >= (int)W || y >= (int)H) return;
-  const size_t pix = (size_t)y * W + x;
+  const bool mine = x < (int)W && y < (int)H;  // this thread's pixel is on the film
+  const size_t pix = mine ? (size_t)y * W + x : 0;
   float* ap = acc + pix * kSpecN + kFilmBins * q;
   float a[kFilmBins];
+  float ws = 0.0f;
+  if (mine) {
 #pragma unroll
-  for (int j = 0; j < kFilmBins / 4; ++j) {
-    float4 t = *reinterpret_cast<const float4*>(ap + 4 * j);
-    a[4 * j] = t.x; a[4 * j + 1] = t.y; a[4 * j + 2] = t.z; a[4 * j + 3] = t.w;
+    for (int j = 0; j < kFilmBins / 4; ++j) {
+      float4 t = *reinterpret_cast<const float4*>(ap + 4 * j);
+      a[4 * j] = t.x; a[4 * j + 1] = t.y; a[4 * j + 2] = t.z; a[4 * j + 3] = t.w;
+    }
+    ws = accw[pix].w;
   }
-  float ws = accw[pix].w;
-  const uint32_t vm = vmask[p];
-  const float* base = S + (ly * kHalo + lx) * kSStride + kFilmBins * q;
-  const uint8_t* bl = black + ly * kHalo + lx;
-  const float* wp = wt + p * 25;
+  const size_t plane = (size_t)W * H;
+  for (uint32_t ps = 0; ps < npass; ++ps) {
+    const float2* pfp = pf + ps * plane;
+    const float* Lp = L + ps * plane * kSpecN;
+    // halo spectra: asynchronous 16-byte global-to-shared copies (cp.async),
+    // zero-filled outside the film tile's clipped window; they land while
+    // the weights are computed
+    for (int i = tid; i < kHalo * kHalo * 16; i += kFilmThreads) {
+      int h = i / 16, c = i % 16;
+      int sy = by0 - 2 + h / kHalo, sx = bx0 - 2 + h % kHalo;
+      bool in = sy >= ty0 && sy <= ty1 && sx >= tx0 && sx <= tx1;
+      const float* src = in ? Lp + ((size_t)sy * W + sx) * kSpecN + 4 * c : Lp;
+      uint32_t dst = (uint32_t)__cvta_generic_to_shared(S + h * kSStride + 4 * c);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(in ? 16 : 0) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    if (tid < kFT * kFT) vmask[tid] = 0u;
+    __syncthreads();
+    // neighbour weights: entry p * 25 + k is neighbour k (row-major in the 5x5 window) of pixel p
+    for (int e = tid; e < kFT * kFT * 25; e += kFilmThreads) {
+      int pe = e / 25, k = e % 25;
+      int xe = bx0 + pe % kFT, ye = by0 + pe / kFT;
+      int sx = xe - 2 + k % 5, sy = ye - 2 + k / 5;
+      float w = 0.0f;
+      if (xe < (int)W && ye < (int)H && sx >= tx0 && sx <= tx1 && sy >= ty0 && sy <= ty1) {
+        float2 f = pfp[(size_t)sy * W + sx];
+        float dx0 = f.x - 0.5f, dy0 = f.y - 0.5f;
+        int pminx = (int)ceilf(dx0 - 2.0f), pmaxx = (int)floorf(dx0 + 2.0f);
+        int pminy = (int)ceilf(dy0 - 2.0f), pmaxy = (int)floorf(dy0 + 2.0f);
+        pminx = max(pminx, tx0);
+        pminy = max(pminy, ty0);
+        pmaxx = min(pmaxx, tx1);
+        pmaxy = min(pmaxy, ty1);
+        if (!(xe < pminx || xe > pmaxx || ye < pminy || ye > pmaxy)) {
+          w = mitchell1(((float)xe - f.x) / 2.0f) * mitchell1(((float)ye - f.y) / 2.0f);
+          atomicOr(&vmask[pe], 1u << k);
+        }
+      }
+      wt[e] = w;
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncthreads();
+    // each sample's black flag, 16 threads (a half-warp) per sample
+    for (int i = tid; i < kHalo * kHalo * 16; i += kFilmThreads) {
+      int h = i / 16, c = i % 16;
+      float4 v = *reinterpret_cast<const float4*>(S + h * kSStride + 4 * c);
+      bool nz = v.x != 0.0f || v.y != 0.0f || v.z != 0.0f || v.w != 0.0f;
+      uint32_t bal = __ballot_sync(0xFFFFFFFFu, nz);
+      if (c == 0) black[h] = ((bal >> (threadIdx.x & 16u)) & 0xFFFFu) == 0u;
+    }
+    __syncthreads();
+    if (mine) {
+      const uint32_t vm = vmask[p];
+      const float* base = S + (ly * kHalo + lx) * kSStride + kFilmBins * q;
+      const uint8_t* bl = black + ly * kHalo + lx;
+      const float* wp = wt + p * 25;
 #pragma unroll
-  for (int k = 0; k < 25; ++k) {
-    const int off = (k / 5) * kHalo + k % 5;
-    const bool v = (vm >> k) & 1u;
-    const float w = wp[k];
-    const bool take = v && !bl[off];
-    const float* sp = base + off * kSStride;
-    if (take) {
+      for (int k = 0; k < 25; ++k) {
+        const int off = (k / 5) * kHalo + k % 5;
+        const bool v = (vm >> k) & 1u;
+        const float w = wp[k];
+        const bool take = v && !bl[off];
+        const float* sp = base + off * kSStride;
+        if (take) {
 #pragma unroll
-      for (int j = 0; j < kFilmBins / 4; ++j) {
-        float4 t = *reinterpret_cast<const float4*>(sp + 4 * j);
-        a[4 * j] = a[4 * j] + t.x * w;
-        a[4 * j + 1] = a[4 * j + 1] + t.y * w;
-        a[4 * j + 2] = a[4 * j + 2] + t.z * w;
-        a[4 * j + 3] = a[4 * j + 3] + t.w * w;
+          for (int j = 0; j < kFilmBins / 4; ++j) {
+            float4 t = *reinterpret_cast<const float4*>(sp + 4 * j);
+            a[4 * j] = a[4 * j] + t.x * w;
+            a[4 * j + 1] = a[4 * j + 1] + t.y * w;
+            a[4 * j + 2] = a[4 * j + 2] + t.z * w;
+            a[4 * j + 3] = a[4 * j + 3] + t.w * w;
+          }
+        }
+        ws = v ? ws + w : ws;
       }
     }
-    ws = v ? ws + w : ws;
+    __syncthreads();  // the next pass restages S, wt, vmask and black
   }
+  if (!mine) return;
 #pragma unroll
   for (int j = 0; j < kFilmBins / 4; ++j)
     *reinterpret_cast<float4*>(ap + 4 * j) = make_float4(a[4 * j], a[4 * j + 1], a[4 * j + 2], a[4 * j + 3]);
@@ -612,26 +629,41 @@ static PassCtx spec_pass_ctx(wpbr_ctx* ctx) {
   return P;
 }
 
+// Room for `slots` passes' film positions and sample spectra.
+cudaError_t spectral_slots(wpbr_ctx* ctx, uint32_t slots) {
+  RenderState& R = ctx->rs;
+  const size_t n = (size_t)R.W * R.H;
+  cudaError_t e = R.pfilm.ensure(slots * n);
+  if (e == cudaSuccess) e = R.spec_L.ensure(slots * n * kSpecN);
+  return e;
+}
+
 // The scalar spawn of the Sampled64 pass, between the camera traversal and
-// the shadow-ray traversal (render_pass_launch).
-cudaError_t spectral_spawn_launch(wpbr_ctx* ctx, const uint32_t* pass_ptr, const uint32_t* order) {
+// the shadow-ray traversal (render_pass_launch); the pass's film positions go
+// to sample slot `slot`.
+cudaError_t spectral_spawn_launch(wpbr_ctx* ctx, const uint32_t* pass_ptr, const uint32_t* order, uint32_t slot) {
   RenderState& R = ctx->rs;
   uint32_t n = R.W * R.H;
   const ShadowQueue sq{R.shadow_rays.p, R.shadow_map.p, R.counters.p + kQueueCounter};
   (ctx->has_metal ? k_sspawn<true> : k_sspawn<false>)<<<div_up(n, kTB), kTB, 0, ctx->stream>>>(
-      spec_pass_ctx(ctx), pass_ptr, R.hit_prim.p, R.pstate.p, sq, R.pfilm.p, order);
+      spec_pass_ctx(ctx), pass_ptr, R.hit_prim.p, R.pstate.p, sq, R.pfilm.p + (size_t)slot * n, order);
   return cudaGetLastError();
 }
 
-// The per-bin finish, film gather and toRGB after the shadow-ray traversal.
-cudaError_t spectral_finish_launch(wpbr_ctx* ctx, const uint32_t* order) {
+// The per-bin finish after the shadow-ray traversal (the pass's spectra to
+// sample slot `slot`), then, when film_slots > 0, the film gather of slots
+// 0 .. film_slots - 1 in slot order.
+cudaError_t spectral_finish_launch(wpbr_ctx* ctx, const uint32_t* order, uint32_t slot, uint32_t film_slots) {
   RenderState& R = ctx->rs;
   uint32_t n = R.W * R.H;
-  SpecCtx C{(const SpecMat*)R.spec_mats.p, (const S64*)R.spec_le.p, R.spec_L.p};
+  SpecCtx C{(const SpecMat*)R.spec_mats.p, (const S64*)R.spec_le.p, R.spec_L.p + (size_t)slot * n * kSpecN};
   k_sfinish<<<div_up((uint64_t)n * kBinLanes, 128), 128, 0, ctx->stream>>>(spec_pass_ctx(ctx), C, R.pstate.p,
                                                                             R.shadow_hit.p, order);
-  dim3 fg(div_up(R.W, kFT), div_up(R.H, kFT));
-  k_sfilm<<<fg, kFilmThreads, 0, ctx->stream>>>(R.W, R.H, R.pfilm.p, R.spec_L.p, R.spec_acc.p, (float4*)R.acc.p);
+  if (film_slots) {
+    dim3 fg(div_up(R.W, kFT), div_up(R.H, kFT));
+    k_sfilm<<<fg, kFilmThreads, 0, ctx->stream>>>(R.W, R.H, R.pfilm.p, R.spec_L.p, film_slots, R.spec_acc.p,
+                                                   (float4*)R.acc.p);
+  }
   return cudaGetLastError();
 }
 
