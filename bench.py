@@ -156,6 +156,15 @@ def ncu_traffic_per_ray():
     return None
 
 
+def ncu_l2():
+    """L2 throughput and L1/L2 hit rates of the traversal kernel from the
+    committed ncu summary (the kernel's working set is L2-resident)."""
+    path = os.path.join(ROOT, "profiles", "trace_c1_traffic.json")
+    if os.path.exists(path):
+        return json.load(open(path)).get("l2")
+    return None
+
+
 def roofline(nbytes, seconds, model, what):
     """Roofline entry of a rate: algorithmic bytes over the measured time,
     against the measured HBM copy bandwidth."""
@@ -964,6 +973,7 @@ def main():
                      # DRAM bytes actually moved (ncu, scaled by rays) over the launch time: most of the
                      # byte model's node and primitive fetches are served from L2
                      "traffic_frac": ((tpr * n) / (trav_ms / 1e3) / 1e9 / peak) if tpr else None,
+                     "l2": ncu_l2(),
                      "bytes_model": "48 + 32*V + 36*P per ray, V=%.2f box tests, P=%.2f triangle tests" % (V, P)},
         "clocks": ck,
         "build": {"mprims_per_s": info["n_prims"] / build_s / 1e6, "ms": build_s * 1e3,
