@@ -22,7 +22,8 @@ constexpr int kPersistBlock = 128;
 // A warp fetches new rays once at least this many of its lanes are idle (or
 // none is busy): a refill costs the whole warp a detour, so batching them
 // pays. 8.4M-ray microbenchmark, closest hit: 1 lane 4.77 ms, 8 4.66, 16
-// 4.39, 20 4.35, 24 4.35, 28 4.42, 32 4.88.
+// 4.39, 20 4.35, 24 4.35, 28 4.42, 32 4.88; with the shared-memory stack
+// entries (closest-hit step): 18 4.139, 20 4.128, 22 4.136 ms.
 #ifndef WPBR_REFILL_MIN
 #define WPBR_REFILL_MIN 20
 #endif
@@ -136,7 +137,9 @@ struct TravStack<STACK, false> {
 // blocks 4.228 / 3.855, 10 at 8 4.232 / 3.858, 12 at 8 4.258 / 3.871, 14 at 8
 // (7 blocks fit) 4.476 / 4.079, none at 8 4.351 / 3.975; 6 or 8 at 9 blocks
 // 4.27 / 3.91; 4-8 at 12 blocks 4.56-4.72 (the L1 left is too small), 12 at
-// 7 blocks 4.437; hits identical in every case.
+// 7 blocks 4.437; hits identical in every case. Again once the far-child
+// prefetch was gone and rays and hits streamed: 6 entries 4.151, 8 4.128,
+// 10 4.129 ms.
 template <int STACK, int KS>
 struct TravStackSh {
   unsigned long long* s_tr;  // this lane's column: entry i at s_tr[i * kPersistBlock]
