@@ -606,6 +606,11 @@ WPBR_API wpbr_status wpbr_collide_device(wpbr_ctx* ctx, const void* d_rays, uint
 // ms, five uneven ones 5.82 ms: every chunk also pays its own ray-order
 // sort).
 constexpr uint64_t kPipeMin = 1ull << 22;
+// Edge chunks of 1/E of the batch; 8.4M rays through pinned buffers, ms per
+// call with the current kernels: E = 4 4.969, 8 4.758, 16 4.855, 32 5.034.
+#ifndef WPBR_PIPE_EDGE
+#define WPBR_PIPE_EDGE 8
+#endif
 
 static wpbr_status collide_pipelined(wpbr_ctx* ctx, const float* rays, uint64_t n, float* hits, uint32_t mode) {
   if (!ctx->io_h2d) WPBR_CUDA(cudaStreamCreateWithFlags(&ctx->io_h2d, cudaStreamNonBlocking));
@@ -615,9 +620,10 @@ static wpbr_status collide_pipelined(wpbr_ctx* ctx, const float* rays, uint64_t 
     if (!ev) WPBR_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   cudaStream_t st = ctx->stream;
   cudaStream_t comp[2] = {st, ctx->io_comp};
-  // four chunks of 1/8, 3/8, 3/8, 1/8 of the batch: the first copy up and the
-  // last copy down, which nothing overlaps, are short
-  uint64_t bounds[5] = {0, n / 8, n / 2, n - n / 8, n};
+  // four chunks of 1/E, 1/2 - 1/E, 1/2 - 1/E, 1/E of the batch: the first
+  // copy up and the last copy down, which nothing overlaps, are short
+  const uint64_t edge = n / WPBR_PIPE_EDGE;
+  uint64_t bounds[5] = {0, edge, n / 2, n - edge, n};
   // everything starts after the work already queued on the context's stream
   WPBR_CUDA(cudaEventRecord(ctx->io_ev[2], st));
   WPBR_CUDA(cudaStreamWaitEvent(ctx->io_h2d, ctx->io_ev[2], 0));
