@@ -91,8 +91,8 @@ def parse():
     p.add_argument("--profile-build", action="store_true",
                    help="LBVH build case for ncu: 8 builds of the 1,310,720-triangle mesh (3 warm-up, 5 timed)")
     p.add_argument("--profile-collide", action="store_true",
-                   help="collide case for ncu: one build of the microbenchmark mesh (45 launches), then three "
-                        "closest-hit collides of all 8,388,608 rays on resident buffers (16 launches each)")
+                   help="collide case for ncu: one build of the microbenchmark mesh (38 launches), then three "
+                        "closest-hit collides of all 8,388,608 rays on resident buffers (13 launches each)")
     p.add_argument("--profile-frame", action="store_true",
                    help="render case for ncu: config 2 (level 8) at 1920x1080, two 8-spp frames")
     return p.parse_args()
