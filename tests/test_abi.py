@@ -57,6 +57,8 @@ def test_instrumentation_entry_points_validate_arguments(W):
     assert L.wpbr_set_kernel_timing(None, 1) == W.ERR_INVALID_ARG
     assert L.wpbr_kernel_timing(None, C.byref(f), C.byref(c)) == W.ERR_INVALID_ARG
     assert L.wpbr_collide(None, None, 0, None, 0) == W.ERR_INVALID_ARG
+    keys = (C.c_uint32 * 4)()
+    assert L.wpbr_debug_ray_order(None, None, 0, keys, keys) == W.ERR_INVALID_ARG
 
 
 def test_no_device_is_reported_not_faked(W):
