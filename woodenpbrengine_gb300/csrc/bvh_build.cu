@@ -723,11 +723,13 @@ __device__ __forceinline__ uint32_t sah_bucket(const V3& lo, const V3& hi, const
 }
 
 // ---------------------------------------------------------------------------
-// A8, segments of more than 32 treelet roots: every SAH level of the build in
-// one cooperative launch (all blocks resident), five phases per level
-// separated by grid barriers:
-//   A   bounds and centroid bounds of every segment (per-tile pre-reduction in
-//       shared memory, then global atomics on order-preserving encodings);
+// A8, segments of more than kMedSeg treelet roots: their SAH levels in one
+// cooperative launch (all blocks resident), phases separated by grid
+// barriers:
+//   A   (root level only) bounds and centroid bounds of the segment
+//       (per-tile pre-reduction in shared memory, then global atomics on
+//       order-preserving encodings); on later levels phase E of the level
+//       before accumulates them by child segment;
 //   B   the bucket of every root, bucket counts and bounds of every segment;
 //   C1  the split decision of every segment (one warp decides, the same float
 //       operations as the sequential loop) and the partition flags of
@@ -741,7 +743,8 @@ __device__ __forceinline__ uint32_t sah_bucket(const V3& lo, const V3& hi, const
 //       node ids, and the next level's segment slots (numbered in position
 //       order) or the small-segment queue;
 //   E   the swap: each pair trades places, the next level's position arrays
-//       are written, and single-root children are linked.
+//       are written, single-root children are linked, and the next level's
+//       segment bounds are accumulated.
 // Segments of 33..kMedSeg roots go to the block-local queue (k_medium_sah),
 // segments of 2..32 roots to the warp-local queue (k_small_sah). A tile is
 // kCoopBlock consecutive positions. Every grid barrier is bounded: past the
@@ -914,10 +917,11 @@ __device__ __forceinline__ void init_segment(uint32_t* acc, uint32_t* bk) {
 }
 
 // A large segment met by a block's batch of positions (shared memory). A
-// batch of kBatch consecutive positions meets at most 2 + (kBatch - 2) / 33
-// = 64 large segments (each holds more than 32 positions), and their ids are
-// consecutive (segments are numbered in position order), so s & 63 names
-// each one's slot without collisions.
+// batch of kBatch consecutive positions meets at most
+// 2 + (kBatch - 2) / (kMedSeg + 1) large segments (each holds more than
+// kMedSeg positions), and their ids are consecutive (segments are numbered in
+// position order), so s & (kSlots - 1) names each one's slot without
+// collisions; their large children, two at most each, take twice as many.
 struct SlotSeg {
   uint32_t s, a, b, node;
   uint32_t spt, mid, best, kk;
