@@ -2339,7 +2339,11 @@ __global__ void k_flatten(uint32_t N, uint32_t* info, const uint32_t* skey, cons
     atomicOr(err, kErrBuild);
     return;
   }
-  atomicMax(depth_max, depth);
+  {  // the tree depth: one atomic per warp's flattened nodes
+    const uint32_t act = __activemask();
+    const uint32_t dmax = __reduce_max_sync(act, depth);
+    if ((threadIdx.x & 31u) == (uint32_t)(__ffs(act) - 1)) atomicMax(depth_max, dmax);
+  }
   float4 bl = nb_lo[X], bh = nb_hi[X];
   float* B = lin_bounds + (size_t)idx * 6;
   B[0] = bl.x; B[1] = bl.y; B[2] = bl.z; B[3] = bh.x; B[4] = bh.y; B[5] = bh.z;
